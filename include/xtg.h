@@ -1,0 +1,251 @@
+/*
+ * xtg.h — C ABI of the GB300 evaluator for xtensor's assign + reduce hot path.
+ *
+ * Everything here is plain C: pointers, sizes, POD structs, status codes.
+ * No C++ exceptions and no torch types cross this boundary.  A caller lowers
+ * an xtensor expression tree (an `xfunction` over containers / strided views,
+ * optionally wrapped by an `xreducer`) into an `xtg_expr` — a postfix list of
+ * nodes plus up to XTG_MAX_LEAVES leaf arrays in device memory — and hands it
+ * to xtg_assign / xtg_reduce / xtg_argreduce.  The library evaluates the whole
+ * tree in one fused sm_103a kernel (compiled once per tree *shape* and cached),
+ * with broadcasting folded into per-leaf stride arithmetic exactly as
+ * xtensor's steppers do it.
+ *
+ * Reference interfaces replaced (paths inside xtensor 0.27.1):
+ *   xtg_assign      <- xt::assign_xexpression / xexpression_assigner<Tag>::assign_data
+ *                      include/xtensor/core/xassign.hpp:214-226, 439-478, 480-486
+ *   xtg_broadcast_shape
+ *                   <- xfunction::broadcast_shape / xt::broadcast_shape
+ *                      include/xtensor/core/xfunction.hpp:709-727,
+ *                      include/xtensor/core/xstrides.hpp:738-794
+ *   xtg_reduce      <- xt::reduce + xreducer_stepper::aggregate(_impl) and
+ *                      reduce_immediate; front-ends sum/prod/amax/amin/mean/
+ *                      variance/stddev/norm_*
+ *                      include/xtensor/reducers/xreducer.hpp:289-565, 987-1079, 1778-1868
+ *                      include/xtensor/core/xmath.hpp:367-423, 777-811, 1803-1911, 2033-2180
+ *                      include/xtensor/reducers/xnorm.hpp:397-526
+ *   xtg_argreduce   <- xt::argmax / xt::argmin (arg_func_impl)
+ *                      include/xtensor/misc/xsort.hpp:1158-1296
+ *   xtg_batch_*     <- no counterpart (new batching layer over the same path)
+ *   xtg_server_*    <- no counterpart (new request server over the same path)
+ *
+ * Strides are in ELEMENTS (as xtensor's strides are), may be zero (broadcast)
+ * or negative (reversed views).  Shapes follow xtensor's row-major convention.
+ */
+#ifndef XTG_H
+#define XTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XTG_MAX_RANK 8
+#define XTG_MAX_LEAVES 8
+#define XTG_MAX_NODES 48
+#define XTG_MAX_SCALARS 16
+
+/* ---- status codes (xtensor throws; the ABI returns) ------------------------
+ * XTG_ERR_BROADCAST  <- xt::broadcast_error        (core/xexception.hpp:122-135)
+ * XTG_ERR_AXIS       <- std::runtime_error "Reducing axes should be sorted/…"
+ *                       (reducers/xreducer.hpp:338-350, 1426-1440)
+ * XTG_ERR_OUT_OF_RANGE <- std::out_of_range from normalize_axis
+ *                       (core/xexception.hpp:287-297, utils/xutils.hpp:349-395)
+ */
+typedef enum {
+    XTG_OK = 0,
+    XTG_ERR_INVALID = 1,       /* malformed argument (null pointer, bad rank, bad dtype) */
+    XTG_ERR_BROADCAST = 2,     /* incompatible shapes */
+    XTG_ERR_AXIS = 3,          /* unsorted / duplicate / out-of-bounds reduction axes */
+    XTG_ERR_OUT_OF_RANGE = 4,  /* axis outside [-rank, rank) */
+    XTG_ERR_SHAPE = 5,         /* destination shape does not match the expression */
+    XTG_ERR_CUDA = 6,          /* CUDA runtime / driver error */
+    XTG_ERR_JIT = 7,           /* kernel compilation failed */
+    XTG_ERR_OOM = 8,           /* device allocation failed or admission refused for memory */
+    XTG_ERR_UNSUPPORTED = 9,   /* a combination this build does not lower */
+    XTG_ERR_TIMEOUT = 10,      /* a bounded wait ran out */
+    XTG_ERR_REJECTED = 11,     /* server admission rejected the request */
+    XTG_ERR_CANCELLED = 12,    /* request cancelled before it ran */
+    XTG_ERR_NOT_FOUND = 13     /* unknown request id / handle */
+} xtg_status;
+
+/* ---- element types ------------------------------------------------------- */
+typedef enum {
+    XTG_BOOL = 0,
+    XTG_INT8 = 1,
+    XTG_UINT8 = 2,
+    XTG_INT16 = 3,
+    XTG_UINT16 = 4,
+    XTG_INT32 = 5,
+    XTG_UINT32 = 6,
+    XTG_INT64 = 7,
+    XTG_UINT64 = 8,
+    XTG_BFLOAT16 = 9,  /* storage type; arithmetic on it is carried out in float32 */
+    XTG_FLOAT32 = 10,
+    XTG_FLOAT64 = 11,
+    XTG_NUM_DTYPES = 12
+} xtg_dtype;
+
+/* ---- expression node opcodes (postfix) -------------------------------------
+ * Binary/unary opcodes mirror xtensor's functors (core/xoperation.hpp:104-143,
+ * core/xmath.hpp:295-341, 589-602, 1101-1108).  A node's `dtype` is its
+ * result type under C++ usual arithmetic conversions (what `decltype(f(a,b))`
+ * gives for the functor in the reference); operands are converted to it
+ * before the operation, comparisons/logical ops compute in the common type of
+ * their operands and produce XTG_BOOL.
+ */
+typedef enum {
+    XTG_OP_LEAF = 0,      /* arg = leaf index */
+    XTG_OP_SCALAR = 1,    /* imm holds the value, dtype its type (xscalar) */
+    /* unary */
+    XTG_OP_NEG = 10, XTG_OP_POS, XTG_OP_EXP, XTG_OP_LOG, XTG_OP_SQRT, XTG_OP_ABS,
+    XTG_OP_SQUARE, XTG_OP_SIN, XTG_OP_COS, XTG_OP_TANH, XTG_OP_LOGICAL_NOT,
+    XTG_OP_BIT_NOT, XTG_OP_CAST,
+    /* binary */
+    XTG_OP_ADD = 40, XTG_OP_SUB, XTG_OP_MUL, XTG_OP_DIV, XTG_OP_MOD,
+    XTG_OP_MAXIMUM, XTG_OP_MINIMUM,
+    XTG_OP_LT, XTG_OP_LE, XTG_OP_GT, XTG_OP_GE, XTG_OP_EQ, XTG_OP_NE,
+    XTG_OP_LOGICAL_AND, XTG_OP_LOGICAL_OR, XTG_OP_BIT_AND, XTG_OP_BIT_OR, XTG_OP_BIT_XOR,
+    XTG_OP_POW,
+    /* ternary: where(cond, a, b)  (conditional_ternary, core/xoperation.hpp:127-143) */
+    XTG_OP_WHERE = 70,
+    /* keep-dims row reductions over the last `arg` axes of the expression
+     * shape, broadcast back over those axes.  They express
+     * `x - mean(x, {trailing}, keep_dims)` style trees so that statistics and
+     * the surrounding elementwise work run in one pass.  aux/imm.i = ddof for
+     * RVAR / RSTD. */
+    XTG_OP_RSUM = 80, XTG_OP_RMEAN, XTG_OP_RVAR, XTG_OP_RSTD, XTG_OP_RMAX, XTG_OP_RMIN
+} xtg_opcode;
+
+typedef union {
+    double f;
+    int64_t i;
+    uint64_t u;
+} xtg_value;
+
+typedef struct {
+    int32_t op;     /* xtg_opcode */
+    int32_t dtype;  /* result xtg_dtype */
+    int32_t arg;    /* leaf index (LEAF), target dtype (CAST), axis count (R*) */
+    int32_t aux;    /* ddof for RVAR/RSTD */
+    xtg_value imm;  /* SCALAR value (f for float types, i/u for integers) */
+} xtg_node;
+
+/* A strided array in device memory (host memory for the oracle).
+ * data points at element (0,…,0). */
+typedef struct {
+    void* data;
+    int32_t dtype;
+    int32_t rank;
+    int64_t shape[XTG_MAX_RANK];
+    int64_t strides[XTG_MAX_RANK];
+} xtg_array;
+
+typedef struct {
+    int32_t n_nodes;
+    int32_t n_leaves;
+    xtg_node nodes[XTG_MAX_NODES];
+    xtg_array leaves[XTG_MAX_LEAVES];
+} xtg_expr;
+
+/* ---- reductions -------------------------------------------------------------
+ * Result-type and initial-value rules follow XTENSOR_REDUCER_FUNCTION
+ * (core/xmath.hpp:367-423), mean_division (core/xmath.hpp:1828-1835),
+ * variance (core/xmath.hpp:2082-2103) and XTENSOR_NORM_FUNCTION
+ * (reducers/xnorm.hpp:397-437). */
+typedef enum {
+    XTG_RED_SUM = 0, XTG_RED_PROD, XTG_RED_AMAX, XTG_RED_AMIN, XTG_RED_MEAN,
+    XTG_RED_VARIANCE, XTG_RED_STDDEV, XTG_RED_NORM_L0, XTG_RED_NORM_L1,
+    XTG_RED_NORM_SQ, XTG_RED_NORM_L2, XTG_RED_NORM_LINF
+} xtg_reduce_op;
+
+typedef enum {
+    XTG_PREC_COMPENSATED = 0, /* float32/bf16: TwoSum double-float accumulation; float64: FP64 */
+    XTG_PREC_PLAIN = 1        /* plain accumulation in the accumulator type */
+} xtg_precision;
+
+typedef struct {
+    int32_t op;           /* xtg_reduce_op */
+    int32_t n_axes;       /* -1: all axes (the no-axis overloads) */
+    int64_t axes[XTG_MAX_RANK]; /* may be negative; normalized then checked sorted+unique */
+    int32_t keep_dims;    /* xt::keep_dims */
+    int32_t has_initial;  /* xt::initial(v) */
+    xtg_value initial;    /* in the accumulator type's domain */
+    int32_t acc_dtype;    /* -1 = default; else the `T` template argument (e.g. sum<int64_t>) */
+    int32_t precision;    /* xtg_precision */
+    int64_t ddof;         /* variance / stddev */
+} xtg_reduce_desc;
+
+typedef enum { XTG_ARGMAX = 0, XTG_ARGMIN = 1 } xtg_arg_op;
+
+typedef void* xtg_stream; /* a cudaStream_t; NULL = legacy default stream */
+
+enum { XTG_MEMCPY_H2D = 1, XTG_MEMCPY_D2H = 2, XTG_MEMCPY_D2D = 3, XTG_MEMCPY_DEFAULT = 4 };
+
+/* ---- runtime --------------------------------------------------------------- */
+const char* xtg_version(void);
+const char* xtg_status_string(xtg_status s);
+/* Message of the last failing call on this thread (empty if none). */
+const char* xtg_last_error(void);
+xtg_status xtg_init(int device);
+xtg_status xtg_device_count(int* count);
+xtg_status xtg_device_info(int* sm_count, int64_t* hbm_bytes, int* cc_major, int* cc_minor);
+xtg_status xtg_mem_info(int64_t* free_bytes, int64_t* total_bytes);
+xtg_status xtg_malloc(void** ptr, size_t bytes, xtg_stream stream); /* stream-ordered pool */
+xtg_status xtg_free(void* ptr, xtg_stream stream);
+xtg_status xtg_host_alloc(void** ptr, size_t bytes);                 /* pinned */
+xtg_status xtg_host_free(void* ptr);
+xtg_status xtg_memcpy(void* dst, const void* src, size_t bytes, int kind, xtg_stream stream);
+xtg_status xtg_memset(void* dst, int value, size_t bytes, xtg_stream stream);
+xtg_status xtg_stream_create(xtg_stream* stream);
+xtg_status xtg_stream_destroy(xtg_stream stream);
+xtg_status xtg_stream_sync(xtg_stream stream);
+xtg_status xtg_device_sync(void);
+size_t xtg_dtype_size(int32_t dtype);
+
+/* ---- shape algebra ----------------------------------------------------------- */
+/* Broadcast shape of all leaves (right-aligned, size-1 / missing dims
+ * broadcast), XTG_ERR_BROADCAST otherwise. */
+xtg_status xtg_broadcast_shape(const xtg_expr* e, int32_t* rank, int64_t* shape);
+/* Result dtype of the expression's root node after type checking. */
+xtg_status xtg_expr_dtype(const xtg_expr* e, int32_t* dtype);
+/* Output shape / dtype of a reduction (performs the axis checks). */
+xtg_status xtg_reduce_shape(const xtg_expr* e, const xtg_reduce_desc* rd,
+                            int32_t* rank, int64_t* shape, int32_t* out_dtype);
+/* Accumulator dtype a reduction computes its sum in (the reference's
+ * init-value/functor result type). */
+xtg_status xtg_reduce_acc_dtype(const xtg_expr* e, const xtg_reduce_desc* rd, int32_t* acc_dtype);
+
+/* ---- evaluation (the hot path) -------------------------------------------------
+ * out must already have the broadcast shape (the container resize of
+ * xassign.hpp:570-607 is the caller's), any strides.  A destination that
+ * overlaps a leaf is only safe when it aliases it element-for-element (same
+ * data pointer and strides), which is what computed assignment (`a += e`)
+ * produces; the xt:: surface evaluates into a temporary otherwise. */
+xtg_status xtg_assign(const xtg_expr* e, const xtg_array* out, xtg_stream stream);
+xtg_status xtg_reduce(const xtg_expr* e, const xtg_reduce_desc* rd,
+                      const xtg_array* out, xtg_stream stream);
+/* has_axis = 0: index into the flattened (row-major) expression. */
+xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis,
+                         const xtg_array* out, xtg_stream stream);
+
+/* ---- kernel cache / tuning ------------------------------------------------------ */
+typedef struct {
+    int64_t compiles;       /* NVRTC compilations this process */
+    int64_t disk_hits;      /* cubins loaded from the on-disk cache */
+    int64_t memory_hits;    /* kernels found in the in-process cache */
+    double compile_seconds; /* total time spent in NVRTC */
+    int64_t launches;       /* kernels launched through this library */
+} xtg_jit_stats;
+xtg_status xtg_get_jit_stats(xtg_jit_stats* st);
+/* Integer knobs: "assign.block", "assign.unroll", "assign.ctas_per_sm",
+ * "reduce.block", "reduce.chunk", "transpose.tile", "batch.*" … ; value < 0 resets. */
+xtg_status xtg_set_option(const char* key, int64_t value);
+xtg_status xtg_get_option(const char* key, int64_t* value);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XTG_H */

@@ -1,0 +1,118 @@
+"""ctypes binding of the C oracle (xt_oracle.c) — test infrastructure only.
+
+Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use this module; the product path never does.  Inputs are host
+numpy arrays wrapped as ``xtg_array`` (HostArray); expressions are the same
+lowered ``xtg_expr`` the GPU library takes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from xtensor_gb300._ffi import MAX_RANK, Array, Expr, ReduceDesc, dtype_code, np_dtype
+from xtensor_gb300.device import HostArray
+from xtensor_gb300.expr import as_expr, lower
+from xtensor_gb300.ops import make_desc
+
+SO = Path(__file__).resolve().parent / "_build" / "liboracle.so"
+_L = None
+
+
+def lib():
+    global _L
+    if _L is None:
+        if not SO.exists():
+            from xtensor_gb300.build import build_oracle
+            build_oracle()
+        L = C.CDLL(str(SO))
+        P = C.POINTER
+        L.orc_assign.argtypes = [P(Expr), P(Array)]
+        L.orc_reduce.argtypes = [P(Expr), P(ReduceDesc), P(Array)]
+        L.orc_argreduce.argtypes = [P(Expr), C.c_int, C.c_int, C.c_int64, P(Array)]
+        L.orc_expr_dtype.argtypes = [P(Expr)]
+        L.orc_broadcast_shape.argtypes = [P(Expr), P(C.c_int32), P(C.c_int64)]
+        L.orc_reduce_result_dtype.argtypes = [P(Expr), P(ReduceDesc)]
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_promote.argtypes = [C.c_int, C.c_int]
+        _L = L
+    return _L
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"oracle status {code}: {msg}")
+        self.status = code
+
+
+def _chk(s):
+    if s != 0:
+        raise OracleError(s, lib().orc_last_error().decode())
+
+
+def host(a: np.ndarray, dtype=None) -> HostArray:
+    return HostArray(a, dtype)
+
+
+def expr_dtype(e) -> int:
+    ex, keep = lower(as_expr(e))
+    return lib().orc_expr_dtype(C.byref(ex))
+
+
+def broadcast_shape(e):
+    ex, keep = lower(as_expr(e))
+    r = C.c_int32()
+    sh = (C.c_int64 * MAX_RANK)()
+    _chk(lib().orc_broadcast_shape(C.byref(ex), C.byref(r), sh))
+    return tuple(sh[i] for i in range(r.value))
+
+
+def assign(e, shape=None, dtype=None) -> np.ndarray:
+    """Evaluate `e` (over HostArray leaves) into a new numpy array."""
+    e = as_expr(e)
+    shape = broadcast_shape(e) if shape is None else tuple(shape)
+    code = expr_dtype(e) if dtype is None else dtype_code(dtype)
+    out = np.zeros(shape, dtype=np_dtype(code))
+    ho = HostArray(out, code)
+    ex, keep = lower(e)
+    o = ho.xtg_array()
+    _chk(lib().orc_assign(C.byref(ex), C.byref(o)))
+    return out
+
+
+def reduce(op, e, axes=None, keep_dims=False, initial=None, acc_dtype=None, ddof=0) -> np.ndarray:
+    e = as_expr(e)
+    rd = make_desc(op, axes=axes, keep_dims=keep_dims, initial=initial, acc_dtype=acc_dtype, ddof=ddof)
+    ex, keep = lower(e)
+    code = lib().orc_reduce_result_dtype(C.byref(ex), C.byref(rd))
+    shape = broadcast_shape(e)
+    rank = len(shape)
+    if axes is None:
+        ax = list(range(rank))
+    else:
+        ax = [a + rank if a < 0 else a for a in ([axes] if isinstance(axes, int) else list(axes))]
+    oshape = tuple((1 if i in ax else n) for i, n in enumerate(shape) if keep_dims or i not in ax)
+    out = np.zeros(oshape, dtype=np_dtype(code))
+    ho = HostArray(out, code)
+    o = ho.xtg_array()
+    _chk(lib().orc_reduce(C.byref(ex), C.byref(rd), C.byref(o)))
+    return out
+
+
+def argreduce(op, e, axis=None) -> np.ndarray:
+    e = as_expr(e)
+    shape = broadcast_shape(e)
+    if axis is None or len(shape) <= 1:
+        oshape = ()
+    else:
+        a = axis + len(shape) if axis < 0 else axis
+        oshape = tuple(n for i, n in enumerate(shape) if i != a)
+    out = np.zeros(oshape, dtype=np.int64)
+    ho = HostArray(out)
+    ex, keep = lower(e)
+    o = ho.xtg_array()
+    code = 0 if op == "argmax" else 1
+    _chk(lib().orc_argreduce(C.byref(ex), code, 0 if axis is None else 1, 0 if axis is None else axis, C.byref(o)))
+    return out

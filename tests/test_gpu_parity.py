@@ -1,0 +1,397 @@
+"""GPU parity: every kernel family against the oracle on seeded inputs.
+
+Tolerances (stated here, checked below):
+  * integer, bool and index results, copies and transposes: bit-exact;
+  * float32/float64 trees of + - * / sqrt, comparisons, select: bit-exact
+    (IEEE operations in the same order, no fused multiply-add);
+  * trees with exp/log/sin/cos/tanh: <= 4 ulp of the magnitude of the terms
+    (CUDA's single-precision exp is within 2 ulp, the reference's libm within 1);
+  * float32 sums/means/norms: |gpu - exact| <= 1e-6 * sum|x| against an FP64
+    evaluation, and within the reference's own error envelope
+    (|gpu - ref| <= |ref - exact| + 1e-6 * sum|x|);
+  * variance/stddev: relative 1e-6 (float32 data) / 1e-12 (float64 data) of
+    the FP64 value;
+  * amax/amin: bit-exact.
+"""
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+import pytest
+
+import xtensor_gb300 as xg
+from xtensor_gb300 import ops
+from xtensor_gb300.device import DeviceArray, HostArray
+from oracle import oracle as O
+
+from util import assert_close_rel, assert_ulp, bf16_bits_to_f32, f32_to_bf16_bits, rng
+
+pytestmark = pytest.mark.gpu
+
+F32_EPS = 2.0**-24
+
+
+def dev(a, dtype=None):
+    return DeviceArray.from_numpy(a, dtype)
+
+
+def H(a, dtype=None):
+    return HostArray(a, dtype)
+
+
+# ---------------------------------------------------------------------------- assign
+def test_c0_expression_small():
+    g = rng(0)
+    A = g.uniform(-1, 1, (64, 96)).astype(np.float32)
+    b = g.standard_normal(96).astype(np.float32)
+    dA, db = dev(A), dev(b)
+    out = DeviceArray.empty(A.shape, "float32")
+    xg.assign(out, dA * db + xg.exp(-dA * dA))
+    got = out.to_numpy()
+    ref = O.assign(H(A) * H(b) + xg.exp(-H(A) * H(A)))
+    scale = np.abs(A * b) + np.exp(-(A.astype(np.float64) ** 2))
+    assert_close_rel(got, ref, 4 * F32_EPS, scale, "A*b + exp(-A*A)")
+
+
+@pytest.mark.parametrize("dt", ["float32", "float64", "int32", "int64", "uint8", "int16"])
+def test_arith_bit_exact(dt):
+    g = rng(1)
+    if dt.startswith("float"):
+        a = g.standard_normal((17, 33)).astype(dt)
+        b = g.standard_normal((33,)).astype(dt) + 2
+    else:
+        info = np.iinfo(dt)
+        a = g.integers(max(info.min, -1000), min(info.max, 1000), (17, 33)).astype(dt)
+        b = g.integers(1, min(info.max, 100), (33,)).astype(dt)
+    for f in [lambda x, y: x + y, lambda x, y: x - y * y, lambda x, y: x * y - x,
+              lambda x, y: xg.maximum(x, y) - xg.minimum(x, y), lambda x, y: xg.where(x > y, x, y * 2)]:
+        e_d = f(dev(a), dev(b))
+        e_h = f(H(a), H(b))
+        code = O.expr_dtype(e_h)
+        assert xg.expr_dtype(e_d) == code
+        out = DeviceArray.empty(a.shape, code)
+        xg.assign(out, e_d)
+        ref = O.assign(e_h)
+        np.testing.assert_array_equal(out.to_numpy(), ref)
+
+
+def test_division_and_sqrt_bit_exact():
+    g = rng(2)
+    a = g.standard_normal((50, 70)).astype(np.float32)
+    b = (g.random((70,)) + 0.5).astype(np.float32)
+    out = DeviceArray.empty(a.shape, "float32")
+    xg.assign(out, xg.sqrt(xg.abs_(dev(a))) / dev(b))
+    ref = O.assign(xg.sqrt(xg.abs_(H(a))) / H(b))
+    assert_ulp(out.to_numpy(), ref, 0, "sqrt/div")
+
+
+def test_mixed_type_promotion():
+    g = rng(3)
+    a = g.integers(-50, 50, (8, 9)).astype(np.int32)
+    b = g.standard_normal((9,)).astype(np.float64)
+    c = g.integers(0, 200, (8, 1)).astype(np.uint8)
+    e_d = dev(a) * dev(b) + dev(c)
+    e_h = H(a) * H(b) + H(c)
+    assert O.expr_dtype(e_h) == xg.DTYPES["float64"] == xg.expr_dtype(e_d)
+    out = DeviceArray.empty((8, 9), "float64")
+    xg.assign(out, e_d)
+    np.testing.assert_array_equal(out.to_numpy(), O.assign(e_h))
+    # uint8 + uint8 is int in C++: no wrap
+    u = g.integers(0, 256, (40,)).astype(np.uint8)
+    e = dev(u) + dev(u)
+    assert xg.expr_dtype(e) == xg.DTYPES["int32"]
+    o2 = DeviceArray.empty((40,), "int32")
+    xg.assign(o2, e)
+    np.testing.assert_array_equal(o2.to_numpy(), u.astype(np.int32) * 2)
+    # storing into uint8 wraps like a static_cast
+    o3 = DeviceArray.empty((40,), "uint8")
+    xg.assign(o3, e)
+    np.testing.assert_array_equal(o3.to_numpy(), (u.astype(np.int32) * 2).astype(np.uint8))
+
+
+def test_scalars_and_literals():
+    g = rng(4)
+    a = g.standard_normal((10, 11)).astype(np.float32)
+    # 2.0 is a double literal: a * 2.0 is exact in float, the tree is float64 in C++
+    for f in [lambda x: x * 2.0 + 1, lambda x: 3 - x, lambda x: x / np.float32(4.0), lambda x: -x + np.float32(0.5)]:
+        out = DeviceArray.empty(a.shape, "float32")
+        xg.assign(out, f(dev(a)))
+        ref = O.assign(f(H(a)), dtype="float32")
+        assert_ulp(out.to_numpy(), ref, 0, "scalar")
+
+
+def test_broadcast_shapes_and_errors():
+    g = rng(5)
+    a = g.standard_normal((3, 1, 5)).astype(np.float32)
+    b = g.standard_normal((4, 1)).astype(np.float32)
+    e = dev(a) + dev(b)
+    assert xg.broadcast_shape(e) == (3, 4, 5)
+    out = DeviceArray.empty((3, 4, 5), "float32")
+    xg.assign(out, e)
+    np.testing.assert_array_equal(out.to_numpy(), a + b)
+    with pytest.raises(xg.XtgError) as ei:
+        xg.broadcast_shape(dev(np.zeros((3, 4), np.float32)) + dev(np.zeros((5,), np.float32)))
+    assert ei.value.status == 2  # broadcast_error
+    # destination of the wrong shape
+    with pytest.raises(xg.XtgError):
+        xg.assign(DeviceArray.empty((3, 4), "float32"), e)
+
+
+@pytest.mark.parametrize("dt", ["float32", "float64", "int32", "int8", "bfloat16"])
+@pytest.mark.parametrize("perm", list(itertools.permutations(range(3))))
+def test_transpose_bit_exact(dt, perm):
+    g = rng(6)
+    shape = (37, 70, 45)
+    if dt == "bfloat16":
+        x = f32_to_bf16_bits(g.standard_normal(shape).astype(np.float32))
+    elif dt.startswith("float"):
+        x = g.standard_normal(shape).astype(dt)
+    else:
+        x = g.integers(-100, 100, shape).astype(dt)
+    d = dev(x, dt)
+    t = d.transpose(perm)
+    out = DeviceArray.empty(t.shape, dt)
+    xg.assign(out, t)
+    np.testing.assert_array_equal(out.to_numpy(), np.ascontiguousarray(x.transpose(perm)))
+
+
+def test_transpose_with_elementwise_and_views():
+    g = rng(7)
+    x = g.standard_normal((64, 48)).astype(np.float32)
+    y = g.standard_normal((48,)).astype(np.float32)
+    dx, dy = dev(x), dev(y)
+    out = DeviceArray.empty((48, 64), "float32")
+    xg.assign(out, dx.transpose() * np.float32(2))
+    np.testing.assert_array_equal(out.to_numpy(), x.T * np.float32(2))
+    # strided views (steps, negative steps, offsets)
+    v = dx[1::3, ::-2]
+    o2 = DeviceArray.empty(v.shape, "float32")
+    xg.assign(o2, v + np.float32(1))
+    np.testing.assert_array_equal(o2.to_numpy(), x[1::3, ::-2] + np.float32(1))
+    # assignment into a strided destination view
+    big = DeviceArray.from_numpy(np.zeros((64, 48), np.float32))
+    dst = big[::2, 3:43]
+    xg.assign(dst, dx[::2, 3:43] * dx[::2, 3:43])
+    exp_ = np.zeros((64, 48), np.float32)
+    exp_[::2, 3:43] = x[::2, 3:43] * x[::2, 3:43]
+    np.testing.assert_array_equal(big.to_numpy(), exp_)
+
+
+def test_unaligned_and_odd_sizes():
+    g = rng(8)
+    for n in [1, 3, 5, 31, 33, 1023, 4097]:
+        a = g.standard_normal(n + 1).astype(np.float32)
+        d = dev(a)[1:]  # 4-byte offset: no 16-byte vectors
+        out = DeviceArray.empty((n,), "float32")
+        xg.assign(out, d * d + np.float32(1))
+        np.testing.assert_array_equal(out.to_numpy(), a[1:] * a[1:] + np.float32(1))
+
+
+def test_math_functions_ulp():
+    g = rng(9)
+    x = g.uniform(0.1, 4, (300,)).astype(np.float32)
+    for fn, name in [(xg.exp, "exp"), (xg.log, "log"), (xg.sin, "sin"), (xg.cos, "cos"), (xg.tanh, "tanh")]:
+        out = DeviceArray.empty(x.shape, "float32")
+        xg.assign(out, fn(dev(x)))
+        ref = O.assign(fn(H(x)))
+        assert_ulp(out.to_numpy(), ref, 4, name)
+    xd = x.astype(np.float64)
+    out = DeviceArray.empty(x.shape, "float64")
+    xg.assign(out, xg.exp(dev(xd)))
+    assert_ulp(out.to_numpy(), O.assign(xg.exp(H(xd))), 2, "exp f64")
+
+
+# ------------------------------------------------------------------------------- reductions
+SHAPES_AXES = [
+    ((7,), [None, [0]]),
+    ((3, 5), [None, [0], [1], [0, 1], []]),
+    ((4, 6, 8), [None, [0], [1], [2], [0, 2], [1, 2], [0, 1]]),
+    ((2, 3, 4, 5), [[1, 3], [0, 1, 3], [2], [0, 2, 3]]),
+    ((33, 65), [[0], [1]]),
+    ((1, 1000), [[1], None]),
+    ((1000, 3), [[0], [1]]),
+    ((5, 1, 7), [[1], [0, 2]]),
+]
+
+
+def _cases():
+    for shape, axes_list in SHAPES_AXES:
+        for axes in axes_list:
+            for kd in (False, True):
+                yield shape, axes, kd
+
+
+@pytest.mark.parametrize("shape,axes,kd", list(_cases()))
+@pytest.mark.parametrize("dt", ["int32", "uint8", "int64"])
+def test_integer_reductions_bit_exact(shape, axes, kd, dt):
+    g = rng(10)
+    x = g.integers(-20 if dt != "uint8" else 0, 20, shape).astype(dt)
+    for op in ["sum", "prod", "amax", "amin", "norm_l0", "norm_l1", "norm_sq"]:
+        if op == "prod" and np.prod(shape) > 40:
+            continue
+        got = ops.reduce(op, dev(x), axes, keep_dims=kd).to_numpy()
+        ref = O.reduce(op, H(x), axes, keep_dims=kd)
+        np.testing.assert_array_equal(got, ref, err_msg=f"{op} {shape} {axes} kd={kd}")
+    # sum<int64_t>
+    got = ops.reduce("sum", dev(x), axes, keep_dims=kd, acc_dtype="int64").to_numpy()
+    np.testing.assert_array_equal(got, O.reduce("sum", H(x), axes, keep_dims=kd, acc_dtype="int64"))
+    # mean of integers: integer sum then double division -> bit-exact too
+    got = ops.reduce("mean", dev(x), axes, keep_dims=kd).to_numpy()
+    np.testing.assert_array_equal(got, O.reduce("mean", H(x), axes, keep_dims=kd))
+
+
+@pytest.mark.parametrize("shape,axes,kd", list(_cases()))
+@pytest.mark.parametrize("dt", ["float32", "float64"])
+def test_float_reductions(shape, axes, kd, dt):
+    g = rng(11)
+    x = g.standard_normal(shape).astype(dt)
+    xd = x.astype(np.float64)
+    ax = None if axes is None else tuple(axes)
+    absx = np.abs(xd).sum(axis=ax, keepdims=kd) if axes != [] else np.abs(xd)
+    exact = xd.sum(axis=ax, keepdims=kd) if axes != [] else xd
+    rel = 1e-6 if dt == "float32" else 1e-13
+    got = ops.reduce("sum", dev(x), axes, keep_dims=kd).to_numpy()
+    ref = O.reduce("sum", H(x), axes, keep_dims=kd)
+    assert_close_rel(got, exact, rel, absx, "sum vs fp64")
+    env = np.abs(ref.astype(np.float64) - exact) + rel * absx
+    assert (np.abs(got - ref) <= env + 1e-300).all(), "sum outside the reference envelope"
+    for op in ["amax", "amin"]:
+        g_ = ops.reduce(op, dev(x), axes, keep_dims=kd).to_numpy()
+        r_ = O.reduce(op, H(x), axes, keep_dims=kd)
+        np.testing.assert_array_equal(g_, r_, err_msg=op)
+    n = int(np.prod([shape[a] for a in (range(len(shape)) if axes is None else axes)])) if axes != [] else 1
+    got = ops.reduce("mean", dev(x), axes, keep_dims=kd).to_numpy()
+    assert_close_rel(got, exact / n, rel, absx / n, "mean")
+    if n > 1:
+        for ddof in (0, 1):
+            vg = ops.reduce("variance", dev(x), axes, keep_dims=kd, ddof=ddof).to_numpy()
+            vr = O.reduce("variance", H(x), axes, keep_dims=kd, ddof=ddof)
+            assert_close_rel(vg, vr, 1e-6 if dt == "float32" else 1e-12, None, f"variance ddof={ddof}")
+        sg = ops.reduce("stddev", dev(x), axes, keep_dims=kd).to_numpy()
+        sr = O.reduce("stddev", H(x), axes, keep_dims=kd)
+        assert_close_rel(sg, sr, 1e-6 if dt == "float32" else 1e-12, None, "stddev")
+    ng = ops.reduce("norm_l2", dev(x), axes, keep_dims=kd).to_numpy()
+    nr = O.reduce("norm_l2", H(x), axes, keep_dims=kd)
+    assert_close_rel(ng, nr, 1e-6 if dt == "float32" else 1e-13, None, "norm_l2")
+
+
+def test_reduction_of_expression_and_initial():
+    g = rng(12)
+    A = g.uniform(-1, 1, (40, 300)).astype(np.float32)
+    b = g.standard_normal(300).astype(np.float32)
+    e_d = dev(A) * dev(b) + xg.exp(-dev(A) * dev(A))
+    got = ops.reduce("sum", e_d, [1]).to_numpy()
+    E = O.assign(H(A) * H(b) + xg.exp(-H(A) * H(A)))
+    exact = E.astype(np.float64).sum(1)
+    assert_close_rel(got, exact, 1e-6, np.abs(E.astype(np.float64)).sum(1), "fused sum(E,{1})")
+    x = np.arange(5 * 5 * 5 * 5, dtype=np.float64).reshape(5, 5, 5, 5)
+    r = ops.reduce("sum", dev(x), [0, 2], keep_dims=True, initial=5.0).to_numpy()
+    np.testing.assert_array_equal(r, x.sum(axis=(0, 2), keepdims=True) + 5)
+    r = ops.reduce("prod", dev(x), [1, 2], keep_dims=True, initial=0.0).to_numpy()
+    assert (r == 0).all()
+
+
+def test_reduction_errors_and_edge_cases():
+    a = dev(np.array([[1, 2, 3], [4, 5, 6]], np.int32))
+    for axes in ([1, 0], [0, 0], [0, 2]):
+        with pytest.raises(xg.XtgError) as ei:
+            ops.reduce("sum", a, axes)
+        assert ei.value.status == 3
+    assert ops.reduce("sum", a, [-1]).to_numpy().tolist() == [6, 15]
+    # zero shape
+    z = dev(np.zeros((0, 1), np.int32))
+    r0 = ops.reduce("sum", z, [0], keep_dims=True).to_numpy()
+    assert r0.shape == (1, 1) and r0[0, 0] == 0
+    r1 = ops.reduce("sum", z, [1], keep_dims=True).to_numpy()
+    assert r1.shape == (0, 1)
+    # empty array -> NaN mean
+    e = dev(np.ones((1, 2, 0, 1), np.float64))
+    assert np.isnan(ops.reduce("mean", e).to_numpy())
+    r2 = ops.reduce("mean", e, [2]).to_numpy()
+    assert r2.shape == (1, 2, 1) and np.isnan(r2).all()
+    # uint8 sum does not overflow (result type int)
+    c = dev(np.ones(1000, np.uint8))
+    assert int(ops.reduce("sum", c).to_numpy()) == 1000
+
+
+def test_signed_zero_and_inf_selection():
+    x = np.array([[0.0, -0.0, -0.0], [-0.0, 0.0, -np.inf]], np.float32)
+    for axes in ([1], [0], None):
+        for op in ("amax", "amin"):
+            got = ops.reduce(op, dev(x), axes).to_numpy()
+            ref = O.reduce(op, H(x), axes)
+            np.testing.assert_array_equal(np.signbit(got), np.signbit(ref))
+            np.testing.assert_array_equal(got, ref)
+    y = np.full((4,), -np.inf, np.float32)
+    assert ops.reduce("amax", dev(y)).to_numpy() == O.reduce("amax", H(y))
+
+
+# ------------------------------------------------------------------------------- arg
+@pytest.mark.parametrize("dt", ["float32", "float64", "int32"])
+def test_argmax_argmin(dt):
+    g = rng(13)
+    x = g.integers(-3, 4, (6, 37, 29)).astype(dt)  # many ties
+    for op in ("argmax", "argmin"):
+        for axis in (None, 0, 1, 2, -1):
+            got = ops.argreduce(op, dev(x), axis).to_numpy()
+            ref = O.argreduce(op, H(x), axis)
+            np.testing.assert_array_equal(got, ref, err_msg=f"{op} axis={axis}")
+    got = ops.argreduce("argmax", dev(x), 1, out_dtype="int32").to_numpy()
+    np.testing.assert_array_equal(got, O.argreduce("argmax", H(x), 1).astype(np.int32))
+
+
+def test_argmax_nan_rules():
+    x = np.array([[np.nan, 1, 2], [1, np.nan, 3], [2, 2, np.nan]], np.float32)
+    for axis in (0, 1, None):
+        for op in ("argmax", "argmin"):
+            np.testing.assert_array_equal(ops.argreduce(op, dev(x), axis).to_numpy(), O.argreduce(op, H(x), axis))
+
+
+def test_reference_argmax_kats():
+    a = np.array([[5, 3, 1], [4, 4, 4]], np.float64)
+    assert ops.argreduce("argmax", dev(a)).to_numpy() == 0
+    np.testing.assert_array_equal(ops.argreduce("argmax", dev(a), 0).to_numpy(), [0, 1, 1])
+    np.testing.assert_array_equal(ops.argreduce("argmax", dev(a), 1).to_numpy(), [0, 0])
+    np.testing.assert_array_equal(ops.argreduce("argmin", dev(a), 0).to_numpy(), [1, 0, 0])
+    np.testing.assert_array_equal(ops.argreduce("argmin", dev(a), 1).to_numpy(), [2, 0])
+    c = np.array([[[1, 2, 3, 4]], [[4, 3, 2, 1]]], np.int32)
+    np.testing.assert_array_equal(ops.argreduce("argmax", dev(c), 2).to_numpy(), [[3], [0]])
+    np.testing.assert_array_equal(ops.argreduce("argmax", dev(c), 0).to_numpy(), [[1, 1, 0, 0]])
+
+
+# ------------------------------------------------------------------------------- fused rows
+@pytest.mark.parametrize("dt,rel", [("float32", 1e-6), ("float64", 1e-12)])
+@pytest.mark.parametrize("shape", [(8, 16, 1024), (5, 3, 100), (4, 2048), (3, 5000)])
+def test_row_normalize(dt, rel, shape):
+    g = rng(14)
+    x = g.standard_normal(shape).astype(dt)
+    d = dev(x)
+    out = DeviceArray.empty(shape, dt)
+    xg.assign(out, (d - xg.rmean(d)) / xg.sqrt(xg.rvar(d) + 1e-5))
+    xd = x.astype(np.float64)
+    m = xd.mean(-1, keepdims=True)
+    s = np.sqrt(xd.var(-1, keepdims=True) + 1e-5)
+    exact = (xd - m) / s
+    got = out.to_numpy().astype(np.float64)
+    scale = (np.abs(xd) + np.abs(m)) / s
+    assert_close_rel(got, exact, 4 * rel if dt == "float32" else rel, scale, "normalize")
+    # the oracle follows the reference (float32 sequential row sums), so it
+    # carries its own error: the GPU must sit inside that envelope
+    hx = H(x)
+    ref = O.assign((hx - xg.rmean(hx)) / xg.sqrt(xg.rvar(hx) + 1e-5), dtype=dt).astype(np.float64)
+    env = np.abs(ref - exact) + (4 * rel if dt == "float32" else rel) * scale
+    assert (np.abs(got - ref) <= env).all(), "normalize outside the reference envelope"
+
+
+def test_row_stats_other_modes():
+    g = rng(15)
+    x = g.standard_normal((6, 7, 33)).astype(np.float32)
+    d = dev(x)
+    for fn, ref in [(lambda v: v - xg.ramax(v), lambda v: v - v.max(-1, keepdims=True)),
+                    (lambda v: v / xg.rsum(v, 2), lambda v: v / v.astype(np.float64).sum((-2, -1), keepdims=True)),
+                    (lambda v: xg.rstd(v, 1, 1) * 1, lambda v: np.broadcast_to(v.astype(np.float64).std(-1, ddof=1, keepdims=True), v.shape))]:
+        out = DeviceArray.empty(x.shape, "float32")
+        xg.assign(out, fn(d))
+        r = ref(x)
+        assert_close_rel(out.to_numpy(), r, 1e-5, np.abs(r) + 1e-3, "row stat")

@@ -1,0 +1,1244 @@
+// xtg_device.cuh — device side of the GB300 evaluator.
+//
+// This header is compiled two ways: by NVRTC (its text is embedded into
+// libxtg.so; every expression tree is instantiated against it at first use,
+// for sm_103a) and by nvcc (translation units that instantiate kernels ahead
+// of time).  It uses no standard-library header so that NVRTC needs no
+// include path.
+//
+// An expression tree is a C++ *type*: e.g. C0's `A*b + exp(-A*A)` becomes
+//   Add<float, Mul<float, L<0,float>, L<1,float>>,
+//              Exp<float, Neg<float, Mul<float, L<0,float>, L<0,float>>>>>
+// — the lowered form of xtensor's xfunction<F, CT...>
+// (include/xtensor/core/xfunction.hpp:203-375).  Each leaf is loaded once per
+// element into registers (LeafSet), then the tree is evaluated as a pure
+// function of those registers.  Broadcasting is stride-0 arithmetic in the
+// per-leaf offset computation, which is what xtensor's steppers do with their
+// `offset` / zero strides (include/xtensor/core/xiterator.hpp:488-497,
+// include/xtensor/core/xstrides.hpp:570-581).
+#pragma once
+
+#ifndef XTG_DEVICE_CUH
+#define XTG_DEVICE_CUH
+
+#define XTG_DI __device__ __forceinline__
+
+#include "xtg_params.h"
+
+namespace xtg {
+
+
+// ---------------------------------------------------------------------------
+// bfloat16 storage type.  Conversions are written from the format definition:
+// bf16 is the top 16 bits of an IEEE binary32; float -> bf16 rounds to
+// nearest-even on the dropped 16 bits, NaN stays a quiet NaN.
+struct bf16 {
+    unsigned short bits;
+    bf16() = default;  // trivial: bf16 lives in unions and shared memory
+    XTG_DI bf16(float f) {
+        u32 u = __float_as_uint(f);
+        if ((u & 0x7fffffffu) > 0x7f800000u) {
+            bits = (unsigned short)((u >> 16) | 0x40u);
+        } else {
+            u32 lsb = (u >> 16) & 1u;
+            u += 0x7fffu + lsb;
+            bits = (unsigned short)(u >> 16);
+        }
+    }
+    XTG_DI bf16(double d) : bf16((float)d) {}
+    XTG_DI bf16(int v) : bf16((float)v) {}
+    XTG_DI bf16(long long v) : bf16((float)v) {}
+    XTG_DI bf16(unsigned int v) : bf16((float)v) {}
+    XTG_DI bf16(unsigned long long v) : bf16((float)v) {}
+    XTG_DI operator float() const { return __uint_as_float(((u32)bits) << 16); }
+};
+
+// ---------------------------------------------------------------------------
+// Conversions: C++ static_cast semantics for arithmetic types, bf16 via float.
+template <class To> struct Cvt {
+    template <class From> static XTG_DI To go(From v) { return (To)v; }
+    static XTG_DI To go(bf16 v) { return (To)(float)v; }
+};
+template <> struct Cvt<bf16> {
+    template <class From> static XTG_DI bf16 go(From v) { return bf16((float)v); }
+    static XTG_DI bf16 go(double v) { return bf16((float)v); }
+    static XTG_DI bf16 go(bf16 v) { return v; }
+};
+template <> struct Cvt<bool> {
+    template <class From> static XTG_DI bool go(From v) { return v != From(0); }
+    static XTG_DI bool go(bf16 v) { return (float)v != 0.f; }
+    static XTG_DI bool go(bool v) { return v; }
+};
+template <class To, class From> XTG_DI To cvt(From v) { return Cvt<To>::go(v); }
+
+// Numeric limits needed for reducer initial values (amax/amin use lowest()/max()).
+template <class T> struct Lim;
+template <> struct Lim<bool> { static XTG_DI bool lowest() { return false; } static XTG_DI bool maxv() { return true; } };
+template <> struct Lim<signed char> { static XTG_DI signed char lowest() { return -128; } static XTG_DI signed char maxv() { return 127; } };
+template <> struct Lim<unsigned char> { static XTG_DI unsigned char lowest() { return 0; } static XTG_DI unsigned char maxv() { return 255; } };
+template <> struct Lim<short> { static XTG_DI short lowest() { return -32768; } static XTG_DI short maxv() { return 32767; } };
+template <> struct Lim<unsigned short> { static XTG_DI unsigned short lowest() { return 0; } static XTG_DI unsigned short maxv() { return 65535; } };
+template <> struct Lim<int> { static XTG_DI int lowest() { return (-2147483647 - 1); } static XTG_DI int maxv() { return 2147483647; } };
+template <> struct Lim<unsigned int> { static XTG_DI unsigned int lowest() { return 0u; } static XTG_DI unsigned int maxv() { return 4294967295u; } };
+template <> struct Lim<long long> { static XTG_DI long long lowest() { return (-9223372036854775807LL - 1); } static XTG_DI long long maxv() { return 9223372036854775807LL; } };
+template <> struct Lim<unsigned long long> { static XTG_DI unsigned long long lowest() { return 0ull; } static XTG_DI unsigned long long maxv() { return 18446744073709551615ull; } };
+template <> struct Lim<float> { static XTG_DI float lowest() { return -3.40282346638528859812e+38f; } static XTG_DI float maxv() { return 3.40282346638528859812e+38f; } };
+template <> struct Lim<double> { static XTG_DI double lowest() { return -1.7976931348623157e+308; } static XTG_DI double maxv() { return 1.7976931348623157e+308; } };
+
+template <class T> struct IsFloat { enum { value = 0 }; };
+template <> struct IsFloat<float> { enum { value = 1 }; };
+template <> struct IsFloat<double> { enum { value = 1 }; };
+template <> struct IsFloat<bf16> { enum { value = 1 }; };
+
+// ---------------------------------------------------------------------------
+// Fast unsigned 32-bit division by a run-time invariant divisor, by the
+// round-up multiply-and-shift method of Granlund & Montgomery (PLDI 1994):
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (mulhi(m, n) + n) >> l, exact for all n < 2^32.
+XTG_DI u32 fdiv(u32 n, const FastDiv& f) {
+    u32 t = __umulhi(f.m, n);
+    return (u32)(((u64)t + n) >> f.l);
+}
+
+// ---------------------------------------------------------------------------
+// Kernel parameter blocks.  Strides/shapes are in elements; offsets 64-bit.
+template <class T> XTG_DI T scalar_as(const Scalars& s, int k);
+template <> XTG_DI float scalar_as<float>(const Scalars& s, int k) { return (float)__longlong_as_double((i64)s.v[k]); }
+template <> XTG_DI double scalar_as<double>(const Scalars& s, int k) { return __longlong_as_double((i64)s.v[k]); }
+template <> XTG_DI bf16 scalar_as<bf16>(const Scalars& s, int k) { return bf16((float)__longlong_as_double((i64)s.v[k])); }
+template <> XTG_DI bool scalar_as<bool>(const Scalars& s, int k) { return s.v[k] != 0; }
+template <> XTG_DI signed char scalar_as<signed char>(const Scalars& s, int k) { return (signed char)(i64)s.v[k]; }
+template <> XTG_DI unsigned char scalar_as<unsigned char>(const Scalars& s, int k) { return (unsigned char)s.v[k]; }
+template <> XTG_DI short scalar_as<short>(const Scalars& s, int k) { return (short)(i64)s.v[k]; }
+template <> XTG_DI unsigned short scalar_as<unsigned short>(const Scalars& s, int k) { return (unsigned short)s.v[k]; }
+template <> XTG_DI int scalar_as<int>(const Scalars& s, int k) { return (int)(i64)s.v[k]; }
+template <> XTG_DI unsigned int scalar_as<unsigned int>(const Scalars& s, int k) { return (unsigned int)s.v[k]; }
+template <> XTG_DI long long scalar_as<long long>(const Scalars& s, int k) { return (i64)s.v[k]; }
+template <> XTG_DI unsigned long long scalar_as<unsigned long long>(const Scalars& s, int k) { return s.v[k]; }
+
+// Decode a flat vector index into a multi-index (innermost in elements).
+template <int R, int VEC, bool BIG>
+XTG_DI void decode(const Space& sp, i64 q, i64 (&idx)[R]) {
+    if (BIG) {
+#pragma unroll
+        for (int d = R - 1; d >= 0; --d) {
+            i64 n = sp.shape[d];
+            i64 qq = q / n;
+            idx[d] = q - qq * n;
+            q = qq;
+        }
+    } else {
+        u32 qu = (u32)q;
+#pragma unroll
+        for (int d = R - 1; d >= 0; --d) {
+            if (d == 0) {
+                idx[0] = qu;
+            } else {
+                u32 qq = fdiv(qu, sp.fd[d]);
+                idx[d] = qu - qq * sp.fd[d].d;
+                qu = qq;
+            }
+        }
+    }
+    idx[R - 1] *= VEC;
+}
+
+template <int R>
+XTG_DI i64 dot_idx(const i64 (&idx)[R], const i64* st) {
+    i64 o = 0;
+#pragma unroll
+    for (int d = 0; d < R; ++d) o += idx[d] * st[d];
+    return o;
+}
+
+// ---------------------------------------------------------------------------
+// Vector memory access.  VEC elements of T at p (p aligned to VEC*sizeof(T)
+// when KIND == CONTIG, which the host checks before choosing VEC > 1).
+enum { K_CONTIG = 0, K_BCAST = 1, K_STRIDED = 2 };
+
+template <int BYTES> struct VecT;
+template <> struct VecT<16> { typedef uint4 t; };
+template <> struct VecT<8> { typedef uint2 t; };
+template <> struct VecT<4> { typedef unsigned int t; };
+template <> struct VecT<2> { typedef unsigned short t; };
+template <> struct VecT<1> { typedef unsigned char t; };
+
+template <class T, int VEC>
+XTG_DI void ld_contig(T (&dst)[VEC], const T* p) {
+    const int B = (int)sizeof(T) * VEC;
+    if (B == 16 || B == 8 || B == 4 || B == 2) {
+        typedef typename VecT<(B > 16 ? 16 : B)>::t V;
+        union { V v; T e[VEC]; } u;
+        u.v = __ldg(reinterpret_cast<const V*>(p));
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dst[j] = u.e[j];
+    } else if (B == 32) {
+        union { uint4 v[2]; T e[VEC]; } u;
+        u.v[0] = __ldg(reinterpret_cast<const uint4*>(p));
+        u.v[1] = __ldg(reinterpret_cast<const uint4*>(p) + 1);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dst[j] = u.e[j];
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dst[j] = p[j];
+    }
+}
+// bool / bf16 / 1-byte types: __ldg has no overload for them, route via bytes.
+template <class T> XTG_DI T ld1(const T* p) { return *p; }
+template <> XTG_DI float ld1<float>(const float* p) { return __ldg(p); }
+template <> XTG_DI double ld1<double>(const double* p) { return __ldg(p); }
+template <> XTG_DI int ld1<int>(const int* p) { return __ldg(p); }
+template <> XTG_DI long long ld1<long long>(const long long* p) { return __ldg(p); }
+
+template <class T, int KIND, int VEC>
+XTG_DI void ld_leaf(T (&dst)[VEC], const T* base, i64 off, i64 inner_stride) {
+    if (KIND == K_CONTIG) {
+        ld_contig<T, VEC>(dst, base + off);
+    } else if (KIND == K_BCAST) {
+        T v = ld1<T>(base + off);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dst[j] = v;
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dst[j] = ld1<T>(base + off + (i64)j * inner_stride);
+    }
+}
+
+template <class T, int KIND, int VEC>
+XTG_DI void st_out(T* base, i64 off, i64 inner_stride, const T (&v)[VEC]) {
+    const int B = (int)sizeof(T) * VEC;
+    if (KIND == K_CONTIG && (B == 16 || B == 8 || B == 4 || B == 2)) {
+        typedef typename VecT<(B > 16 ? 16 : B)>::t V;
+        union { V v; T e[VEC]; } u;
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) u.e[j] = v[j];
+        *reinterpret_cast<V*>(base + off) = u.v;
+    } else if (KIND == K_CONTIG && B == 32) {
+        union { uint4 v[2]; T e[VEC]; } u;
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) u.e[j] = v[j];
+        reinterpret_cast<uint4*>(base + off)[0] = u.v[0];
+        reinterpret_cast<uint4*>(base + off)[1] = u.v[1];
+    } else if (KIND == K_CONTIG) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) base[off + j] = v[j];
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) base[off + (i64)j * inner_stride] = v[j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Leaf sets: a compile-time list of (type, access kind) and the register
+// storage for VEC values of each.
+template <class T, int KIND> struct LeafSpec {
+    typedef T type;
+    enum { kind = KIND };
+};
+
+template <int VEC, class... S> struct Regs;
+template <int VEC> struct Regs<VEC> {};
+template <int VEC, class S0, class... S> struct Regs<VEC, S0, S...> {
+    typedef typename S0::type elem0;
+    typename S0::type v[VEC];
+    Regs<VEC, S...> rest;
+};
+template <int I> struct RegAt {
+    template <class R> static XTG_DI auto& get(R& r) { return RegAt<I - 1>::get(r.rest); }
+    template <class R> static XTG_DI const auto& cget(const R& r) { return RegAt<I - 1>::cget(r.rest); }
+};
+template <> struct RegAt<0> {
+    template <class R> static XTG_DI auto& get(R& r) { return r.v; }
+    template <class R> static XTG_DI const auto& cget(const R& r) { return r.v; }
+};
+
+template <class... S> struct LeafSet {
+    enum { N = sizeof...(S) };
+    template <int VEC> struct R { typedef Regs<VEC, S...> type; };
+};
+
+// Load all leaves for one vector position; offsets from a multi-index.
+template <int I, int VEC, int R, class... S> struct LoadAll;
+template <int I, int VEC, int R> struct LoadAll<I, VEC, R> {
+    template <class RG> static XTG_DI void run(RG&, const void* const*, const i64 (*)[XTG_KMAX_RANK], const i64 (&)[R]) {}
+};
+template <int I, int VEC, int R, class S0, class... S> struct LoadAll<I, VEC, R, S0, S...> {
+    template <class RG>
+    static XTG_DI void run(RG& rg, const void* const* ptr, const i64 (*st)[XTG_KMAX_RANK], const i64 (&idx)[R]) {
+        typedef typename S0::type T;
+        i64 off = dot_idx<R>(idx, st[I]);
+        ld_leaf<T, S0::kind, VEC>(rg.v, reinterpret_cast<const T*>(ptr[I]), off, st[I][R - 1]);
+        LoadAll<I + 1, VEC, R, S...>::run(rg.rest, ptr, st, idx);
+    }
+};
+template <class LS> struct LoadLeaves;
+template <class... S> struct LoadLeaves<LeafSet<S...>> {
+    template <int VEC, int R, class RG>
+    static XTG_DI void run(RG& rg, const void* const* ptr, const i64 (*st)[XTG_KMAX_RANK], const i64 (&idx)[R]) {
+        LoadAll<0, VEC, R, S...>::run(rg, ptr, st, idx);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Evaluation context: scalar immediates plus row statistics (for the fused
+// row kernels).  Nodes evaluate at vector lane j.
+template <int NSTAT> struct Ctx {
+    const Scalars* scal;
+    double stat[NSTAT > 0 ? NSTAT : 1];
+};
+
+// Leaves / scalars / row statistics as tree terminals.
+template <int I, class T> struct L {
+    typedef T type;
+    template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C&) { return RegAt<I>::cget(r)[j]; }
+};
+template <int K, class T> struct S {
+    typedef T type;
+    template <class RG, class C> static XTG_DI T ev(const RG&, int, const C& c) { return scalar_as<T>(*c.scal, K); }
+};
+// A row statistic produced by a fused row reducer (index K of Ctx::stat).
+template <int K, class T> struct Stat {
+    typedef T type;
+    template <class RG, class C> static XTG_DI T ev(const RG&, int, const C& c) { return (T)c.stat[K]; }
+};
+
+// Unary functors (include/xtensor/core/xoperation.hpp:104-125,
+// include/xtensor/core/xmath.hpp:295-341, 1101-1108).
+#define XTG_UNARY(NAME, EXPR)                                                              \
+    template <class T, class A> struct NAME {                                              \
+        typedef T type;                                                                    \
+        template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C& c) {   \
+            typedef typename A::type TA;                                                   \
+            T a = cvt<T>(A::ev(r, j, c));                                                  \
+            (void)sizeof(TA);                                                              \
+            return EXPR;                                                                   \
+        }                                                                                  \
+    };
+XTG_UNARY(Neg, (T)(-a))
+XTG_UNARY(Pos, (T)(+a))
+XTG_UNARY(Square, (T)(a * a))
+XTG_UNARY(LogicalNot, (T)(!a))
+XTG_UNARY(BitNot, (T)(~a))
+XTG_UNARY(Cast, a)
+#undef XTG_UNARY
+
+// Math functions: float overloads call the single-precision CUDA functions,
+// double overloads the double ones (std::exp(float) vs std::exp(double)).
+XTG_DI float m_exp(float x) { return expf(x); }
+XTG_DI double m_exp(double x) { return exp(x); }
+XTG_DI float m_log(float x) { return logf(x); }
+XTG_DI double m_log(double x) { return log(x); }
+XTG_DI float m_sqrt(float x) { return sqrtf(x); }
+XTG_DI double m_sqrt(double x) { return sqrt(x); }
+XTG_DI float m_sin(float x) { return sinf(x); }
+XTG_DI double m_sin(double x) { return sin(x); }
+XTG_DI float m_cos(float x) { return cosf(x); }
+XTG_DI double m_cos(double x) { return cos(x); }
+XTG_DI float m_tanh(float x) { return tanhf(x); }
+XTG_DI double m_tanh(double x) { return tanh(x); }
+XTG_DI float m_pow(float x, float y) { return powf(x, y); }
+XTG_DI double m_pow(double x, double y) { return pow(x, y); }
+template <class T> XTG_DI T m_abs(T x) { return x < T(0) ? T(-x) : x; }
+XTG_DI float m_abs(float x) { return fabsf(x); }
+XTG_DI double m_abs(double x) { return fabs(x); }
+
+#define XTG_MATH1(NAME, FN)                                                               \
+    template <class T, class A> struct NAME {                                             \
+        typedef T type;                                                                   \
+        template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C& c) {  \
+            return FN(cvt<T>(A::ev(r, j, c)));                                            \
+        }                                                                                 \
+    };
+XTG_MATH1(Exp, m_exp)
+XTG_MATH1(Log, m_log)
+XTG_MATH1(Sqrt, m_sqrt)
+XTG_MATH1(Abs, m_abs)
+XTG_MATH1(Sin, m_sin)
+XTG_MATH1(Cos, m_cos)
+XTG_MATH1(Tanh, m_tanh)
+#undef XTG_MATH1
+
+// Binary arithmetic: operands converted to the node type T (the C++ common
+// type the host computed), then the operator applied.
+#define XTG_BINARY(NAME, EXPR)                                                            \
+    template <class T, class A, class B> struct NAME {                                    \
+        typedef T type;                                                                   \
+        template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C& c) {  \
+            T a = cvt<T>(A::ev(r, j, c));                                                 \
+            T b = cvt<T>(B::ev(r, j, c));                                                 \
+            return EXPR;                                                                  \
+        }                                                                                 \
+    };
+XTG_BINARY(Add, (T)(a + b))
+XTG_BINARY(Sub, (T)(a - b))
+XTG_BINARY(Mul, (T)(a * b))
+XTG_BINARY(Div, (T)(a / b))
+XTG_BINARY(Mod, (T)(a % b))
+XTG_BINARY(BitAnd, (T)(a & b))
+XTG_BINARY(BitOr, (T)(a | b))
+XTG_BINARY(BitXor, (T)(a ^ b))
+XTG_BINARY(Pow, m_pow(a, b))
+// maximum/minimum keep the reference's select order: select(t1 > t2, t1, t2)
+// (include/xtensor/core/xmath.hpp:589-602).
+XTG_BINARY(Maximum, (a > b ? a : b))
+XTG_BINARY(Minimum, (a < b ? a : b))
+#undef XTG_BINARY
+
+// Comparisons and logical ops: computed in the common type CT, result bool.
+#define XTG_CMP(NAME, OP)                                                                 \
+    template <class CT, class A, class B> struct NAME {                                   \
+        typedef bool type;                                                                \
+        template <class RG, class C> static XTG_DI bool ev(const RG& r, int j, const C& c) { \
+            CT a = cvt<CT>(A::ev(r, j, c));                                               \
+            CT b = cvt<CT>(B::ev(r, j, c));                                               \
+            return a OP b;                                                                \
+        }                                                                                 \
+    };
+XTG_CMP(Lt, <)
+XTG_CMP(Le, <=)
+XTG_CMP(Gt, >)
+XTG_CMP(Ge, >=)
+XTG_CMP(Eq, ==)
+XTG_CMP(Ne, !=)
+XTG_CMP(LogicalAnd, &&)
+XTG_CMP(LogicalOr, ||)
+#undef XTG_CMP
+
+template <class T, class Cd, class A, class B> struct Where {
+    typedef T type;
+    template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C& c) {
+        return cvt<bool>(Cd::ev(r, j, c)) ? cvt<T>(A::ev(r, j, c)) : cvt<T>(B::ev(r, j, c));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// K1: fused elementwise assignment  out[i] = Tree(leaves at i)
+// Replaces linear_assigner / strided_loop_assigner / stepper_assigner
+// (include/xtensor/core/xassign.hpp:644-695, 701-849, 855-1358) for any
+// destination and leaf strides.  Grid-stride over vectors of VEC elements;
+// each thread keeps U independent vectors in flight (U * leaves * 16 B of
+// loads outstanding) so that HBM latency is hidden with few CTAs per SM.
+template <class Tree, class LS, class OutT, int OUTKIND, int VEC, int R, int U, bool BIG>
+__global__ void __launch_bounds__(256) k_assign(const AssignParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    Ctx<0> c;
+    c.scal = &p.scal;
+    const i64 step = (i64)gridDim.x * blockDim.x * U;
+    for (i64 base = (i64)blockIdx.x * blockDim.x * U + threadIdx.x; base < p.sp.nvec; base += step) {
+        RG rg[U];
+        i64 ooff[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            i64 q = base + (i64)u * blockDim.x;
+            if (q < p.sp.nvec) {
+                i64 idx[R];
+                decode<R, VEC, BIG>(p.sp, q, idx);
+                LoadLeaves<LS>::template run<VEC, R>(rg[u], p.leaf, p.leaf_strides, idx);
+                ooff[u] = dot_idx<R>(idx, p.out_strides);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            i64 q = base + (i64)u * blockDim.x;
+            if (q < p.sp.nvec) {
+                OutT v[VEC];
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) v[j] = cvt<OutT>(Tree::ev(rg[u], j, c));
+                st_out<OutT, OUTKIND, VEC>(reinterpret_cast<OutT*>(p.out), ooff[u], p.out_strides[R - 1], v);
+            }
+        }
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Generic warp shuffle of a POD accumulator (word by word).
+template <class A> XTG_DI A shfl_xor_pod(const A& a, int m) {
+    union U { A a; u32 w[(sizeof(A) + 3) / 4]; };
+    U in, out;
+    in.a = a;
+#pragma unroll
+    for (int i = 0; i < (int)((sizeof(A) + 3) / 4); ++i) out.w[i] = __shfl_xor_sync(0xffffffffu, in.w[i], m);
+    return out.a;
+}
+
+// Deterministic group reduction: warp butterfly, then warp 0 folds the
+// per-warp results in warp order.  Result valid in thread 0 of the group
+// (GROUP == 32: lane 0 of the warp; GROUP == block: thread 0).
+template <int GROUP, class A> XTG_DI A group_reduce(A a, A* smem) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+        A o = shfl_xor_pod(a, m);
+        a.merge(o);
+    }
+    if (GROUP <= 32) return a;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) smem[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        A r = smem[0];
+        for (int w = 1; w < nw; ++w) r.merge(smem[w]);
+        a = r;
+    }
+    return a;
+}
+
+// Knuth's TwoSum: s = fl(a + b), e = (a + b) - s exactly.
+XTG_DI void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// ---------------------------------------------------------------------------
+// Reduction accumulators.  Each is POD: init(p), add(x, pos), merge(other),
+// and result<Out>(p).  `pos` is the element's row-major position inside the
+// reduced index space; only the selection reducers use it.
+
+// Plain accumulation in the accumulator type A (integers: exact modulo 2^n,
+// so any order gives the reference's result bit for bit; float64: FP64).
+// OP 0 = plus, 1 = multiplies (XTENSOR_REDUCER_FUNCTION sum / prod,
+// include/xtensor/core/xmath.hpp:1803,1823).
+template <class A, int OP> struct AccPlain {
+    A s;
+    XTG_DI void init(const RedParams& p);
+    template <class X> XTG_DI void add(X x, i64) {
+        if (OP == 0) s = (A)(s + cvt<A>(x)); else s = (A)(s * cvt<A>(x));
+    }
+    XTG_DI void merge(const AccPlain& o) {
+        if (OP == 0) s = (A)(s + o.s); else s = (A)(s * o.s);
+    }
+    XTG_DI double dval() const { return (double)s; }
+};
+
+// float32 compensated sum: (hi, lo) double-float accumulation with TwoSum at
+// every add and every merge, so the compensation survives the warp, block and
+// grid combines.
+struct AccSumC {
+    float hi, lo;
+    XTG_DI void init(const RedParams& p);
+    template <class X> XTG_DI void add(X x, i64) {
+        float v = cvt<float>(x), s, e;
+        two_sum(hi, v, s, e);
+        hi = s;
+        lo += e;
+    }
+    XTG_DI void addf(float v) {
+        float s, e;
+        two_sum(hi, v, s, e);
+        hi = s;
+        lo += e;
+    }
+    XTG_DI void merge(const AccSumC& o) {
+        float s, e;
+        two_sum(hi, o.hi, s, e);
+        hi = s;
+        lo = (lo + o.lo) + e;
+    }
+    XTG_DI double dval() const { return (double)hi + (double)lo; }
+};
+
+// Selection reducers amax / amin: the reference folds f(acc, x) =
+// acc > x ? acc : x (include/xtensor/core/xmath.hpp:589-602, 777-811) from
+// lowest()/max(), so among equal values the LAST one visited wins (this is
+// visible for +0/-0).  The position makes that rule order-independent.
+template <class A, int MAXOP> struct AccSel {
+    A v;
+    i64 pos;
+    XTG_DI void init(const RedParams& p);
+    template <class X> XTG_DI void add(X x, i64 ps) {
+        A a = cvt<A>(x);
+        bool keep = MAXOP ? (v > a) : (v < a);
+        if (!keep) { v = a; pos = ps; }
+    }
+    XTG_DI void merge(const AccSel& o) {
+        bool take;
+        if (MAXOP) take = (o.v > v) || (!(v > o.v) && o.pos > pos);
+        else take = (o.v < v) || (!(v < o.v) && o.pos > pos);
+        if (take) { v = o.v; pos = o.pos; }
+    }
+    XTG_DI double dval() const { return (double)v; }
+};
+
+// Moments for mean / variance / stddev.  Data are shifted by k (the first
+// element of the output's reduction set), then sum(d) and sum(d*d) are
+// accumulated — in double-float for float32/bf16 data (TwoSum + exact
+// products by fma), in FP64 for float64 data; partial states from different
+// blocks combine in FP64.  MODE 0 = mean (k = 0, no second moment),
+// 1 = variance, 2 = stddev.
+template <class C, int MODE> struct AccMom;
+template <int MODE> struct AccMom<float, MODE> {
+    float k;
+    AccSumC s1, s2;
+    XTG_DI void init(const RedParams& p);
+    template <class X> XTG_DI void add(X x, i64) {
+        float d = cvt<float>(x) - k;
+        s1.addf(d);
+        if (MODE != 0) {
+            float q = d * d;
+            float qe = fmaf(d, d, -q);
+            s2.addf(q);
+            s2.lo += qe;
+        }
+    }
+    XTG_DI void merge(const AccMom& o) { s1.merge(o.s1); if (MODE != 0) s2.merge(o.s2); }
+};
+template <int MODE> struct AccMom<double, MODE> {
+    double k, s1, s2;
+    XTG_DI void init(const RedParams& p);
+    template <class X> XTG_DI void add(X x, i64) {
+        double d = cvt<double>(x) - k;
+        s1 += d;
+        if (MODE != 0) s2 = fma(d, d, s2);
+    }
+    XTG_DI void merge(const AccMom& o) { s1 += o.s1; s2 += o.s2; }
+};
+
+// Norms (include/xtensor/reducers/xnorm.hpp:397-437): accumulate in the
+// big-promoted type.  NK 0 = l0 (count of non-zeros), 1 = l1 (sum |x|),
+// 2 = sq (sum x*x), 3 = linf (max |x| from 0, std::max then math::maximum).
+template <class A, int NK> struct AccNorm {
+    A s;
+    XTG_DI void init(const RedParams&) { s = A(0); }
+    template <class X> XTG_DI void add(X x, i64) {
+        if (NK == 0) s = s + (A)(x != X(0) ? 1 : 0);
+        else if (NK == 1) s = s + (A)m_abs(x);
+        else if (NK == 2) s = s + (A)(x * x);
+        else { A a = (A)m_abs(x); s = (s < a) ? a : s; }
+    }
+    XTG_DI void merge(const AccNorm& o) {
+        if (NK == 3) s = (s > o.s) ? s : o.s; else s = s + o.s;
+    }
+    XTG_DI double dval() const { return (double)s; }
+};
+// float32 / bf16 squares and absolute values in double-float.
+template <int NK> struct AccNormC {
+    AccSumC a;
+    XTG_DI void init(const RedParams&) { a.hi = 0.f; a.lo = 0.f; }
+    template <class X> XTG_DI void add(X x, i64) {
+        float f = cvt<float>(x);
+        if (NK == 1) {
+            a.addf(fabsf(f));
+        } else {
+            float q = f * f;
+            float qe = fmaf(f, f, -q);
+            a.addf(q);
+            a.lo += qe;
+        }
+    }
+    XTG_DI void merge(const AccNormC& o) { a.merge(o.a); }
+    XTG_DI double dval() const { return a.dval(); }
+};
+
+// Arg-reductions (include/xtensor/misc/xsort.hpp:1158-1296): strict compare,
+// first index wins; NaN never wins unless it is the very first element (the
+// reference then returns 0 because nothing compares greater than NaN).
+template <class A, int MAXOP> struct AccArg {
+    A v;
+    i64 idx;  // -1: empty
+    XTG_DI void init(const RedParams&) { idx = -1; v = A(0); }
+    template <class X> XTG_DI void add(X x, i64 ps) {
+        A a = cvt<A>(x);
+        if (idx < 0) {
+            if (a == a || ps == 0) { v = a; idx = ps; }
+        } else if (MAXOP ? (a > v) : (a < v)) {
+            v = a;
+            idx = ps;
+        }
+    }
+    XTG_DI void merge(const AccArg& o) {
+        if (o.idx < 0) return;
+        if (idx < 0) { v = o.v; idx = o.idx; return; }
+        bool nan_me = !(v == v), nan_o = !(o.v == o.v);
+        if (nan_me) return;
+        if (nan_o) { v = o.v; idx = o.idx; return; }
+        bool take = MAXOP ? (o.v > v) : (o.v < v);
+        if (!take && !(MAXOP ? (v > o.v) : (v < o.v)) && o.idx < idx) take = true;
+        if (take) { v = o.v; idx = o.idx; }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Reduction parameters.  Output space = kept dims (rank RO), reduced space =
+// reduced dims (rank RR).  For the ROW strategy the innermost reduced dim is
+// vectorised (rshape[RR-1] counted in vectors); for COL the innermost kept
+// dim is (oshape[RO-1] counted in vectors).
+template <class A, int OP> XTG_DI void AccPlain<A, OP>::init(const RedParams& p) {
+    s = IsFloat<A>::value ? (A)p.init_f : (A)p.init_i;
+}
+XTG_DI void AccSumC::init(const RedParams& p) { hi = (float)p.init_f; lo = 0.f; }
+template <class A, int MAXOP> XTG_DI void AccSel<A, MAXOP>::init(const RedParams& p) {
+    v = IsFloat<A>::value ? (A)p.init_f : (A)p.init_i;
+    pos = -1;
+}
+template <int MODE> XTG_DI void AccMom<float, MODE>::init(const RedParams&) {
+    k = 0.f;
+    s1.hi = s1.lo = s2.hi = s2.lo = 0.f;
+}
+template <int MODE> XTG_DI void AccMom<double, MODE>::init(const RedParams&) { k = 0.0; s1 = s2 = 0.0; }
+
+// Shift for the moment accumulators (the output's first element).
+template <class A> struct Shift {
+    template <class X> static XTG_DI void set(A&, X) {}
+};
+template <int MODE> struct Shift<AccMom<float, MODE>> {
+    template <class X> static XTG_DI void set(AccMom<float, MODE>& a, X x) { a.k = MODE == 0 ? 0.f : cvt<float>(x); }
+};
+template <int MODE> struct Shift<AccMom<double, MODE>> {
+    template <class X> static XTG_DI void set(AccMom<double, MODE>& a, X x) { a.k = MODE == 0 ? 0.0 : cvt<double>(x); }
+};
+template <class A> struct NeedsShift { enum { value = 0 }; };
+template <int MODE> struct NeedsShift<AccMom<float, MODE>> { enum { value = MODE != 0 }; };
+template <int MODE> struct NeedsShift<AccMom<double, MODE>> { enum { value = MODE != 0 }; };
+
+// Finalisation: accumulator state -> output element (merging xt::initial
+// last, as xreducer_stepper::aggregate does, xreducer.hpp:1778-1799).
+template <class Out, class A> struct Fin;
+template <class Out, class A, int OP> struct Fin<Out, AccPlain<A, OP>> {
+    static XTG_DI Out go(const AccPlain<A, OP>& a, const RedParams& p) {
+        A r = a.s;
+        if (p.has_initial) {
+            A iv = IsFloat<A>::value ? (A)p.initial_f : (A)p.initial_i;
+            r = OP == 0 ? (A)(iv + r) : (A)(iv * r);
+        }
+        return cvt<Out>(r);
+    }
+};
+template <class Out> struct Fin<Out, AccSumC> {
+    static XTG_DI Out go(const AccSumC& a, const RedParams& p) {
+        double r = a.dval();
+        if (p.has_initial) r = p.initial_f + r;
+        return cvt<Out>(r);
+    }
+};
+template <class Out, class A, int MAXOP> struct Fin<Out, AccSel<A, MAXOP>> {
+    static XTG_DI Out go(const AccSel<A, MAXOP>& a, const RedParams& p) {
+        A r = a.v;
+        if (p.has_initial) {
+            A iv = IsFloat<A>::value ? (A)p.initial_f : (A)p.initial_i;
+            r = MAXOP ? (iv > r ? iv : r) : (iv < r ? iv : r);
+        }
+        return cvt<Out>(r);
+    }
+};
+// mean: sum / divisor in double (mean_division, xmath.hpp:1828-1835);
+// variance: (sum d^2 - (sum d)^2 / n) / divisor; stddev: sqrt of that.
+template <int MODE> XTG_DI void mom_sums(const AccMom<float, MODE>& a, double& s1, double& s2) {
+    s1 = a.s1.dval();
+    s2 = a.s2.dval();
+}
+template <int MODE> XTG_DI void mom_sums(const AccMom<double, MODE>& a, double& s1, double& s2) {
+    s1 = a.s1;
+    s2 = a.s2;
+}
+template <class Out, class C, int MODE> struct Fin<Out, AccMom<C, MODE>> {
+    static XTG_DI Out go(const AccMom<C, MODE>& a, const RedParams& p) {
+        double s1, s2;
+        mom_sums(a, s1, s2);
+        if (MODE == 0) return cvt<Out>(s1 / p.divisor);
+        double n = (double)p.n_red;
+        double m2 = s2 - s1 * (s1 / n);
+        if (m2 < 0.0) m2 = 0.0;
+        double var = m2 / p.divisor;
+        return cvt<Out>(MODE == 2 ? sqrt(var) : var);
+    }
+};
+template <class Out, class A, int NK> struct Fin<Out, AccNorm<A, NK>> {
+    static XTG_DI Out go(const AccNorm<A, NK>& a, const RedParams&) { return cvt<Out>(a.s); }
+};
+template <class Out, int NK> struct Fin<Out, AccNormC<NK>> {
+    static XTG_DI Out go(const AccNormC<NK>& a, const RedParams&) { return cvt<Out>(a.dval()); }
+};
+template <class Out, class A, int MAXOP> struct Fin<Out, AccArg<A, MAXOP>> {
+    static XTG_DI Out go(const AccArg<A, MAXOP>& a, const RedParams&) { return cvt<Out>(a.idx < 0 ? 0 : a.idx); }
+};
+// Post-processing applied after Fin: POST 1 = sqrt (norm_l2 = sqrt(norm_sq),
+// include/xtensor/reducers/xnorm.hpp:494-526); POST 2 = division by the
+// mean divisor in double (mean_division, include/xtensor/core/xmath.hpp:1828-1835).
+template <int POST, class Out, class V> XTG_DI Out post(V v, const RedParams& p) {
+    if (POST == 1) return cvt<Out>(m_sqrt(cvt<double>(v)));
+    if (POST == 2) return cvt<Out>(cvt<double>(v) / p.divisor);
+    return cvt<Out>(v);
+}
+// Value type handed from Fin to post: POST 2 keeps the sum in double.
+template <int POST, class Out> struct FinT { typedef Out type; };
+template <class Out> struct FinT<2, Out> { typedef double type; };
+template <class Out, class Acc, int POST> XTG_DI Out finish(const Acc& a, const RedParams& p) {
+    typedef typename FinT<POST, Out>::type M;
+    return post<POST, Out>(Fin<M, Acc>::go(a, p), p);
+}
+
+// Offsets of every leaf at a (kept, reduced) multi-index pair.
+template <int NL, int RO, int RR>
+XTG_DI void red_offsets(const RedParams& p, const i64 (&ko)[RO], const i64 (&ro)[RR], i64 (&off)[XTG_KMAX_LEAVES]) {
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+        i64 o = 0;
+#pragma unroll
+        for (int d = 0; d < RO; ++d) o += ko[d] * p.lks[l][d];
+#pragma unroll
+        for (int d = 0; d < RR; ++d) o += ro[d] * p.lrs[l][d];
+        off[l] = o;
+    }
+}
+
+template <int R, bool BIG>
+XTG_DI void decode_dims(const i64* shape, const FastDiv* fd, i64 q, i64 (&idx)[R]) {
+    if (BIG || R == 1) {
+#pragma unroll
+        for (int d = R - 1; d >= 1; --d) {
+            i64 n = shape[d];
+            i64 qq = q / n;
+            idx[d] = q - qq * n;
+            q = qq;
+        }
+        idx[0] = q;
+    } else {
+        u32 qu = (u32)q;
+#pragma unroll
+        for (int d = R - 1; d >= 1; --d) {
+            u32 qq = fdiv(qu, fd[d]);
+            idx[d] = qu - qq * fd[d].d;
+            qu = qq;
+        }
+        idx[0] = qu;
+    }
+}
+
+// Loads of all leaves at explicit offsets (vector along a given inner stride).
+template <int I, int VEC, class... S> struct LoadAt;
+template <int I, int VEC> struct LoadAt<I, VEC> {
+    template <class RG> static XTG_DI void run(RG&, const void* const*, const i64*, const i64*) {}
+};
+template <int I, int VEC, class S0, class... S> struct LoadAt<I, VEC, S0, S...> {
+    template <class RG> static XTG_DI void run(RG& rg, const void* const* ptr, const i64* off, const i64* inner) {
+        typedef typename S0::type T;
+        ld_leaf<T, S0::kind, VEC>(rg.v, reinterpret_cast<const T*>(ptr[I]), off[I], inner[I]);
+        LoadAt<I + 1, VEC, S...>::run(rg.rest, ptr, off, inner);
+    }
+};
+template <class LS> struct LoadLeavesAt;
+template <class... S> struct LoadLeavesAt<LeafSet<S...>> {
+    template <int VEC, class RG> static XTG_DI void run(RG& rg, const void* const* ptr, const i64* off, const i64* inner) {
+        LoadAt<0, VEC, S...>::run(rg, ptr, off, inner);
+    }
+};
+// All leaves but leaf 0 (the transposing kernel fills leaf 0 from shared memory).
+template <class LS> struct LoadRest;
+template <class S0, class... S> struct LoadRest<LeafSet<S0, S...>> {
+    template <class RG> static XTG_DI void run(RG& rg, const void* const* ptr, const i64* off, const i64* inner) {
+        LoadAt<1, 1, S...>::run(rg.rest, ptr, off, inner);
+    }
+};
+
+// K3/K5: ROW strategy — the reduced run is contiguous (or broadcast) for the
+// leaves; a group (warp or CTA) owns one (output, split) work item and strides
+// over its vectors.  Work items: w = o * nsplit + s.
+template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int GROUP, bool BIG>
+__global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    __shared__ Acc smem[32];
+    Ctx<0> c;
+    c.scal = &p.scal;
+    const int gsz = GROUP <= 32 ? 32 : (int)blockDim.x;
+    const int groups_per_block = (int)blockDim.x / gsz;
+    const int gtid = (int)threadIdx.x % gsz;
+    const i64 gid = (i64)blockIdx.x * groups_per_block + (int)threadIdx.x / gsz;
+    const i64 ngroups = (i64)gridDim.x * groups_per_block;
+    const i64 nwork = p.n_out * p.nsplit;
+    i64 inner[XTG_KMAX_LEAVES];
+#pragma unroll
+    for (int l = 0; l < LS::N; ++l) inner[l] = p.lrs[l][RR - 1];
+    for (i64 w = gid; w < nwork; w += ngroups) {
+        const i64 o = w / p.nsplit;
+        const i64 s = w - o * p.nsplit;
+        i64 ko[RO];
+        decode_dims<RO, true>(p.oshape, p.ofd, o, ko);
+        Acc acc;
+        acc.init(p);
+        if (NeedsShift<Acc>::value && p.n_red > 0) {
+            i64 r0[RR];
+#pragma unroll
+            for (int d = 0; d < RR; ++d) r0[d] = 0;
+            i64 off[XTG_KMAX_LEAVES];
+            red_offsets<LS::N, RO, RR>(p, ko, r0, off);
+            typename LS::template R<1>::type rg1;
+            LoadLeavesAt<LS>::template run<1>(rg1, p.leaf, off, inner);
+            Shift<Acc>::set(acc, Tree::ev(rg1, 0, c));
+        }
+        const i64 rb = s * p.chunk;
+        i64 re = rb + p.chunk;
+        if (re > p.n_redv) re = p.n_redv;
+        for (i64 r = rb + gtid; r < re; r += gsz) {
+            i64 ri[RR];
+            decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);
+            ri[RR - 1] *= VEC;
+            i64 off[XTG_KMAX_LEAVES];
+            red_offsets<LS::N, RO, RR>(p, ko, ri, off);
+            RG rg;
+            LoadLeavesAt<LS>::template run<VEC>(rg, p.leaf, off, inner);
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) acc.add(Tree::ev(rg, j, c), r * VEC + j);
+        }
+        acc = group_reduce<GROUP>(acc, smem);
+        if (gtid == 0) {
+            if (p.nsplit > 1) {
+                reinterpret_cast<Acc*>(p.partial)[w] = acc;
+            } else {
+                i64 oo = 0;
+#pragma unroll
+                for (int d = 0; d < RO; ++d) oo += ko[d] * p.ostr[d];
+                reinterpret_cast<Out*>(p.out)[oo] = finish<Out, Acc, POST>(acc, p);
+            }
+        }
+        if (GROUP > 32) __syncthreads();
+    }
+}
+
+// K4: COL strategy — the innermost kept dim is contiguous; each thread owns
+// VEC consecutive outputs and walks the reduced space (U loads in flight).
+// Work items: w = s * n_outv + ov (consecutive threads -> consecutive outputs).
+template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int U, bool BIG>
+__global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    Ctx<0> c;
+    c.scal = &p.scal;
+    const i64 nwork = p.n_outv * p.nsplit;
+    i64 inner[XTG_KMAX_LEAVES];
+#pragma unroll
+    for (int l = 0; l < LS::N; ++l) inner[l] = p.lks[l][RO - 1];
+    for (i64 w = (i64)blockIdx.x * blockDim.x + threadIdx.x; w < nwork; w += (i64)gridDim.x * blockDim.x) {
+        const i64 s = w / p.n_outv;
+        const i64 ov = w - s * p.n_outv;
+        i64 ko[RO];
+        decode_dims<RO, BIG>(p.oshape, p.ofd, ov, ko);
+        ko[RO - 1] *= VEC;
+        Acc acc[VEC];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) acc[j].init(p);
+        if (NeedsShift<Acc>::value && p.n_red > 0) {
+            i64 r0[RR];
+#pragma unroll
+            for (int d = 0; d < RR; ++d) r0[d] = 0;
+            i64 off[XTG_KMAX_LEAVES];
+            red_offsets<LS::N, RO, RR>(p, ko, r0, off);
+            RG rg;
+            LoadLeavesAt<LS>::template run<VEC>(rg, p.leaf, off, inner);
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) Shift<Acc>::set(acc[j], Tree::ev(rg, j, c));
+        }
+        const i64 rb = s * p.chunk;
+        i64 re = rb + p.chunk;
+        if (re > p.n_redv) re = p.n_redv;
+        for (i64 r = rb; r < re; r += U) {
+            RG rg[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (r + u < re) {
+                    i64 ri[RR];
+                    decode_dims<RR, BIG>(p.rshape, p.rfd, r + u, ri);
+                    i64 off[XTG_KMAX_LEAVES];
+                    red_offsets<LS::N, RO, RR>(p, ko, ri, off);
+                    LoadLeavesAt<LS>::template run<VEC>(rg[u], p.leaf, off, inner);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (r + u < re) {
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) acc[j].add(Tree::ev(rg[u], j, c), r + u);
+                }
+            }
+        }
+        // flat output index of the first of the VEC outputs
+        i64 ofl = 0;
+#pragma unroll
+        for (int d = 0; d < RO; ++d) ofl = ofl * (d == RO - 1 ? p.oshape[d] * VEC : p.oshape[d]) + ko[d];
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            if (p.nsplit > 1) {
+                reinterpret_cast<Acc*>(p.partial)[(ofl + j) * p.nsplit + s] = acc[j];
+            } else {
+                i64 oo = 0;
+#pragma unroll
+                for (int d = 0; d < RO; ++d) oo += ko[d] * p.ostr[d];
+                oo += (i64)j * p.ostr[RO - 1];
+                reinterpret_cast<Out*>(p.out)[oo] = finish<Out, Acc, POST>(acc[j], p);
+            }
+        }
+    }
+}
+
+// Deterministic combine of split partials: one CTA per output, threads take
+// splits t, t+blockDim, … in order, then a fixed block tree.
+template <class Acc, class Out, int POST, int RO>
+__global__ void __launch_bounds__(256) k_reduce_combine(const RedParams p) {
+    __shared__ Acc smem[32];
+    const Acc* part = reinterpret_cast<const Acc*>(p.partial);
+    for (i64 o = blockIdx.x; o < p.n_out; o += gridDim.x) {
+        Acc a;
+        a.init(p);
+        for (i64 s = threadIdx.x; s < p.nsplit; s += blockDim.x) {
+            if (s == (i64)threadIdx.x) a = part[o * p.nsplit + s];
+            else a.merge(part[o * p.nsplit + s]);
+        }
+        a = group_reduce<256>(a, smem);
+        if (threadIdx.x == 0) {
+            i64 ko[RO];
+            decode_dims<RO, true>(p.oshape, p.ofd, o, ko);
+            i64 oo = 0;
+#pragma unroll
+            for (int d = 0; d < RO; ++d) oo += ko[d] * p.ostr[d];
+            reinterpret_cast<Out*>(p.out)[oo] = finish<Out, Acc, POST>(a, p);
+        }
+        __syncthreads();
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// K2: tiled transposing assignment (transpose / permuted strided_view into a
+// contiguous destination — the case xtensor sends to the scalar
+// stepper_assigner, include/xtensor/core/xassign.hpp:1087, 1341).
+// Dims are in destination order after collapsing; dim B = R-1 is contiguous
+// in the destination, dim A (p.da) is the one along which leaf 0 — the
+// transposed source — is unit-stride.  A TILE x TILE tile goes through shared
+// memory: loads walk A (coalesced for leaf 0), stores walk B (coalesced for
+// the destination).  Other leaves are read directly at (a, b).
+template <class Tree, class LS, class OutT, int NB, int TILE, int ROWS>
+__global__ void __launch_bounds__(TILE * ROWS) k_transpose(const TransposeParams p) {
+    typedef typename LS::template R<1>::type RG;
+    typedef typename RG::elem0 T0;
+    __shared__ T0 tile[TILE][TILE + 1];
+    Ctx<0> c;
+    c.scal = &p.scal;
+    const int tx = threadIdx.x % TILE, ty = threadIdx.x / TILE;
+    for (i64 t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
+        i64 tb = t % p.ntile_b;
+        i64 rest = t / p.ntile_b;
+        i64 ta = rest % p.ntile_a;
+        i64 bt = rest / p.ntile_a;
+        i64 boff[XTG_KMAX_LEAVES];
+        i64 obo = 0;
+#pragma unroll
+        for (int l = 0; l < LS::N; ++l) boff[l] = 0;
+#pragma unroll
+        for (int d = NB - 1; d >= 0; --d) {
+            i64 n = p.bshape[d];
+            i64 q = bt / n;
+            i64 id = bt - q * n;
+            bt = q;
+            obo += id * p.obs[d];
+#pragma unroll
+            for (int l = 0; l < LS::N; ++l) boff[l] += id * p.lbs[l][d];
+        }
+        const i64 a0 = ta * TILE, b0 = tb * TILE;
+        const T0* src = reinterpret_cast<const T0*>(p.leaf[0]);
+        {
+            const i64 a = a0 + tx;
+#pragma unroll
+            for (int bb = ty; bb < TILE; bb += ROWS) {
+                const i64 b = b0 + bb;
+                if (a < p.sa && b < p.sb) tile[bb][tx] = ld1<T0>(src + boff[0] + a * p.la[0] + b * p.lb[0]);
+            }
+        }
+        __syncthreads();
+        {
+            const i64 b = b0 + tx;
+#pragma unroll
+            for (int aa = ty; aa < TILE; aa += ROWS) {
+                const i64 a = a0 + aa;
+                if (a < p.sa && b < p.sb) {
+                    RG rg;
+                    rg.v[0] = tile[tx][aa];
+                    i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
+#pragma unroll
+                    for (int l = 0; l < LS::N; ++l) { off[l] = boff[l] + a * p.la[l] + b * p.lb[l]; inner[l] = 0; }
+                    LoadRest<LS>::run(rg, p.leaf, off, inner);
+                    reinterpret_cast<OutT*>(p.out)[obo + a * p.oa + b * p.ob] = cvt<OutT>(Tree::ev(rg, 0, c));
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K7: fused row statistics.  Trees holding keep-dims reductions over the
+// trailing axes — C1's (x - mean(x,{2},kd)) / sqrt(variance(x,{2},kd) + eps),
+// which the reference evaluates with three passes and a temporary
+// (include/xtensor/core/xmath.hpp:2082-2103) — run as ONE pass: a group
+// (warp or CTA) loads a whole row into registers, computes every statistic
+// from registers (two-pass mean / sum of squared deviations, compensated),
+// then evaluates the tree and stores the row.  HBM traffic: one read, one
+// write.
+// A statistic: MODE 0 sum, 1 mean, 2 variance, 3 stddev, 4 max, 5 min;
+// C = compute type (float: compensated double-float; double: FP64); Sub is
+// the subtree it reduces.
+template <int K, int MODE, class C, class Sub> struct RStat {};
+template <class... X> struct StatList {};
+
+struct DSum {
+    double s;
+    XTG_DI void merge(const DSum& o) { s += o.s; }
+};
+// Row sums: FP64 for float64 (and integer) data, double-float for float32.
+template <int GROUP, class C> struct RowSum {
+    typedef DSum A;
+    static XTG_DI void zero(A& a) { a.s = 0.0; }
+    template <class X> static XTG_DI void add(A& a, X v) { a.s += cvt<double>(v); }
+    template <class X> static XTG_DI void addsq(A& a, X d) {
+        double x = cvt<double>(d);
+        a.s = fma(x, x, a.s);
+    }
+    static XTG_DI double val(const A& a) { return a.s; }
+};
+template <int GROUP> struct RowSum<GROUP, float> {
+    typedef AccSumC A;
+    static XTG_DI void zero(A& a) { a.hi = 0.f; a.lo = 0.f; }
+    static XTG_DI void add(A& a, float v) { a.addf(v); }
+    static XTG_DI void addsq(A& a, float d) {
+        float q = d * d;
+        float qe = fmaf(d, d, -q);
+        a.addf(q);
+        a.lo += qe;
+    }
+    static XTG_DI double val(const A& a) { return a.dval(); }
+};
+template <int GROUP, class A> XTG_DI A bcast_group(A a, A* smem) {
+    if (GROUP <= 32) {
+        union U { A a; u32 w[(sizeof(A) + 3) / 4]; };
+        U u;
+        u.a = a;
+#pragma unroll
+        for (int i = 0; i < (int)((sizeof(A) + 3) / 4); ++i) u.w[i] = __shfl_sync(0xffffffffu, u.w[i], 0);
+        return u.a;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) smem[0] = a;
+    __syncthreads();
+    A r = smem[0];
+    return r;
+}
+
+template <class LST> struct Stats;
+template <> struct Stats<StatList<>> {
+    template <int GROUP, int VEC, int NV, class RG, class CT>
+    static XTG_DI void run(const RG (&)[NV], const bool (&)[NV][VEC], CT&, const RowParams&, void*) {}
+};
+template <int K, int MODE, class C, class Sub, class... Rest> struct Stats<StatList<RStat<K, MODE, C, Sub>, Rest...>> {
+    template <int GROUP, int VEC, int NV, class RG, class CT>
+    static XTG_DI void run(const RG (&rg)[NV], const bool (&ok)[NV][VEC], CT& c, const RowParams& p, void* smem) {
+        typedef RowSum<GROUP, C> RS;
+        typedef typename RS::A A;
+        if (MODE <= 3) {
+            A s;
+            RS::zero(s);
+#pragma unroll
+            for (int n = 0; n < NV; ++n)
+#pragma unroll
+                for (int j = 0; j < VEC; ++j)
+                    if (ok[n][j]) RS::add(s, cvt<C>(Sub::ev(rg[n], j, c)));
+            s = group_reduce<GROUP>(s, reinterpret_cast<A*>(smem));
+            s = bcast_group<GROUP>(s, reinterpret_cast<A*>(smem));
+            double sum = RS::val(s);
+            if (MODE == 0) {
+                c.stat[K] = sum;
+            } else {
+                double mean = sum / (double)p.row_len;
+                if (MODE == 1) {
+                    c.stat[K] = sum / p.div[K];
+                } else {
+                    const C m = (C)mean;
+                    A q;
+                    RS::zero(q);
+#pragma unroll
+                    for (int n = 0; n < NV; ++n)
+#pragma unroll
+                        for (int j = 0; j < VEC; ++j)
+                            if (ok[n][j]) RS::addsq(q, (C)(cvt<C>(Sub::ev(rg[n], j, c)) - m));
+                    q = group_reduce<GROUP>(q, reinterpret_cast<A*>(smem));
+                    q = bcast_group<GROUP>(q, reinterpret_cast<A*>(smem));
+                    // correct for the rounding of the mean to C:
+                    // sum (x - m)^2 = sum (x - mean)^2 + n (mean - m)^2
+                    double dm = mean - (double)m;
+                    double m2 = RS::val(q) - (double)p.row_len * dm * dm;
+                    if (m2 < 0.0) m2 = 0.0;
+                    double var = m2 / p.div[K];
+                    c.stat[K] = MODE == 3 ? sqrt(var) : var;
+                }
+            }
+        } else {
+            AccSel<C, MODE == 4> a;
+            a.v = MODE == 4 ? Lim<C>::lowest() : Lim<C>::maxv();
+            a.pos = -1;
+#pragma unroll
+            for (int n = 0; n < NV; ++n)
+#pragma unroll
+                for (int j = 0; j < VEC; ++j)
+                    if (ok[n][j]) a.add(cvt<C>(Sub::ev(rg[n], j, c)), (i64)((n * GROUP) + (int)(threadIdx.x % GROUP)) * VEC + j);
+            a = group_reduce<GROUP>(a, reinterpret_cast<AccSel<C, MODE == 4>*>(smem));
+            a = bcast_group<GROUP>(a, reinterpret_cast<AccSel<C, MODE == 4>*>(smem));
+            c.stat[K] = (double)a.v;
+        }
+        Stats<StatList<Rest...>>::template run<GROUP, VEC, NV>(rg, ok, c, p, smem);
+    }
+};
+
+template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int GROUP, int RO, int NSTAT>
+__global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    __shared__ __align__(16) unsigned char smem_raw[32 * 48];
+    Ctx<NSTAT> c;
+    c.scal = &p.scal;
+    const int gsz = GROUP <= 32 ? 32 : (int)blockDim.x;
+    const int gpb = (int)blockDim.x / gsz;
+    const int gt = (int)threadIdx.x % gsz;
+    const i64 gid = (i64)blockIdx.x * gpb + (int)threadIdx.x / gsz;
+    const i64 ng = (i64)gridDim.x * gpb;
+    for (i64 row = gid; row < p.n_rows; row += ng) {
+        i64 ko[RO];
+        decode_dims<RO, true>(p.oshape, (const FastDiv*)0, row, ko);
+        i64 base[XTG_KMAX_LEAVES];
+#pragma unroll
+        for (int l = 0; l < LS::N; ++l) {
+            i64 o = 0;
+#pragma unroll
+            for (int d = 0; d < RO; ++d) o += ko[d] * p.lo[l][d];
+            base[l] = o;
+        }
+        RG rg[NV];
+        bool ok[NV][VEC];
+#pragma unroll
+        for (int n = 0; n < NV; ++n) {
+            const i64 e0 = ((i64)n * gsz + gt) * VEC;
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) ok[n][j] = (e0 + j) < p.row_len;
+            if (e0 < p.row_len) {
+                i64 off[XTG_KMAX_LEAVES];
+#pragma unroll
+                for (int l = 0; l < LS::N; ++l) off[l] = base[l] + e0 * p.li[l];
+                LoadLeavesAt<LS>::template run<VEC>(rg[n], p.leaf, off, p.li);
+            }
+        }
+        Stats<SL>::template run<GROUP, VEC, NV>(rg, ok, c, p, (void*)smem_raw);
+        i64 ob = 0;
+#pragma unroll
+        for (int d = 0; d < RO; ++d) ob += ko[d] * p.oo[d];
+#pragma unroll
+        for (int n = 0; n < NV; ++n) {
+            const i64 e0 = ((i64)n * gsz + gt) * VEC;
+            if (e0 < p.row_len) {
+                OutT v[VEC];
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) v[j] = cvt<OutT>(Tree::ev(rg[n], j, c));
+                st_out<OutT, K_CONTIG, VEC>(reinterpret_cast<OutT*>(p.out), ob + e0 * p.oi, p.oi, v);
+            }
+        }
+    }
+}
+
+}  // namespace xtg
+#endif

@@ -1,0 +1,97 @@
+// xtg_internal.h — shared host-side declarations of libxtg (not installed).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/xtg.h"
+
+namespace xtgh {
+
+// ---- errors ---------------------------------------------------------------
+xtg_status fail(xtg_status s, const std::string& msg);
+xtg_status cuda_fail(cudaError_t e, const char* what);
+xtg_status cu_fail(CUresult e, const char* what);
+void clear_error();
+
+#define XTG_CUDA(call)                                         \
+    do {                                                       \
+        cudaError_t _e = (call);                               \
+        if (_e != cudaSuccess) return ::xtgh::cuda_fail(_e, #call); \
+    } while (0)
+#define XTG_CU(call)                                           \
+    do {                                                       \
+        CUresult _e = (call);                                  \
+        if (_e != CUDA_SUCCESS) return ::xtgh::cu_fail(_e, #call); \
+    } while (0)
+#define XTG_TRY(call)                                          \
+    do {                                                       \
+        xtg_status _s = (call);                                \
+        if (_s != XTG_OK) return _s;                           \
+    } while (0)
+
+// ---- driver API (resolved at run time through cudaGetDriverEntryPointByVersion
+// so that the library loads on machines without a driver) -------------------------
+struct Drv {
+    CUresult (*Init)(unsigned int) = nullptr;
+    CUresult (*CtxGetCurrent)(CUcontext*) = nullptr;
+    CUresult (*CtxSetCurrent)(CUcontext) = nullptr;
+    CUresult (*ModuleLoadData)(CUmodule*, const void*) = nullptr;
+    CUresult (*ModuleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+    CUresult (*LaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                             CUstream, void**, void**) = nullptr;
+    CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
+    CUresult (*GetErrorString)(CUresult, const char**) = nullptr;
+};
+const Drv& drv();
+
+// ---- device ----------------------------------------------------------------
+struct DeviceInfo {
+    int device = -1;
+    int sm_count = 0;
+    int cc_major = 0, cc_minor = 0;
+    int64_t hbm = 0;
+    int max_threads_per_sm = 0;
+};
+// Initialises the runtime on the current (or default) device once, makes the
+// primary context current on the calling thread.
+xtg_status ensure_device(DeviceInfo** info);
+
+// ---- options -----------------------------------------------------------------
+int64_t opt(const char* key, int64_t dflt);
+// Option "jit.dry_run": plan and compile kernels without a GPU (no launches).
+bool dry_run();
+
+// ---- dtypes -------------------------------------------------------------------
+struct DTypeInfo {
+    const char* cname;  // C++ spelling used in kernel names
+    int size;
+    bool is_float;
+    bool is_signed;
+    bool is_int;
+};
+const DTypeInfo& dt(int dtype);
+bool valid_dtype(int dtype);
+
+// ---- JIT ------------------------------------------------------------------------
+struct Kernel {
+    CUfunction fn = nullptr;
+    std::string name;
+    int max_blocks_per_sm = 0;  // occupancy at the block size it was queried for
+    int block = 0;
+};
+// Compiles (or fetches) the kernel whose name expression is `expr`
+// (e.g. "xtg::k_assign<...>").  `block` is used for the occupancy query.
+xtg_status get_kernel(const std::string& expr, int block, Kernel** k);
+xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream);
+void count_launch();
+
+// ---- scratch ---------------------------------------------------------------------
+xtg_status scratch_alloc(void** p, size_t bytes, cudaStream_t s);
+xtg_status scratch_free(void* p, cudaStream_t s);
+
+}  // namespace xtgh

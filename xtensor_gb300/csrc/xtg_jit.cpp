@@ -1,0 +1,222 @@
+// xtg_jit.cpp — instantiates the kernel templates of xtg_device.cuh for one
+// expression-tree type at first use.  NVRTC compiles the instantiation to an
+// sm_103a cubin (arch-specific target of the running device), the cubin is
+// cached on disk and in-process, and launches go through the driver API on
+// the runtime's primary context.  This is the "compile-time lowering" of an
+// xfunction tree, performed when the tree shape is first seen instead of when
+// the caller's translation unit is built.
+#include <nvrtc.h>
+
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <unordered_map>
+
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include "xtg_internal.h"
+#include "_gen/xtg_device_src.h"  // kXtgParamsSrc / kXtgDeviceSrc: texts of the two headers
+
+namespace xtgh {
+
+namespace {
+
+struct JitState {
+    std::mutex mu;
+    std::unordered_map<std::string, std::unique_ptr<Kernel>> kernels;
+    xtg_jit_stats st{};
+};
+JitState& js() {
+    static JitState s;
+    return s;
+}
+std::atomic<int64_t> g_launches{0};
+
+uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
+    for (unsigned char c : s) {
+        h ^= c;
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+std::string cache_dir() {
+    const char* d = getenv("XTG_CACHE_DIR");
+    std::string dir;
+    if (d && *d) dir = d;
+    else {
+        const char* home = getenv("HOME");
+        dir = std::string(home && *home ? home : "/tmp") + "/.cache/xtensor_gb300";
+    }
+    return dir;
+}
+
+void mkdirs(const std::string& path) {
+    std::string cur;
+    for (size_t i = 0; i < path.size(); ++i) {
+        cur += path[i];
+        if (path[i] == '/' && cur.size() > 1) mkdir(cur.c_str(), 0755);
+    }
+    mkdir(path.c_str(), 0755);
+}
+
+bool read_file(const std::string& p, std::string& out) {
+    std::ifstream f(p, std::ios::binary);
+    if (!f) return false;
+    std::ostringstream ss;
+    ss << f.rdbuf();
+    out = ss.str();
+    return true;
+}
+
+void write_file_atomic(const std::string& p, const std::string& data) {
+    std::string tmp = p + ".tmp." + std::to_string(getpid());
+    {
+        std::ofstream f(tmp, std::ios::binary);
+        if (!f) return;
+        f.write(data.data(), (std::streamsize)data.size());
+    }
+    rename(tmp.c_str(), p.c_str());
+}
+
+xtg_status compile(const std::string& expr, const std::string& arch, std::string& cubin, std::string& lowered) {
+    const char* hdr_src[2] = {kXtgParamsSrc, kXtgDeviceSrc};
+    const char* hdr_name[2] = {"xtg_params.h", "xtg_device.cuh"};
+    nvrtcProgram prog;
+    const char* src = "#include \"xtg_device.cuh\"\n";
+    nvrtcResult r = nvrtcCreateProgram(&prog, src, "xtg_jit.cu", 2, hdr_src, hdr_name);
+    if (r != NVRTC_SUCCESS) return fail(XTG_ERR_JIT, std::string("nvrtcCreateProgram: ") + nvrtcGetErrorString(r));
+    std::string name_expr = "&" + expr;
+    nvrtcAddNameExpression(prog, name_expr.c_str());
+    std::string archopt = "--gpu-architecture=" + arch;
+    const char* opts[] = {archopt.c_str(), "--std=c++17", "--fmad=false", "-DXTG_NVRTC=1"};
+    r = nvrtcCompileProgram(prog, 4, opts);
+    if (r != NVRTC_SUCCESS) {
+        size_t n = 0;
+        nvrtcGetProgramLogSize(prog, &n);
+        std::string log(n, '\0');
+        if (n) nvrtcGetProgramLog(prog, &log[0]);
+        nvrtcDestroyProgram(&prog);
+        if (log.size() > 4000) log = log.substr(0, 4000) + "...";
+        return fail(XTG_ERR_JIT, "NVRTC failed for " + expr + ":\n" + log);
+    }
+    const char* low = nullptr;
+    nvrtcGetLoweredName(prog, name_expr.c_str(), &low);
+    lowered = low ? low : "";
+    size_t n = 0;
+    nvrtcGetCUBINSize(prog, &n);
+    cubin.assign(n, '\0');
+    if (n) nvrtcGetCUBIN(prog, &cubin[0]);
+    nvrtcDestroyProgram(&prog);
+    if (lowered.empty() || cubin.empty()) return fail(XTG_ERR_JIT, "NVRTC produced no cubin for " + expr);
+    return XTG_OK;
+}
+
+}  // namespace
+
+xtg_status get_kernel(const std::string& expr, int block, Kernel** out) {
+    DeviceInfo* dev;
+    XTG_TRY(ensure_device(&dev));
+    JitState& S = js();
+    std::lock_guard<std::mutex> lk(S.mu);
+    auto it = S.kernels.find(expr);
+    if (it != S.kernels.end()) {
+        S.st.memory_hits++;
+        *out = it->second.get();
+        return XTG_OK;
+    }
+    char arch[32];
+    snprintf(arch, sizeof arch, "sm_%d%da", dev->cc_major, dev->cc_minor);
+    int vmaj = 0, vmin = 0;
+    nvrtcVersion(&vmaj, &vmin);
+    const std::string key_src = expr + "\n" + arch + "\n" + std::to_string(vmaj) + "." + std::to_string(vmin) + "\n";
+    uint64_t h = fnv1a(kXtgDeviceSrc, fnv1a(kXtgParamsSrc, fnv1a(key_src)));
+    char hex[32];
+    snprintf(hex, sizeof hex, "%016llx", (unsigned long long)h);
+    const std::string dir = cache_dir();
+    const std::string path = dir + "/" + hex + ".cubin";
+
+    std::string blob, cubin, lowered;
+    bool from_disk = false;
+    if (read_file(path, blob) && blob.size() > 8) {
+        uint32_t nl = 0;
+        memcpy(&nl, blob.data(), 4);
+        if (nl > 0 && 4 + (size_t)nl < blob.size()) {
+            lowered.assign(blob.data() + 4, nl);
+            cubin.assign(blob.data() + 4 + nl, blob.size() - 4 - nl);
+            from_disk = true;
+        }
+    }
+    if (!from_disk) {
+        auto t0 = std::chrono::steady_clock::now();
+        XTG_TRY(compile(expr, arch, cubin, lowered));
+        auto t1 = std::chrono::steady_clock::now();
+        S.st.compiles++;
+        S.st.compile_seconds += std::chrono::duration<double>(t1 - t0).count();
+        mkdirs(dir);
+        uint32_t nl = (uint32_t)lowered.size();
+        std::string b(4, '\0');
+        memcpy(&b[0], &nl, 4);
+        write_file_atomic(path, b + lowered + cubin);
+    } else {
+        S.st.disk_hits++;
+    }
+    if (dry_run()) {
+        std::unique_ptr<Kernel> k(new Kernel);
+        k->name = expr;
+        k->block = block;
+        k->max_blocks_per_sm = 4;
+        *out = k.get();
+        S.kernels.emplace(expr, std::move(k));
+        return XTG_OK;
+    }
+    CUmodule mod;
+    CUresult cr = drv().ModuleLoadData(&mod, cubin.data());
+    if (cr != CUDA_SUCCESS) {
+        if (from_disk) unlink(path.c_str());
+        return cu_fail(cr, "cuModuleLoadData");
+    }
+    std::unique_ptr<Kernel> k(new Kernel);
+    XTG_CU(drv().ModuleGetFunction(&k->fn, mod, lowered.c_str()));
+    k->name = expr;
+    k->block = block;
+    int nb = 0;
+    if (drv().OccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, block, 0) != CUDA_SUCCESS) nb = 1;
+    k->max_blocks_per_sm = nb > 0 ? nb : 1;
+    *out = k.get();
+    S.kernels.emplace(expr, std::move(k));
+    return XTG_OK;
+}
+
+xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream) {
+    if (grid == 0) return XTG_OK;
+    if (dry_run()) {
+        g_launches.fetch_add(1, std::memory_order_relaxed);
+        return XTG_OK;
+    }
+    void* args[1] = {params};
+    XTG_CU(drv().LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, 0, (CUstream)stream, args, nullptr));
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    return XTG_OK;
+}
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+}  // namespace xtgh
+
+extern "C" xtg_status xtg_get_jit_stats(xtg_jit_stats* st) {
+    if (!st) return xtgh::fail(XTG_ERR_INVALID, "null stats");
+    xtgh::JitState& S = xtgh::js();
+    std::lock_guard<std::mutex> lk(S.mu);
+    *st = S.st;
+    st->launches = xtgh::g_launches.load();
+    return XTG_OK;
+}

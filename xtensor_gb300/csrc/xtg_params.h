@@ -1,0 +1,99 @@
+// xtg_params.h — kernel parameter blocks shared by the host planner and the
+// device code (plain POD, no CUDA qualifiers, so g++ and NVRTC both see the
+// same layout).  Shapes and strides are in elements; offsets are 64-bit.
+#pragma once
+#ifndef XTG_PARAMS_H
+#define XTG_PARAMS_H
+
+namespace xtg {
+
+typedef long long i64;
+typedef unsigned long long u64;
+typedef unsigned int u32;
+
+// Divisor for the multiply-and-shift division of the device code.
+struct FastDiv {
+    u32 d, m, l;
+};
+
+#define XTG_KMAX_RANK 8
+#define XTG_KMAX_LEAVES 8
+#define XTG_KMAX_SCAL 16
+
+struct Scalars {
+    u64 v[XTG_KMAX_SCAL];
+};
+// Iteration space: rank R dims; dim R-1 is the vectorised one.  `shape` holds
+// extents with the innermost one in vectors; `fd` the matching divisors.
+struct Space {
+    i64 shape[XTG_KMAX_RANK];
+    FastDiv fd[XTG_KMAX_RANK];
+    i64 nvec;  // product of shape[] (innermost counted in vectors)
+};
+
+struct AssignParams {
+    Space sp;
+    void* out;
+    i64 out_strides[XTG_KMAX_RANK];
+    const void* leaf[XTG_KMAX_LEAVES];
+    i64 leaf_strides[XTG_KMAX_LEAVES][XTG_KMAX_RANK];
+    Scalars scal;
+};
+
+struct TransposeParams {
+    i64 sa, sb;            // extents of A and B
+    i64 ntile_a, ntile_b;
+    i64 n_tiles;           // nbatch * ntile_a * ntile_b
+    i64 bshape[XTG_KMAX_RANK];  // batch dims (all except A and B), outer first
+    int nbd;
+    void* out;
+    i64 oa, ob;            // destination strides along A, B
+    i64 obs[XTG_KMAX_RANK];     // destination strides over batch dims
+    const void* leaf[XTG_KMAX_LEAVES];
+    i64 la[XTG_KMAX_LEAVES], lb[XTG_KMAX_LEAVES];
+    i64 lbs[XTG_KMAX_LEAVES][XTG_KMAX_RANK];
+    Scalars scal;
+};
+
+struct RedParams {
+    i64 oshape[XTG_KMAX_RANK];
+    FastDiv ofd[XTG_KMAX_RANK];
+    i64 rshape[XTG_KMAX_RANK];
+    FastDiv rfd[XTG_KMAX_RANK];
+    i64 n_out;      // outputs (elements)
+    i64 n_outv;     // output vectors (COL) or outputs (ROW)
+    i64 n_red;      // reduced elements per output
+    i64 n_redv;     // reduced vectors (ROW) or elements (COL)
+    i64 chunk;      // reduced vectors/elements per split
+    i64 nsplit;
+    const void* leaf[XTG_KMAX_LEAVES];
+    i64 lks[XTG_KMAX_LEAVES][XTG_KMAX_RANK];  // leaf strides over kept dims
+    i64 lrs[XTG_KMAX_LEAVES][XTG_KMAX_RANK];  // leaf strides over reduced dims
+    void* out;
+    i64 ostr[XTG_KMAX_RANK];                  // output strides over kept dims
+    void* partial;                            // nsplit > 1: n_out * nsplit states
+    Scalars scal;
+    double init_f;
+    i64 init_i;
+    int has_initial;
+    double initial_f;
+    i64 initial_i;
+    double divisor;  // mean / variance divisor (already integer-divided like the reference)
+};
+
+struct RowParams {
+    i64 n_rows;
+    i64 row_len;
+    i64 oshape[XTG_KMAX_RANK];  // outer (row) dims
+    const void* leaf[XTG_KMAX_LEAVES];
+    i64 lo[XTG_KMAX_LEAVES][XTG_KMAX_RANK];  // leaf strides over outer dims
+    i64 li[XTG_KMAX_LEAVES];                 // leaf stride along the row
+    void* out;
+    i64 oo[XTG_KMAX_RANK];
+    i64 oi;
+    Scalars scal;
+    double div[XTG_KMAX_SCAL];  // per statistic divisor (mean: n, var: n - ddof)
+};
+
+}  // namespace xtg
+#endif

@@ -1,0 +1,71 @@
+// xtg_plan.h — host-side planning of expression trees (internal).
+#pragma once
+
+#include <array>
+#include <string>
+#include <vector>
+
+#include "xtg_internal.h"
+#include "xtg_params.h"
+
+namespace xtgh {
+
+// One node of a parsed expression tree.
+struct PNode {
+    int op = 0;
+    int dtype = -1;   // inferred result type (after fp32 demotion when enabled)
+    int cxx_dtype = -1;  // C++ result type before demotion
+    int arg = 0, aux = 0;
+    xtg_value imm{};
+    std::vector<int> kids;
+    int scal = -1;    // scalar slot
+    int leaf = -1;    // leaf slot (after dedup)
+    int stat = -1;    // row-statistic slot (R* nodes)
+};
+
+struct Tree {
+    std::vector<PNode> nodes;
+    int root = -1;
+    std::vector<xtg_array> leaves;  // deduplicated
+    std::vector<uint64_t> scalars;  // encoded immediates
+    int n_rstats = 0;
+    int rstat_axes = -1;            // trailing-axis count shared by R* nodes
+    bool has_f64_leaf = false;
+    int rank = 0;                   // broadcast rank
+    int64_t shape[XTG_MAX_RANK] = {0};
+};
+
+// Parse + type-check + broadcast.  `demote` enables float32 evaluation of
+// float64 nodes (only when no leaf is float64).
+xtg_status build_tree(const xtg_expr* e, bool demote, Tree& t);
+int promote(int a, int b);
+bool is_rop(int op);
+// Type string of the subtree at node `n` (leaf indices through `leaf_map`).
+std::string tree_type(const Tree& t, int n, const std::vector<int>& leaf_map);
+// Broadcast strides of leaf `l` against the tree's shape (rank t.rank).
+void leaf_bstrides(const Tree& t, int l, int64_t* st);
+// Broadcast strides of array `a` against a target shape of rank `rank`.
+void bstrides_to(const xtg_array& a, int rank, const int64_t* shape, int64_t* st);
+
+// An iteration space with the strides of several arrays over it.
+struct Dims {
+    int R = 0;
+    int64_t shape[XTG_MAX_RANK];
+    std::vector<std::array<int64_t, XTG_MAX_RANK>> st;
+};
+// Drop extent-1 dims and merge dims that are contiguous for every array
+// (row-major order of the merged dims is preserved).
+void collapse(Dims& D);
+xtg::FastDiv make_fd(uint64_t d);
+
+// Scratch for split reductions: stream-ordered allocation unless a fixed
+// buffer is supplied.
+struct ScratchSpec {
+    void* fixed = nullptr;
+    size_t fixed_bytes = 0;
+};
+xtg_status reduce_impl(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, cudaStream_t stream,
+                       const ScratchSpec* scratch);
+xtg_status assign_tree(const Tree& t, const xtg_array* out, cudaStream_t stream);
+
+}  // namespace xtgh

@@ -1,0 +1,131 @@
+"""Evaluation entry points: assign (xt::noalias(out) = e), reductions
+(xt::sum / mean / variance / amax / norm_l2 ... with axes, keep_dims,
+initial, evaluation type T) and arg-reductions (xt::argmax / argmin)."""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, Optional
+
+from ._ffi import ARG_MAX, ARG_MIN, RED, MAX_RANK, ReduceDesc, check, dtype_code, lib
+from .device import DeviceArray, _sh
+from .expr import as_expr, lower
+
+
+def assign(out: DeviceArray, e, stream=None) -> DeviceArray:
+    ex, keep = lower(as_expr(e))
+    o = out.xtg_array()
+    check(lib().xtg_assign(C.byref(ex), C.byref(o), _sh(stream)))
+    return out
+
+
+def broadcast_shape(e) -> tuple:
+    ex, keep = lower(as_expr(e))
+    r = C.c_int32()
+    sh = (C.c_int64 * MAX_RANK)()
+    check(lib().xtg_broadcast_shape(C.byref(ex), C.byref(r), sh))
+    return tuple(sh[i] for i in range(r.value))
+
+
+def expr_dtype(e) -> int:
+    ex, keep = lower(as_expr(e))
+    d = C.c_int32()
+    check(lib().xtg_expr_dtype(C.byref(ex), C.byref(d)))
+    return d.value
+
+
+def make_desc(op: str, axes=None, keep_dims=False, initial=None, acc_dtype=None, ddof=0, precision=0) -> ReduceDesc:
+    rd = ReduceDesc()
+    rd.op = RED[op]
+    if axes is None:
+        rd.n_axes = -1
+    else:
+        if isinstance(axes, int):
+            axes = [axes]
+        axes = list(axes)
+        rd.n_axes = len(axes)
+        for i, a in enumerate(axes):
+            rd.axes[i] = int(a)
+    rd.keep_dims = 1 if keep_dims else 0
+    rd.acc_dtype = -1 if acc_dtype is None else dtype_code(acc_dtype)
+    rd.precision = precision
+    rd.ddof = ddof
+    if initial is not None:
+        rd.has_initial = 1
+        if isinstance(initial, float):
+            rd.initial.f = initial
+        else:
+            rd.initial.i = int(initial)
+    return rd
+
+
+def reduce_shape(op: str, e, **kw):
+    ex, keep = lower(as_expr(e))
+    rd = make_desc(op, **kw)
+    r = C.c_int32()
+    sh = (C.c_int64 * MAX_RANK)()
+    dt = C.c_int32()
+    check(lib().xtg_reduce_shape(C.byref(ex), C.byref(rd), C.byref(r), sh, C.byref(dt)))
+    return tuple(sh[i] for i in range(r.value)), dt.value
+
+
+def reduce(op: str, e, axes=None, keep_dims=False, initial=None, acc_dtype=None, ddof=0, precision=0,
+           out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
+    """Evaluate a reducer into a new (or given) device array."""
+    e = as_expr(e)
+    kw = dict(axes=axes, keep_dims=keep_dims, initial=initial, acc_dtype=acc_dtype, ddof=ddof, precision=precision)
+    if out is None:
+        shape, dt = reduce_shape(op, e, **kw)
+        out = DeviceArray.empty(shape, dt, stream)
+    ex, keep = lower(e)
+    rd = make_desc(op, **kw)
+    o = out.xtg_array()
+    check(lib().xtg_reduce(C.byref(ex), C.byref(rd), C.byref(o), _sh(stream)))
+    return out
+
+
+def argreduce(op: str, e, axis=None, out_dtype="int64", out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
+    from .ops import broadcast_shape as _bs
+    e = as_expr(e)
+    shape = _bs(e)
+    if axis is None or len(shape) <= 1:
+        oshape = ()
+    else:
+        a = axis + len(shape) if axis < 0 else axis
+        oshape = tuple(n for i, n in enumerate(shape) if i != a)
+    if out is None:
+        out = DeviceArray.empty(oshape, out_dtype, stream)
+    ex, keep = lower(e)
+    o = out.xtg_array()
+    code = ARG_MAX if op == "argmax" else ARG_MIN
+    check(lib().xtg_argreduce(C.byref(ex), code, 0 if axis is None else 1, 0 if axis is None else int(axis),
+                              C.byref(o), _sh(stream)))
+    return out
+
+
+def _red(name):
+    def f(e, axes=None, **kw):
+        return reduce(name, e, axes, **kw)
+    f.__name__ = name
+    return f
+
+
+sum = _red("sum")  # noqa: A001
+prod = _red("prod")
+amax = _red("amax")
+amin = _red("amin")
+mean = _red("mean")
+variance = _red("variance")
+stddev = _red("stddev")
+norm_l0 = _red("norm_l0")
+norm_l1 = _red("norm_l1")
+norm_sq = _red("norm_sq")
+norm_l2 = _red("norm_l2")
+norm_linf = _red("norm_linf")
+
+
+def argmax(e, axis=None, **kw):
+    return argreduce("argmax", e, axis, **kw)
+
+
+def argmin(e, axis=None, **kw):
+    return argreduce("argmin", e, axis, **kw)
