@@ -1,0 +1,465 @@
+#!/usr/bin/env python
+"""bench.py — HBM throughput of the assign + reduce hot path on GB300.
+
+Workload (one step): the strided/axis-work configuration — x float32 AND
+float64 of shape (256, 512, 1024), N(0,1), seed 1 — evaluated through the C
+ABI:  t = transpose(x, {2,0,1}) into a contiguous array;
+y = (x - mean(x,{2},keep_dims)) / sqrt(variance(x,{2},keep_dims) + 1e-5);
+amax(x, {0,2}); int32 argmax(x, 1).  Inputs (0.5 / 1 GiB) are larger than
+L2 (129 MB), so no flush is needed between steps.
+
+value      = algorithmic bytes of one step (each input read once, each output
+             written once) / device time per step, GB/s, inputs resident in HBM;
+e2e        = the same metric with host buffers: pinned host->device copies of
+             the inputs and device->host copies of every result inside the
+             timed region;
+roofline   = the dominant kernel's algorithmic GB/s (CUDA events on its
+             launching stream) over the measured HBM copy bandwidth;
+cpu_baseline = the compiled CPU port of the reference's code path
+             (oracle/xt_baseline.c) on the host cores, same workload.
+
+--impl reference times that CPU port alone (the reference itself cannot be
+built: it needs xtl, absent on this image).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SHAPE = (256, 512, 1024)
+N = SHAPE[0] * SHAPE[1] * SHAPE[2]
+METRIC = "HBM GB/s (frac of roofline) assign+reduce; served p50/p99 ms vs plain"
+WORKLOAD = ("strided/axis work: x float32+float64 (256,512,1024) N(0,1) seed 1; transpose {2,0,1} to contiguous; "
+            "y=(x-mean(x,{2},kd))/sqrt(var(x,{2},kd)+1e-5); amax {0,2}; int32 argmax axis 1")
+
+
+def op_bytes(s: int) -> dict:
+    """Algorithmic bytes per op for element size s."""
+    return {
+        "transpose": 2 * N * s,
+        "normalize": 2 * N * s,
+        "amax": N * s + SHAPE[1] * s,
+        "argmax": N * s + SHAPE[0] * SHAPE[2] * 4,
+    }
+
+
+def step_bytes() -> int:
+    return sum(op_bytes(4).values()) + sum(op_bytes(8).values())
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier + max-over-ranks over gloo (timings only: the workload is
+    replicated per GPU, there is no data-path collective)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_info()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
+# ------------------------------------------------------------------------------ clocks
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.12)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------ workload
+def make_inputs():
+    g = np.random.default_rng(1)
+    x32 = g.standard_normal(SHAPE, dtype=np.float32)
+    x64 = g.standard_normal(SHAPE, dtype=np.float64)
+    return x32, x64
+
+
+class GpuStep:
+    """The step as prebuilt C-ABI calls (lowered once, launched every step)."""
+
+    def __init__(self, x32, x64, stream):
+        import xtensor_gb300 as xg
+        from xtensor_gb300 import ops
+        from xtensor_gb300.device import DeviceArray
+        from xtensor_gb300.expr import lower
+
+        self.xg, self.lib = xg, xg.lib()
+        self.stream = stream
+        self.calls = []  # (op name, dtype size, fn)
+        self.keep = []
+        self.dev_in, self.dev_out = [], []
+        for x in (x32, x64):
+            s = x.dtype.itemsize
+            dx = DeviceArray.from_numpy(x)
+            t = DeviceArray.empty((SHAPE[2], SHAPE[0], SHAPE[1]), x.dtype)
+            y = DeviceArray.empty(SHAPE, x.dtype)
+            am = DeviceArray.empty((SHAPE[1],), x.dtype)
+            ai = DeviceArray.empty((SHAPE[0], SHAPE[2]), "int32")
+            self.dev_in.append(dx)
+            self.dev_out.append((t, y, am, ai))
+            e_t, k1 = lower(dx.transpose((2, 0, 1)))
+            o_t = t.xtg_array()
+            e_y, k2 = lower((dx - xg.rmean(dx)) / xg.sqrt(xg.rvar(dx) + 1e-5))
+            o_y = y.xtg_array()
+            e_x, k3 = lower(dx)
+            rd = ops.make_desc("amax", axes=[0, 2])
+            o_am = am.xtg_array()
+            o_ai = ai.xtg_array()
+            self.keep += [e_t, k1, o_t, e_y, k2, o_y, e_x, k3, rd, o_am, o_ai]
+            L, st = self.lib, stream
+            self.calls += [
+                ("transpose", s, lambda e=e_t, o=o_t: L.xtg_assign(C.byref(e), C.byref(o), st)),
+                ("normalize", s, lambda e=e_y, o=o_y: L.xtg_assign(C.byref(e), C.byref(o), st)),
+                ("amax", s, lambda e=e_x, r=rd, o=o_am: L.xtg_reduce(C.byref(e), C.byref(r), C.byref(o), st)),
+                ("argmax", s, lambda e=e_x, o=o_ai: L.xtg_argreduce(C.byref(e), 0, 1, 1, C.byref(o), st)),
+            ]
+
+    def run(self, events=None):
+        from xtensor_gb300._ffi import check
+        for i, (_, _, fn) in enumerate(self.calls):
+            if events is not None:
+                check(self.lib.xtg_event_record(events[i], self.stream))
+            check(fn())
+        if events is not None:
+            check(self.lib.xtg_event_record(events[len(self.calls)], self.stream))
+
+
+def ev_create(lib, n):
+    from xtensor_gb300._ffi import check
+    evs = []
+    for _ in range(n):
+        e = C.c_void_p()
+        check(lib.xtg_event_create(C.byref(e)))
+        evs.append(e.value)
+    return evs
+
+
+def ev_ms(lib, a, b) -> float:
+    from xtensor_gb300._ffi import check
+    f = C.c_float()
+    check(lib.xtg_event_elapsed_ms(a, b, C.byref(f)))
+    return float(f.value)
+
+
+# ------------------------------------------------------------------------------ CPU port
+def cpu_port_time(x32, x64, reps_budget_s=20.0):
+    """Time the compiled CPU port of the reference's path on the host cores."""
+    from oracle.oracle import SO, lib as olib  # noqa: F401
+    olib()
+    L = C.CDLL(str(SO))
+    P = C.c_void_p
+    i64 = C.c_int64
+    for nm in ("transpose_201", "amax_02"):
+        for t in ("f32", "f64"):
+            getattr(L, f"bl_{nm}_{t}").argtypes = [P, P, i64, i64, i64]
+    for t in ("f32", "f64"):
+        getattr(L, f"bl_normalize_{t}").argtypes = [P, P, i64, i64, C.c_double]
+        getattr(L, f"bl_argmax_1_{t}").argtypes = [P, P, i64, i64, i64, P]
+    outs = {}
+    for x in (x32, x64):
+        outs[x.dtype.itemsize] = dict(
+            t=np.empty((SHAPE[2], SHAPE[0], SHAPE[1]), x.dtype), y=np.empty(SHAPE, x.dtype),
+            am=np.empty((SHAPE[1],), x.dtype), ai=np.empty((SHAPE[0], SHAPE[2]), np.int32),
+            tmp=np.empty((SHAPE[0], SHAPE[2], SHAPE[1]), x.dtype))
+
+    def one():
+        t0 = time.perf_counter()
+        for x in (x32, x64):
+            tn = "f32" if x.dtype == np.float32 else "f64"
+            o = outs[x.dtype.itemsize]
+            d0, d1, d2 = SHAPE
+            getattr(L, f"bl_transpose_201_{tn}")(x.ctypes.data, o["t"].ctypes.data, d0, d1, d2)
+            getattr(L, f"bl_normalize_{tn}")(x.ctypes.data, o["y"].ctypes.data, d0 * d1, d2, 1e-5)
+            getattr(L, f"bl_amax_02_{tn}")(x.ctypes.data, o["am"].ctypes.data, d0, d1, d2)
+            getattr(L, f"bl_argmax_1_{tn}")(x.ctypes.data, o["ai"].ctypes.data, d0, d1, d2, o["tmp"].ctypes.data)
+        return time.perf_counter() - t0
+
+    times = [one()]
+    while sum(times) < reps_budget_s and len(times) < 3:
+        times.append(one())
+    return min(times), len(times), outs
+
+
+def cores() -> int:
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+# ------------------------------------------------------------------------------ arms
+def run_reference(args):
+    ws, rank, local = dist_info()
+    if rank != 0:
+        return 0
+    x32, x64 = make_inputs()
+    total = step_bytes()
+    times = []
+    for i in range(args.warmup + args.steps):
+        t, _, _ = cpu_port_time(x32, x64, reps_budget_s=0.0)
+        if i >= args.warmup:
+            times.append(t)
+    sec = statistics.median(times)
+    val = total / sec / 1e9
+    line = {
+        "metric": METRIC, "value": round(val, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32,f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": WORKLOAD, "elements": N, "algorithmic_bytes_per_step": total},
+        "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": cores(), "kind": "port",
+                         "sample": "full workload per step (compiled C port of the reference's loops, OpenMP)"},
+        "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference itself cannot be built (xtl 0.8.0 is absent); oracle/xt_baseline.c restates its code path",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import xtensor_gb300 as xg
+    from xtensor_gb300._ffi import check
+
+    D = Dist()
+    xg.init(D.local)
+    lib = xg.lib()
+    st = C.c_void_p()
+    check(lib.xtg_stream_create(C.byref(st)))
+    stream = st.value
+    x32, x64 = make_inputs()
+    step = GpuStep(x32, x64, stream)
+    nops = len(step.calls)
+    for _ in range(args.warmup):
+        step.run()
+    check(lib.xtg_stream_sync(stream))
+
+    # ---- device-resident timing
+    evs = [ev_create(lib, nops + 1) for _ in range(args.steps)]
+    per_op = [0.0] * nops
+    t0, t1 = ev_create(lib, 2)
+    clocks = Clocks(D.local)
+    clocks.start()
+    time.sleep(0.15)
+    D.barrier()
+    check(lib.xtg_device_sync())
+    l0 = xg.jit_stats()["launches"]
+    check(lib.xtg_event_record(t0, stream))
+    for k in range(args.steps):
+        step.run(evs[k])
+    check(lib.xtg_event_record(t1, stream))
+    check(lib.xtg_event_sync(t1))
+    check(lib.xtg_device_sync())
+    l1 = xg.jit_stats()["launches"]
+    D.barrier()
+    clk = clocks.stop()
+    for k in range(args.steps):
+        for i in range(nops):
+            per_op[i] += ev_ms(lib, evs[k][i], evs[k][i + 1])
+    kern_ms = sum(per_op) / args.steps  # device time inside the kernels
+    wall_ms = ev_ms(lib, t0, t1) / args.steps
+    ms = D.max(wall_ms)
+    total = step_bytes() * D.ws
+    value = total / (ms / 1e3) / 1e9
+
+    # dominant kernel
+    names = [f"{nm}_{'f32' if s == 4 else 'f64'}" for nm, s, _ in step.calls]
+    avg = [t / args.steps for t in per_op]
+    dom = int(np.argmax(avg))
+    nm, s, _ = step.calls[dom]
+    dom_bytes = op_bytes(s)[nm]
+    achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(names[dom])
+        except Exception:
+            traffic = None
+    per_kernel = {names[i]: {"ms": round(avg[i], 4), "GB/s": round(op_bytes(step.calls[i][1])[step.calls[i][0]] / (avg[i] / 1e3) / 1e9, 1),
+                             "frac": round(op_bytes(step.calls[i][1])[step.calls[i][0]] / (avg[i] / 1e3) / 1e9 / peak, 3)}
+                  for i in range(nops)}
+
+    # ---- end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(lib, step, x32, x64, stream, max(1, min(args.steps, 5)), D)
+
+    # ---- CPU baseline (rank 0, N=1)
+    cpu = None
+    if D.rank == 0 and D.ws == 1 and not args.no_cpu:
+        sec, reps, _ = cpu_port_time(x32, x64)
+        cpu = {"value": round(step_bytes() / sec / 1e9, 3), "unit": "GB/s", "cores": cores(), "kind": "port",
+               "sample": f"full workload, best of {reps} (compiled C port of the reference's loops, OpenMP {cores()} threads)"}
+
+    if D.rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": D.ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32,f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "elements": N, "algorithmic_bytes_per_step": step_bytes(),
+                       "l2": "inputs (512 MiB f32, 1 GiB f64) larger than L2 (129 MB): no flush",
+                       "parallelism": f"replicas x{D.ws}", "kernel_ms_per_step": round(kern_ms, 4)},
+            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6800 GB/s"},
+            "per_kernel": per_kernel,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(l1 - l0),
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    return 0
+
+
+def run_e2e(lib, step, x32, x64, stream, steps, D):
+    from xtensor_gb300._ffi import check
+    H2D, D2H = 1, 2
+    hin, hout = [], []
+    for x, dx in zip((x32, x64), step.dev_in):
+        p = C.c_void_p()
+        check(lib.xtg_host_alloc(C.byref(p), x.nbytes))
+        C.memmove(p.value, x.ctypes.data, x.nbytes)
+        hin.append((p.value, dx.ptr, x.nbytes))
+    for outs in step.dev_out:
+        for o in outs:
+            p = C.c_void_p()
+            check(lib.xtg_host_alloc(C.byref(p), o.nbytes))
+            hout.append((p.value, o.ptr, o.nbytes))
+    h2d = sum(n for _, _, n in hin)
+    d2h = sum(n for _, _, n in hout)
+
+    def one():
+        for h, d, n in hin:
+            check(lib.xtg_memcpy(d, h, n, H2D, stream))
+        step.run()
+        for h, d, n in hout:
+            check(lib.xtg_memcpy(h, d, n, D2H, stream))
+
+    one()
+    check(lib.xtg_stream_sync(stream))
+    t0, t1 = ev_create(lib, 2)
+    D.barrier()
+    check(lib.xtg_event_record(t0, stream))
+    for _ in range(steps):
+        one()
+    check(lib.xtg_event_record(t1, stream))
+    check(lib.xtg_event_sync(t1))
+    ms = D.max(ev_ms(lib, t0, t1) / steps)
+    for h, _, _ in hin + hout:
+        lib.xtg_host_free(h)
+    return {"value": round(step_bytes() * D.ws / (ms / 1e3) / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": round(ms, 3), "steps": steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="xtg", choices=["xtg", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--shape", default=None, help="profiling only: d0,d1,d2 instead of 256,512,1024")
+    args = ap.parse_args()
+    if args.shape:
+        global SHAPE, N
+        SHAPE = tuple(int(v) for v in args.shape.split(","))
+        N = SHAPE[0] * SHAPE[1] * SHAPE[2]
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    from xtensor_gb300.build import build
+    build()
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -205,6 +205,14 @@ xtg_status xtg_stream_sync(xtg_stream stream);
 xtg_status xtg_device_sync(void);
 size_t xtg_dtype_size(int32_t dtype);
 
+/* CUDA events (timing on the launching stream). */
+typedef void* xtg_event;
+xtg_status xtg_event_create(xtg_event* ev);
+xtg_status xtg_event_destroy(xtg_event ev);
+xtg_status xtg_event_record(xtg_event ev, xtg_stream stream);
+xtg_status xtg_event_sync(xtg_event ev);
+xtg_status xtg_event_elapsed_ms(xtg_event start, xtg_event end, float* ms);
+
 /* ---- shape algebra ----------------------------------------------------------- */
 /* Broadcast shape of all leaves (right-aligned, size-1 / missing dims
  * broadcast), XTG_ERR_BROADCAST otherwise. */

@@ -1,0 +1,138 @@
+/*
+ * xt_baseline.c — compiled CPU port of the reference's code path for the
+ * benchmark workloads.  TEST / BASELINE INFRASTRUCTURE ONLY: timed as the
+ * CPU baseline by bench.py (and cross-checked against the GPU by tests); the
+ * product library never uses it.
+ *
+ * Each routine restates what xtensor 0.27.1 executes for the call, in the
+ * same loop order and arithmetic types, compiled -O2 with OpenMP over the
+ * loops the reference parallelises (assignment: xassign.hpp:725-842,
+ * 1148-1286) and — more generously than the reference, whose lazy reducers
+ * are single-threaded — over independent reduction outputs:
+ *
+ *   bl_transpose_201_*  xt::xarray<T> t = xt::transpose(x, {2, 0, 1});
+ *                       the stepper_assigner walks the destination in
+ *                       row-major order reading the permuted source
+ *                       (xassign.hpp:644-695, 1087, 1341).
+ *   bl_normalize_*      (x - mean(x,{2},keep_dims)) / sqrt(variance(x,{2},keep_dims) + eps):
+ *                       mean = sum in T (sequential) / (double)n
+ *                       (xmath.hpp:1828-1858); variance = mean of
+ *                       square(x - mean) in double (xmath.hpp:2082-2103);
+ *                       the elementwise tree in double, stored as T.
+ *   bl_amax_02_*        xt::amax(x, {0, 2}): per output, innermost axis folds
+ *                       select(acc > v) from lowest(), outer axis merges
+ *                       (xreducer.hpp:1801-1828, xmath.hpp:589-602, 777-793).
+ *   bl_argmax_1_*       xt::argmax(x, 1): a transposed copy moving axis 1
+ *                       last, then a strict-greater scan per row
+ *                       (xsort.hpp:1158-1235).
+ *   bl_c0_*             E = A * b + exp(-A * A); r = sum(E, {1}).
+ *   bl_sum_*            full sums (sequential, as the lazy reducer).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define DEF_TRANSPOSE(T, NAME)                                                           \
+    void bl_transpose_201_##NAME(const T* x, T* out, int64_t d0, int64_t d1, int64_t d2) { \
+        _Pragma("omp parallel for schedule(static)")                                      \
+        for (int64_t k = 0; k < d2; ++k) {                                                 \
+            T* o = out + k * d0 * d1;                                                      \
+            for (int64_t i = 0; i < d0; ++i)                                               \
+                for (int64_t j = 0; j < d1; ++j) o[i * d1 + j] = x[(i * d1 + j) * d2 + k];  \
+        }                                                                                  \
+    }
+DEF_TRANSPOSE(float, f32)
+DEF_TRANSPOSE(double, f64)
+
+#define DEF_NORMALIZE(T, NAME)                                                                   \
+    void bl_normalize_##NAME(const T* x, T* y, int64_t rows, int64_t n, double eps) {            \
+        _Pragma("omp parallel for schedule(static)")                                              \
+        for (int64_t r = 0; r < rows; ++r) {                                                       \
+            const T* xr = x + r * n;                                                               \
+            T s = 0;                                                                               \
+            for (int64_t k = 0; k < n; ++k) s = s + xr[k];                                         \
+            double mean = (double)s / (double)n;                                                   \
+            double q = 0;                                                                          \
+            for (int64_t k = 0; k < n; ++k) {                                                      \
+                double d = (double)xr[k] - mean;                                                   \
+                q = q + d * d;                                                                     \
+            }                                                                                      \
+            double var = q / (double)n;                                                            \
+            double den = sqrt(var + eps);                                                          \
+            T* yr = y + r * n;                                                                     \
+            for (int64_t k = 0; k < n; ++k) yr[k] = (T)(((double)xr[k] - mean) / den);             \
+        }                                                                                          \
+    }
+DEF_NORMALIZE(float, f32)
+DEF_NORMALIZE(double, f64)
+
+#define DEF_AMAX(T, NAME, LOWEST)                                                        \
+    void bl_amax_02_##NAME(const T* x, T* out, int64_t d0, int64_t d1, int64_t d2) {     \
+        _Pragma("omp parallel for schedule(static)")                                      \
+        for (int64_t j = 0; j < d1; ++j) {                                                 \
+            T res = 0;                                                                     \
+            for (int64_t i = 0; i < d0; ++i) {                                             \
+                const T* row = x + (i * d1 + j) * d2;                                      \
+                T acc = LOWEST;                                                            \
+                for (int64_t k = 0; k < d2; ++k) acc = acc > row[k] ? acc : row[k];        \
+                res = i == 0 ? acc : (res > acc ? res : acc);                              \
+            }                                                                              \
+            out[j] = res;                                                                  \
+        }                                                                                  \
+    }
+DEF_AMAX(float, f32, -3.40282346638528859812e+38f)
+DEF_AMAX(double, f64, -1.7976931348623157e+308)
+
+#define DEF_ARGMAX(T, NAME)                                                                          \
+    void bl_argmax_1_##NAME(const T* x, int32_t* out, int64_t d0, int64_t d1, int64_t d2, T* tmp) {  \
+        /* eval_type input = transpose(e, {0, 2, 1}) */                                              \
+        _Pragma("omp parallel for schedule(static)")                                                  \
+        for (int64_t i = 0; i < d0; ++i)                                                               \
+            for (int64_t k = 0; k < d2; ++k)                                                           \
+                for (int64_t j = 0; j < d1; ++j) tmp[(i * d2 + k) * d1 + j] = x[(i * d1 + j) * d2 + k]; \
+        _Pragma("omp parallel for schedule(static)")                                                  \
+        for (int64_t r = 0; r < d0 * d2; ++r) {                                                        \
+            const T* row = tmp + r * d1;                                                               \
+            T v = row[0];                                                                              \
+            int64_t idx = 0;                                                                           \
+            for (int64_t j = 1; j < d1; ++j)                                                           \
+                if (row[j] > v) {                                                                      \
+                    v = row[j];                                                                        \
+                    idx = j;                                                                           \
+                }                                                                                      \
+            out[r] = (int32_t)idx;                                                                     \
+        }                                                                                              \
+    }
+DEF_ARGMAX(float, f32)
+DEF_ARGMAX(double, f64)
+
+void bl_c0_assign(const float* A, const float* b, float* E, int64_t n, int64_t m) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t j = 0; j < m; ++j) {
+            float a = A[i * m + j];
+            E[i * m + j] = a * b[j] + expf(-a * a);
+        }
+}
+
+void bl_c0_sum(const float* E, float* r, int64_t n, int64_t m) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        float s = 0.f;
+        for (int64_t j = 0; j < m; ++j) s = s + E[i * m + j];
+        r[i] = s;
+    }
+}
+
+float bl_sum_f32(const float* x, int64_t n) {
+    float s = 0.f;
+    for (int64_t i = 0; i < n; ++i) s = s + x[i];
+    return s;
+}
+
+int64_t bl_sum_i32_i64(const int32_t* x, int64_t n) {
+    int64_t s = 0;
+    for (int64_t i = 0; i < n; ++i) s += x[i];
+    return s;
+}

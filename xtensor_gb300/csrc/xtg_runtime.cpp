@@ -298,6 +298,36 @@ xtg_status xtg_device_sync(void) {
 
 size_t xtg_dtype_size(int32_t dtype) { return valid_dtype(dtype) ? (size_t)dt(dtype).size : 0; }
 
+xtg_status xtg_event_create(xtg_event* ev) {
+    if (!ev) return fail(XTG_ERR_INVALID, "null event");
+    XTG_TRY(ensure_device(nullptr));
+    cudaEvent_t e;
+    XTG_CUDA(cudaEventCreate(&e));
+    *ev = (xtg_event)e;
+    return XTG_OK;
+}
+
+xtg_status xtg_event_destroy(xtg_event ev) {
+    if (ev) XTG_CUDA(cudaEventDestroy((cudaEvent_t)ev));
+    return XTG_OK;
+}
+
+xtg_status xtg_event_record(xtg_event ev, xtg_stream stream) {
+    XTG_CUDA(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)stream));
+    return XTG_OK;
+}
+
+xtg_status xtg_event_sync(xtg_event ev) {
+    XTG_CUDA(cudaEventSynchronize((cudaEvent_t)ev));
+    return XTG_OK;
+}
+
+xtg_status xtg_event_elapsed_ms(xtg_event start, xtg_event end, float* ms) {
+    if (!ms) return fail(XTG_ERR_INVALID, "null output");
+    XTG_CUDA(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)end));
+    return XTG_OK;
+}
+
 xtg_status xtg_set_option(const char* key, int64_t value) {
     if (!key) return fail(XTG_ERR_INVALID, "null key");
     std::lock_guard<std::mutex> lk(g_opt_mu);
