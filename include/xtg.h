@@ -239,6 +239,25 @@ xtg_status xtg_reduce(const xtg_expr* e, const xtg_reduce_desc* rd,
 xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis,
                          const xtg_array* out, xtg_stream stream);
 
+/* ---- reduction without allocation ------------------------------------------------
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory while they reduce — code running during CUDA stream capture (where
+ * cudaMalloc is not permitted), code whose device memory is owned by its own
+ * allocator or budget, loops that must never enter an allocator.
+ * Sum of the n contiguous float32 values at device pointer x, written to the
+ * float at device pointer out — the same kernels and plan as xtg_reduce(sum,
+ * all axes) on that array, with the split-reduction partials in a static
+ * device buffer of XTG_NOALLOC_SCRATCH_BYTES (every GPU the library is used
+ * on keeps it until exit).  Inputs whose plan would need more partials than
+ * the buffer holds, or more than 2^32 vectors, are rejected with
+ * XTG_ERR_UNSUPPORTED.  The first call on a device resolves the buffer's
+ * address (cudaGetSymbolAddress, which also loads the library's device code):
+ * make that first call before any stream capture.  All calls share the
+ * buffer: calls whose kernels may overlap on the GPU (unordered streams) race
+ * and must be serialised by the caller. */
+#define XTG_NOALLOC_SCRATCH_BYTES (256u * 1024u)
+xtg_status xtg_sum_f32_noalloc(const float* x, int64_t n, float* out, xtg_stream stream);
+
 /* ---- kernel cache / tuning ------------------------------------------------------ */
 typedef struct {
     int64_t compiles;       /* NVRTC compilations this process */
