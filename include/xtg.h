@@ -267,6 +267,9 @@ typedef struct {
     int64_t launches;       /* kernels launched through this library */
 } xtg_jit_stats;
 xtg_status xtg_get_jit_stats(xtg_jit_stats* st);
+/* Kernel names ("k_assign<...>;k_reduce_combine<...>") launched by the last
+ * evaluation call on this thread — introspection for tests and tuning. */
+const char* xtg_last_kernels(void);
 /* Integer knobs: "assign.block", "assign.unroll", "assign.ctas_per_sm",
  * "reduce.block", "reduce.chunk", "transpose.tile", "batch.*" … ; value < 0 resets. */
 xtg_status xtg_set_option(const char* key, int64_t value);

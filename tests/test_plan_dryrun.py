@@ -1,0 +1,107 @@
+"""Planning and kernel compilation without a GPU.
+
+In dry-run mode libxtg plans every call against a GB300-shaped device,
+compiles the chosen kernel instantiations with NVRTC for sm_103a and skips
+the launch.  These tests check which kernel family each workload of the
+benchmark configurations lowers to, and that every one of them compiles."""
+from __future__ import annotations
+
+import pytest
+
+import xtensor_gb300 as xg
+from xtensor_gb300 import ops
+from xtensor_gb300._ffi import last_kernels
+from xtensor_gb300.device import DeviceArray
+
+
+@pytest.fixture(autouse=True)
+def dry():
+    xg.set_option("jit.dry_run", 1)
+    yield
+    xg.set_option("jit.dry_run", -1)
+
+
+_next = [0x100000000]
+
+
+def fake(shape, dtype):
+    p = _next[0]
+    _next[0] += 1 << 36
+    return DeviceArray(shape, dtype, p)
+
+
+def fam(names):
+    return [n.split("<", 1)[0] for n in names]
+
+
+def test_c0_plain_small():
+    A, b = fake((2048, 2048), "float32"), fake((2048,), "float32")
+    E = fake((2048, 2048), "float32")
+    xg.assign(E, A * b + xg.exp(-A * A))
+    ks = last_kernels()
+    assert fam(ks) == ["k_assign"]
+    assert ", 4, 2, " in ks[0]  # 16-byte vectors over a 2-D (rows x 2048) space
+    r = fake((2048,), "float32")
+    ops.reduce("sum", A * b + xg.exp(-A * A), [1], out=r)  # E not materialised
+    assert fam(last_kernels()) == ["k_reduce_row"]
+    assert "AccSumC" in last_kernels()[0]
+
+
+@pytest.mark.parametrize("dt", ["float32", "float64"])
+def test_c1_strided_axis(dt):
+    x = fake((256, 512, 1024), dt)
+    t = fake((1024, 256, 512), dt)
+    xg.assign(t, x.transpose((2, 0, 1)))
+    assert fam(last_kernels()) == ["k_transpose"]
+    y = fake((256, 512, 1024), dt)
+    xg.assign(y, (x - xg.rmean(x)) / xg.sqrt(xg.rvar(x) + 1e-5))
+    ks = last_kernels()
+    assert fam(ks) == ["k_rowfused"] and "RStat<0, 1" in ks[0] and "RStat<1, 2" in ks[0]
+    am = fake((512,), dt)
+    ops.reduce("amax", x, [0, 2], out=am)
+    assert fam(last_kernels())[0] == "k_reduce_row"
+    ai = fake((256, 1024), "int32")
+    ops.argreduce("argmax", x, 1, out=ai)
+    assert fam(last_kernels())[0] == "k_reduce_col"
+
+
+def test_c2_precision_full_reductions():
+    n = 1 << 28
+    for dt, acc in [("float32", "AccSumC"), ("bfloat16", "AccSumC")]:
+        x = fake((n,), dt)
+        out = fake((), "float32")
+        ops.reduce("sum", x, out=out)
+        ks = last_kernels()
+        assert fam(ks) == ["k_reduce_row", "k_reduce_combine"] and acc in ks[0]
+        for op, a in [("mean", "AccSumC"), ("variance", "AccMom<float, 1>"), ("norm_l2", "AccNormC<2>")]:
+            o = fake((), "float64")
+            ops.reduce(op, x, out=o)
+            assert a in last_kernels()[0], (op, last_kernels())
+    xi = fake((n,), "int32")
+    o = fake((), "int64")
+    ops.reduce("sum", xi, acc_dtype="int64", out=o)
+    assert "AccPlain<long long, 0>" in last_kernels()[0]
+
+
+def test_views_and_broadcast_plans():
+    x = fake((64, 48), "float32")
+    o = fake((32, 40), "float32")
+    xg.assign(o, x[::2, 3:43] + xg.scalar(1.0, "float32"))
+    assert fam(last_kernels()) == ["k_assign"]
+    o2 = fake((48, 64), "float32")
+    xg.assign(o2, x.transpose() * xg.scalar(2.0, "float32"))
+    assert fam(last_kernels()) == ["k_transpose"]
+
+
+def test_type_and_shape_errors_are_reported_before_launch():
+    a = fake((3, 4), "float32")
+    b = fake((5,), "float32")
+    with pytest.raises(xg.XtgError) as ei:
+        xg.assign(fake((3, 4), "float32"), a + b)
+    assert ei.value.status == 2
+    with pytest.raises(xg.XtgError) as ei:
+        ops.reduce("sum", a, [1, 0], out=fake((), "float32"))
+    assert ei.value.status == 3
+    with pytest.raises(xg.XtgError) as ei:
+        xg.assign(fake((3, 4), "float32"), a % a)
+    assert ei.value.status == 1

@@ -157,6 +157,8 @@ def _extend_signatures(L) -> None:
         "xtg_event_record": (st, [vp, vp]),
         "xtg_event_elapsed_ms": (st, [vp, vp, C.POINTER(C.c_float)]),
         "xtg_event_sync": (st, [vp]),
+        "xtg_last_kernels": (C.c_char_p, []),
+        "xtg_sum_f32_noalloc": (st, [vp, i64, vp, vp]),
     }
     for name, (res, args) in extra.items():
         f = getattr(L, name, None)
@@ -173,6 +175,12 @@ def check(status: int) -> None:
 
 def set_option(key: str, value: int) -> None:
     check(lib().xtg_set_option(key.encode(), int(value)))
+
+
+def last_kernels() -> list[str]:
+    """Kernels launched by the last evaluation call on this thread."""
+    s = lib().xtg_last_kernels().decode()
+    return [k for k in s.split(";") if k]
 
 
 def jit_stats() -> dict:

@@ -423,6 +423,7 @@ extern "C" xtg_status xtg_assign(const xtg_expr* e, const xtg_array* out, xtg_st
     if (!out) return fail(XTG_ERR_INVALID, "null destination");
     if (!valid_dtype(out->dtype) || out->rank < 0 || out->rank > XTG_MAX_RANK)
         return fail(XTG_ERR_INVALID, "bad destination descriptor");
+    begin_call();
     Tree t;
     const bool demote = opt("fp32_compute", 1) != 0 && out->dtype != XTG_FLOAT64;
     XTG_TRY(build_tree(e, demote, t));

@@ -89,6 +89,8 @@ struct Kernel {
 xtg_status get_kernel(const std::string& expr, int block, Kernel** k);
 xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream);
 void count_launch();
+// Resets the per-thread record of launched kernels (start of an API call).
+void begin_call();
 
 // ---- scratch ---------------------------------------------------------------------
 xtg_status scratch_alloc(void** p, size_t bytes, cudaStream_t s);

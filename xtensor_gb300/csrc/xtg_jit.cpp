@@ -122,12 +122,18 @@ xtg_status compile(const std::string& expr, const std::string& arch, std::string
 
 }  // namespace
 
+static thread_local std::string t_last_kernels;
+
+void begin_call() { t_last_kernels.clear(); }
+
 xtg_status get_kernel(const std::string& expr, int block, Kernel** out) {
     DeviceInfo* dev;
     XTG_TRY(ensure_device(&dev));
     JitState& S = js();
     std::lock_guard<std::mutex> lk(S.mu);
-    auto it = S.kernels.find(expr);
+    // dry-run kernels have no function handle: keep them apart
+    const std::string key = dry_run() ? "dry:" + expr : expr;
+    auto it = S.kernels.find(key);
     if (it != S.kernels.end()) {
         S.st.memory_hits++;
         *out = it->second.get();
@@ -175,7 +181,7 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out) {
         k->block = block;
         k->max_blocks_per_sm = 4;
         *out = k.get();
-        S.kernels.emplace(expr, std::move(k));
+        S.kernels.emplace(key, std::move(k));
         return XTG_OK;
     }
     CUmodule mod;
@@ -192,12 +198,14 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out) {
     if (drv().OccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, block, 0) != CUDA_SUCCESS) nb = 1;
     k->max_blocks_per_sm = nb > 0 ? nb : 1;
     *out = k.get();
-    S.kernels.emplace(expr, std::move(k));
+    S.kernels.emplace(key, std::move(k));
     return XTG_OK;
 }
 
 xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream) {
     if (grid == 0) return XTG_OK;
+    if (!t_last_kernels.empty()) t_last_kernels += ";";
+    t_last_kernels += k->name.compare(0, 5, "xtg::") == 0 ? k->name.substr(5) : k->name;
     if (dry_run()) {
         g_launches.fetch_add(1, std::memory_order_relaxed);
         return XTG_OK;
@@ -211,6 +219,8 @@ xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaSt
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 }  // namespace xtgh
+
+extern "C" const char* xtg_last_kernels(void) { return xtgh::t_last_kernels.c_str(); }
 
 extern "C" xtg_status xtg_get_jit_stats(xtg_jit_stats* st) {
     if (!st) return xtgh::fail(XTG_ERR_INVALID, "null stats");

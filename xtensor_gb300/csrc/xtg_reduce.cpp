@@ -507,11 +507,13 @@ xtg_status xtg_reduce_acc_dtype(const xtg_expr* e, const xtg_reduce_desc* rd, in
 }
 
 xtg_status xtg_reduce(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, xtg_stream stream) {
+    begin_call();
     return reduce_impl(e, rd, out, (cudaStream_t)stream, nullptr);
 }
 
 xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis, const xtg_array* out,
                          xtg_stream stream) {
+    begin_call();
     return argreduce_impl(e, op, has_axis, axis, out, (cudaStream_t)stream);
 }
 
