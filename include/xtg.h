@@ -204,6 +204,10 @@ xtg_status xtg_stream_destroy(xtg_stream stream);
 xtg_status xtg_stream_sync(xtg_stream stream);
 xtg_status xtg_device_sync(void);
 size_t xtg_dtype_size(int32_t dtype);
+/* Kernels never trap: a bounded wait that gives up sets a device error word
+ * and the kernel returns.  This synchronises the device, reads and clears
+ * the word: XTG_ERR_TIMEOUT if it was set. */
+xtg_status xtg_check_device_errors(void);
 
 /* CUDA events (timing on the launching stream). */
 typedef void* xtg_event;

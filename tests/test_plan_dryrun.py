@@ -56,7 +56,10 @@ def test_c1_strided_axis(dt):
     y = fake((256, 512, 1024), dt)
     xg.assign(y, (x - xg.rmean(x)) / xg.sqrt(xg.rvar(x) + 1e-5))
     ks = last_kernels()
-    assert fam(ks) == ["k_rowfused"] and "RStat<0, 1" in ks[0] and "RStat<1, 2" in ks[0]
+    # rows of 1024 contiguous elements: the bulk-copy (TMA) double-buffered variant
+    assert fam(ks) == ["k_rowfused_tma"] and "RStat<0, 1" in ks[0] and "RStat<1, 2" in ks[0]
+    if dt == "float64":
+        assert "FmaRecipSub<double" in ks[0]
     am = fake((512,), dt)
     ops.reduce("amax", x, [0, 2], out=am)
     assert fam(last_kernels())[0] == "k_reduce_row"

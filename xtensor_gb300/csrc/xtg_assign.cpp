@@ -183,7 +183,11 @@ xtg_status assign_tree(const Tree& t, const xtg_array* out, cudaStream_t stream)
             if (l != tl) order.push_back(l);
         std::vector<int> map(NL), kinds(NL, 2);
         for (int i = 0; i < NL; ++i) map[order[i]] = i;
-        const int TILE = 32, ROWS = 8;
+        // 64-wide tiles for <= 4-byte elements (256 B per warp row access),
+        // 32-wide for 8-byte ones
+        const int esz = dt(t.leaves[tl].dtype).size;
+        const int TILE = esz <= 4 ? (int)opt("transpose.tile_small", 64) : 32;
+        const int ROWS = esz <= 4 ? 256 / TILE : 8;
         xtg::TransposeParams p;
         memset(&p, 0, sizeof p);
         p.sa = D.shape[ta];
@@ -402,10 +406,47 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
             div = n_rows ? (double)((total - ddof) / n_rows) : 0.0;
         }
         p.div[x.stat] = div;
+        p.rdiv[x.stat] = 1.0 / div;
+        p.fdiv[x.stat] = (float)div;
     }
+    p.rrow_len = 1.0 / (double)row_len;
+    p.frow_len = (float)row_len;
     sl += ">";
-    std::string name = "xtg::k_rowfused<" + tree_type(t, t.root, map) + ", " + sl + ", " + leafset(t, order, kinds) +
-                       ", " + dt(out.dtype).cname + ", " + std::to_string(vec) + ", " + std::to_string(nv) + ", " +
+    const bool recip = opt("row.recip_div_f64", 1) != 0;
+    const std::string tree = tree_type(t, t.root, map, recip);
+
+    // Bulk-copy variant: every leaf contiguous along the row, 16-byte rows,
+    // warp-sized groups, output contiguous along the row.
+    bool tma = opt("row.tma", 1) != 0 && group == 32 && li[0] == 1 && NL > 0;
+    unsigned buf_bytes = 0;
+    for (int l = 0; tma && l < NL; ++l) {
+        const int sz = dt(t.leaves[l].dtype).size;
+        const int64_t rb = row_len * sz;
+        if (kinds[l] != 0 || rb % 16 || !aligned(t.leaves[l].data, 16)) tma = false;
+        for (int d = 0; tma && d < D.R; ++d)
+            if ((D.st[1 + l][d] * sz) % 16) tma = false;
+        if (tma) {
+            p.loff[l] = buf_bytes;
+            p.lbytes[l] = (unsigned)rb;
+            buf_bytes += (unsigned)rb;
+        }
+    }
+    const int tma_block = 128;
+    const size_t dyn = (size_t)buf_bytes * 2 * (tma_block / 32);
+    if (tma && dyn > 200 * 1024) tma = false;
+    if (tma) {
+        p.buf_bytes = buf_bytes;
+        XTG_TRY(device_error_word(&p.err));
+        std::string name = "xtg::k_rowfused_tma<" + tree + ", " + sl + ", " + leafset(t, order, kinds) + ", " +
+                           dt(out.dtype).cname + ", " + std::to_string(vec) + ", " + std::to_string(nv) + ", " +
+                           std::to_string(D.R) + ", " + std::to_string(t.n_rstats) + ">";
+        Kernel* kr;
+        XTG_TRY(get_kernel(name, tma_block, &kr, dyn));
+        int64_t need = (n_rows + 3) / 4;
+        return launch(kr, grid_for(kr, need), tma_block, &p, stream, dyn);
+    }
+    std::string name = "xtg::k_rowfused<" + tree + ", " + sl + ", " + leafset(t, order, kinds) + ", " +
+                       dt(out.dtype).cname + ", " + std::to_string(vec) + ", " + std::to_string(nv) + ", " +
                        std::to_string(group) + ", " + std::to_string(D.R) + ", " + std::to_string(t.n_rstats) + ">";
     const int block = 256;
     Kernel* kr;

@@ -283,8 +283,9 @@ template <class... S> struct LoadLeaves<LeafSet<S...>> {
 // Evaluation context: scalar immediates plus row statistics (for the fused
 // row kernels).  Nodes evaluate at vector lane j.
 template <int NSTAT> struct Ctx {
-    const Scalars* scal;
-    double stat[NSTAT > 0 ? NSTAT : 1];
+    Scalars scal;  // by value: immediates live in registers, conversions hoist
+    double stat[NSTAT > 0 ? NSTAT : 1];   // row statistics (FP64 consumers)
+    float statf[NSTAT > 0 ? NSTAT : 1];   // the same, rounded once (FP32 consumers)
 };
 
 // Leaves / scalars / row statistics as tree terminals.
@@ -294,12 +295,18 @@ template <int I, class T> struct L {
 };
 template <int K, class T> struct S {
     typedef T type;
-    template <class RG, class C> static XTG_DI T ev(const RG&, int, const C& c) { return scalar_as<T>(*c.scal, K); }
+    template <class RG, class C> static XTG_DI T ev(const RG&, int, const C& c) { return scalar_as<T>(c.scal, K); }
 };
 // A row statistic produced by a fused row reducer (index K of Ctx::stat).
+template <class T> struct StatGet {
+    template <class C> static XTG_DI T get(const C& c, int k) { return (T)c.stat[k]; }
+};
+template <> struct StatGet<float> {
+    template <class C> static XTG_DI float get(const C& c, int k) { return c.statf[k]; }
+};
 template <int K, class T> struct Stat {
     typedef T type;
-    template <class RG, class C> static XTG_DI T ev(const RG&, int, const C& c) { return (T)c.stat[K]; }
+    template <class RG, class C> static XTG_DI T ev(const RG&, int, const C& c) { return StatGet<T>::get(c, K); }
 };
 
 // Unary functors (include/xtensor/core/xoperation.hpp:104-125,
@@ -422,7 +429,7 @@ template <class Tree, class LS, class OutT, int OUTKIND, int VEC, int R, int U, 
 __global__ void __launch_bounds__(256) k_assign(const AssignParams p) {
     typedef typename LS::template R<VEC>::type RG;
     Ctx<0> c;
-    c.scal = &p.scal;
+    c.scal = p.scal;
     const i64 step = (i64)gridDim.x * blockDim.x * U;
     for (i64 base = (i64)blockIdx.x * blockDim.x * U + threadIdx.x; base < p.sp.nvec; base += step) {
         RG rg[U];
@@ -540,6 +547,25 @@ struct AccSumC {
     XTG_DI double dval() const { return (double)hi + (double)lo; }
 };
 
+// Ordered comparison of float64 values on the integer pipes (GB300 runs
+// FP64 compares at its reduced FP64 rate).  Exactly IEEE `a > b`: NaN
+// compares false, -0 == +0; the sign-magnitude bits become a two's-
+// complement key, which orders all other values.
+XTG_DI bool f64_gt(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
+    if (ma > 0x7ff0000000000000LL || mb > 0x7ff0000000000000LL) return false;
+    const long long ka = ia < 0 ? -ma : ma, kb = ib < 0 ? -mb : mb;
+    return ka > kb;
+}
+template <class T> struct Cmp {
+    static XTG_DI bool gt(T a, T b) { return a > b; }
+    static XTG_DI bool lt(T a, T b) { return a < b; }
+};
+// (Measured on GB300: the integer form costs more issue slots than the
+// native DSETP in the selection reducers, so Cmp<double> stays native and
+// f64_gt is kept for callers that are FP64-pipe bound.)
+
 // Selection reducers amax / amin: the reference folds f(acc, x) =
 // acc > x ? acc : x (include/xtensor/core/xmath.hpp:589-602, 777-811) from
 // lowest()/max(), so among equal values the LAST one visited wins (this is
@@ -550,13 +576,13 @@ template <class A, int MAXOP> struct AccSel {
     XTG_DI void init(const RedParams& p);
     template <class X> XTG_DI void add(X x, i64 ps) {
         A a = cvt<A>(x);
-        bool keep = MAXOP ? (v > a) : (v < a);
+        bool keep = MAXOP ? Cmp<A>::gt(v, a) : Cmp<A>::lt(v, a);
         if (!keep) { v = a; pos = ps; }
     }
     XTG_DI void merge(const AccSel& o) {
         bool take;
-        if (MAXOP) take = (o.v > v) || (!(v > o.v) && o.pos > pos);
-        else take = (o.v < v) || (!(v < o.v) && o.pos > pos);
+        if (MAXOP) take = Cmp<A>::gt(o.v, v) || (!Cmp<A>::gt(v, o.v) && o.pos > pos);
+        else take = Cmp<A>::lt(o.v, v) || (!Cmp<A>::lt(v, o.v) && o.pos > pos);
         if (take) { v = o.v; pos = o.pos; }
     }
     XTG_DI double dval() const { return (double)v; }
@@ -643,7 +669,7 @@ template <class A, int MAXOP> struct AccArg {
         A a = cvt<A>(x);
         if (idx < 0) {
             if (a == a || ps == 0) { v = a; idx = ps; }
-        } else if (MAXOP ? (a > v) : (a < v)) {
+        } else if (MAXOP ? Cmp<A>::gt(a, v) : Cmp<A>::lt(a, v)) {
             v = a;
             idx = ps;
         }
@@ -654,8 +680,8 @@ template <class A, int MAXOP> struct AccArg {
         bool nan_me = !(v == v), nan_o = !(o.v == o.v);
         if (nan_me) return;
         if (nan_o) { v = o.v; idx = o.idx; return; }
-        bool take = MAXOP ? (o.v > v) : (o.v < v);
-        if (!take && !(MAXOP ? (v > o.v) : (v < o.v)) && o.idx < idx) take = true;
+        bool take = MAXOP ? Cmp<A>::gt(o.v, v) : Cmp<A>::lt(o.v, v);
+        if (!take && !(MAXOP ? Cmp<A>::gt(v, o.v) : Cmp<A>::lt(v, o.v)) && o.idx < idx) take = true;
         if (take) { v = o.v; idx = o.idx; }
     }
 };
@@ -841,7 +867,7 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
     typedef typename LS::template R<VEC>::type RG;
     __shared__ Acc smem[32];
     Ctx<0> c;
-    c.scal = &p.scal;
+    c.scal = p.scal;
     const int gsz = GROUP <= 32 ? 32 : (int)blockDim.x;
     const int groups_per_block = (int)blockDim.x / gsz;
     const int gtid = (int)threadIdx.x % gsz;
@@ -871,16 +897,31 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
         const i64 rb = s * p.chunk;
         i64 re = rb + p.chunk;
         if (re > p.n_redv) re = p.n_redv;
-        for (i64 r = rb + gtid; r < re; r += gsz) {
-            i64 ri[RR];
-            decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);
-            ri[RR - 1] *= VEC;
-            i64 off[XTG_KMAX_LEAVES];
-            red_offsets<LS::N, RO, RR>(p, ko, ri, off);
-            RG rg;
-            LoadLeavesAt<LS>::template run<VEC>(rg, p.leaf, off, inner);
+        // U vectors in flight per thread; each thread still visits its
+        // positions in increasing order
+        constexpr int U = 4;
+        for (i64 r0 = rb + gtid; r0 < re; r0 += (i64)gsz * U) {
+            RG rg[U];
 #pragma unroll
-            for (int j = 0; j < VEC; ++j) acc.add(Tree::ev(rg, j, c), r * VEC + j);
+            for (int u = 0; u < U; ++u) {
+                const i64 r = r0 + (i64)u * gsz;
+                if (r < re) {
+                    i64 ri[RR];
+                    decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);
+                    ri[RR - 1] *= VEC;
+                    i64 off[XTG_KMAX_LEAVES];
+                    red_offsets<LS::N, RO, RR>(p, ko, ri, off);
+                    LoadLeavesAt<LS>::template run<VEC>(rg[u], p.leaf, off, inner);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const i64 r = r0 + (i64)u * gsz;
+                if (r < re) {
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) acc.add(Tree::ev(rg[u], j, c), r * VEC + j);
+                }
+            }
         }
         acc = group_reduce<GROUP>(acc, smem);
         if (gtid == 0) {
@@ -904,7 +945,7 @@ template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO,
 __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
     typedef typename LS::template R<VEC>::type RG;
     Ctx<0> c;
-    c.scal = &p.scal;
+    c.scal = p.scal;
     const i64 nwork = p.n_outv * p.nsplit;
     i64 inner[XTG_KMAX_LEAVES];
 #pragma unroll
@@ -971,6 +1012,23 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
     }
 }
 
+// Combine for few splits per output: one thread per output merges its
+// partials in split order.
+template <class Acc, class Out, int POST, int RO>
+__global__ void __launch_bounds__(256) k_reduce_combine_thread(const RedParams p) {
+    const Acc* part = reinterpret_cast<const Acc*>(p.partial);
+    for (i64 o = (i64)blockIdx.x * blockDim.x + threadIdx.x; o < p.n_out; o += (i64)gridDim.x * blockDim.x) {
+        Acc a = part[o * p.nsplit];
+        for (i64 s = 1; s < p.nsplit; ++s) a.merge(part[o * p.nsplit + s]);
+        i64 ko[RO];
+        decode_dims<RO, true>(p.oshape, p.ofd, o, ko);
+        i64 oo = 0;
+#pragma unroll
+        for (int d = 0; d < RO; ++d) oo += ko[d] * p.ostr[d];
+        reinterpret_cast<Out*>(p.out)[oo] = finish<Out, Acc, POST>(a, p);
+    }
+}
+
 // Deterministic combine of split partials: one CTA per output, threads take
 // splits t, t+blockDim, … in order, then a fixed block tree.
 template <class Acc, class Out, int POST, int RO>
@@ -1013,7 +1071,7 @@ __global__ void __launch_bounds__(TILE * ROWS) k_transpose(const TransposeParams
     typedef typename RG::elem0 T0;
     __shared__ T0 tile[TILE][TILE + 1];
     Ctx<0> c;
-    c.scal = &p.scal;
+    c.scal = p.scal;
     const int tx = threadIdx.x % TILE, ty = threadIdx.x / TILE;
     for (i64 t = blockIdx.x; t < p.n_tiles; t += gridDim.x) {
         i64 tb = t % p.ntile_b;
@@ -1123,6 +1181,26 @@ template <int GROUP, class A> XTG_DI A bcast_group(A a, A* smem) {
     return r;
 }
 
+// Per-row finalisation of the fused statistics in the row's precision.
+template <class C> struct RowFin {  // float64 (and integer) rows: FP64
+    template <class A> static XTG_DI double total(const A& a) { return a.s; }
+    static XTG_DI double scale(double v, const RowParams& p, int k) { return v * p.rdiv[k]; }
+    static XTG_DI double mean(double sum, const RowParams& p) { return sum * p.rrow_len; }
+    template <class CT> static XTG_DI void put(CT& c, int k, double v) {
+        c.stat[k] = v;
+        c.statf[k] = (float)v;
+    }
+};
+template <> struct RowFin<float> {  // float32 rows: double-float sums rounded once, FP32 after
+    static XTG_DI float total(const AccSumC& a) { return a.hi + a.lo; }
+    static XTG_DI float scale(float v, const RowParams& p, int k) { return v / p.fdiv[k]; }
+    static XTG_DI float mean(float sum, const RowParams& p) { return sum / p.frow_len; }
+    template <class CT> static XTG_DI void put(CT& c, int k, float v) {
+        c.statf[k] = v;
+        c.stat[k] = (double)v;
+    }
+};
+
 template <class LST> struct Stats;
 template <> struct Stats<StatList<>> {
     template <int GROUP, int VEC, int NV, class RG, class CT>
@@ -1133,7 +1211,7 @@ template <int K, int MODE, class C, class Sub, class... Rest> struct Stats<StatL
     static XTG_DI void run(const RG (&rg)[NV], const bool (&ok)[NV][VEC], CT& c, const RowParams& p, void* smem) {
         typedef RowSum<GROUP, C> RS;
         typedef typename RS::A A;
-        if (MODE <= 3) {
+        if constexpr (MODE <= 3) {
             A s;
             RS::zero(s);
 #pragma unroll
@@ -1143,32 +1221,27 @@ template <int K, int MODE, class C, class Sub, class... Rest> struct Stats<StatL
                     if (ok[n][j]) RS::add(s, cvt<C>(Sub::ev(rg[n], j, c)));
             s = group_reduce<GROUP>(s, reinterpret_cast<A*>(smem));
             s = bcast_group<GROUP>(s, reinterpret_cast<A*>(smem));
-            double sum = RS::val(s);
+            // per-row scalar work in C's own precision (float rows never
+            // touch the FP64 pipe; float64 rows multiply by host reciprocals)
+            const C sum = RowFin<C>::total(s);
             if (MODE == 0) {
-                c.stat[K] = sum;
+                RowFin<C>::put(c, K, sum);
+            } else if (MODE == 1) {
+                RowFin<C>::put(c, K, RowFin<C>::scale(sum, p, K));
             } else {
-                double mean = sum / (double)p.row_len;
-                if (MODE == 1) {
-                    c.stat[K] = sum / p.div[K];
-                } else {
-                    const C m = (C)mean;
-                    A q;
-                    RS::zero(q);
+                const C m = RowFin<C>::mean(sum, p);
+                A q;
+                RS::zero(q);
 #pragma unroll
-                    for (int n = 0; n < NV; ++n)
+                for (int n = 0; n < NV; ++n)
 #pragma unroll
-                        for (int j = 0; j < VEC; ++j)
-                            if (ok[n][j]) RS::addsq(q, (C)(cvt<C>(Sub::ev(rg[n], j, c)) - m));
-                    q = group_reduce<GROUP>(q, reinterpret_cast<A*>(smem));
-                    q = bcast_group<GROUP>(q, reinterpret_cast<A*>(smem));
-                    // correct for the rounding of the mean to C:
-                    // sum (x - m)^2 = sum (x - mean)^2 + n (mean - m)^2
-                    double dm = mean - (double)m;
-                    double m2 = RS::val(q) - (double)p.row_len * dm * dm;
-                    if (m2 < 0.0) m2 = 0.0;
-                    double var = m2 / p.div[K];
-                    c.stat[K] = MODE == 3 ? sqrt(var) : var;
-                }
+                    for (int j = 0; j < VEC; ++j)
+                        if (ok[n][j]) RS::addsq(q, (C)(cvt<C>(Sub::ev(rg[n], j, c)) - m));
+                q = group_reduce<GROUP>(q, reinterpret_cast<A*>(smem));
+                q = bcast_group<GROUP>(q, reinterpret_cast<A*>(smem));
+                C var = RowFin<C>::scale(RowFin<C>::total(q), p, K);
+                if (var < C(0)) var = C(0);
+                RowFin<C>::put(c, K, MODE == 3 ? m_sqrt(var) : var);
             }
         } else {
             AccSel<C, MODE == 4> a;
@@ -1182,6 +1255,7 @@ template <int K, int MODE, class C, class Sub, class... Rest> struct Stats<StatL
             a = group_reduce<GROUP>(a, reinterpret_cast<AccSel<C, MODE == 4>*>(smem));
             a = bcast_group<GROUP>(a, reinterpret_cast<AccSel<C, MODE == 4>*>(smem));
             c.stat[K] = (double)a.v;
+            c.statf[K] = (float)a.v;
         }
         Stats<StatList<Rest...>>::template run<GROUP, VEC, NV>(rg, ok, c, p, smem);
     }
@@ -1192,7 +1266,7 @@ __global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
     typedef typename LS::template R<VEC>::type RG;
     __shared__ __align__(16) unsigned char smem_raw[32 * 48];
     Ctx<NSTAT> c;
-    c.scal = &p.scal;
+    c.scal = p.scal;
     const int gsz = GROUP <= 32 ? 32 : (int)blockDim.x;
     const int gpb = (int)blockDim.x / gsz;
     const int gt = (int)threadIdx.x % gsz;
@@ -1239,6 +1313,184 @@ __global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
         }
     }
 }
+
+// ---------------------------------------------------------------------------
+// K7 with bulk copies.  Each warp owns rows; the rows of every leaf stream
+// into a per-warp double buffer in shared memory with one cp.async.bulk per
+// leaf per row (the TMA engine's 1-D bulk copy, completion counted in bytes
+// on an mbarrier), issued one row ahead, so HBM reads of row i+1 overlap the
+// statistics and the stores of row i.  Requires every leaf to be contiguous
+// along the row, rows 16-byte aligned and a multiple of 16 bytes.
+XTG_DI unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+XTG_DI void mbar_init(u64* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+XTG_DI void mbar_expect_tx(u64* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+XTG_DI bool mbar_try_wait(u64* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+XTG_DI void bulk_g2s(void* dst, const void* src, unsigned bytes, u64* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+XTG_DI void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+XTG_DI void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+template <class T, int VEC>
+XTG_DI void ld_smem(T (&dst)[VEC], const T* p) {
+    const int B = (int)sizeof(T) * VEC;
+    if (B == 16 || B == 8 || B == 4) {
+        typedef typename VecT<B>::t V;
+        union { V v; T e[VEC]; } u;
+        u.v = *reinterpret_cast<const V*>(p);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dst[j] = u.e[j];
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dst[j] = p[j];
+    }
+}
+template <int I, int VEC, class... S> struct SmemLoad;
+template <int I, int VEC> struct SmemLoad<I, VEC> {
+    template <class RG> static XTG_DI void run(RG&, const unsigned char*, const unsigned*, i64) {}
+};
+template <int I, int VEC, class S0, class... S> struct SmemLoad<I, VEC, S0, S...> {
+    template <class RG> static XTG_DI void run(RG& rg, const unsigned char* buf, const unsigned* loff, i64 e0) {
+        typedef typename S0::type T;
+        ld_smem<T, VEC>(rg.v, reinterpret_cast<const T*>(buf + loff[I]) + e0);
+        SmemLoad<I + 1, VEC, S...>::run(rg.rest, buf, loff, e0);
+    }
+};
+template <class LS> struct LoadRowSmem;
+template <class... S> struct LoadRowSmem<LeafSet<S...>> {
+    template <int VEC, class RG> static XTG_DI void run(RG& rg, const unsigned char* buf, const unsigned* loff, i64 e0) {
+        SmemLoad<0, VEC, S...>::run(rg, buf, loff, e0);
+    }
+};
+
+template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int RO, int NSTAT>
+__global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    extern __shared__ __align__(128) unsigned char dsmem[];
+    __shared__ __align__(16) unsigned char red_smem[32 * 48];
+    __shared__ u64 bars[8];
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    const int nw = (int)blockDim.x >> 5;
+    u64* mybar = bars + 2 * warp;
+    unsigned char* buf[2] = {dsmem + (size_t)(2 * warp) * p.buf_bytes, dsmem + (size_t)(2 * warp + 1) * p.buf_bytes};
+    if (lane == 0) {
+        mbar_init(&mybar[0], 1);
+        mbar_init(&mybar[1], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    Ctx<NSTAT> c;
+    c.scal = p.scal;
+    const i64 gid = (i64)blockIdx.x * nw + warp;
+    const i64 ng = (i64)gridDim.x * nw;
+    auto issue = [&](i64 row, int b) {
+        if (lane == 0) {
+            i64 ko[RO];
+            decode_dims<RO, true>(p.oshape, (const FastDiv*)0, row, ko);
+            mbar_expect_tx(&mybar[b], p.buf_bytes);
+#pragma unroll
+            for (int l = 0; l < LS::N; ++l) {
+                i64 o = 0;
+#pragma unroll
+                for (int d = 0; d < RO; ++d) o += ko[d] * p.lo[l][d];
+                const unsigned char* src = reinterpret_cast<const unsigned char*>(p.leaf[l]) + o * (p.lbytes[l] / p.row_len);
+                bulk_g2s(buf[b] + p.loff[l], src, p.lbytes[l], &mybar[b]);
+            }
+        }
+    };
+    int it = 0;
+    if (gid < p.n_rows) issue(gid, 0);
+    for (i64 row = gid; row < p.n_rows; row += ng, ++it) {
+        const int b = it & 1;
+        if (row + ng < p.n_rows) issue(row + ng, b ^ 1);
+        const unsigned parity = (unsigned)(it >> 1) & 1u;
+        bool done = false;
+        for (int k = 0; k < (1 << 22); ++k) {
+            if (mbar_try_wait(&mybar[b], parity)) {
+                done = true;
+                break;
+            }
+        }
+        if (!done) {
+            // give up: flag it, wait (bounded) for the copy into the other
+            // buffer if one was issued, and leave
+            if (lane == 0) atomicExch(p.err, 1);
+            if (row + ng < p.n_rows) {
+                const unsigned par2 = (unsigned)((it + 1) >> 1) & 1u;
+                for (int k = 0; k < (1 << 22); ++k)
+                    if (mbar_try_wait(&mybar[b ^ 1], par2)) break;
+            }
+            return;
+        }
+        RG rg[NV];
+        bool ok[NV][VEC];
+#pragma unroll
+        for (int n = 0; n < NV; ++n) {
+            const i64 e0 = ((i64)n * 32 + lane) * VEC;
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) ok[n][j] = (e0 + j) < p.row_len;
+            if (e0 < p.row_len) LoadRowSmem<LS>::template run<VEC>(rg[n], buf[b], p.loff, e0);
+        }
+        Stats<SL>::template run<32, VEC, NV>(rg, ok, c, p, (void*)red_smem);
+        i64 ko[RO];
+        decode_dims<RO, true>(p.oshape, (const FastDiv*)0, row, ko);
+        i64 ob = 0;
+#pragma unroll
+        for (int d = 0; d < RO; ++d) ob += ko[d] * p.oo[d];
+#pragma unroll
+        for (int n = 0; n < NV; ++n) {
+            const i64 e0 = ((i64)n * 32 + lane) * VEC;
+            if (e0 < p.row_len) {
+                OutT v[VEC];
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) v[j] = cvt<OutT>(Tree::ev(rg[n], j, c));
+                st_out<OutT, K_CONTIG, VEC>(reinterpret_cast<OutT*>(p.out), ob + e0, 1, v);
+            }
+        }
+        // all lanes are done reading buffer b before it is refilled
+        fence_proxy_async_smem();
+        __syncwarp();
+    }
+}
+
+// a * (1 / b) with b invariant over a row (the reciprocal is computed once
+// per row by common-subexpression elimination over the unrolled elements):
+// used for float64 rows, where a division costs ~10 FP64 operations on GB300.
+template <class T, class A, class B> struct MulRecip {
+    typedef T type;
+    template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C& c) {
+        T a = cvt<T>(A::ev(r, j, c));
+        T b = cvt<T>(B::ev(r, j, c));
+        return a * (T(1) / b);
+    }
+};
+
+// (a - m) / b with m and b invariant over a row, as one fused multiply-add
+// per element: a * r - m * r with r = 1 / b (r and m * r once per row).
+template <class T, class A, class M, class B> struct FmaRecipSub {
+    typedef T type;
+    template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C& c) {
+        const T a = cvt<T>(A::ev(r, j, c));
+        const T m = cvt<T>(M::ev(r, j, c));
+        const T rb = T(1) / cvt<T>(B::ev(r, j, c));
+        return fma(a, rb, -(m * rb));
+    }
+};
 
 }  // namespace xtg
 #endif

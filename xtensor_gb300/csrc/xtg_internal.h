@@ -46,6 +46,7 @@ struct Drv {
                              CUstream, void**, void**) = nullptr;
     CUresult (*OccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
     CUresult (*GetErrorString)(CUresult, const char**) = nullptr;
+    CUresult (*FuncSetAttribute)(CUfunction, CUfunction_attribute, int) = nullptr;
 };
 const Drv& drv();
 
@@ -83,11 +84,15 @@ struct Kernel {
     std::string name;
     int max_blocks_per_sm = 0;  // occupancy at the block size it was queried for
     int block = 0;
+    size_t dyn_smem = 0;        // dynamic shared memory the occupancy was queried with
 };
 // Compiles (or fetches) the kernel whose name expression is `expr`
-// (e.g. "xtg::k_assign<...>").  `block` is used for the occupancy query.
-xtg_status get_kernel(const std::string& expr, int block, Kernel** k);
-xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream);
+// (e.g. "xtg::k_assign<...>").  `block` / `dyn_smem` are used for the
+// occupancy query (and dyn_smem > 48 KiB raises the kernel's limit).
+xtg_status get_kernel(const std::string& expr, int block, Kernel** k, size_t dyn_smem = 0);
+xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream, size_t dyn_smem = 0);
+// A device word that kernels set when a bounded wait gives up.
+xtg_status device_error_word(int** p);
 void count_launch();
 // Resets the per-thread record of launched kernels (start of an API call).
 void begin_call();

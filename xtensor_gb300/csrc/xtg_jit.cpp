@@ -126,7 +126,26 @@ static thread_local std::string t_last_kernels;
 
 void begin_call() { t_last_kernels.clear(); }
 
-xtg_status get_kernel(const std::string& expr, int block, Kernel** out) {
+// Occupancy for a (block, dynamic shared memory) configuration; raises the
+// kernel's dynamic shared memory limit above the 48 KiB default when needed.
+static xtg_status configure(Kernel* k, int block, size_t dyn_smem) {
+    if (dry_run() || !k->fn) {
+        k->block = block;
+        k->dyn_smem = dyn_smem;
+        return XTG_OK;
+    }
+    if (k->block == block && k->dyn_smem == dyn_smem && k->max_blocks_per_sm > 0) return XTG_OK;
+    if (dyn_smem > 48 * 1024)
+        XTG_CU(drv().FuncSetAttribute(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn_smem));
+    int nb = 0;
+    if (drv().OccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, block, dyn_smem) != CUDA_SUCCESS) nb = 1;
+    k->max_blocks_per_sm = nb > 0 ? nb : 1;
+    k->block = block;
+    k->dyn_smem = dyn_smem;
+    return XTG_OK;
+}
+
+xtg_status get_kernel(const std::string& expr, int block, Kernel** out, size_t dyn_smem) {
     DeviceInfo* dev;
     XTG_TRY(ensure_device(&dev));
     JitState& S = js();
@@ -137,7 +156,7 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out) {
     if (it != S.kernels.end()) {
         S.st.memory_hits++;
         *out = it->second.get();
-        return XTG_OK;
+        return configure(*out, block, dyn_smem);
     }
     char arch[32];
     snprintf(arch, sizeof arch, "sm_%d%da", dev->cc_major, dev->cc_minor);
@@ -193,16 +212,14 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out) {
     std::unique_ptr<Kernel> k(new Kernel);
     XTG_CU(drv().ModuleGetFunction(&k->fn, mod, lowered.c_str()));
     k->name = expr;
-    k->block = block;
-    int nb = 0;
-    if (drv().OccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, block, 0) != CUDA_SUCCESS) nb = 1;
-    k->max_blocks_per_sm = nb > 0 ? nb : 1;
+    k->max_blocks_per_sm = 0;
+    XTG_TRY(configure(k.get(), block, dyn_smem));
     *out = k.get();
     S.kernels.emplace(key, std::move(k));
     return XTG_OK;
 }
 
-xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream) {
+xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream, size_t dyn_smem) {
     if (grid == 0) return XTG_OK;
     if (!t_last_kernels.empty()) t_last_kernels += ";";
     t_last_kernels += k->name.compare(0, 5, "xtg::") == 0 ? k->name.substr(5) : k->name;
@@ -211,7 +228,7 @@ xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaSt
         return XTG_OK;
     }
     void* args[1] = {params};
-    XTG_CU(drv().LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, 0, (CUstream)stream, args, nullptr));
+    XTG_CU(drv().LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, (unsigned)dyn_smem, (CUstream)stream, args, nullptr));
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return XTG_OK;
 }

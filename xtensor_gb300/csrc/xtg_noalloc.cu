@@ -37,6 +37,7 @@ typedef L<0, float> Tree;
 
 #define XTG_NOALLOC_ROW(VEC, GROUP) xtg::k_reduce_row<Tree, LS, AccSumC, float, 0, VEC, 1, 1, GROUP, false>
 #define XTG_NOALLOC_COMBINE xtg::k_reduce_combine<AccSumC, float, 0, 1>
+#define XTG_NOALLOC_COMBINE_THREAD xtg::k_reduce_combine_thread<AccSumC, float, 0, 1>
 
 struct DeviceState {
     bool ready = false;
@@ -152,7 +153,11 @@ extern "C" xtg_status xtg_sum_f32_noalloc(const float* x, int64_t n, float* out,
     else group == 256 ? launch_row<1, 256>(p, grid, st) : launch_row<1, 32>(p, grid, st);
     XTG_CUDA(cudaGetLastError());
     count_launch();
-    if (nsplit > 1) {
+    if (nsplit > 1 && nsplit <= opt("reduce.thread_combine_max", 64)) {
+        XTG_NOALLOC_COMBINE_THREAD<<<1, 256, 0, st>>>(p);
+        XTG_CUDA(cudaGetLastError());
+        count_launch();
+    } else if (nsplit > 1) {
         XTG_NOALLOC_COMBINE<<<1, 256, 0, st>>>(p);
         XTG_CUDA(cudaGetLastError());
         count_launch();

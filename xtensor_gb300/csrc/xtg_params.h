@@ -93,6 +93,15 @@ struct RowParams {
     i64 oi;
     Scalars scal;
     double div[XTG_KMAX_SCAL];  // per statistic divisor (mean: n, var: n - ddof)
+    double rdiv[XTG_KMAX_SCAL]; // 1 / div (float64 rows multiply)
+    float fdiv[XTG_KMAX_SCAL];  // div as float (float32 rows divide in FP32)
+    double rrow_len;            // 1 / row_len
+    float frow_len;             // row_len as float
+    // bulk-copy (TMA) variant: per-warp buffer layout in shared memory
+    unsigned loff[XTG_KMAX_LEAVES];   // byte offset of each leaf's row inside a buffer
+    unsigned lbytes[XTG_KMAX_LEAVES]; // bytes of one row of each leaf (multiple of 16)
+    unsigned buf_bytes;               // bytes of one buffer (all leaves)
+    int* err;                         // set to 1 when a bounded wait gives up
 };
 
 }  // namespace xtg

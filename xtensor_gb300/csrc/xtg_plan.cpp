@@ -259,10 +259,25 @@ void leaf_bstrides(const Tree& t, int l, int64_t* st) {
     }
 }
 
-std::string tree_type(const Tree& t, int n, const std::vector<int>& map) {
+static bool leaf_free(const Tree& t, int n) {
+    if (t.nodes[n].op == XTG_OP_LEAF) return false;
+    if (is_rop(t.nodes[n].op)) return true;  // a statistic is one value per row
+    for (int c : t.nodes[n].kids)
+        if (!leaf_free(t, c)) return false;
+    return true;
+}
+
+std::string tree_type(const Tree& t, int n, const std::vector<int>& map, bool recip) {
     const PNode& x = t.nodes[n];
     const std::string T = dt(x.dtype).cname;
-    auto k = [&](int i) { return tree_type(t, x.kids[i], map); };
+    auto k = [&](int i) { return tree_type(t, x.kids[i], map, recip); };
+    if (recip && x.op == XTG_OP_DIV && x.dtype == XTG_FLOAT64 && leaf_free(t, x.kids[1])) {
+        const PNode& a = t.nodes[x.kids[0]];
+        if (a.op == XTG_OP_SUB && a.dtype == XTG_FLOAT64 && leaf_free(t, a.kids[1]))
+            return "xtg::FmaRecipSub<" + T + ", " + tree_type(t, a.kids[0], map, recip) + ", " +
+                   tree_type(t, a.kids[1], map, recip) + ", " + k(1) + ">";
+        return "xtg::MulRecip<" + T + ", " + k(0) + ", " + k(1) + ">";
+    }
     switch (x.op) {
         case XTG_OP_LEAF:
             return "xtg::L<" + std::to_string(map[x.leaf]) + ", " + dt(t.leaves[x.leaf].dtype).cname + ">";

@@ -318,11 +318,13 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
     if (st == XTG_OK && nsplit > 1) {
         xtg::RedParams pc = p;
         if (!row) pc.oshape[RO - 1] *= vec;  // combine decodes flat element indices
-        std::string name = "xtg::k_reduce_combine<" + accname + ", " + outc + ", " + std::to_string(post) + ", " +
-                           std::to_string(RO) + ">";
+        // few splits: a thread per output merges them in order; many: a CTA
+        const bool per_thread = nsplit <= opt("reduce.thread_combine_max", 64);
+        std::string name = std::string(per_thread ? "xtg::k_reduce_combine_thread<" : "xtg::k_reduce_combine<") +
+                           accname + ", " + outc + ", " + std::to_string(post) + ", " + std::to_string(RO) + ">";
         Kernel* kc;
         st = get_kernel(name, 256, &kc);
-        if (st == XTG_OK) st = launch(kc, grid_cap(kc, n_out), 256, &pc, stream);
+        if (st == XTG_OK) st = launch(kc, grid_cap(kc, per_thread ? (n_out + 255) / 256 : n_out), 256, &pc, stream);
     }
     if (part && !(scratch && scratch->fixed)) {
         xtg_status fs = scratch_free(part, stream);

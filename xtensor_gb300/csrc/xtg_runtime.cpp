@@ -47,6 +47,7 @@ static xtg_status resolve_driver() {
     XTG_TRY(resolve("cuLaunchKernel", g_drv.LaunchKernel));
     XTG_TRY(resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", g_drv.OccupancyMaxActiveBlocksPerMultiprocessor));
     XTG_TRY(resolve("cuGetErrorString", g_drv.GetErrorString));
+    XTG_TRY(resolve("cuFuncSetAttribute", g_drv.FuncSetAttribute));
     return XTG_OK;
 }
 
@@ -146,6 +147,22 @@ xtg_status scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
     XTG_CUDA(cudaMallocAsync(p, bytes, s));
     return XTG_OK;
 }
+static int* g_err_word = nullptr;
+
+xtg_status device_error_word(int** p) {
+    if (dry_run()) {
+        *p = (int*)(uintptr_t)0x7e0000000000ull;
+        return XTG_OK;
+    }
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    if (!g_err_word) {
+        XTG_CUDA(cudaMalloc((void**)&g_err_word, 256));
+        XTG_CUDA(cudaMemset(g_err_word, 0, 256));
+    }
+    *p = g_err_word;
+    return XTG_OK;
+}
+
 xtg_status scratch_free(void* p, cudaStream_t s) {
     if (dry_run()) return XTG_OK;
     if (p) XTG_CUDA(cudaFreeAsync(p, s));
@@ -297,6 +314,19 @@ xtg_status xtg_device_sync(void) {
 }
 
 size_t xtg_dtype_size(int32_t dtype) { return valid_dtype(dtype) ? (size_t)dt(dtype).size : 0; }
+
+xtg_status xtg_check_device_errors(void) {
+    XTG_TRY(ensure_device(nullptr));
+    if (dry_run() || !g_err_word) return XTG_OK;
+    int v = 0;
+    XTG_CUDA(cudaDeviceSynchronize());
+    XTG_CUDA(cudaMemcpy(&v, g_err_word, sizeof v, cudaMemcpyDeviceToHost));
+    if (v) {
+        XTG_CUDA(cudaMemset(g_err_word, 0, sizeof v));
+        return fail(XTG_ERR_TIMEOUT, "a kernel's bounded wait gave up (device error word was set)");
+    }
+    return XTG_OK;
+}
 
 xtg_status xtg_event_create(xtg_event* ev) {
     if (!ev) return fail(XTG_ERR_INVALID, "null event");
