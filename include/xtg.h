@@ -243,6 +243,51 @@ xtg_status xtg_reduce(const xtg_expr* e, const xtg_reduce_desc* rd,
 xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis,
                          const xtg_array* out, xtg_stream stream);
 
+/* ---- batching ------------------------------------------------------------------------
+ * No counterpart in the reference (a new layer over the same path).  Many
+ * instances of ONE expression shape — same opcodes, leaf dtypes and ranks;
+ * any sizes, strides and pointers — evaluated by one persistent launch whose
+ * CTAs pull equal-work tiles (runs of rows of one instance) from a device
+ * counter.  Each instance is a 2-D (rows, cols) evaluation (rank-1 leaves are
+ * one row).  `rd` NULL: elementwise assignment into each instance's output;
+ * otherwise a reduction over the last axis (rd->axes = {-1} or {rank-1}),
+ * output (rows,) — e.g. sum(A * v + C, {1}) for 4096 uneven instances.
+ * The template's leaves fix dtypes and ranks; xtg_batch_add binds each
+ * instance's leaves in the template's leaf order.  xtg_batch_build uploads the
+ * work list and picks the launch configuration (sub-warp group width, tile
+ * size, CTAs per SM) — autotune = 1 measures the candidates on the instances
+ * and caches the winner on disk per shape class; xtg_batch_capture records
+ * one run into a CUDA graph that xtg_batch_replay launches. */
+typedef struct xtg_batch xtg_batch;
+typedef struct {
+    int64_t instances;
+    int64_t tiles;
+    int64_t elements;
+    int64_t algorithmic_bytes; /* leaves read once + outputs written once */
+    int32_t group_lanes;
+    int32_t unroll;
+    int32_t ctas_per_sm;
+    int32_t tuned;             /* 0 default, 1 measured now, 2 from the on-disk cache */
+    int64_t tile_elems;
+    int32_t graph_ready;
+    int32_t pad;
+} xtg_batch_info;
+xtg_status xtg_batch_create(const xtg_expr* templ, const xtg_reduce_desc* rd, xtg_batch** b);
+xtg_status xtg_batch_add(xtg_batch* b, const xtg_array* leaves, int32_t n_leaves, const xtg_array* out);
+xtg_status xtg_batch_build(xtg_batch* b, int32_t autotune, xtg_stream stream);
+xtg_status xtg_batch_run(xtg_batch* b, xtg_stream stream);
+xtg_status xtg_batch_capture(xtg_batch* b, xtg_stream stream); /* stream must not be NULL */
+xtg_status xtg_batch_replay(xtg_batch* b, xtg_stream stream);
+xtg_status xtg_batch_get_info(const xtg_batch* b, xtg_batch_info* info);
+xtg_status xtg_batch_destroy(xtg_batch* b);
+
+/* Seeded synthetic data on the device (the benchmarks' inputs): element i of
+ * a contiguous array gets a value from a counter-based generator keyed by
+ * (seed, i), independent of the launch configuration.  dist: 0 uniform
+ * [p0, p1), 1 normal(mean p0, sd p1), 2 sign-random lognormal(mu p0, sigma
+ * p1), 3 integer uniform [p0, p1]. */
+xtg_status xtg_fill_random(const xtg_array* a, int32_t dist, double p0, double p1, uint64_t seed, xtg_stream stream);
+
 /* ---- reduction without allocation ------------------------------------------------
  * No counterpart in the reference.  For callers that must not allocate device
  * memory while they reduce — code running during CUDA stream capture (where

@@ -108,3 +108,19 @@ def test_type_and_shape_errors_are_reported_before_launch():
     with pytest.raises(xg.XtgError) as ei:
         xg.assign(fake((3, 4), "float32"), a % a)
     assert ei.value.status == 1
+
+
+def test_batch_plans_and_compiles():
+    from xtensor_gb300.batch import Batch
+    A0, v0, C0 = fake((10, 20), "float32"), fake((20,), "float32"), fake((10, 20), "float32")
+    b = Batch(A0 * v0 + C0, reduce="sum")
+    for r, c in [(10, 20), (1, 16), (4096, 2048), (7, 33)]:
+        A, v, Cm = fake((r, c), "float32"), fake((c,), "float32"), fake((r, c), "float32")
+        b.add(A * v + Cm, fake((r,), "float32"))
+    b.build(autotune=False)
+    info = b.info()
+    assert info["instances"] == 4 and info["tiles"] >= 4
+    assert info["algorithmic_bytes"] == sum(4 * (2 * r * c + c + r) for r, c in [(10, 20), (1, 16), (4096, 2048), (7, 33)])
+    ba = Batch(A0 * v0 + C0)
+    ba.add(A0 * v0 + C0, fake((10, 20), "float32"))
+    ba.build(autotune=False)

@@ -510,7 +510,7 @@ XTG_DI void two_sum(float a, float b, float& s, float& e) {
 // include/xtensor/core/xmath.hpp:1803,1823).
 template <class A, int OP> struct AccPlain {
     A s;
-    XTG_DI void init(const RedParams& p);
+    template <class P> XTG_DI void init(const P& p);
     template <class X> XTG_DI void add(X x, i64) {
         if (OP == 0) s = (A)(s + cvt<A>(x)); else s = (A)(s * cvt<A>(x));
     }
@@ -525,7 +525,7 @@ template <class A, int OP> struct AccPlain {
 // grid combines.
 struct AccSumC {
     float hi, lo;
-    XTG_DI void init(const RedParams& p);
+    template <class P> XTG_DI void init(const P& p);
     template <class X> XTG_DI void add(X x, i64) {
         float v = cvt<float>(x), s, e;
         two_sum(hi, v, s, e);
@@ -573,7 +573,7 @@ template <class T> struct Cmp {
 template <class A, int MAXOP> struct AccSel {
     A v;
     i64 pos;
-    XTG_DI void init(const RedParams& p);
+    template <class P> XTG_DI void init(const P& p);
     template <class X> XTG_DI void add(X x, i64 ps) {
         A a = cvt<A>(x);
         bool keep = MAXOP ? Cmp<A>::gt(v, a) : Cmp<A>::lt(v, a);
@@ -598,7 +598,7 @@ template <class C, int MODE> struct AccMom;
 template <int MODE> struct AccMom<float, MODE> {
     float k;
     AccSumC s1, s2;
-    XTG_DI void init(const RedParams& p);
+    template <class P> XTG_DI void init(const P& p);
     template <class X> XTG_DI void add(X x, i64) {
         float d = cvt<float>(x) - k;
         s1.addf(d);
@@ -613,7 +613,7 @@ template <int MODE> struct AccMom<float, MODE> {
 };
 template <int MODE> struct AccMom<double, MODE> {
     double k, s1, s2;
-    XTG_DI void init(const RedParams& p);
+    template <class P> XTG_DI void init(const P& p);
     template <class X> XTG_DI void add(X x, i64) {
         double d = cvt<double>(x) - k;
         s1 += d;
@@ -627,7 +627,7 @@ template <int MODE> struct AccMom<double, MODE> {
 // 2 = sq (sum x*x), 3 = linf (max |x| from 0, std::max then math::maximum).
 template <class A, int NK> struct AccNorm {
     A s;
-    XTG_DI void init(const RedParams&) { s = A(0); }
+    template <class P> XTG_DI void init(const P&) { s = A(0); }
     template <class X> XTG_DI void add(X x, i64) {
         if (NK == 0) s = s + (A)(x != X(0) ? 1 : 0);
         else if (NK == 1) s = s + (A)m_abs(x);
@@ -642,7 +642,7 @@ template <class A, int NK> struct AccNorm {
 // float32 / bf16 squares and absolute values in double-float.
 template <int NK> struct AccNormC {
     AccSumC a;
-    XTG_DI void init(const RedParams&) { a.hi = 0.f; a.lo = 0.f; }
+    template <class P> XTG_DI void init(const P&) { a.hi = 0.f; a.lo = 0.f; }
     template <class X> XTG_DI void add(X x, i64) {
         float f = cvt<float>(x);
         if (NK == 1) {
@@ -664,7 +664,7 @@ template <int NK> struct AccNormC {
 template <class A, int MAXOP> struct AccArg {
     A v;
     i64 idx;  // -1: empty
-    XTG_DI void init(const RedParams&) { idx = -1; v = A(0); }
+    template <class P> XTG_DI void init(const P&) { idx = -1; v = A(0); }
     template <class X> XTG_DI void add(X x, i64 ps) {
         A a = cvt<A>(x);
         if (idx < 0) {
@@ -691,19 +691,19 @@ template <class A, int MAXOP> struct AccArg {
 // reduced dims (rank RR).  For the ROW strategy the innermost reduced dim is
 // vectorised (rshape[RR-1] counted in vectors); for COL the innermost kept
 // dim is (oshape[RO-1] counted in vectors).
-template <class A, int OP> XTG_DI void AccPlain<A, OP>::init(const RedParams& p) {
+template <class A, int OP> template <class P> XTG_DI void AccPlain<A, OP>::init(const P& p) {
     s = IsFloat<A>::value ? (A)p.init_f : (A)p.init_i;
 }
-XTG_DI void AccSumC::init(const RedParams& p) { hi = (float)p.init_f; lo = 0.f; }
-template <class A, int MAXOP> XTG_DI void AccSel<A, MAXOP>::init(const RedParams& p) {
+template <class P> XTG_DI void AccSumC::init(const P& p) { hi = (float)p.init_f; lo = 0.f; }
+template <class A, int MAXOP> template <class P> XTG_DI void AccSel<A, MAXOP>::init(const P& p) {
     v = IsFloat<A>::value ? (A)p.init_f : (A)p.init_i;
     pos = -1;
 }
-template <int MODE> XTG_DI void AccMom<float, MODE>::init(const RedParams&) {
+template <int MODE> template <class P> XTG_DI void AccMom<float, MODE>::init(const P&) {
     k = 0.f;
     s1.hi = s1.lo = s2.hi = s2.lo = 0.f;
 }
-template <int MODE> XTG_DI void AccMom<double, MODE>::init(const RedParams&) { k = 0.0; s1 = s2 = 0.0; }
+template <int MODE> template <class P> XTG_DI void AccMom<double, MODE>::init(const P&) { k = 0.0; s1 = s2 = 0.0; }
 
 // Shift for the moment accumulators (the output's first element).
 template <class A> struct Shift {
@@ -723,7 +723,7 @@ template <int MODE> struct NeedsShift<AccMom<double, MODE>> { enum { value = MOD
 // last, as xreducer_stepper::aggregate does, xreducer.hpp:1778-1799).
 template <class Out, class A> struct Fin;
 template <class Out, class A, int OP> struct Fin<Out, AccPlain<A, OP>> {
-    static XTG_DI Out go(const AccPlain<A, OP>& a, const RedParams& p) {
+    template <class P> static XTG_DI Out go(const AccPlain<A, OP>& a, const P& p) {
         A r = a.s;
         if (p.has_initial) {
             A iv = IsFloat<A>::value ? (A)p.initial_f : (A)p.initial_i;
@@ -733,14 +733,14 @@ template <class Out, class A, int OP> struct Fin<Out, AccPlain<A, OP>> {
     }
 };
 template <class Out> struct Fin<Out, AccSumC> {
-    static XTG_DI Out go(const AccSumC& a, const RedParams& p) {
+    template <class P> static XTG_DI Out go(const AccSumC& a, const P& p) {
         double r = a.dval();
         if (p.has_initial) r = p.initial_f + r;
         return cvt<Out>(r);
     }
 };
 template <class Out, class A, int MAXOP> struct Fin<Out, AccSel<A, MAXOP>> {
-    static XTG_DI Out go(const AccSel<A, MAXOP>& a, const RedParams& p) {
+    template <class P> static XTG_DI Out go(const AccSel<A, MAXOP>& a, const P& p) {
         A r = a.v;
         if (p.has_initial) {
             A iv = IsFloat<A>::value ? (A)p.initial_f : (A)p.initial_i;
@@ -760,7 +760,7 @@ template <int MODE> XTG_DI void mom_sums(const AccMom<double, MODE>& a, double& 
     s2 = a.s2;
 }
 template <class Out, class C, int MODE> struct Fin<Out, AccMom<C, MODE>> {
-    static XTG_DI Out go(const AccMom<C, MODE>& a, const RedParams& p) {
+    template <class P> static XTG_DI Out go(const AccMom<C, MODE>& a, const P& p) {
         double s1, s2;
         mom_sums(a, s1, s2);
         if (MODE == 0) return cvt<Out>(s1 / p.divisor);
@@ -772,18 +772,18 @@ template <class Out, class C, int MODE> struct Fin<Out, AccMom<C, MODE>> {
     }
 };
 template <class Out, class A, int NK> struct Fin<Out, AccNorm<A, NK>> {
-    static XTG_DI Out go(const AccNorm<A, NK>& a, const RedParams&) { return cvt<Out>(a.s); }
+    template <class P> static XTG_DI Out go(const AccNorm<A, NK>& a, const P&) { return cvt<Out>(a.s); }
 };
 template <class Out, int NK> struct Fin<Out, AccNormC<NK>> {
-    static XTG_DI Out go(const AccNormC<NK>& a, const RedParams&) { return cvt<Out>(a.dval()); }
+    template <class P> static XTG_DI Out go(const AccNormC<NK>& a, const P&) { return cvt<Out>(a.dval()); }
 };
 template <class Out, class A, int MAXOP> struct Fin<Out, AccArg<A, MAXOP>> {
-    static XTG_DI Out go(const AccArg<A, MAXOP>& a, const RedParams&) { return cvt<Out>(a.idx < 0 ? 0 : a.idx); }
+    template <class P> static XTG_DI Out go(const AccArg<A, MAXOP>& a, const P&) { return cvt<Out>(a.idx < 0 ? 0 : a.idx); }
 };
 // Post-processing applied after Fin: POST 1 = sqrt (norm_l2 = sqrt(norm_sq),
 // include/xtensor/reducers/xnorm.hpp:494-526); POST 2 = division by the
 // mean divisor in double (mean_division, include/xtensor/core/xmath.hpp:1828-1835).
-template <int POST, class Out, class V> XTG_DI Out post(V v, const RedParams& p) {
+template <int POST, class Out, class V, class P> XTG_DI Out post(V v, const P& p) {
     if (POST == 1) return cvt<Out>(m_sqrt(cvt<double>(v)));
     if (POST == 2) return cvt<Out>(cvt<double>(v) / p.divisor);
     return cvt<Out>(v);
@@ -791,7 +791,7 @@ template <int POST, class Out, class V> XTG_DI Out post(V v, const RedParams& p)
 // Value type handed from Fin to post: POST 2 keeps the sum in double.
 template <int POST, class Out> struct FinT { typedef Out type; };
 template <class Out> struct FinT<2, Out> { typedef double type; };
-template <class Out, class Acc, int POST> XTG_DI Out finish(const Acc& a, const RedParams& p) {
+template <class Out, class Acc, int POST, class P> XTG_DI Out finish(const Acc& a, const P& p) {
     typedef typename FinT<POST, Out>::type M;
     return post<POST, Out>(Fin<M, Acc>::go(a, p), p);
 }
@@ -1479,6 +1479,134 @@ template <class T, class A, class B> struct MulRecip {
         return a * (T(1) / b);
     }
 };
+
+// ---------------------------------------------------------------------------
+// K8: batched persistent kernels.  Thousands of instances of one tree with
+// uneven (rows, cols) run in ONE launch: CTAs pull tiles (a run of rows of
+// one instance, sized to about the same number of elements) from a device
+// counter until the list is exhausted; a sub-warp group of GL lanes owns a
+// row.  Row reductions: each row's result is produced by one group in a fixed
+// order, so results do not depend on which CTA took the tile.
+template <class Tree, class LS, class Acc, class Out, int POST, int GL, int U>
+__global__ void __launch_bounds__(256) k_batch_rowreduce(const BatchParams p) {
+    typedef typename LS::template R<1>::type RG;
+    __shared__ i64 s_tile;
+    Ctx<0> c;
+    c.scal = p.scal;
+    const int g = (int)threadIdx.x / GL, gl = (int)threadIdx.x % GL, ngroups = (int)blockDim.x / GL;
+    FinP fp;
+    fp.init_f = p.init_f;
+    fp.init_i = p.init_i;
+    fp.has_initial = p.has_initial;
+    fp.initial_f = p.initial_f;
+    fp.initial_i = p.initial_i;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile = (i64)atomicAdd(p.counter, 1);
+        __syncthreads();
+        const i64 t = s_tile;
+        if (t >= p.ntiles) break;
+        const BatchTile tl = p.tiles[t];
+        const BatchInst* I = p.inst + tl.inst;
+        const i64 cols = I->cols;
+        fp.divisor = I->divisor;
+        fp.n_red = cols;
+        i64 cs[XTG_KMAX_LEAVES], rsv[XTG_KMAX_LEAVES];
+#pragma unroll
+        for (int l = 0; l < LS::N; ++l) {
+            cs[l] = I->cs[l];
+            rsv[l] = I->rs[l];
+        }
+        for (int r0 = 0; r0 < tl.nrows; r0 += ngroups) {
+            const int r = r0 + g;
+            const bool active = r < tl.nrows;
+            const i64 row = tl.row0 + r;
+            Acc acc;
+            acc.init(fp);
+            if (active) {
+                i64 base[XTG_KMAX_LEAVES];
+#pragma unroll
+                for (int l = 0; l < LS::N; ++l) base[l] = row * rsv[l];
+                if (NeedsShift<Acc>::value && cols > 0) {
+                    RG r1;
+                    LoadLeavesAt<LS>::template run<1>(r1, I->leaf, base, cs);
+                    Shift<Acc>::set(acc, Tree::ev(r1, 0, c));
+                }
+                for (i64 c0 = gl; c0 < cols; c0 += (i64)GL * U) {
+                    RG rg[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const i64 col = c0 + (i64)u * GL;
+                        if (col < cols) {
+                            i64 off[XTG_KMAX_LEAVES];
+#pragma unroll
+                            for (int l = 0; l < LS::N; ++l) off[l] = base[l] + col * cs[l];
+                            LoadLeavesAt<LS>::template run<1>(rg[u], I->leaf, off, cs);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const i64 col = c0 + (i64)u * GL;
+                        if (col < cols) acc.add(Tree::ev(rg[u], 0, c), col);
+                    }
+                }
+            }
+#pragma unroll
+            for (int m = GL / 2; m >= 1; m >>= 1) {
+                Acc o = shfl_xor_pod(acc, m);
+                acc.merge(o);
+            }
+            if (active && gl == 0) reinterpret_cast<Out*>(I->out)[row * I->ors] = finish<Out, Acc, POST>(acc, fp);
+        }
+    }
+}
+
+template <class Tree, class LS, class OutT, int GL, int U>
+__global__ void __launch_bounds__(256) k_batch_assign(const BatchParams p) {
+    typedef typename LS::template R<1>::type RG;
+    __shared__ i64 s_tile;
+    Ctx<0> c;
+    c.scal = p.scal;
+    const int g = (int)threadIdx.x / GL, gl = (int)threadIdx.x % GL, ngroups = (int)blockDim.x / GL;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile = (i64)atomicAdd(p.counter, 1);
+        __syncthreads();
+        const i64 t = s_tile;
+        if (t >= p.ntiles) break;
+        const BatchTile tl = p.tiles[t];
+        const BatchInst* I = p.inst + tl.inst;
+        const i64 cols = I->cols;
+        for (int r = g; r < tl.nrows; r += ngroups) {
+            const i64 row = tl.row0 + r;
+            i64 base[XTG_KMAX_LEAVES], cs[XTG_KMAX_LEAVES];
+#pragma unroll
+            for (int l = 0; l < LS::N; ++l) {
+                base[l] = row * I->rs[l];
+                cs[l] = I->cs[l];
+            }
+            OutT* out = reinterpret_cast<OutT*>(I->out) + row * I->ors;
+            for (i64 c0 = gl; c0 < cols; c0 += (i64)GL * U) {
+                RG rg[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const i64 col = c0 + (i64)u * GL;
+                    if (col < cols) {
+                        i64 off[XTG_KMAX_LEAVES];
+#pragma unroll
+                        for (int l = 0; l < LS::N; ++l) off[l] = base[l] + col * cs[l];
+                        LoadLeavesAt<LS>::template run<1>(rg[u], I->leaf, off, cs);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const i64 col = c0 + (i64)u * GL;
+                    if (col < cols) out[col * I->ocs] = cvt<OutT>(Tree::ev(rg[u], 0, c));
+                }
+            }
+        }
+    }
+}
 
 // (a - m) / b with m and b invariant over a row, as one fused multiply-add
 // per element: a * r - m * r with r = 1 / b (r and m * r once per row).

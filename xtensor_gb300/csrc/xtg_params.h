@@ -104,5 +104,44 @@ struct RowParams {
     int* err;                         // set to 1 when a bounded wait gives up
 };
 
+// Batched evaluation: many instances of one expression shape, each a 2-D
+// (rows, cols) space with its own pointers and strides.
+struct BatchInst {
+    const void* leaf[XTG_KMAX_LEAVES];
+    i64 rs[XTG_KMAX_LEAVES];  // leaf strides between rows (0: broadcast)
+    i64 cs[XTG_KMAX_LEAVES];  // leaf strides between columns
+    void* out;
+    i64 ors, ocs;             // destination strides (reductions use ors only)
+    i64 rows, cols;
+    double divisor;           // mean divisor of a row
+};
+struct BatchTile {
+    int inst;
+    int nrows;
+    i64 row0;
+};
+struct BatchParams {
+    const BatchInst* inst;
+    const BatchTile* tiles;
+    i64 ntiles;
+    int* counter;             // next tile; zeroed before every launch
+    Scalars scal;
+    double init_f;
+    i64 init_i;
+    int has_initial;
+    double initial_f;
+    i64 initial_i;
+};
+// Per-row finishing parameters (the fields the accumulators' finishers read).
+struct FinP {
+    double init_f;
+    i64 init_i;
+    int has_initial;
+    double initial_f;
+    i64 initial_i;
+    double divisor;
+    i64 n_red;
+};
+
 }  // namespace xtg
 #endif

@@ -149,7 +149,7 @@ static bool same_array(const xtg_array& a, const xtg_array& b) {
     return true;
 }
 
-xtg_status build_tree(const xtg_expr* e, bool demote, Tree& t) {
+xtg_status build_tree(const xtg_expr* e, bool demote, Tree& t, bool dedup) {
     if (!e) return fail(XTG_ERR_INVALID, "null expression");
     if (e->n_nodes <= 0 || e->n_nodes > XTG_MAX_NODES) return fail(XTG_ERR_INVALID, "bad node count");
     if (e->n_leaves < 0 || e->n_leaves > XTG_MAX_LEAVES) return fail(XTG_ERR_INVALID, "bad leaf count");
@@ -180,7 +180,7 @@ xtg_status build_tree(const xtg_expr* e, bool demote, Tree& t) {
                 if (!valid_dtype(a.dtype)) return fail(XTG_ERR_INVALID, "leaf with invalid dtype");
                 if (a.rank < 0 || a.rank > XTG_MAX_RANK) return fail(XTG_ERR_INVALID, "leaf rank out of range");
                 int found = -1;
-                for (size_t k = 0; k < t.leaves.size(); ++k)
+                for (size_t k = 0; dedup && k < t.leaves.size(); ++k)
                     if (same_array(t.leaves[k], a)) found = (int)k;
                 if (found < 0) {
                     found = (int)t.leaves.size();
@@ -220,6 +220,7 @@ xtg_status build_tree(const xtg_expr* e, bool demote, Tree& t) {
     }
     if (st.size() != 1) return fail(XTG_ERR_INVALID, "malformed postfix expression (stack not 1 at end)");
     t.root = st[0];
+    t.expr_slot = leaf_slot;
     if (t.leaves.empty() && t.nodes[t.root].op != XTG_OP_SCALAR)
         return fail(XTG_ERR_INVALID, "expression without leaves");
     if (t.n_rstats > XTG_MAX_SCALARS) return fail(XTG_ERR_UNSUPPORTED, "too many row reductions");

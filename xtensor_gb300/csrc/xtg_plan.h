@@ -33,11 +33,14 @@ struct Tree {
     bool has_f64_leaf = false;
     int rank = 0;                   // broadcast rank
     int64_t shape[XTG_MAX_RANK] = {0};
+    std::vector<int> expr_slot;     // xtg_expr leaf index -> leaf slot (-1: unused)
 };
 
 // Parse + type-check + broadcast.  `demote` enables float32 evaluation of
-// float64 nodes (only when no leaf is float64).
-xtg_status build_tree(const xtg_expr* e, bool demote, Tree& t);
+// float64 nodes (only when no leaf is float64).  `dedup` merges leaves that
+// describe the same array (off for batch templates, whose leaves are
+// placeholders).
+xtg_status build_tree(const xtg_expr* e, bool demote, Tree& t, bool dedup = true);
 int promote(int a, int b);
 bool is_rop(int op);
 // Type string of the subtree at node `n` (leaf indices through `leaf_map`).
@@ -69,5 +72,18 @@ struct ScratchSpec {
 xtg_status reduce_impl(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, cudaStream_t stream,
                        const ScratchSpec* scratch);
 xtg_status assign_tree(const Tree& t, const xtg_array* out, cudaStream_t stream);
+
+// Accumulator type string, post-operation and initial values of a reduction.
+struct AccChoice {
+    std::string acc;
+    int post = 0;
+    double init_f = 0;
+    int64_t init_i = 0;
+    int has_initial = 0;
+    double initial_f = 0;
+    int64_t initial_i = 0;
+    int result_dtype = -1;
+};
+xtg_status choose_acc(const Tree& t, const xtg_reduce_desc* rd, AccChoice& ch);
 
 }  // namespace xtgh

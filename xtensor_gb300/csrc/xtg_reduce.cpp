@@ -333,36 +333,15 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
     return st;
 }
 
-static bool out_matches(const xtg_array& out, int rank, const int64_t* shape) {
-    if (out.rank != rank) return false;
-    for (int d = 0; d < rank; ++d)
-        if (out.shape[d] != shape[d]) return false;
-    return true;
-}
-
-xtg_status reduce_impl(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, cudaStream_t stream,
-                       const ScratchSpec* scratch) {
-    if (!rd || !out) return fail(XTG_ERR_INVALID, "null argument");
-    Tree t;
-    XTG_TRY(build_tree(e, opt("fp32_compute", 1) != 0, t));
-    if (t.n_rstats) return fail(XTG_ERR_UNSUPPORTED, "row statistics inside a reduction operand");
-    RedShape S;
-    XTG_TRY(red_shape(t, rd, rd->keep_dims != 0, S));
+// Accumulator, post-operation and initial values of a reduction (shared by
+// xtg_reduce and the batched layer).
+xtg_status choose_acc(const Tree& t, const xtg_reduce_desc* rd, AccChoice& ch) {
     const int vt = t.nodes[t.root].cxx_dtype;
     const int rt = result_type(rd, vt);
-    if (out->dtype != rt)
-        return fail(XTG_ERR_INVALID, "destination dtype " + std::to_string(out->dtype) + " differs from the result type " +
-                                         std::to_string(rt));
-    if (!out_matches(*out, S.out_rank, S.out_shape)) return fail(XTG_ERR_SHAPE, "destination shape mismatch");
-    if (!out->data) return fail(XTG_ERR_INVALID, "null destination data");
-    XTG_TRY(ensure_device(nullptr));
-
     // the element compute type (after fp32 demotion)
     const int ct = vcomp(t.nodes[t.root].dtype);
     std::string acc;
     int post = 0;
-    xtg::RedParams p;
-    memset(&p, 0, sizeof p);
     double f0 = 0;
     int64_t i0 = 0;
     const bool comp = rd->precision == XTG_PREC_COMPENSATED;
@@ -405,16 +384,58 @@ xtg_status reduce_impl(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_a
         case XTG_RED_NORM_LINF: acc = std::string("xtg::AccNorm<") + dt(vcomp(rt)).cname + ", 3>"; break;
         default: return fail(XTG_ERR_INVALID, "unknown reduction op");
     }
-    p.init_f = f0;
-    p.init_i = i0;
-    p.has_initial = rd->has_initial;
+    ch.acc = acc;
+    ch.post = post;
+    ch.init_f = f0;
+    ch.init_i = i0;
+    ch.has_initial = rd->has_initial;
+    ch.initial_f = 0;
+    ch.initial_i = 0;
+    ch.result_dtype = rt;
     if (rd->has_initial) {
-        int at = dt(rt).is_float ? 1 : 0;
-        if (at) p.initial_f = rd->initial.f;
-        else p.initial_i = rd->initial.i;
+        if (dt(rt).is_float) ch.initial_f = rd->initial.f;
+        else ch.initial_i = rd->initial.i;
         if (rd->op == XTG_RED_MEAN || rd->op == XTG_RED_VARIANCE || rd->op == XTG_RED_STDDEV || rd->op >= XTG_RED_NORM_L0)
-            p.has_initial = 0;
+            ch.has_initial = 0;
     }
+    return XTG_OK;
+}
+
+static bool out_matches(const xtg_array& out, int rank, const int64_t* shape) {
+    if (out.rank != rank) return false;
+    for (int d = 0; d < rank; ++d)
+        if (out.shape[d] != shape[d]) return false;
+    return true;
+}
+
+xtg_status reduce_impl(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, cudaStream_t stream,
+                       const ScratchSpec* scratch) {
+    if (!rd || !out) return fail(XTG_ERR_INVALID, "null argument");
+    Tree t;
+    XTG_TRY(build_tree(e, opt("fp32_compute", 1) != 0, t));
+    if (t.n_rstats) return fail(XTG_ERR_UNSUPPORTED, "row statistics inside a reduction operand");
+    RedShape S;
+    XTG_TRY(red_shape(t, rd, rd->keep_dims != 0, S));
+    const int vt = t.nodes[t.root].cxx_dtype;
+    const int rt = result_type(rd, vt);
+    if (out->dtype != rt)
+        return fail(XTG_ERR_INVALID, "destination dtype " + std::to_string(out->dtype) + " differs from the result type " +
+                                         std::to_string(rt));
+    if (!out_matches(*out, S.out_rank, S.out_shape)) return fail(XTG_ERR_SHAPE, "destination shape mismatch");
+    if (!out->data) return fail(XTG_ERR_INVALID, "null destination data");
+    XTG_TRY(ensure_device(nullptr));
+
+    xtg::RedParams p;
+    memset(&p, 0, sizeof p);
+    AccChoice ch;
+    XTG_TRY(choose_acc(t, rd, ch));
+    const std::string acc = ch.acc;
+    const int post = ch.post;
+    p.init_f = ch.init_f;
+    p.init_i = ch.init_i;
+    p.has_initial = ch.has_initial;
+    p.initial_f = ch.initial_f;
+    p.initial_i = ch.initial_i;
     // mean / variance divisor: (size - ddof) / n_outputs with integer division
     int64_t size = 1, n_out = 1;
     for (int d = 0; d < t.rank; ++d) size *= t.shape[d];
