@@ -535,6 +535,182 @@ def run_c3(args):
     return 0
 
 
+def c4_pool(n_templates, seed=4):
+    """Request templates of the serving mix: kinds of the four configurations,
+    element counts log-uniform in [1e3, 1e8], dtypes float32/float64/int32 at
+    50/25/25 %, operands generated on the device (seeded)."""
+    import xtensor_gb300 as xg
+    from xtensor_gb300 import ops
+    from xtensor_gb300.batch import fill_random
+    from xtensor_gb300.device import DeviceArray
+    from xtensor_gb300.server import ARGREDUCE, ASSIGN, REDUCE
+
+    g = np.random.default_rng(seed)
+    pool = []
+    sd = [0]
+
+    def arr(shape, dt):
+        sd[0] += 1
+        a = DeviceArray.empty(shape, dt)
+        if dt == "int32":
+            return fill_random(a, "integers", -1000, 1000, 4_000_000 + sd[0])
+        return fill_random(a, "normal", 0, 1, 4_000_000 + sd[0])
+
+    for i in range(n_templates):
+        n = int(round(10 ** g.uniform(3, 8)))
+        dt = ["float32", "float32", "float64", "int32"][g.integers(0, 4)]
+        kinds = ["c0", "c1", "c2", "c3"] if dt != "int32" else ["c1", "c2", "c3"]
+        k = kinds[g.integers(0, len(kinds))]
+        cols = int(min(4096, max(16, 2 ** round(np.log2(max(n, 16) ** 0.5)))))
+        rows = max(1, n // cols)
+        if k == "c0":
+            A, b = arr((rows, cols), dt), arr((cols,), dt)
+            e = A * b + xg.exp(-A * A)
+            if g.integers(0, 2):
+                pool.append((ASSIGN, None, e, None, (rows, cols), [A, b], 2 * rows * cols + cols))
+            else:
+                pool.append((REDUCE, "sum", e, [1], (rows,), [A, b], rows * cols + cols + rows))
+        elif k == "c3":
+            A, v, Cm = arr((rows, cols), dt), arr((cols,), dt), arr((rows, cols), dt)
+            pool.append((REDUCE, "sum", A * v + Cm, [1], (rows,), [A, v, Cm], 2 * rows * cols + cols + rows))
+        elif k == "c2":
+            x = arr((n,), dt)
+            op = "sum" if dt == "int32" else ["sum", "mean", "variance", "norm_l2"][g.integers(0, 4)]
+            pool.append((REDUCE, op, x, None, (), [x], n + 1))
+        else:
+            d2 = min(1024, cols)
+            d1 = max(1, min(512, rows))
+            d0 = max(1, n // (d1 * d2))
+            x = arr((d0, d1, d2), dt)
+            sub = ["transpose", "normalize", "amax", "argmax"][g.integers(0, 4)] if dt != "int32" else \
+                ["transpose", "amax", "argmax"][g.integers(0, 3)]
+            m = d0 * d1 * d2
+            if sub == "transpose":
+                pool.append((ASSIGN, None, x.transpose((2, 0, 1)), None, (d2, d0, d1), [x], 2 * m))
+            elif sub == "normalize":
+                pool.append((ASSIGN, None, (x - xg.rmean(x)) / xg.sqrt(xg.rvar(x) + 1e-5), None, (d0, d1, d2), [x], 2 * m))
+            elif sub == "amax":
+                pool.append((REDUCE, "amax", x, [0, 2], (d1,), [x], m + d1))
+            else:
+                pool.append((ARGREDUCE, "argmax", x, 1, (d0, d2), [x], m + d0 * d2))
+    return pool
+
+
+def run_c4(args):
+    """Serving: Poisson arrivals (rate sweep) of requests drawn from the
+    pool; served (xtg_server: admission by HBM budget, continuous batching,
+    multi-stream overlap) vs plain (each request evaluated synchronously in
+    arrival order, one launch per expression).  Latency = completion - arrival."""
+    import xtensor_gb300 as xg
+    from xtensor_gb300._ffi import ITEMSIZE, check
+    from xtensor_gb300 import ops
+    from xtensor_gb300.device import DeviceArray, Stream
+    from xtensor_gb300.server import ARGREDUCE, ASSIGN, REDUCE, Server
+
+    xg.init(0)
+    lib = xg.lib()
+    pool = c4_pool(args.templates)
+    outs = []
+    for kind, op, e, axes, shape, keep, elems in pool:
+        if kind == ASSIGN:
+            outs.append(DeviceArray.empty(shape, xg.expr_dtype(e)))
+        elif kind == ARGREDUCE:
+            outs.append(DeviceArray.empty(shape, "int64"))
+        else:
+            sh, code = ops.reduce_shape(op, e, axes=axes)
+            outs.append(DeviceArray.empty(sh, code))
+    check(lib.xtg_device_sync())
+
+    def req_bytes(i):
+        kind, op, e, axes, shape, keep, elems = pool[i]
+        return sum(a.nbytes for a in keep) + outs[i].nbytes
+
+    srv = Server(streams=8, max_inflight=128, batch_min_group=3)
+    reqs = [srv.request(kind, e, outs[i], op=op, axes=axes, arg_axis=axes)[0] for i, (kind, op, e, axes, *_r) in
+            enumerate(pool)]
+    s = Stream()
+
+    def plain_one(i):
+        kind, op, e, axes, shape, keep, elems = pool[i]
+        r = reqs[i]
+        if kind == ASSIGN:
+            check(lib.xtg_assign(C.byref(r.expr), C.byref(r.out), s.handle))
+        elif kind == REDUCE:
+            check(lib.xtg_reduce(C.byref(r.expr), C.byref(r.rd), C.byref(r.out), s.handle))
+        else:
+            check(lib.xtg_argreduce(C.byref(r.expr), r.arg_op, r.has_axis, r.axis, C.byref(r.out), s.handle))
+        s.sync()
+
+    # warm-up: every template once through both paths (kernel compilation)
+    for i in range(len(pool)):
+        plain_one(i)
+    ids = []
+    for i in range(len(pool)):
+        rid = C.c_uint64()
+        check(srv.L.xtg_server_submit(srv.h, C.byref(reqs[i]), C.byref(rid)))
+        ids.append(rid.value)
+    for rid in ids:
+        srv.wait(rid, 600000)
+    srv.reset_stats()
+
+    g = np.random.default_rng(44)
+    rates = [float(r) for r in args.rates.split(",")]
+    results = []
+    for rate in rates:
+        n = args.requests
+        gaps = g.exponential(1.0 / rate, n)
+        arrivals = np.cumsum(gaps)
+        picks = g.integers(0, len(pool), n)
+        total_bytes = sum(req_bytes(int(p)) for p in picks)
+        # plain
+        lat = []
+        t0 = time.perf_counter()
+        for a, p in zip(arrivals, picks):
+            while time.perf_counter() - t0 < a:
+                pass
+            plain_one(int(p))
+            lat.append((time.perf_counter() - t0 - a) * 1e3)
+        plain_wall = time.perf_counter() - t0
+        # served
+        srv.reset_stats()
+        ids = []
+        t0 = time.perf_counter()
+        for a, p in zip(arrivals, picks):
+            while time.perf_counter() - t0 < a:
+                pass
+            rid = C.c_uint64()
+            check(srv.L.xtg_server_submit(srv.h, C.byref(reqs[int(p)]), C.byref(rid)))
+            ids.append(rid.value)
+        srv.drain(600000)
+        served_wall = time.perf_counter() - t0
+        for rid in ids:
+            srv.wait(rid, 600000)
+        st = srv.stats()
+        lat.sort()
+        results.append({
+            "rate_req_s": rate, "requests": n,
+            "plain": {"p50_ms": round(lat[n // 2], 3), "p99_ms": round(lat[int(0.99 * (n - 1))], 3),
+                      "req_s": round(n / plain_wall, 1), "GB/s": round(total_bytes / plain_wall / 1e9, 1)},
+            "served": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                       "req_s": round(n / served_wall, 1), "GB/s": round(total_bytes / served_wall / 1e9, 1),
+                       "batched_requests": st["batched_requests"], "batch_launches": st["batch_launches"],
+                       "waves": st["waves"]},
+        })
+    best = max(results, key=lambda r: r["served"]["req_s"])
+    line = {
+        "metric": "served p50/p99 ms vs plain (Poisson mix of the four expression kinds)", "unit": "req/s",
+        "value": best["served"]["req_s"], "higher_is_better": True, "n_gpus": 1, "dtype": "f32,f64,int32",
+        "data": "synthetic (device generator, seed 4)",
+        "config": {"workload": "serving: Poisson arrivals, kinds of configs 0-3, elements log-uniform 1e3..1e8, "
+                               "float32/float64/int32 50/25/25", "templates": len(pool),
+                   "pool_bytes": int(sum(req_bytes(i) for i in range(len(pool))))},
+        "sweep": results,
+    }
+    srv.close()
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -544,15 +720,19 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--shape", default=None, help="profiling only: d0,d1,d2 instead of 256,512,1024")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c3"],
-                    help="c1: strided/axis work (default, the headline); c3: batching of uneven instances")
+    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4"],
+                    help="c1: strided/axis work (default, the headline); c3: batching of uneven instances; "
+                         "c4: served Poisson request mix")
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--templates", type=int, default=256)
+    ap.add_argument("--requests", type=int, default=2000)
+    ap.add_argument("--rates", default="2000,16000,48000,96000")
     args = ap.parse_args()
-    if args.workload == "c3":
+    if args.workload in ("c3", "c4"):
         from xtensor_gb300.build import build
         build()
-        return run_c3(args)
+        return run_c3(args) if args.workload == "c3" else run_c4(args)
     if args.shape:
         global SHAPE, N
         SHAPE = tuple(int(v) for v in args.shape.split(","))

@@ -281,6 +281,62 @@ xtg_status xtg_batch_replay(xtg_batch* b, xtg_stream stream);
 xtg_status xtg_batch_get_info(const xtg_batch* b, xtg_batch_info* info);
 xtg_status xtg_batch_destroy(xtg_batch* b);
 
+/* ---- request server -------------------------------------------------------------------
+ * No counterpart in the reference.  A request is one evaluation on operands
+ * already resident in device memory: an assignment (out = expr), a reduction
+ * (out = reduce(expr, rd)) or an arg-reduction.  xtg_server_submit never
+ * blocks on the GPU: a scheduler thread admits pending requests while the
+ * in-flight limit and the HBM budget allow (a request's cost is its declared
+ * workspace plus the scratch its plan needs), groups admitted small requests
+ * of the same tree shape into one batched launch, dispatches the others on a
+ * pool of streams so their work overlaps, and completes requests from
+ * stream callbacks.  Requests that arrive while others run join the next
+ * admission round (continuous batching).  Latency = completion - submit. */
+typedef struct xtg_server xtg_server;
+typedef struct {
+    int32_t streams;             /* concurrent CUDA streams (default 8) */
+    int32_t max_inflight;        /* admitted, unfinished requests (default 256) */
+    int64_t hbm_budget_bytes;    /* admission budget; 0: 90% of free HBM at creation */
+    int64_t batch_max_elems;     /* requests up to this many elements may be grouped (default 1<<20) */
+    int32_t batch_min_group;     /* smallest group launched as one batch (default 4) */
+    int32_t pad;
+} xtg_server_config;
+enum { XTG_REQ_ASSIGN = 0, XTG_REQ_REDUCE = 1, XTG_REQ_ARGREDUCE = 2 };
+typedef struct {
+    int32_t kind;                /* XTG_REQ_* */
+    int32_t arg_op;              /* argreduce: XTG_ARGMAX / XTG_ARGMIN */
+    int32_t has_axis;
+    int32_t pad;
+    int64_t axis;
+    int64_t workspace_bytes;     /* extra device memory the caller attributes to it */
+    xtg_expr expr;
+    xtg_reduce_desc rd;
+    xtg_array out;
+} xtg_request;
+typedef struct {
+    int32_t status;              /* xtg_status of the evaluation */
+    int32_t batched;             /* 1 if it ran inside a grouped launch */
+    double queue_ms;             /* submit -> dispatch */
+    double total_ms;             /* submit -> completion */
+} xtg_request_result;
+typedef struct {
+    int64_t submitted, completed, failed, rejected, cancelled, inflight, pending;
+    int64_t waves, batched_requests, batch_launches;
+    int64_t hbm_budget, hbm_reserved;
+    double p50_ms, p99_ms, mean_ms;   /* over completed requests since the last reset */
+} xtg_server_stats;
+xtg_status xtg_server_create(const xtg_server_config* cfg, xtg_server** s);
+xtg_status xtg_server_submit(xtg_server* s, const xtg_request* r, uint64_t* id);
+/* timeout_ms < 0: wait forever; XTG_ERR_TIMEOUT when it runs out (the request
+ * stays queued / in flight). */
+xtg_status xtg_server_wait(xtg_server* s, uint64_t id, int64_t timeout_ms, xtg_request_result* res);
+/* Cancels a request that has not been dispatched yet (XTG_ERR_NOT_FOUND otherwise). */
+xtg_status xtg_server_cancel(xtg_server* s, uint64_t id);
+xtg_status xtg_server_drain(xtg_server* s, int64_t timeout_ms);
+xtg_status xtg_server_get_stats(xtg_server* s, xtg_server_stats* st);
+xtg_status xtg_server_reset_stats(xtg_server* s);
+xtg_status xtg_server_destroy(xtg_server* s);
+
 /* Seeded synthetic data on the device (the benchmarks' inputs): element i of
  * a contiguous array gets a value from a counter-based generator keyed by
  * (seed, i), independent of the launch configuration.  dist: 0 uniform

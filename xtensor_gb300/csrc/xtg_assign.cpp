@@ -465,8 +465,10 @@ extern "C" xtg_status xtg_assign(const xtg_expr* e, const xtg_array* out, xtg_st
     if (!valid_dtype(out->dtype) || out->rank < 0 || out->rank > XTG_MAX_RANK)
         return fail(XTG_ERR_INVALID, "bad destination descriptor");
     begin_call();
-    Tree t;
-    const bool demote = opt("fp32_compute", 1) != 0 && out->dtype != XTG_FLOAT64;
-    XTG_TRY(build_tree(e, demote, t));
-    return assign_tree(t, out, (cudaStream_t)stream);
+    return with_plan_cache(0, e, nullptr, out, 0, 0, 0, (cudaStream_t)stream, [&]() -> xtg_status {
+        Tree t;
+        const bool demote = opt("fp32_compute", 1) != 0 && out->dtype != XTG_FLOAT64;
+        XTG_TRY(build_tree(e, demote, t));
+        return assign_tree(t, out, (cudaStream_t)stream);
+    });
 }

@@ -36,12 +36,15 @@ struct xtg_batch {
     int out_dtype = -1;
     int64_t elements = 0;
     int64_t bytes = 0;
-    // device state
+    // device state (stream-ordered allocations; host copies stay alive until
+    // the batch is destroyed, so uploads never wait for the stream)
     xtg::BatchInst* d_inst = nullptr;
     xtg::BatchTile* d_tiles = nullptr;
     int* d_counter = nullptr;
     int64_t ntiles = 0;
     size_t tiles_cap = 0;
+    std::vector<std::vector<xtg::BatchTile>> h_tiles;
+    cudaStream_t stream = nullptr;  // stream of the last allocation / launch
     // configuration
     int gl = 32, unroll = 4, cpsm = 4;
     int64_t tile_elems = 32768;
@@ -132,16 +135,17 @@ xtg_status make_tiles(xtg_batch* b, int64_t te, std::vector<xtg::BatchTile>& til
 }
 
 xtg_status upload_tiles(xtg_batch* b, int64_t te, cudaStream_t s) {
-    std::vector<xtg::BatchTile> tiles;
+    b->h_tiles.emplace_back();
+    std::vector<xtg::BatchTile>& tiles = b->h_tiles.back();
     XTG_TRY(make_tiles(b, te, tiles));
     if (tiles.size() > b->tiles_cap) {
-        if (b->d_tiles) XTG_CUDA(cudaFree(b->d_tiles));
+        if (b->d_tiles) XTG_CUDA(cudaFreeAsync(b->d_tiles, s));
         b->tiles_cap = tiles.size() + 64;
-        XTG_CUDA(cudaMalloc((void**)&b->d_tiles, b->tiles_cap * sizeof(xtg::BatchTile)));
+        XTG_CUDA(cudaMallocAsync((void**)&b->d_tiles, b->tiles_cap * sizeof(xtg::BatchTile), s));
     }
     if (!tiles.empty())
         XTG_CUDA(cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(xtg::BatchTile), cudaMemcpyHostToDevice, s));
-    XTG_CUDA(cudaStreamSynchronize(s));
+    b->stream = s;
     b->ntiles = (int64_t)tiles.size();
     b->tile_elems = te;
     return XTG_OK;
@@ -167,7 +171,8 @@ std::string kernel_name(xtg_batch* b, const Tree& t, int gl, const AccChoice* ch
 xtg_status launch_once(xtg_batch* b, cudaStream_t s) {
     DeviceInfo* dev;
     XTG_TRY(ensure_device(&dev));
-    XTG_CUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int), s));
+    if (!dry_run()) XTG_CUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int), s));
+    b->stream = s;
     int64_t cap = (int64_t)std::min(b->k->max_blocks_per_sm, b->cpsm) * dev->sm_count;
     unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(b->ntiles, cap));
     return launch(b->k, grid, 256, &b->params, s);
@@ -278,10 +283,11 @@ xtg_status xtg_batch_build(xtg_batch* b, int32_t autotune, xtg_stream stream) {
     }
     // device work list
     if (!dry_run()) {
-        if (!b->d_inst) XTG_CUDA(cudaMalloc((void**)&b->d_inst, b->inst.size() * sizeof(xtg::BatchInst)));
+        if (!b->d_inst) XTG_CUDA(cudaMallocAsync((void**)&b->d_inst, b->inst.size() * sizeof(xtg::BatchInst), s));
         XTG_CUDA(cudaMemcpyAsync(b->d_inst, b->inst.data(), b->inst.size() * sizeof(xtg::BatchInst),
                                  cudaMemcpyHostToDevice, s));
-        if (!b->d_counter) XTG_CUDA(cudaMalloc((void**)&b->d_counter, 256));
+        if (!b->d_counter) XTG_CUDA(cudaMallocAsync((void**)&b->d_counter, 256, s));
+        b->stream = s;
     }
     memset(&b->params, 0, sizeof b->params);
     b->params.inst = b->d_inst;
@@ -442,9 +448,10 @@ xtg_status xtg_batch_destroy(xtg_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (!dry_run()) {
-        if (b->d_inst) cudaFree(b->d_inst);
-        if (b->d_tiles) cudaFree(b->d_tiles);
-        if (b->d_counter) cudaFree(b->d_counter);
+        // stream-ordered: the frees wait for the batch's last launch
+        if (b->d_inst) cudaFreeAsync(b->d_inst, b->stream);
+        if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->stream);
+        if (b->d_counter) cudaFreeAsync(b->d_counter, b->stream);
     }
     delete b;
     return XTG_OK;

@@ -90,7 +90,32 @@ struct Kernel {
 // (e.g. "xtg::k_assign<...>").  `block` / `dyn_smem` are used for the
 // occupancy query (and dyn_smem > 48 KiB raises the kernel's limit).
 xtg_status get_kernel(const std::string& expr, int block, Kernel** k, size_t dyn_smem = 0);
-xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream, size_t dyn_smem = 0);
+// Launch with a parameter block of `psize` bytes.  scratch_off >= 0: byte
+// offset of a pointer to the call's split-reduction scratch inside the
+// block (patched when a cached plan is replayed with fresh scratch).
+xtg_status launch_raw(Kernel* k, unsigned grid, unsigned block, const void* params, size_t psize, cudaStream_t stream,
+                      size_t dyn_smem, int scratch_off);
+template <class P>
+xtg_status launch(Kernel* k, unsigned grid, unsigned block, P* params, cudaStream_t stream, size_t dyn_smem = 0,
+                  int scratch_off = -1) {
+    return launch_raw(k, grid, block, params, sizeof(P), stream, dyn_smem, scratch_off);
+}
+
+// ---- plan recording / replay (xtg_plancache.cpp) ------------------------------
+struct RecLaunch {
+    Kernel* k;
+    unsigned grid, block;
+    size_t smem;
+    std::vector<unsigned char> params;
+    int scratch_off;
+};
+struct Recorder {
+    std::vector<RecLaunch> launches;
+    size_t scratch_bytes = 0;
+    int scratch_allocs = 0;
+};
+Recorder*& recorder();  // the calling thread's active recorder (nullptr: none)
+int64_t opt_generation();  // increments whenever an option changes
 // A device word that kernels set when a bounded wait gives up.
 xtg_status device_error_word(int** p);
 void count_launch();

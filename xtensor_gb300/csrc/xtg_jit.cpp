@@ -219,15 +219,31 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out, size_t d
     return XTG_OK;
 }
 
-xtg_status launch(Kernel* k, unsigned grid, unsigned block, void* params, cudaStream_t stream, size_t dyn_smem) {
+Recorder*& recorder() {
+    static thread_local Recorder* r = nullptr;
+    return r;
+}
+
+xtg_status launch_raw(Kernel* k, unsigned grid, unsigned block, const void* params, size_t psize, cudaStream_t stream,
+                      size_t dyn_smem, int scratch_off) {
     if (grid == 0) return XTG_OK;
+    if (Recorder* rec = recorder()) {
+        RecLaunch l;
+        l.k = k;
+        l.grid = grid;
+        l.block = block;
+        l.smem = dyn_smem;
+        l.params.assign((const unsigned char*)params, (const unsigned char*)params + psize);
+        l.scratch_off = scratch_off;
+        rec->launches.push_back(std::move(l));
+    }
     if (!t_last_kernels.empty()) t_last_kernels += ";";
     t_last_kernels += k->name.compare(0, 5, "xtg::") == 0 ? k->name.substr(5) : k->name;
     if (dry_run()) {
         g_launches.fetch_add(1, std::memory_order_relaxed);
         return XTG_OK;
     }
-    void* args[1] = {params};
+    void* args[1] = {const_cast<void*>(params)};
     XTG_CU(drv().LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, (unsigned)dyn_smem, (CUstream)stream, args, nullptr));
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return XTG_OK;

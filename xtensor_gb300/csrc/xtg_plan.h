@@ -86,4 +86,27 @@ struct AccChoice {
 };
 xtg_status choose_acc(const Tree& t, const xtg_reduce_desc* rd, AccChoice& ch);
 
+// ---- plan cache (xtg_plancache.cpp) -----------------------------------------------
+bool plan_cache_enabled();
+std::vector<unsigned char> plan_key(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out,
+                                    int32_t a0, int32_t a1, int64_t a2);
+bool plan_replay(const std::vector<unsigned char>& key, cudaStream_t s, xtg_status* st);
+void plan_store(std::vector<unsigned char>&& key, Recorder& rec);
+
+// Runs `fn` (a planning + launching call) through the plan cache.
+template <class F>
+xtg_status with_plan_cache(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, int32_t a0,
+                           int32_t a1, int64_t a2, cudaStream_t s, F&& fn) {
+    if (!e || !out || !plan_cache_enabled() || recorder()) return fn();
+    std::vector<unsigned char> key = plan_key(kind, e, rd, out, a0, a1, a2);
+    xtg_status st;
+    if (plan_replay(key, s, &st)) return st;
+    Recorder rec;
+    recorder() = &rec;
+    st = fn();
+    recorder() = nullptr;
+    if (st == XTG_OK) plan_store(std::move(key), rec);
+    return st;
+}
+
 }  // namespace xtgh

@@ -290,6 +290,8 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         }
     }
     p.partial = part;
+    // where a replayed plan patches in its fresh scratch (stream-ordered only)
+    const int part_off = (part && !(scratch && scratch->fixed)) ? (int)offsetof(xtg::RedParams, partial) : -1;
 
     Kernel* k;
     xtg_status st;
@@ -302,7 +304,7 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         if (st == XTG_OK) {
             int64_t items = n_out * nsplit;
             int64_t need = group == 32 ? (items + 7) / 8 : items;
-            st = launch(k, grid_cap(k, need), 256, &p, stream);
+            st = launch(k, grid_cap(k, need), 256, &p, stream, 0, part_off);
         }
     } else {
         const int U = (int)opt("reduce.col_unroll", 4);
@@ -312,7 +314,7 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         st = get_kernel(name, 256, &k);
         if (st == XTG_OK) {
             int64_t need = (p.n_outv * nsplit + 255) / 256;
-            st = launch(k, grid_cap(k, need), 256, &p, stream);
+            st = launch(k, grid_cap(k, need), 256, &p, stream, 0, part_off);
         }
     }
     if (st == XTG_OK && nsplit > 1) {
@@ -324,7 +326,8 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
                            accname + ", " + outc + ", " + std::to_string(post) + ", " + std::to_string(RO) + ">";
         Kernel* kc;
         st = get_kernel(name, 256, &kc);
-        if (st == XTG_OK) st = launch(kc, grid_cap(kc, per_thread ? (n_out + 255) / 256 : n_out), 256, &pc, stream);
+        if (st == XTG_OK)
+            st = launch(kc, grid_cap(kc, per_thread ? (n_out + 255) / 256 : n_out), 256, &pc, stream, 0, part_off);
     }
     if (part && !(scratch && scratch->fixed)) {
         xtg_status fs = scratch_free(part, stream);
@@ -531,13 +534,16 @@ xtg_status xtg_reduce_acc_dtype(const xtg_expr* e, const xtg_reduce_desc* rd, in
 
 xtg_status xtg_reduce(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, xtg_stream stream) {
     begin_call();
-    return reduce_impl(e, rd, out, (cudaStream_t)stream, nullptr);
+    if (!rd) return fail(XTG_ERR_INVALID, "null reduce descriptor");
+    return with_plan_cache(1, e, rd, out, 0, 0, 0, (cudaStream_t)stream,
+                           [&]() { return reduce_impl(e, rd, out, (cudaStream_t)stream, nullptr); });
 }
 
 xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis, const xtg_array* out,
                          xtg_stream stream) {
     begin_call();
-    return argreduce_impl(e, op, has_axis, axis, out, (cudaStream_t)stream);
+    return with_plan_cache(2, e, nullptr, out, op, has_axis, axis, (cudaStream_t)stream,
+                           [&]() { return argreduce_impl(e, op, has_axis, axis, out, (cudaStream_t)stream); });
 }
 
 }  // extern "C"

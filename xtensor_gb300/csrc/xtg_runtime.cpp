@@ -2,6 +2,7 @@
 // reporting of the C ABI.  xtensor reports failures by exceptions
 // (XTENSOR_THROW, include/xtensor/core/xtensor_config.hpp:27-33); across a C
 // ABI they become xtg_status codes plus a thread-local message.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -131,6 +132,9 @@ xtg_status ensure_device(DeviceInfo** info) {
 // ---- options ------------------------------------------------------------------------------
 static std::mutex g_opt_mu;
 static std::map<std::string, int64_t> g_opts;
+static std::atomic<int64_t> g_opt_gen{0};
+
+int64_t opt_generation() { return g_opt_gen.load(); }
 
 int64_t opt(const char* key, int64_t dflt) {
     std::lock_guard<std::mutex> lk(g_opt_mu);
@@ -140,6 +144,10 @@ int64_t opt(const char* key, int64_t dflt) {
 
 xtg_status scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
     if (bytes == 0) bytes = 16;
+    if (Recorder* rec = recorder()) {
+        rec->scratch_bytes = bytes;
+        rec->scratch_allocs++;
+    }
     if (dry_run()) {
         *p = (void*)(uintptr_t)0x7f0000000000ull;
         return XTG_OK;
@@ -363,6 +371,7 @@ xtg_status xtg_set_option(const char* key, int64_t value) {
     std::lock_guard<std::mutex> lk(g_opt_mu);
     if (value < 0) g_opts.erase(key);
     else g_opts[key] = value;
+    g_opt_gen.fetch_add(1);
     return XTG_OK;
 }
 

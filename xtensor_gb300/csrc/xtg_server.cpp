@@ -1,0 +1,466 @@
+// xtg_server.cpp — request server with admission by HBM budget and
+// continuous batching (no counterpart in xtensor, which evaluates one
+// expression at a time on the calling thread).
+//
+// Threads: callers submit (never blocking on the GPU); one scheduler thread
+// admits and dispatches; CUDA stream callbacks complete requests.
+//   admission — in arrival order, a pending request is admitted when the
+//     in-flight count is below the limit and its cost (declared workspace +
+//     the split-reduction scratch its plan may take) fits the remaining HBM
+//     budget; a request that waited longer than the aging limit blocks later
+//     ones from overtaking it.  Requests larger than the whole budget are
+//     rejected at submit.
+//   dispatch — admitted small requests (at most batch_max_elems elements,
+//     2-D, elementwise or last-axis reductions) with the same tree shape and
+//     immediates form a group launched as ONE batched kernel; everything else
+//     goes out individually.  Units are spread round-robin over the stream
+//     pool so their work overlaps on the device.
+//   completion — cudaLaunchHostFunc after each unit marks its requests done
+//     with a host timestamp and releases their budget; the scheduler frees
+//     batch work lists once their units completed.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "xtg_plan.h"
+
+using namespace xtgh;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+struct Req {
+    uint64_t id = 0;
+    xtg_request r;
+    int64_t cost = 0;
+    int64_t elems = 0;
+    bool batchable = false;
+    std::string sig;
+    Clock::time_point t_submit, t_dispatch, t_done;
+    int status = XTG_OK;
+    bool finished = false;
+    bool dispatched = false;
+    bool batched = false;
+};
+
+struct Unit;
+
+}  // namespace
+
+struct xtg_server {
+    xtg_server_config cfg;
+    std::vector<cudaStream_t> streams;
+    size_t next_stream = 0;
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_done;
+    std::deque<Req*> pending;
+    std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
+    std::vector<Unit*> finished_units;
+    uint64_t next_id = 1;
+    uint64_t events = 0;  // submits + completions + cancels: admission retries only when it changes
+    int64_t budget = 0, reserved = 0, inflight = 0;
+    bool stop = false;
+    std::thread sched;
+    xtg_server_stats st{};
+    std::vector<double> lat;
+};
+
+namespace {
+
+struct Unit {
+    xtg_server* srv;
+    std::vector<Req*> reqs;
+    xtg_batch* batch = nullptr;
+};
+
+void CUDART_CB on_unit_done(void* p) {
+    Unit* u = (Unit*)p;
+    xtg_server* s = u->srv;
+    const auto now = Clock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (Req* r : u->reqs) {
+        r->t_done = now;
+        r->finished = true;
+        s->inflight--;
+        s->reserved -= r->cost;
+        s->st.completed++;
+        s->lat.push_back(std::chrono::duration<double, std::milli>(now - r->t_submit).count());
+    }
+    s->finished_units.push_back(u);
+    s->events++;
+    s->cv_done.notify_all();
+    s->cv_sched.notify_all();
+}
+
+// Completion of a unit once the stream reaches this point (inline in dry-run
+// mode, where nothing runs on a device).
+void complete_after(cudaStream_t st, Unit* u) {
+    if (dry_run()) {
+        on_unit_done(u);
+        return;
+    }
+    if (cudaLaunchHostFunc(st, on_unit_done, u) != cudaSuccess) {
+        cudaGetLastError();
+        cudaStreamSynchronize(st);
+        on_unit_done(u);
+    }
+}
+
+int64_t elems_of(const xtg_expr& e, int64_t* shape_rank = nullptr) {
+    int32_t rank = 0;
+    int64_t sh[XTG_MAX_RANK];
+    if (xtg_broadcast_shape(&e, &rank, sh) != XTG_OK) return -1;
+    int64_t n = 1;
+    for (int d = 0; d < rank; ++d) n *= sh[d];
+    if (shape_rank) *shape_rank = rank;
+    return n;
+}
+
+std::string signature(const xtg_request& r) {
+    std::string s = std::to_string(r.kind) + ":" + std::to_string(r.out.dtype) + ":";
+    if (r.kind == XTG_REQ_REDUCE)
+        s += std::to_string(r.rd.op) + "," + std::to_string(r.rd.acc_dtype) + "," + std::to_string(r.rd.precision) + "," +
+             std::to_string(r.rd.has_initial) + "," + std::to_string(r.rd.initial.i) + ":";
+    for (int i = 0; i < r.expr.n_nodes; ++i) {
+        const xtg_node& n = r.expr.nodes[i];
+        s += std::to_string(n.op) + "/" + std::to_string(n.dtype) + "/" + std::to_string(n.arg) + "/" +
+             std::to_string(n.aux) + "/" + std::to_string(n.imm.u) + ";";
+    }
+    for (int i = 0; i < r.expr.n_leaves; ++i)
+        s += "L" + std::to_string(r.expr.leaves[i].dtype) + "r" + std::to_string(r.expr.leaves[i].rank);
+    return s;
+}
+
+void complete_failed(xtg_server* s, const std::vector<Req*>& rs, int status) {
+    const auto now = Clock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (Req* r : rs) {
+        r->status = status;
+        r->t_done = now;
+        r->finished = true;
+        s->inflight--;
+        s->reserved -= r->cost;
+        s->st.failed++;
+    }
+    s->events++;
+    s->cv_done.notify_all();
+    s->cv_sched.notify_all();
+}
+
+int dispatch_one(Req* r, cudaStream_t st) {
+    const int64_t every = opt("server.inject_fail_every", 0);
+    if (every > 0 && (int64_t)(r->id % (uint64_t)every) == 0) {
+        fail(XTG_ERR_CUDA, "injected dispatch failure");
+        return XTG_ERR_CUDA;
+    }
+    switch (r->r.kind) {
+        case XTG_REQ_ASSIGN: return xtg_assign(&r->r.expr, &r->r.out, st);
+        case XTG_REQ_REDUCE: return xtg_reduce(&r->r.expr, &r->r.rd, &r->r.out, st);
+        case XTG_REQ_ARGREDUCE:
+            return xtg_argreduce(&r->r.expr, r->r.arg_op, r->r.has_axis, r->r.axis, &r->r.out, st);
+    }
+    return XTG_ERR_INVALID;
+}
+
+void dispatch(xtg_server* s, std::vector<Req*>& admitted) {
+    // group batchable requests by signature
+    std::map<std::string, std::vector<Req*>> groups;
+    std::vector<Req*> singles;
+    for (Req* r : admitted) {
+        if (r->batchable) groups[r->sig].push_back(r);
+        else singles.push_back(r);
+    }
+    for (auto& kv : groups) {
+        if ((int)kv.second.size() < s->cfg.batch_min_group) {
+            singles.insert(singles.end(), kv.second.begin(), kv.second.end());
+            continue;
+        }
+        cudaStream_t st = s->streams[s->next_stream++ % s->streams.size()];
+        const auto now = Clock::now();
+        Req* f = kv.second[0];
+        xtg_batch* b = nullptr;
+        int rc = xtg_batch_create(&f->r.expr, f->r.kind == XTG_REQ_REDUCE ? &f->r.rd : nullptr, &b);
+        for (size_t i = 0; rc == XTG_OK && i < kv.second.size(); ++i)
+            rc = xtg_batch_add(b, kv.second[i]->r.expr.leaves, kv.second[i]->r.expr.n_leaves, &kv.second[i]->r.out);
+        if (rc == XTG_OK) rc = xtg_batch_build(b, 0, st);
+        if (rc == XTG_OK) rc = xtg_batch_run(b, st);
+        if (rc != XTG_OK) {
+            if (b) xtg_batch_destroy(b);
+            // fall back to individual dispatch for this group
+            singles.insert(singles.end(), kv.second.begin(), kv.second.end());
+            continue;
+        }
+        Unit* u = new Unit{s, kv.second, b};
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (Req* r : kv.second) {
+                r->t_dispatch = now;
+                r->dispatched = true;
+                r->batched = true;
+            }
+            s->st.batch_launches++;
+            s->st.batched_requests += (int64_t)kv.second.size();
+        }
+        complete_after(st, u);
+    }
+    // individual requests: round-robin over the streams, one completion
+    // callback per stream for this wave
+    std::vector<Unit*> per_stream(s->streams.size(), nullptr);
+    for (Req* r : singles) {
+        const size_t si = s->next_stream++ % s->streams.size();
+        cudaStream_t st = s->streams[si];
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            r->t_dispatch = Clock::now();
+            r->dispatched = true;
+        }
+        int rc = dispatch_one(r, st);
+        if (rc != XTG_OK) {
+            complete_failed(s, {r}, rc);
+            continue;
+        }
+        if (!per_stream[si]) per_stream[si] = new Unit{s, {}, nullptr};
+        per_stream[si]->reqs.push_back(r);
+    }
+    for (size_t si = 0; si < per_stream.size(); ++si)
+        if (per_stream[si]) complete_after(s->streams[si], per_stream[si]);
+}
+
+void scheduler(xtg_server* s) {
+    ensure_device(nullptr);
+    const double aging_ms = (double)opt("server.aging_ms", 50);
+    uint64_t seen = ~0ull;
+    for (;;) {
+        std::vector<Req*> admitted;
+        std::vector<Unit*> done;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            // wake for work to clean up, for a change that may let a pending
+            // request in, or to finish once stopping has drained the device
+            s->cv_sched.wait(lk, [&] {
+                return !s->finished_units.empty() || (!s->pending.empty() && s->events != seen) ||
+                       (s->stop && s->inflight == 0);
+            });
+            seen = s->events;
+            done.swap(s->finished_units);
+            if (s->stop && s->pending.empty() && s->inflight == 0 && done.empty()) break;
+            const auto now = Clock::now();
+            // option "server.paused": hold admissions (tests of queueing, cancel, timeouts)
+            const bool paused = opt("server.paused", 0) != 0;
+            for (auto it = s->pending.begin(); !paused && it != s->pending.end();) {
+                Req* r = *it;
+                if (s->inflight >= s->cfg.max_inflight) break;
+                if (s->reserved + r->cost > s->budget) {
+                    const double waited = std::chrono::duration<double, std::milli>(now - r->t_submit).count();
+                    if (waited > aging_ms) break;  // do not let later requests starve this one
+                    ++it;
+                    continue;
+                }
+                s->reserved += r->cost;
+                s->inflight++;
+                admitted.push_back(r);
+                it = s->pending.erase(it);
+            }
+            if (!admitted.empty()) s->st.waves++;
+        }
+        for (Unit* u : done) {
+            if (u->batch) xtg_batch_destroy(u->batch);
+            delete u;
+        }
+        if (!admitted.empty()) dispatch(s, admitted);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+xtg_status xtg_server_create(const xtg_server_config* cfg, xtg_server** out) {
+    if (!out) return fail(XTG_ERR_INVALID, "null output");
+    XTG_TRY(ensure_device(nullptr));
+    std::unique_ptr<xtg_server> s(new xtg_server());
+    xtg_server_config c{};
+    if (cfg) c = *cfg;
+    if (c.streams <= 0) c.streams = 8;
+    if (c.max_inflight <= 0) c.max_inflight = 256;
+    if (c.batch_max_elems <= 0) c.batch_max_elems = 1 << 20;
+    if (c.batch_min_group <= 0) c.batch_min_group = 4;
+    s->cfg = c;
+    if (c.hbm_budget_bytes > 0) {
+        s->budget = c.hbm_budget_bytes;
+    } else if (dry_run()) {
+        s->budget = (int64_t)1 << 36;
+    } else {
+        size_t f = 0, t = 0;
+        XTG_CUDA(cudaMemGetInfo(&f, &t));
+        s->budget = (int64_t)(f * 0.9);
+    }
+    for (int i = 0; i < c.streams; ++i) {
+        cudaStream_t st = nullptr;
+        if (!dry_run()) XTG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        s->streams.push_back(st);
+    }
+    s->st.hbm_budget = s->budget;
+    xtg_server* raw = s.release();
+    raw->sched = std::thread(scheduler, raw);
+    *out = raw;
+    return XTG_OK;
+}
+
+xtg_status xtg_server_submit(xtg_server* s, const xtg_request* r, uint64_t* id) {
+    if (!s || !r) return fail(XTG_ERR_INVALID, "null argument");
+    std::unique_ptr<Req> q(new Req());
+    q->r = *r;
+    q->t_submit = Clock::now();
+    int64_t rank = 0;
+    q->elems = elems_of(r->expr, &rank);
+    if (q->elems < 0) return fail(XTG_ERR_INVALID, std::string("request expression: ") + xtg_last_error());
+    int64_t scratch = 0;
+    if (r->kind == XTG_REQ_REDUCE || r->kind == XTG_REQ_ARGREDUCE) {
+        int64_t n_out = 1;
+        for (int d = 0; d < r->out.rank; ++d) n_out *= r->out.shape[d];
+        scratch = (opt("reduce.target_items", 8192) + n_out) * 32;
+    }
+    q->cost = std::max<int64_t>(0, r->workspace_bytes) + scratch;
+    const bool last_axis = r->kind == XTG_REQ_REDUCE && r->rd.n_axes == 1 &&
+                           (r->rd.axes[0] == -1 || r->rd.axes[0] == rank - 1) && r->rd.op != XTG_RED_VARIANCE &&
+                           r->rd.op != XTG_RED_STDDEV && r->rd.op != XTG_RED_PROD;
+    q->batchable = rank >= 1 && rank <= 2 && q->elems <= s->cfg.batch_max_elems &&
+                   (r->kind == XTG_REQ_ASSIGN || last_axis);
+    for (int i = 0; q->batchable && i < r->expr.n_nodes; ++i)
+        if (r->expr.nodes[i].op >= XTG_OP_RSUM) q->batchable = false;
+    if (q->batchable) q->sig = signature(*r);
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->st.submitted++;
+    if (q->cost > s->budget) {
+        s->st.rejected++;
+        return fail(XTG_ERR_REJECTED, "request needs more device memory than the server's HBM budget");
+    }
+    q->id = s->next_id++;
+    if (id) *id = q->id;
+    s->pending.push_back(q.get());
+    s->reqs.emplace(q->id, std::move(q));
+    s->events++;
+    s->cv_sched.notify_one();
+    return XTG_OK;
+}
+
+xtg_status xtg_server_wait(xtg_server* s, uint64_t id, int64_t timeout_ms, xtg_request_result* res) {
+    if (!s) return fail(XTG_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return fail(XTG_ERR_NOT_FOUND, "unknown request id");
+    Req* r = it->second.get();
+    auto pred = [&] { return r->finished; };
+    if (timeout_ms < 0) s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
+        return fail(XTG_ERR_TIMEOUT, "request not finished before the timeout");
+    if (res) {
+        res->status = r->status;
+        res->batched = r->batched ? 1 : 0;
+        res->queue_ms = r->dispatched ? std::chrono::duration<double, std::milli>(r->t_dispatch - r->t_submit).count() : 0;
+        res->total_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    }
+    const int status = r->status;
+    s->reqs.erase(it);
+    if (status != XTG_OK) return fail((xtg_status)status, "request failed");
+    return XTG_OK;
+}
+
+xtg_status xtg_server_cancel(xtg_server* s, uint64_t id) {
+    if (!s) return fail(XTG_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (auto it = s->pending.begin(); it != s->pending.end(); ++it) {
+        if ((*it)->id == id) {
+            Req* r = *it;
+            s->pending.erase(it);
+            r->status = XTG_ERR_CANCELLED;
+            r->finished = true;
+            r->t_done = Clock::now();
+            s->st.cancelled++;
+            s->events++;
+            s->cv_done.notify_all();
+            s->cv_sched.notify_all();
+            return XTG_OK;
+        }
+    }
+    return fail(XTG_ERR_NOT_FOUND, "request is not pending (unknown, dispatched or finished)");
+}
+
+xtg_status xtg_server_drain(xtg_server* s, int64_t timeout_ms) {
+    if (!s) return fail(XTG_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto pred = [&] { return s->pending.empty() && s->inflight == 0; };
+    if (timeout_ms < 0) s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
+        return fail(XTG_ERR_TIMEOUT, "server did not drain before the timeout");
+    return XTG_OK;
+}
+
+xtg_status xtg_server_get_stats(xtg_server* s, xtg_server_stats* out) {
+    if (!s || !out) return fail(XTG_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->st;
+    out->inflight = s->inflight;
+    out->pending = (int64_t)s->pending.size();
+    out->hbm_reserved = s->reserved;
+    std::vector<double> l = s->lat;
+    if (!l.empty()) {
+        std::sort(l.begin(), l.end());
+        auto q = [&](double f) { return l[std::min(l.size() - 1, (size_t)(f * (double)(l.size() - 1) + 0.5))]; };
+        out->p50_ms = q(0.50);
+        out->p99_ms = q(0.99);
+        double sum = 0;
+        for (double v : l) sum += v;
+        out->mean_ms = sum / (double)l.size();
+    }
+    return XTG_OK;
+}
+
+xtg_status xtg_server_reset_stats(xtg_server* s) {
+    if (!s) return fail(XTG_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    const int64_t budget = s->st.hbm_budget;
+    s->st = xtg_server_stats{};
+    s->st.hbm_budget = budget;
+    s->lat.clear();
+    return XTG_OK;
+}
+
+xtg_status xtg_server_destroy(xtg_server* s) {
+    if (!s) return XTG_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        // requests never dispatched are cancelled
+        for (Req* r : s->pending) {
+            r->status = XTG_ERR_CANCELLED;
+            r->finished = true;
+        }
+        s->pending.clear();
+        s->cv_sched.notify_all();
+    }
+    if (s->sched.joinable()) s->sched.join();
+    for (cudaStream_t st : s->streams) {
+        if (!st) continue;
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
+    }
+    for (Unit* u : s->finished_units) {
+        if (u->batch) xtg_batch_destroy(u->batch);
+        delete u;
+    }
+    delete s;
+    return XTG_OK;
+}
+
+}  // extern "C"
