@@ -1,0 +1,301 @@
+// C++ call sites of xtensor compiled against the GB300 evaluator's xt::
+// surface (include/xtensor/...).  The cases restate known-answer tests of
+// the reference (file:line of xtensor 0.27.1's test/ directory beside each);
+// the bodies are the same xtensor calls, evaluated on the GPU.
+#include <cmath>
+#include <cstdio>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "xtensor/containers/xarray.hpp"
+#include "xtensor/containers/xtensor.hpp"
+#include "xtensor/core/xmath.hpp"
+#include "xtensor/core/xnoalias.hpp"
+#include "xtensor/misc/xmanipulation.hpp"
+#include "xtensor/misc/xsort.hpp"
+#include "xtensor/reducers/xnorm.hpp"
+#include "xtensor/reducers/xreducer.hpp"
+#include "xtensor/views/xview.hpp"
+
+static int g_fail = 0, g_run = 0;
+static std::vector<std::pair<std::string, std::function<void()>>>& registry() {
+    static std::vector<std::pair<std::string, std::function<void()>>> r;
+    return r;
+}
+struct Reg {
+    Reg(const char* n, std::function<void()> f) { registry().emplace_back(n, f); }
+};
+#define TEST(A, B)                                 \
+    static void A##_##B();                         \
+    static Reg reg_##A##_##B(#A "." #B, A##_##B);  \
+    static void A##_##B()
+#define EXPECT_TRUE(c)                                                                    \
+    do {                                                                                  \
+        if (!(c)) {                                                                       \
+            std::printf("  FAIL %s:%d: %s\n", __FILE__, __LINE__, #c);                     \
+            ++g_fail;                                                                     \
+        }                                                                                 \
+    } while (0)
+#define EXPECT_EQ(a, b) EXPECT_TRUE((a) == (b))
+#define EXPECT_NEAR(a, b, tol) EXPECT_TRUE(std::abs((double)(a) - (double)(b)) <= (tol))
+#define EXPECT_THROW(stmt, ex)          \
+    do {                                \
+        bool caught = false;            \
+        try {                           \
+            stmt;                       \
+        } catch (const ex&) {           \
+            caught = true;              \
+        }                               \
+        EXPECT_TRUE(caught);            \
+    } while (0)
+
+using namespace xt;
+
+// test_xreducer.cpp:54-82 (xreducer_features), :355-362 (sum), :475-481 (sum_all)
+TEST(xreducer, sum_features) {
+    xarray<double> a = ones<double>({3, 2, 4, 6, 5});
+    for (std::size_t i = 0; i < 2; ++i)
+        for (std::size_t j = 0; j < 6; ++j) a(1, i, 1, j, 1) = 2;
+    xarray<double> res = sum(a, {1, 3});
+    EXPECT_EQ(res.shape(), (std::vector<std::size_t>{3, 4, 5}));
+    EXPECT_EQ((double)res(0, 0, 0), 12.0);
+    EXPECT_EQ((double)res(1, 1, 1), 24.0);
+    EXPECT_EQ(sum(a)(), 732.0);
+}
+
+// test_xreducer.cpp:390-397 (sum_tensor), :399-410 (single_axis_sugar)
+TEST(xreducer, sum_tensor_and_sugar) {
+    xtensor<double, 2> m = {{1, 2}, {3, 4}};
+    xarray<double> res = xt::sum(m, {0});
+    EXPECT_EQ(res.dimension(), std::size_t(1));
+    EXPECT_EQ((double)res(0), 4.0);
+    EXPECT_EQ((double)res(1), 6.0);
+    xarray<double> r3 = xt::sum(m, {1});
+    xarray<double> r4 = xt::sum(m, 1);
+    EXPECT_EQ(r3, r4);
+}
+
+// test_xreducer.cpp:442-473 (sum2): negative axes and no uint8 overflow
+TEST(xreducer, sum2) {
+    xarray<double> u = ones<double>({2, 4});
+    xarray<double> e0 = 2 * ones<double>({4});
+    xarray<double> r0 = sum(u, {0});
+    EXPECT_EQ(e0, r0);
+    xarray<double> e1 = 4 * ones<double>({2});
+    xarray<double> rm1 = sum(u, {-1});
+    std::array<std::size_t, 1> a_us = {1};
+    xarray<double> ru = sum(u, a_us);
+    EXPECT_EQ(e1, rm1);
+    EXPECT_EQ(e1, ru);
+    xarray<uint8_t> c = ones<uint8_t>({1000});
+    EXPECT_EQ(sum(c)(), 1000);
+}
+
+// test_xreducer.cpp:507-512 (prod<long long>)
+TEST(xreducer, prod) {
+    xarray<uint8_t> c = 2 * ones<uint8_t>({34});
+    EXPECT_EQ(prod<long long>(c)(), 1LL << 34);
+}
+
+// test_xreducer.cpp:542-570 (mean)
+TEST(xreducer, mean) {
+    xtensor<double, 2> input{{-1.0, 0.0}, {1.0, 0.0}};
+    EXPECT_EQ(mean(input)(), 0.0);
+    xarray<double> m1 = mean(input, {1});
+    EXPECT_EQ((double)m1(0), -0.5);
+    EXPECT_EQ((double)m1(1), 0.5);
+    xarray<uint8_t> c = {1, 2};
+    EXPECT_EQ(mean(c)(), 1.5);
+}
+
+// test_xreducer.cpp:213-220 (errors), :1081-1088 (double_axis)
+TEST(xreducer, errors) {
+    xarray<int> a = {{1, 2, 3}, {4, 5, 6}};
+    EXPECT_THROW(xarray<int> r = xt::sum(a, {1, 0}), std::runtime_error);
+    EXPECT_THROW(xarray<int> r = xt::sum(a, {0, 2}), std::runtime_error);
+    EXPECT_THROW(xarray<int> r = xt::sum(a, {0, 0}), std::runtime_error);
+}
+
+// test_xreducer.cpp:773-781 (chaining_reducers)
+TEST(xreducer, chaining) {
+    xarray<double> a = {{1., 2.}, {3., 4.}};
+    auto b = a - xt::sum(a, {0});
+    auto c = xt::sum(b, {0});
+    EXPECT_EQ((double)c(0), -4.);
+    EXPECT_EQ((double)c(1), -6.);
+}
+
+// test_xreducer.cpp:964-1018 (keep_dims, initial_value)
+TEST(xreducer, keep_dims_initial) {
+    xarray<double> a = arange<double>(5 * 5 * 5 * 5);
+    a.reshape(std::vector<std::size_t>{5, 5, 5, 5});
+    xarray<double> res = xt::sum(a, {0, 1}, xt::keep_dims | xt::evaluation_strategy::immediate);
+    EXPECT_EQ(res.shape(), (std::vector<std::size_t>{1, 1, 5, 5}));
+    xarray<double> r5 = xt::sum(a, {0, 2}, xt::keep_dims | initial(5));
+    xarray<double> r0 = xt::sum(a, {0, 2}, xt::keep_dims);
+    xarray<double> r0p5 = r0 + 5;
+    EXPECT_EQ(r5, r0p5);
+    xarray<double> z = xt::prod(a, {1, 2}, initial(0));
+    EXPECT_EQ(xt::amax(z)(), 0.0);
+}
+
+// test_xreducer.cpp:1044-1079 (zero_shape, empty_array)
+TEST(xreducer, zero_and_empty) {
+    xarray<int> x = zeros<int>({0, 1});
+    xarray<int> r0 = xt::sum(x, {0}, xt::keep_dims);
+    EXPECT_EQ(r0.shape(), (std::vector<std::size_t>{1, 1}));
+    EXPECT_EQ((int)r0(0, 0), 0);
+    xarray<double> a = ones<double>({1, 2, 0, 1});
+    EXPECT_TRUE(std::isnan(xt::mean(a)()));
+}
+
+// test_xnorm.cpp:97-187
+TEST(xnorm, scalar_array_and_matrix) {
+    xarray<int> a = -ones<int>({9});
+    EXPECT_EQ(norm_l0(a)(), 9u);
+    EXPECT_EQ(norm_l1(a)(), 9);
+    EXPECT_EQ(norm_sq(a)(), 9);
+    EXPECT_EQ(norm_l2(a)(), 3.0);
+    EXPECT_EQ(norm_linf(a)(), 1);
+    xarray<double> m = {{-1.0, 2.0}, {-3.0, 4.0}};
+    EXPECT_EQ(norm_l1(m)(), 10.0);
+    EXPECT_EQ(norm_sq(m)(), 30.0);
+    EXPECT_EQ(norm_linf(m)(), 4.0);
+}
+
+// test_xsort.cpp:217-281 (argmin, argmax)
+TEST(xsort, argmin_argmax) {
+    xarray<double> a = {{5, 3, 1}, {4, 4, 4}};
+    EXPECT_EQ(argmin(a)(), 2u);
+    xarray<std::size_t> ex2 = {1, 0, 0};
+    EXPECT_EQ(argmin(a, 0), ex2);
+    xarray<std::size_t> ex3 = {2, 0};
+    EXPECT_EQ(argmin(a, 1), ex3);
+    EXPECT_EQ(argmax(a)(), 0u);
+    xarray<std::size_t> mx2 = {0, 1, 1};
+    EXPECT_EQ(argmax(a, 0), mx2);
+    xtensor<int, 3> c = {{{1, 2, 3, 4}}, {{4, 3, 2, 1}}};
+    xtensor<std::size_t, 2> ex4 = {{3}, {0}};
+    EXPECT_EQ(argmax(c, 2), ex4);
+    xtensor<std::size_t, 2> ex5 = {{1, 1, 0, 0}};
+    EXPECT_EQ(argmax(c, 0), ex5);
+}
+
+// test_xnoalias.cpp: noalias assignment and computed assignment in place
+TEST(xnoalias, assign_and_computed) {
+    xarray<double> a = {{1, 2}, {3, 4}};
+    xarray<double> b = {{10, 20}, {30, 40}};
+    xarray<double> r = ones<double>({2, 2});
+    noalias(r) = a + b;
+    xarray<double> e = {{11, 22}, {33, 44}};
+    EXPECT_EQ(r, e);
+    noalias(r) += a;
+    xarray<double> e2 = {{12, 24}, {36, 48}};
+    EXPECT_EQ(r, e2);
+    r = r - r(0, 0);  // `=` with aliasing: evaluated into a temporary
+    EXPECT_EQ((double)r(1, 1), 36.0);
+}
+
+// test_xfunction.cpp:76-111 (broadcast shapes and broadcast_error)
+TEST(xfunction, broadcasting) {
+    xarray<double> a = ones<double>({3, 1, 5});
+    xarray<double> b = ones<double>({4, 1});
+    xarray<double> c = a + b;
+    EXPECT_EQ(c.shape(), (std::vector<std::size_t>{3, 4, 5}));
+    xarray<double> d = ones<double>({3, 4});
+    xarray<double> f = ones<double>({5});
+    EXPECT_THROW(xarray<double> g = d + f, xt::broadcast_error);
+}
+
+// test_xstrided_view.cpp:764-772 (transpose), test_strided_assign.cpp (views)
+TEST(xstrided_view, transpose_and_views) {
+    xarray<int> a = {{1, 2, 3}, {4, 5, 6}};
+    xarray<int> t = xt::transpose(a);
+    xarray<int> et = {{1, 4}, {2, 5}, {3, 6}};
+    EXPECT_EQ(t, et);
+    xarray<int> v = xt::view(a, xt::all(), xt::range(1, 3));
+    xarray<int> ev = {{2, 3}, {5, 6}};
+    EXPECT_EQ(v, ev);
+    xarray<int> row = xt::view(a, 1);
+    xarray<int> er = {4, 5, 6};
+    EXPECT_EQ(row, er);
+    auto lhs = xt::view(a, xt::all(), 0);
+    lhs = xt::view(a, xt::all(), 2) * 10;
+    xarray<int> ea = {{30, 2, 3}, {60, 5, 6}};
+    EXPECT_EQ(a, ea);
+}
+
+// the configurations' expressions through C++ call sites
+TEST(configs, c0_expression_and_row_sum) {
+    const std::size_t n = 256, m = 512;
+    xarray<float> A = xt::zeros<float>({n, m});
+    xarray<float> b = xt::zeros<float>({m});
+    {
+        std::vector<float> ha(n * m), hb(m);
+        for (std::size_t i = 0; i < n * m; ++i) ha[i] = (float)((int)(i * 7919 % 2001) - 1000) / 1000.0f;
+        for (std::size_t j = 0; j < m; ++j) hb[j] = (float)((int)(j * 31 % 17) - 8) / 4.0f;
+        A.upload(ha);
+        b.upload(hb);
+    }
+    xarray<float> E = A * b + xt::exp(-A * A);
+    xarray<float> r = xt::sum(E, {1});
+    auto hE = E.to_host();
+    auto hA = A.to_host();
+    auto hb = b.to_host();
+    double worst = 0;
+    for (std::size_t i = 0; i < n * m; ++i) {
+        const double ref = (double)hA[i] * hb[i % m] + std::exp(-(double)hA[i] * hA[i]);
+        worst = std::max(worst, std::abs(ref - hE[i]) / (std::abs((double)hA[i] * hb[i % m]) + 1.0));
+    }
+    EXPECT_TRUE(worst < 4e-7);
+    auto hr = r.to_host();
+    for (std::size_t i = 0; i < n; ++i) {
+        double s = 0, sa = 0;
+        for (std::size_t j = 0; j < m; ++j) {
+            s += hE[i * m + j];
+            sa += std::abs(hE[i * m + j]);
+        }
+        EXPECT_TRUE(std::abs(hr[i] - s) <= 1e-6 * sa);
+    }
+}
+
+TEST(configs, c1_normalize_transpose_amax_argmax) {
+    xarray<float> x = xt::zeros<float>({8, 16, 1024});
+    {
+        std::vector<float> h(8 * 16 * 1024);
+        for (std::size_t i = 0; i < h.size(); ++i) h[i] = (float)std::sin(0.37 * (double)i) * 3.0f;
+        x.upload(h);
+    }
+    xarray<float> y = (x - xt::mean(x, {2}, xt::keep_dims)) / xt::sqrt(xt::variance(x, {2}, xt::keep_dims) + 1e-5);
+    EXPECT_EQ(y.shape(), (std::vector<std::size_t>{8, 16, 1024}));
+    xarray<double> ym = xt::mean(y, {2});
+    xarray<double> yv = xt::variance(y, {2});
+    auto hm = ym.to_host();
+    auto hv = yv.to_host();
+    for (auto v : hm) EXPECT_NEAR(v, 0.0, 1e-5);
+    for (auto v : hv) EXPECT_NEAR(v, 1.0, 1e-4);
+    xarray<float> t = xt::transpose(x, {2, 0, 1});
+    EXPECT_EQ(t.shape(), (std::vector<std::size_t>{1024, 8, 16}));
+    EXPECT_EQ((float)t(5, 3, 7), (float)x(3, 7, 5));
+    xarray<float> am = xt::amax(x, {0, 2});
+    EXPECT_EQ(am.shape(), (std::vector<std::size_t>{16}));
+    xarray<std::size_t> ai = xt::argmax(x, 1);
+    EXPECT_EQ(ai.shape(), (std::vector<std::size_t>{8, 1024}));
+}
+
+int main() {
+    for (auto& t : registry()) {
+        const int before = g_fail;
+        ++g_run;
+        try {
+            t.second();
+        } catch (const std::exception& e) {
+            std::printf("  FAIL %s: exception %s\n", t.first.c_str(), e.what());
+            ++g_fail;
+        }
+        std::printf("%s %s\n", g_fail == before ? "[ OK ]" : "[FAIL]", t.first.c_str());
+    }
+    std::printf("%d tests, %d failed checks\n", g_run, g_fail);
+    return g_fail ? 1 : 0;
+}

@@ -72,9 +72,13 @@ def reduce(op: str, e, axes=None, keep_dims=False, initial=None, acc_dtype=None,
            out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
     """Evaluate a reducer into a new (or given) device array."""
     e = as_expr(e)
-    kw = dict(axes=axes, keep_dims=keep_dims, initial=initial, acc_dtype=acc_dtype, ddof=ddof, precision=precision)
+    kw = dict(axes=axes, keep_dims=keep_dims, initial=None, acc_dtype=acc_dtype, ddof=ddof, precision=precision)
+    shape, dt = reduce_shape(op, e, **kw)
+    if initial is not None:  # xt::initial(v) is converted to the result type
+        from ._ffi import DTYPES
+        initial = float(initial) if dt in (DTYPES["float32"], DTYPES["float64"], DTYPES["bfloat16"]) else int(initial)
+    kw["initial"] = initial
     if out is None:
-        shape, dt = reduce_shape(op, e, **kw)
         out = DeviceArray.empty(shape, dt, stream)
     ex, keep = lower(e)
     rd = make_desc(op, **kw)
