@@ -315,16 +315,55 @@ def test_reduction_errors_and_edge_cases():
     assert int(ops.reduce("sum", c).to_numpy()) == 1000
 
 
-def test_signed_zero_and_inf_selection():
-    x = np.array([[0.0, -0.0, -0.0], [-0.0, 0.0, -np.inf]], np.float32)
+@pytest.mark.parametrize("dt", ["float32", "float64"])
+def test_signed_zero_and_inf_selection(dt):
+    x = np.array([[0.0, -0.0, -0.0], [-0.0, 0.0, -np.inf]], dt)
     for axes in ([1], [0], None):
         for op in ("amax", "amin"):
             got = ops.reduce(op, dev(x), axes).to_numpy()
             ref = O.reduce(op, H(x), axes)
             np.testing.assert_array_equal(np.signbit(got), np.signbit(ref))
             np.testing.assert_array_equal(got, ref)
-    y = np.full((4,), -np.inf, np.float32)
+    y = np.full((4,), -np.inf, dt)
     assert ops.reduce("amax", dev(y)).to_numpy() == O.reduce("amax", H(y))
+
+
+def test_float64_selection_prefilter_edges():
+    """float64 amax/amin/argmax/argmin skip most FP64 compares with a 32-bit
+    key of the high word: values equal in the high word, signed zeros,
+    infinities, subnormals and the largest finite values must still select
+    exactly like the plain fold."""
+    g = rng(21)
+    base = np.float64(1.5)
+    hi_ties = base + np.arange(64) * np.finfo(np.float64).eps  # same high word, different low words
+    specials = np.array([0.0, -0.0, np.inf, -np.inf, 5e-324, -5e-324, np.finfo(np.float64).max,
+                         -np.finfo(np.float64).max, 2.2250738585072014e-308], np.float64)
+    rows = []
+    for r in range(40):
+        v = g.permutation(np.concatenate([hi_ties, -hi_ties, specials, g.standard_normal(60)]))
+        if r % 4 == 1:
+            v = np.where(np.isinf(v), 0.0, v)
+        if r % 4 == 2:
+            v = v[g.permutation(v.size)] * 1e-310
+        rows.append(v)
+    x = np.stack(rows)
+    for axes in ([1], [0], None):
+        for op in ("amax", "amin"):
+            got = ops.reduce(op, dev(x), axes).to_numpy()
+            ref = O.reduce(op, H(x), axes)
+            np.testing.assert_array_equal(np.signbit(got), np.signbit(ref))
+            np.testing.assert_array_equal(got, ref)
+    for axis in (None, 0, 1):
+        for op in ("argmax", "argmin"):
+            np.testing.assert_array_equal(ops.argreduce(op, dev(x), axis).to_numpy(), O.argreduce(op, H(x), axis))
+    # long rows of near-equal values: the winner sits in the low word only
+    y = np.broadcast_to(hi_ties, (3, 2048, 64)).reshape(3, -1).copy()
+    for i in range(3):
+        y[i] = y[i][g.permutation(y.shape[1])]
+    for op in ("amax", "amin"):
+        np.testing.assert_array_equal(ops.reduce(op, dev(y), [1]).to_numpy(), O.reduce(op, H(y), [1]))
+    for op in ("argmax", "argmin"):
+        np.testing.assert_array_equal(ops.argreduce(op, dev(y), 1).to_numpy(), O.argreduce(op, H(y), 1))
 
 
 # ------------------------------------------------------------------------------- arg
@@ -341,8 +380,9 @@ def test_argmax_argmin(dt):
     np.testing.assert_array_equal(got, O.argreduce("argmax", H(x), 1).astype(np.int32))
 
 
-def test_argmax_nan_rules():
-    x = np.array([[np.nan, 1, 2], [1, np.nan, 3], [2, 2, np.nan]], np.float32)
+@pytest.mark.parametrize("dt", ["float32", "float64"])
+def test_argmax_nan_rules(dt):
+    x = np.array([[np.nan, 1, 2], [1, np.nan, 3], [2, 2, np.nan]], dt)
     for axis in (0, 1, None):
         for op in ("argmax", "argmin"):
             np.testing.assert_array_equal(ops.argreduce(op, dev(x), axis).to_numpy(), O.argreduce(op, H(x), axis))
@@ -382,6 +422,63 @@ def test_row_normalize(dt, rel, shape):
     ref = O.assign((hx - xg.rmean(hx)) / xg.sqrt(xg.rvar(hx) + 1e-5), dtype=dt).astype(np.float64)
     env = np.abs(ref - exact) + (4 * rel if dt == "float32" else rel) * scale
     assert (np.abs(got - ref) <= env).all(), "normalize outside the reference envelope"
+
+
+def _exact_row_moments(row):
+    from fractions import Fraction
+    v = [Fraction(float(t)) for t in row]
+    s = sum(v)
+    m = s / len(v)
+    return s, m, sum((t - m) ** 2 for t in v)
+
+
+@pytest.mark.parametrize("n", [1024, 100, 7, 3000])
+def test_row_moments_float64(n):
+    """float64 row sums, means and variances inside fused row trees are exact
+    up to the final rounding for rows whose elements share the top binade,
+    whatever the mean (no cancellation): offsets of 1e6 and 1e12 over unit
+    spread, wide dynamic ranges, integer values near 2^52, subnormals; rows
+    with an infinity or NaN follow IEEE arithmetic."""
+    g = rng(22)
+    kinds = [g.standard_normal(n), g.standard_normal(n) + 1e6, g.standard_normal(n) * 1e-3 + 1e12,
+             g.standard_normal(n) * np.exp(g.uniform(-30, 30, n)),
+             g.integers(-2**52, 2**52, n).astype(np.float64), g.standard_normal(n) * 1e-310,
+             np.full(n, 3.25), np.zeros(n)]
+    x = np.stack(kinds)
+    d = dev(x)
+    outs = {}
+    for name, fn in [("sum", xg.rsum), ("mean", xg.rmean), ("var", xg.rvar), ("std", xg.rstd)]:
+        o = DeviceArray.empty(x.shape, "float64")
+        xg.assign(o, fn(d) + 0.0 * d)
+        outs[name] = o.to_numpy()[:, 0]
+        assert (o.to_numpy() == outs[name][:, None]).all()
+    for i, row in enumerate(x):
+        s, m, q = _exact_row_moments(row)
+        # each element is rounded to the ulp of the row's top binade, then
+        # the sum is exact and rounded once (the mean twice more)
+        mx = float(np.max(np.abs(row)))
+        ulp_top = np.ldexp(1.0, max(int(np.frexp(mx)[1]) - 53, -1074)) if mx > 0 else 0.0
+        tol_s = n * ulp_top / 2 + 2.3e-16 * abs(float(s))
+        assert abs(outs["sum"][i] - float(s)) <= tol_s, (i, outs["sum"][i], float(s))
+        assert abs(outs["mean"][i] - float(m)) <= tol_s / n + 4.5e-16 * abs(float(m)), (i, outs["mean"][i], float(m))
+        var = float(q / n)
+        if var > 1e-290:
+            assert abs(outs["var"][i] - var) <= 1e-14 * var, (i, outs["var"][i], var)
+            assert abs(outs["std"][i] - np.sqrt(var)) <= 1e-14 * np.sqrt(var)
+        else:
+            assert abs(outs["var"][i]) <= 1e-290
+    # rows with non-finite values: the IEEE path (same results as numpy)
+    y = g.standard_normal((4, n))
+    y[0, n // 2] = np.inf
+    y[1, 0] = np.nan
+    y[2, -1] = -np.inf
+    y[3, n // 3] = np.inf
+    y[3, n // 4] = -np.inf
+    o = DeviceArray.empty(y.shape, "float64")
+    xg.assign(o, xg.rmean(dev(y)) + 0.0 * dev(y))
+    got = o.to_numpy()[:, 0]
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(y.mean(-1)))
+    np.testing.assert_array_equal(got[~np.isnan(got)], y.mean(-1)[~np.isnan(got)])
 
 
 def test_row_stats_other_modes():

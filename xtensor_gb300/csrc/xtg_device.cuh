@@ -547,24 +547,10 @@ struct AccSumC {
     XTG_DI double dval() const { return (double)hi + (double)lo; }
 };
 
-// Ordered comparison of float64 values on the integer pipes (GB300 runs
-// FP64 compares at its reduced FP64 rate).  Exactly IEEE `a > b`: NaN
-// compares false, -0 == +0; the sign-magnitude bits become a two's-
-// complement key, which orders all other values.
-XTG_DI bool f64_gt(double a, double b) {
-    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
-    const long long ma = ia & 0x7fffffffffffffffLL, mb = ib & 0x7fffffffffffffffLL;
-    if (ma > 0x7ff0000000000000LL || mb > 0x7ff0000000000000LL) return false;
-    const long long ka = ia < 0 ? -ma : ma, kb = ib < 0 ? -mb : mb;
-    return ka > kb;
-}
 template <class T> struct Cmp {
     static XTG_DI bool gt(T a, T b) { return a > b; }
     static XTG_DI bool lt(T a, T b) { return a < b; }
 };
-// (Measured on GB300: the integer form costs more issue slots than the
-// native DSETP in the selection reducers, so Cmp<double> stays native and
-// f64_gt is kept for callers that are FP64-pipe bound.)
 
 // Selection reducers amax / amin: the reference folds f(acc, x) =
 // acc > x ? acc : x (include/xtensor/core/xmath.hpp:589-602, 777-811) from
@@ -574,6 +560,11 @@ template <class A, int MAXOP> struct AccSel {
     A v;
     i64 pos;
     template <class P> XTG_DI void init(const P& p);
+    XTG_DI void start(A v0) {
+        v = v0;
+        pos = -1;
+    }
+    XTG_DI A value() const { return v; }
     template <class X> XTG_DI void add(X x, i64 ps) {
         A a = cvt<A>(x);
         bool keep = MAXOP ? Cmp<A>::gt(v, a) : Cmp<A>::lt(v, a);
@@ -586,6 +577,75 @@ template <class A, int MAXOP> struct AccSel {
         if (take) { v = o.v; pos = o.pos; }
     }
     XTG_DI double dval() const { return (double)v; }
+};
+
+// float64 order on the integer pipes (GB300 issues FP64 compares at its
+// reduced FP64 rate).  key64 maps the bits of every non-NaN double to a signed
+// integer in the same order (-0 lands just below +0); it is its own inverse.
+// "Special" values — zeros, subnormals below 2^-1042, infinities and NaNs
+// (high word magnitude 0 or >= 0x7ff00000) — take an exact IEEE path out of
+// line (-0 == +0, NaN rules); between any other value and the running best,
+// whatever that is, the key order is the IEEE order.
+XTG_DI i64 key64(i64 b) { return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
+XTG_DI double unkey64(i64 k) { return __longlong_as_double(key64(k)); }
+XTG_DI bool f64_special(i64 b) { return (unsigned)(((int)(b >> 32) & 0x7fffffff) - 1) >= 0x7fefffffu; }
+XTG_DI bool f64_isnan_bits(i64 b) { return (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+#define XTG_KEY_MIN ((i64)0x8000000000000000ULL)  // unkey64 of either end is a NaN
+#define XTG_KEY_MAX ((i64)0x7fffffffffffffffLL)
+struct KeyPos {
+    i64 k, p;
+};
+// amax/amin update by a special value: the plain fold `keep = v > a`; a NaN
+// best is stored as the end key that lets the next element in (the fold
+// replaces a NaN accumulator by whatever follows).
+template <int MAXOP> __device__ __noinline__ KeyPos sel_special(i64 kv, i64 pos, double a, i64 ps) {
+    const double v = unkey64(kv);
+    const bool keep = MAXOP ? (v > a) : (v < a);
+    KeyPos r;
+    r.k = kv;
+    r.p = pos;
+    if (!keep) {
+        const i64 b = __double_as_longlong(a);
+        r.k = f64_isnan_bits(b) ? (MAXOP ? XTG_KEY_MIN : XTG_KEY_MAX) : key64(b);
+        r.p = ps;
+    }
+    return r;
+}
+template <int MAXOP> struct AccSel<double, MAXOP> {
+    i64 kv;  // key64 of the best value
+    i64 pos;
+    template <class P> XTG_DI void init(const P& p) { start(p.init_f); }
+    XTG_DI void start(double v0) {
+        const i64 b = __double_as_longlong(v0);
+        kv = f64_isnan_bits(b) ? (MAXOP ? XTG_KEY_MIN : XTG_KEY_MAX) : key64(b);
+        pos = -1;
+    }
+    XTG_DI double value() const { return unkey64(kv); }
+    template <class X> XTG_DI void add(X x, i64 ps) {
+        const i64 b = __double_as_longlong(cvt<double>(x));
+        if (f64_special(b)) {
+            const KeyPos r = sel_special<MAXOP>(kv, pos, __longlong_as_double(b), ps);
+            kv = r.k;
+            pos = r.p;
+            return;
+        }
+        const i64 ka = key64(b);
+        if (MAXOP ? (ka >= kv) : (ka <= kv)) {  // equal keys = equal values: the later one wins
+            kv = ka;
+            pos = ps;
+        }
+    }
+    XTG_DI void merge(const AccSel& o) {
+        const double v = value(), ov = o.value();
+        bool take;
+        if (MAXOP) take = (ov > v) || (!(v > ov) && o.pos > pos);
+        else take = (ov < v) || (!(v < ov) && o.pos > pos);
+        if (take) {
+            kv = o.kv;
+            pos = o.pos;
+        }
+    }
+    XTG_DI double dval() const { return value(); }
 };
 
 // Moments for mean / variance / stddev.  Data are shifted by k (the first
@@ -685,6 +745,69 @@ template <class A, int MAXOP> struct AccArg {
         if (take) { v = o.v; idx = o.idx; }
     }
 };
+// float64 arg-reductions on key64.  The empty state holds the end key that
+// every non-NaN value beats; a NaN taken as the very first element is held as
+// the other end key, which nothing beats.
+template <int MAXOP> __device__ __noinline__ KeyPos arg_special(i64 kv, i64 idx, double a, i64 ps) {
+    KeyPos r;
+    r.k = kv;
+    r.p = idx;
+    const i64 b = __double_as_longlong(a);
+    const bool nan = f64_isnan_bits(b);
+    bool take;
+    if (idx < 0) take = !nan || ps == 0;
+    else take = MAXOP ? (a > unkey64(kv)) : (a < unkey64(kv));
+    if (take) {
+        r.k = nan ? (MAXOP ? XTG_KEY_MAX : XTG_KEY_MIN) : key64(b);
+        r.p = ps;
+    }
+    return r;
+}
+template <int MAXOP> struct AccArg<double, MAXOP> {
+    i64 kv;
+    i64 idx;  // -1: empty
+    template <class P> XTG_DI void init(const P&) {
+        idx = -1;
+        kv = MAXOP ? XTG_KEY_MIN : XTG_KEY_MAX;
+    }
+    XTG_DI double value() const { return unkey64(kv); }
+    template <class X> XTG_DI void add(X x, i64 ps) {
+        const i64 b = __double_as_longlong(cvt<double>(x));
+        if (f64_special(b)) {
+            const KeyPos r = arg_special<MAXOP>(kv, idx, __longlong_as_double(b), ps);
+            kv = r.k;
+            idx = r.p;
+            return;
+        }
+        const i64 ka = key64(b);
+        if (MAXOP ? (ka > kv) : (ka < kv)) {  // strict: the first of equal values stays
+            kv = ka;
+            idx = ps;
+        }
+    }
+    XTG_DI void merge(const AccArg& o) {
+        if (o.idx < 0) return;
+        if (idx < 0) {
+            kv = o.kv;
+            idx = o.idx;
+            return;
+        }
+        const double v = value(), ov = o.value();
+        const bool nan_me = !(v == v), nan_o = !(ov == ov);
+        if (nan_me) return;
+        if (nan_o) {
+            kv = o.kv;
+            idx = o.idx;
+            return;
+        }
+        bool take = MAXOP ? (ov > v) : (ov < v);
+        if (!take && !(MAXOP ? (v > ov) : (v < ov)) && o.idx < idx) take = true;
+        if (take) {
+            kv = o.kv;
+            idx = o.idx;
+        }
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Reduction parameters.  Output space = kept dims (rank RO), reduced space =
@@ -741,7 +864,7 @@ template <class Out> struct Fin<Out, AccSumC> {
 };
 template <class Out, class A, int MAXOP> struct Fin<Out, AccSel<A, MAXOP>> {
     template <class P> static XTG_DI Out go(const AccSel<A, MAXOP>& a, const P& p) {
-        A r = a.v;
+        A r = a.value();
         if (p.has_initial) {
             A iv = IsFloat<A>::value ? (A)p.initial_f : (A)p.initial_i;
             r = MAXOP ? (iv > r ? iv : r) : (iv < r ? iv : r);
@@ -926,6 +1049,7 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
         acc = group_reduce<GROUP>(acc, smem);
         if (gtid == 0) {
             if (p.nsplit > 1) {
+                static_assert(sizeof(Acc) <= 32, "split partial slots are 32 bytes");
                 reinterpret_cast<Acc*>(p.partial)[w] = acc;
             } else {
                 i64 oo = 0;
@@ -1201,6 +1325,188 @@ template <> struct RowFin<float> {  // float32 rows: double-float sums rounded o
     }
 };
 
+// float64 row moments on the integer pipes.  GB300 issues FP64 at a small
+// fraction of its FP32 rate, so sum / mean / variance of a float64 row are
+// computed in fixed point instead.  With Ef the largest exponent field in
+// the row, every element becomes the integer
+//   X = round(x * 2^(1075 - Ef)),   |X| < 2^53,
+// which is exact for the elements in the top binade; smaller ones are
+// rounded to the top binade's ulp (so a row sum is within n/2 of that ulp
+// plus one final rounding).  From there on everything is exact:  Each lane (at most 256 elements)
+// keeps sum X and sum X^2 exactly in 64-bit words (X = Xh * 2^27 + Xl, so
+// X^2 = Xh^2 2^54 + 2 Xh Xl 2^27 + Xl^2 as three sums of 32x32-bit
+// products); lanes combine in 128-bit, and
+//   n * sum (X - mean)^2 = n * sum X^2 - (sum X)^2
+// is evaluated in 192-bit integers, so no cancellation can occur whatever the
+// mean.  Rows holding an infinity or NaN take the FP64 path.
+struct IMaxI {
+    int v;
+    XTG_DI void merge(const IMaxI& o) { v = v > o.v ? v : o.v; }
+};
+struct U128 {
+    u64 lo, hi;
+};
+struct U192 {
+    u64 w0, w1, w2;
+};
+XTG_DI U128 u128_shl(u64 v, int n) {  // v * 2^n, 0 < n < 64
+    U128 r;
+    r.lo = v << n;
+    r.hi = v >> (64 - n);
+    return r;
+}
+XTG_DI U128 u128_add(U128 a, U128 b) {
+    U128 r;
+    r.lo = a.lo + b.lo;
+    r.hi = a.hi + b.hi + (r.lo < a.lo ? 1ull : 0ull);
+    return r;
+}
+XTG_DI U128 u128_sub(U128 a, U128 b) {
+    U128 r;
+    r.lo = a.lo - b.lo;
+    r.hi = a.hi - b.hi - (a.lo < b.lo ? 1ull : 0ull);
+    return r;
+}
+XTG_DI U192 u192_mul(U128 a, u64 m) {  // a * m
+    U192 r;
+    r.w0 = a.lo * m;
+    const u64 c0 = __umul64hi(a.lo, m);
+    const u64 p1 = a.hi * m;
+    r.w1 = c0 + p1;
+    r.w2 = __umul64hi(a.hi, m) + (r.w1 < c0 ? 1ull : 0ull);
+    return r;
+}
+XTG_DI U192 u192_add(U192 a, U192 b) {
+    U192 r;
+    r.w0 = a.w0 + b.w0;
+    const u64 c0 = r.w0 < a.w0 ? 1ull : 0ull;
+    const u64 t = a.w1 + b.w1;
+    const u64 c1 = t < a.w1 ? 1ull : 0ull;
+    r.w1 = t + c0;
+    r.w2 = a.w2 + b.w2 + c1 + (r.w1 < t ? 1ull : 0ull);
+    return r;
+}
+XTG_DI U192 u192_sub(U192 a, U192 b) {
+    U192 r;
+    r.w0 = a.w0 - b.w0;
+    const u64 b0 = a.w0 < b.w0 ? 1ull : 0ull;
+    const u64 t = a.w1 - b.w1;
+    const u64 b1 = a.w1 < b.w1 ? 1ull : 0ull;
+    r.w1 = t - b0;
+    r.w2 = a.w2 - b.w2 - b1 - (t < b0 ? 1ull : 0ull);
+    return r;
+}
+// lane / group partial sums: sum X as a signed 128-bit (two's complement)
+// word pair, sum X^2 as unsigned 128-bit
+struct FixMom {
+    U128 s1, s2;
+    XTG_DI void merge(const FixMom& o) {
+        s1 = u128_add(s1, o.s1);
+        s2 = u128_add(s2, o.s2);
+    }
+};
+XTG_DI int exp_field(double x) {
+    const int e = (__double2hiint(x) >> 20) & 0x7ff;
+    return e ? e : 1;  // subnormals scale like exponent field 1
+}
+XTG_DI i64 to_fixed(double x, int ef_max) {
+    const int hi = __double2hiint(x);
+    const unsigned lo = (unsigned)__double2loint(x);
+    const int e = (hi >> 20) & 0x7ff;
+    // twice the significand (< 2^54), so that one shift and one add round
+    const u64 m2 = (((u64)(unsigned)((hi & 0xfffff) | (e ? 0x100000 : 0)) << 32) | lo) << 1;
+    int sh = ef_max - (e ? e : 1);
+    sh = sh < 63 ? sh : 63;
+    const i64 v = (i64)(((m2 >> sh) + 1) >> 1);  // significand / 2^sh, rounded half away from zero
+    return hi < 0 ? -v : v;
+}
+
+template <int GROUP, int VEC, int NV, int MODE, class Sub, class RG, class CT>
+XTG_DI bool fixed_moments(const RG (&rg)[NV], const bool (&ok)[NV][VEC], const CT& c, const RowParams& p, void* smem,
+                          double& sum, double& sdev2) {
+    static_assert(NV * VEC <= 256, "per-lane 64-bit sums hold at most 256 elements");
+    const i64 n = p.row_len;
+    IMaxI em;
+    em.v = 1;
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+            if (ok[i][j]) {
+                const int e = exp_field(cvt<double>(Sub::ev(rg[i], j, c)));
+                em.v = em.v > e ? em.v : e;
+            }
+    em = group_reduce<GROUP>(em, reinterpret_cast<IMaxI*>(smem));
+    em = bcast_group<GROUP>(em, reinterpret_cast<IMaxI*>(smem));
+    if (em.v >= 0x7ff || n > 65536) return false;
+    i64 s1 = 0, a = 0, b = 0;
+    u64 cc = 0;
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+            if (ok[i][j]) {
+                const i64 x = to_fixed(cvt<double>(Sub::ev(rg[i], j, c)), em.v);
+                s1 += x;
+                if (MODE >= 2) {
+                    const int xh = (int)(x >> 27);                      // |xh| <= 2^26
+                    const int xl = (int)((unsigned)x & 0x7ffffffu);     // 0 <= xl < 2^27
+                    a += (i64)xh * xh;
+                    b += (i64)xh * xl;
+                    cc += (u64)(unsigned)xl * (unsigned)xl;
+                }
+            }
+    FixMom f;
+    f.s1.lo = (u64)s1;
+    f.s1.hi = s1 < 0 ? ~0ull : 0ull;
+    f.s2.lo = 0;
+    f.s2.hi = 0;
+    if (MODE >= 2) {
+        // lane sum X^2 = a 2^54 + b 2^28 + cc  (>= 0, < 2^116)
+        U128 t = u128_shl((u64)a, 54);
+        const U128 bt = u128_shl((u64)(b < 0 ? -b : b), 28);
+        t = b < 0 ? u128_sub(t, bt) : u128_add(t, bt);
+        U128 ct;
+        ct.lo = cc;
+        ct.hi = 0;
+        f.s2 = u128_add(t, ct);
+    }
+    f = group_reduce<GROUP>(f, reinterpret_cast<FixMom*>(smem));
+    f = bcast_group<GROUP>(f, reinterpret_cast<FixMom*>(smem));
+    const int sig = em.v - 1075;  // x = X * 2^sig
+    // |sum X| < 2^69: convert the magnitude (a negative two's-complement
+    // pair would round its low word near 2^64)
+    U128 m1 = f.s1;
+    const bool neg = (i64)m1.hi < 0;
+    if (neg) {
+        U128 z;
+        z.lo = 0;
+        z.hi = 0;
+        m1 = u128_sub(z, m1);
+    }
+    // m1.hi < 2^6: the upper 70 - 32 bits are exact in a double, so the one
+    // addition below is the only rounding
+    const double mag = ((double)m1.hi * 4294967296.0 + (double)(m1.lo >> 32)) * 4294967296.0 +
+                       (double)(m1.lo & 0xffffffffull);
+    sum = scalbn(neg ? -mag : mag, sig);
+    sdev2 = 0.0;
+    if (MODE >= 2) {
+        // sum X^2 < 2^122, n <= 2^16: n * sum X^2 - (sum X)^2 in 192 bits
+        // (exact, >= 0)
+        U192 sq = u192_mul(m1, m1.lo);
+        const U192 sqh = u192_mul(m1, m1.hi);  // times 2^64
+        U192 sh;
+        sh.w0 = 0;
+        sh.w1 = sqh.w0;
+        sh.w2 = sqh.w1;
+        sq = u192_add(sq, sh);
+        const U192 q = u192_sub(u192_mul(f.s2, (u64)n), sq);
+        const double qd = ((double)q.w2 * 18446744073709551616.0 + (double)q.w1) * 18446744073709551616.0 + (double)q.w0;
+        sdev2 = scalbn(qd / (double)n, 2 * sig);
+    }
+    return true;
+}
+
 template <class LST> struct Stats;
 template <> struct Stats<StatList<>> {
     template <int GROUP, int VEC, int NV, class RG, class CT>
@@ -1211,42 +1517,75 @@ template <int K, int MODE, class C, class Sub, class... Rest> struct Stats<StatL
     static XTG_DI void run(const RG (&rg)[NV], const bool (&ok)[NV][VEC], CT& c, const RowParams& p, void* smem) {
         typedef RowSum<GROUP, C> RS;
         typedef typename RS::A A;
+        bool fixed_done = false;
+        if constexpr (MODE <= 3 && sizeof(C) == 8) {
+            double sum, sdev2;
+            if (fixed_moments<GROUP, VEC, NV, MODE, Sub>(rg, ok, c, p, smem, sum, sdev2)) {
+                fixed_done = true;
+                if (MODE == 0) {
+                    RowFin<C>::put(c, K, sum);
+                } else if (MODE == 1) {
+                    RowFin<C>::put(c, K, RowFin<C>::scale(sum, p, K));
+                } else {
+                    const double var = sdev2 * p.rdiv[K];
+                    RowFin<C>::put(c, K, MODE == 3 ? m_sqrt(var) : var);
+                }
+            }
+        }
         if constexpr (MODE <= 3) {
-            A s;
-            RS::zero(s);
-#pragma unroll
-            for (int n = 0; n < NV; ++n)
-#pragma unroll
-                for (int j = 0; j < VEC; ++j)
-                    if (ok[n][j]) RS::add(s, cvt<C>(Sub::ev(rg[n], j, c)));
-            s = group_reduce<GROUP>(s, reinterpret_cast<A*>(smem));
-            s = bcast_group<GROUP>(s, reinterpret_cast<A*>(smem));
-            // per-row scalar work in C's own precision (float rows never
-            // touch the FP64 pipe; float64 rows multiply by host reciprocals)
-            const C sum = RowFin<C>::total(s);
-            if (MODE == 0) {
-                RowFin<C>::put(c, K, sum);
-            } else if (MODE == 1) {
-                RowFin<C>::put(c, K, RowFin<C>::scale(sum, p, K));
-            } else {
-                const C m = RowFin<C>::mean(sum, p);
-                A q;
-                RS::zero(q);
+            if (!fixed_done) {
+                A s;
+                RS::zero(s);
 #pragma unroll
                 for (int n = 0; n < NV; ++n)
 #pragma unroll
                     for (int j = 0; j < VEC; ++j)
-                        if (ok[n][j]) RS::addsq(q, (C)(cvt<C>(Sub::ev(rg[n], j, c)) - m));
-                q = group_reduce<GROUP>(q, reinterpret_cast<A*>(smem));
-                q = bcast_group<GROUP>(q, reinterpret_cast<A*>(smem));
-                C var = RowFin<C>::scale(RowFin<C>::total(q), p, K);
-                if (var < C(0)) var = C(0);
-                RowFin<C>::put(c, K, MODE == 3 ? m_sqrt(var) : var);
+                        if (ok[n][j]) RS::add(s, cvt<C>(Sub::ev(rg[n], j, c)));
+                s = group_reduce<GROUP>(s, reinterpret_cast<A*>(smem));
+                s = bcast_group<GROUP>(s, reinterpret_cast<A*>(smem));
+                // per-row scalar work in C's own precision (float rows never
+                // touch the FP64 pipe; float64 rows multiply by host reciprocals)
+                const C sum = RowFin<C>::total(s);
+                if (MODE == 0) {
+                    RowFin<C>::put(c, K, sum);
+                } else if (MODE == 1) {
+                    RowFin<C>::put(c, K, RowFin<C>::scale(sum, p, K));
+                } else {
+                    const C m = RowFin<C>::mean(sum, p);
+                    A q;
+                    RS::zero(q);
+                    if constexpr (sizeof(C) == 4) {
+                        // squared deviations are all >= 0 (no cancellation):
+                        // four interleaved FP32 fma chains per lane (relative
+                        // error below (n/(4*lanes) + 2) ulp), then compensated
+                        // across lanes
+                        float qa[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                        for (int n = 0; n < NV; ++n)
+#pragma unroll
+                            for (int j = 0; j < VEC; ++j)
+                                if (ok[n][j]) {
+                                    const float d = cvt<float>(Sub::ev(rg[n], j, c)) - m;
+                                    qa[(n * VEC + j) & 3] = fmaf(d, d, qa[(n * VEC + j) & 3]);
+                                }
+                        q.hi = (qa[0] + qa[1]) + (qa[2] + qa[3]);
+                    } else {
+#pragma unroll
+                        for (int n = 0; n < NV; ++n)
+#pragma unroll
+                            for (int j = 0; j < VEC; ++j)
+                                if (ok[n][j]) RS::addsq(q, (C)(cvt<C>(Sub::ev(rg[n], j, c)) - m));
+                    }
+                    q = group_reduce<GROUP>(q, reinterpret_cast<A*>(smem));
+                    q = bcast_group<GROUP>(q, reinterpret_cast<A*>(smem));
+                    C var = RowFin<C>::scale(RowFin<C>::total(q), p, K);
+                    if (var < C(0)) var = C(0);
+                    RowFin<C>::put(c, K, MODE == 3 ? m_sqrt(var) : var);
+                }
             }
         } else {
             AccSel<C, MODE == 4> a;
-            a.v = MODE == 4 ? Lim<C>::lowest() : Lim<C>::maxv();
-            a.pos = -1;
+            a.start(MODE == 4 ? Lim<C>::lowest() : Lim<C>::maxv());
 #pragma unroll
             for (int n = 0; n < NV; ++n)
 #pragma unroll
@@ -1254,14 +1593,15 @@ template <int K, int MODE, class C, class Sub, class... Rest> struct Stats<StatL
                     if (ok[n][j]) a.add(cvt<C>(Sub::ev(rg[n], j, c)), (i64)((n * GROUP) + (int)(threadIdx.x % GROUP)) * VEC + j);
             a = group_reduce<GROUP>(a, reinterpret_cast<AccSel<C, MODE == 4>*>(smem));
             a = bcast_group<GROUP>(a, reinterpret_cast<AccSel<C, MODE == 4>*>(smem));
-            c.stat[K] = (double)a.v;
-            c.statf[K] = (float)a.v;
+            c.stat[K] = (double)a.value();
+            c.statf[K] = (float)a.value();
         }
         Stats<StatList<Rest...>>::template run<GROUP, VEC, NV>(rg, ok, c, p, smem);
     }
 };
 
-template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int GROUP, int RO, int NSTAT>
+// FULL: row_len == NV * group size * VEC, so no element needs a bounds mask.
+template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int GROUP, int RO, int NSTAT, int FULL>
 __global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
     typedef typename LS::template R<VEC>::type RG;
     __shared__ __align__(16) unsigned char smem_raw[32 * 48];
@@ -1289,8 +1629,8 @@ __global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
         for (int n = 0; n < NV; ++n) {
             const i64 e0 = ((i64)n * gsz + gt) * VEC;
 #pragma unroll
-            for (int j = 0; j < VEC; ++j) ok[n][j] = (e0 + j) < p.row_len;
-            if (e0 < p.row_len) {
+            for (int j = 0; j < VEC; ++j) ok[n][j] = FULL || (e0 + j) < p.row_len;
+            if (FULL || e0 < p.row_len) {
                 i64 off[XTG_KMAX_LEAVES];
 #pragma unroll
                 for (int l = 0; l < LS::N; ++l) off[l] = base[l] + e0 * p.li[l];
@@ -1304,7 +1644,7 @@ __global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
 #pragma unroll
         for (int n = 0; n < NV; ++n) {
             const i64 e0 = ((i64)n * gsz + gt) * VEC;
-            if (e0 < p.row_len) {
+            if (FULL || e0 < p.row_len) {
                 OutT v[VEC];
 #pragma unroll
                 for (int j = 0; j < VEC; ++j) v[j] = cvt<OutT>(Tree::ev(rg[n], j, c));
@@ -1378,7 +1718,7 @@ template <class... S> struct LoadRowSmem<LeafSet<S...>> {
     }
 };
 
-template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int RO, int NSTAT>
+template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int RO, int NSTAT, int FULL>
 __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
     typedef typename LS::template R<VEC>::type RG;
     extern __shared__ __align__(128) unsigned char dsmem[];
@@ -1387,7 +1727,7 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
     const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
     const int nw = (int)blockDim.x >> 5;
     u64* mybar = bars + 2 * warp;
-    unsigned char* buf[2] = {dsmem + (size_t)(2 * warp) * p.buf_bytes, dsmem + (size_t)(2 * warp + 1) * p.buf_bytes};
+    unsigned char* const buf0 = dsmem + (size_t)(2 * warp) * p.buf_bytes;  // buffer b at buf0 + b * buf_bytes
     if (lane == 0) {
         mbar_init(&mybar[0], 1);
         mbar_init(&mybar[1], 1);
@@ -1409,7 +1749,7 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
 #pragma unroll
                 for (int d = 0; d < RO; ++d) o += ko[d] * p.lo[l][d];
                 const unsigned char* src = reinterpret_cast<const unsigned char*>(p.leaf[l]) + o * (p.lbytes[l] / p.row_len);
-                bulk_g2s(buf[b] + p.loff[l], src, p.lbytes[l], &mybar[b]);
+                bulk_g2s(buf0 + (size_t)b * p.buf_bytes + p.loff[l], src, p.lbytes[l], &mybar[b]);
             }
         }
     };
@@ -1443,8 +1783,8 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
         for (int n = 0; n < NV; ++n) {
             const i64 e0 = ((i64)n * 32 + lane) * VEC;
 #pragma unroll
-            for (int j = 0; j < VEC; ++j) ok[n][j] = (e0 + j) < p.row_len;
-            if (e0 < p.row_len) LoadRowSmem<LS>::template run<VEC>(rg[n], buf[b], p.loff, e0);
+            for (int j = 0; j < VEC; ++j) ok[n][j] = FULL || (e0 + j) < p.row_len;
+            if (FULL || e0 < p.row_len) LoadRowSmem<LS>::template run<VEC>(rg[n], buf0 + (size_t)b * p.buf_bytes, p.loff, e0);
         }
         Stats<SL>::template run<32, VEC, NV>(rg, ok, c, p, (void*)red_smem);
         i64 ko[RO];
@@ -1455,7 +1795,7 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
 #pragma unroll
         for (int n = 0; n < NV; ++n) {
             const i64 e0 = ((i64)n * 32 + lane) * VEC;
-            if (e0 < p.row_len) {
+            if (FULL || e0 < p.row_len) {
                 OutT v[VEC];
 #pragma unroll
                 for (int j = 0; j < VEC; ++j) v[j] = cvt<OutT>(Tree::ev(rg[n], j, c));

@@ -268,13 +268,14 @@ static bool leaf_free(const Tree& t, int n) {
     return true;
 }
 
-std::string tree_type(const Tree& t, int n, const std::vector<int>& map, bool recip) {
+std::string tree_type(const Tree& t, int n, const std::vector<int>& map, int recip) {
     const PNode& x = t.nodes[n];
     const std::string T = dt(x.dtype).cname;
     auto k = [&](int i) { return tree_type(t, x.kids[i], map, recip); };
-    if (recip && x.op == XTG_OP_DIV && x.dtype == XTG_FLOAT64 && leaf_free(t, x.kids[1])) {
+    const bool rdt = (x.dtype == XTG_FLOAT64 && (recip & 1)) || (x.dtype == XTG_FLOAT32 && (recip & 2));
+    if (rdt && x.op == XTG_OP_DIV && leaf_free(t, x.kids[1])) {
         const PNode& a = t.nodes[x.kids[0]];
-        if (a.op == XTG_OP_SUB && a.dtype == XTG_FLOAT64 && leaf_free(t, a.kids[1]))
+        if (a.op == XTG_OP_SUB && a.dtype == x.dtype && leaf_free(t, a.kids[1]))
             return "xtg::FmaRecipSub<" + T + ", " + tree_type(t, a.kids[0], map, recip) + ", " +
                    tree_type(t, a.kids[1], map, recip) + ", " + k(1) + ">";
         return "xtg::MulRecip<" + T + ", " + k(0) + ", " + k(1) + ">";
