@@ -413,7 +413,8 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
     p.frow_len = (float)row_len;
     sl += ">";
     const int recip = (opt("row.recip_div_f64", 1) != 0 ? 1 : 0) | (opt("row.recip_div_f32", 1) != 0 ? 2 : 0);
-    const std::string tree = tree_type(t, t.root, map, recip);
+    int nstat = t.n_rstats;  // real statistics, then the reciprocal nodes' row-invariant slots
+    const std::string tree = tree_type(t, t.root, map, recip, &nstat);
     const int full = (int64_t)nv * group * vec == row_len ? 1 : 0;
 
     // Bulk-copy variant: every leaf contiguous along the row, 16-byte rows,
@@ -440,7 +441,7 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
         XTG_TRY(device_error_word(&p.err));
         std::string name = "xtg::k_rowfused_tma<" + tree + ", " + sl + ", " + leafset(t, order, kinds) + ", " +
                            dt(out.dtype).cname + ", " + std::to_string(vec) + ", " + std::to_string(nv) + ", " +
-                           std::to_string(D.R) + ", " + std::to_string(t.n_rstats) + ", " + std::to_string(full) + ">";
+                           std::to_string(D.R) + ", " + std::to_string(nstat) + ", " + std::to_string(full) + ">";
         Kernel* kr;
         XTG_TRY(get_kernel(name, tma_block, &kr, dyn));
         int64_t need = (n_rows + 3) / 4;
@@ -448,7 +449,7 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
     }
     std::string name = "xtg::k_rowfused<" + tree + ", " + sl + ", " + leafset(t, order, kinds) + ", " +
                        dt(out.dtype).cname + ", " + std::to_string(vec) + ", " + std::to_string(nv) + ", " +
-                       std::to_string(group) + ", " + std::to_string(D.R) + ", " + std::to_string(t.n_rstats) + ", " +
+                       std::to_string(group) + ", " + std::to_string(D.R) + ", " + std::to_string(nstat) + ", " +
                        std::to_string(full) + ">";
     const int block = 256;
     Kernel* kr;

@@ -286,6 +286,7 @@ template <int NSTAT> struct Ctx {
     Scalars scal;  // by value: immediates live in registers, conversions hoist
     double stat[NSTAT > 0 ? NSTAT : 1];   // row statistics (FP64 consumers)
     float statf[NSTAT > 0 ? NSTAT : 1];   // the same, rounded once (FP32 consumers)
+    unsigned fixmask;                     // statistics already produced for this row (bit K)
 };
 
 // Leaves / scalars / row statistics as tree terminals.
@@ -300,9 +301,26 @@ template <int K, class T> struct S {
 // A row statistic produced by a fused row reducer (index K of Ctx::stat).
 template <class T> struct StatGet {
     template <class C> static XTG_DI T get(const C& c, int k) { return (T)c.stat[k]; }
+    template <class C> static XTG_DI void put(C& c, int k, T v) {
+        c.stat[k] = (double)v;
+        c.statf[k] = (float)v;
+    }
 };
 template <> struct StatGet<float> {
     template <class C> static XTG_DI float get(const C& c, int k) { return c.statf[k]; }
+    template <class C> static XTG_DI void put(C& c, int k, float v) {
+        c.statf[k] = v;
+        c.stat[k] = (double)v;
+    }
+};
+// Row-invariant subtrees evaluated once per row before the output pass: the
+// reciprocal nodes (MulRecip, FmaRecipSub) store theirs in statistic slots
+// after the real statistics.  Prep walks the tree; nodes without work recurse.
+template <class N> struct Prep {
+    template <class RG, class C> static XTG_DI void run(const RG&, C&) {}
+};
+template <template <class...> class N, class... X> struct Prep<N<X...>> {
+    template <class RG, class C> static XTG_DI void run(const RG& r, C& c) { (Prep<X>::run(r, c), ...); }
 };
 template <int K, class T> struct Stat {
     typedef T type;
@@ -1289,15 +1307,12 @@ template <int GROUP> struct RowSum<GROUP, float> {
     }
     static XTG_DI double val(const A& a) { return a.dval(); }
 };
+// After group_reduce every lane of a warp group already holds the total: the
+// xor butterfly merges the same operands in every lane, and every merge is
+// symmetric (sums, exact TwoSum errors, selection with position ties), so a
+// warp group needs no broadcast.
 template <int GROUP, class A> XTG_DI A bcast_group(A a, A* smem) {
-    if (GROUP <= 32) {
-        union U { A a; u32 w[(sizeof(A) + 3) / 4]; };
-        U u;
-        u.a = a;
-#pragma unroll
-        for (int i = 0; i < (int)((sizeof(A) + 3) / 4); ++i) u.w[i] = __shfl_sync(0xffffffffu, u.w[i], 0);
-        return u.a;
-    }
+    if (GROUP <= 32) return a;
     __syncthreads();
     if (threadIdx.x == 0) smem[0] = a;
     __syncthreads();
@@ -1507,6 +1522,39 @@ XTG_DI bool fixed_moments(const RG (&rg)[NV], const bool (&ok)[NV][VEC], const C
     return true;
 }
 
+template <class A, class B> struct SameT { enum { value = 0 }; };
+template <class A> struct SameT<A, A> { enum { value = 1 }; };
+// Statistics of the same float64 operand share one pass of fixed_moments:
+// the highest moment any of them needs, and who receives the results.
+template <class Sub, class... R> struct SameSubMode { enum { value = -1 }; };
+template <class Sub, int K2, int M2, class C2, class S2, class... R> struct SameSubMode<Sub, RStat<K2, M2, C2, S2>, R...> {
+    enum {
+        rest = SameSubMode<Sub, R...>::value,
+        mine = (SameT<Sub, S2>::value && sizeof(C2) == 8 && M2 <= 3) ? M2 : -1,
+        value = rest > mine ? rest : mine
+    };
+};
+template <int MODE, int K, class CT> XTG_DI void put_moment(CT& c, const RowParams& p, double sum, double sdev2) {
+    if (MODE == 0) {
+        RowFin<double>::put(c, K, sum);
+    } else if (MODE == 1) {
+        RowFin<double>::put(c, K, RowFin<double>::scale(sum, p, K));
+    } else {
+        const double var = sdev2 * p.rdiv[K];
+        RowFin<double>::put(c, K, MODE == 3 ? m_sqrt(var) : var);
+    }
+    if (K < 32) c.fixmask |= 1u << K;
+}
+template <class Sub, class... R> struct PutSameSub {
+    template <class CT> static XTG_DI void run(CT&, const RowParams&, double, double) {}
+};
+template <class Sub, int K2, int M2, class C2, class S2, class... R> struct PutSameSub<Sub, RStat<K2, M2, C2, S2>, R...> {
+    template <class CT> static XTG_DI void run(CT& c, const RowParams& p, double sum, double sdev2) {
+        if constexpr (SameT<Sub, S2>::value && sizeof(C2) == 8 && M2 <= 3 && K2 < 32) put_moment<M2, K2>(c, p, sum, sdev2);
+        PutSameSub<Sub, R...>::run(c, p, sum, sdev2);
+    }
+};
+
 template <class LST> struct Stats;
 template <> struct Stats<StatList<>> {
     template <int GROUP, int VEC, int NV, class RG, class CT>
@@ -1519,16 +1567,16 @@ template <int K, int MODE, class C, class Sub, class... Rest> struct Stats<StatL
         typedef typename RS::A A;
         bool fixed_done = false;
         if constexpr (MODE <= 3 && sizeof(C) == 8) {
-            double sum, sdev2;
-            if (fixed_moments<GROUP, VEC, NV, MODE, Sub>(rg, ok, c, p, smem, sum, sdev2)) {
-                fixed_done = true;
-                if (MODE == 0) {
-                    RowFin<C>::put(c, K, sum);
-                } else if (MODE == 1) {
-                    RowFin<C>::put(c, K, RowFin<C>::scale(sum, p, K));
-                } else {
-                    const double var = sdev2 * p.rdiv[K];
-                    RowFin<C>::put(c, K, MODE == 3 ? m_sqrt(var) : var);
+            if (K < 32 && ((c.fixmask >> K) & 1u)) {
+                fixed_done = true;  // produced with an earlier statistic of the same operand
+            } else {
+                constexpr int later = SameSubMode<Sub, Rest...>::value;
+                constexpr int MX = later > MODE ? later : MODE;
+                double sum, sdev2;
+                if (fixed_moments<GROUP, VEC, NV, MX, Sub>(rg, ok, c, p, smem, sum, sdev2)) {
+                    fixed_done = true;
+                    put_moment<MODE, K>(c, p, sum, sdev2);
+                    PutSameSub<Sub, Rest...>::run(c, p, sum, sdev2);
                 }
             }
         }
@@ -1637,7 +1685,9 @@ __global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
                 LoadLeavesAt<LS>::template run<VEC>(rg[n], p.leaf, off, p.li);
             }
         }
+        c.fixmask = 0;
         Stats<SL>::template run<GROUP, VEC, NV>(rg, ok, c, p, (void*)smem_raw);
+        Prep<Tree>::run(rg[0], c);
         i64 ob = 0;
 #pragma unroll
         for (int d = 0; d < RO; ++d) ob += ko[d] * p.oo[d];
@@ -1786,7 +1836,9 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
             for (int j = 0; j < VEC; ++j) ok[n][j] = FULL || (e0 + j) < p.row_len;
             if (FULL || e0 < p.row_len) LoadRowSmem<LS>::template run<VEC>(rg[n], buf0 + (size_t)b * p.buf_bytes, p.loff, e0);
         }
+        c.fixmask = 0;
         Stats<SL>::template run<32, VEC, NV>(rg, ok, c, p, (void*)red_smem);
+        Prep<Tree>::run(rg[0], c);
         i64 ko[RO];
         decode_dims<RO, true>(p.oshape, (const FastDiv*)0, row, ko);
         i64 ob = 0;
@@ -1808,15 +1860,20 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
     }
 }
 
-// a * (1 / b) with b invariant over a row (the reciprocal is computed once
-// per row by common-subexpression elimination over the unrolled elements):
-// used for float64 rows, where a division costs ~10 FP64 operations on GB300.
-template <class T, class A, class B> struct MulRecip {
+// a * (1 / b) with b invariant over a row: the reciprocal is computed once
+// per row (Prep) into statistic slot KR (a division costs ~10 FP64
+// operations on GB300, and an IEEE FP32 division several instructions).
+template <class T, class A, class B, int KR> struct MulRecip {
     typedef T type;
     template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C& c) {
-        T a = cvt<T>(A::ev(r, j, c));
-        T b = cvt<T>(B::ev(r, j, c));
-        return a * (T(1) / b);
+        return cvt<T>(A::ev(r, j, c)) * StatGet<T>::get(c, KR);
+    }
+};
+template <class T, class A, class B, int KR> struct Prep<MulRecip<T, A, B, KR>> {
+    template <class RG, class C> static XTG_DI void run(const RG& r, C& c) {
+        Prep<A>::run(r, c);
+        Prep<B>::run(r, c);
+        StatGet<T>::put(c, KR, T(1) / cvt<T>(B::ev(r, 0, c)));
     }
 };
 
@@ -1949,14 +2006,22 @@ __global__ void __launch_bounds__(256) k_batch_assign(const BatchParams p) {
 }
 
 // (a - m) / b with m and b invariant over a row, as one fused multiply-add
-// per element: a * r - m * r with r = 1 / b (r and m * r once per row).
-template <class T, class A, class M, class B> struct FmaRecipSub {
+// per element: a * r - m * r with r = 1 / b; r (slot KR) and m * r (slot KM)
+// are computed once per row (Prep).
+template <class T, class A, class M, class B, int KR, int KM> struct FmaRecipSub {
     typedef T type;
     template <class RG, class C> static XTG_DI T ev(const RG& r, int j, const C& c) {
-        const T a = cvt<T>(A::ev(r, j, c));
-        const T m = cvt<T>(M::ev(r, j, c));
-        const T rb = T(1) / cvt<T>(B::ev(r, j, c));
-        return fma(a, rb, -(m * rb));
+        return fma(cvt<T>(A::ev(r, j, c)), StatGet<T>::get(c, KR), -StatGet<T>::get(c, KM));
+    }
+};
+template <class T, class A, class M, class B, int KR, int KM> struct Prep<FmaRecipSub<T, A, M, B, KR, KM>> {
+    template <class RG, class C> static XTG_DI void run(const RG& r, C& c) {
+        Prep<A>::run(r, c);
+        Prep<M>::run(r, c);
+        Prep<B>::run(r, c);
+        const T rb = T(1) / cvt<T>(B::ev(r, 0, c));
+        StatGet<T>::put(c, KR, rb);
+        StatGet<T>::put(c, KM, cvt<T>(M::ev(r, 0, c)) * rb);
     }
 };
 

@@ -268,17 +268,24 @@ static bool leaf_free(const Tree& t, int n) {
     return true;
 }
 
-std::string tree_type(const Tree& t, int n, const std::vector<int>& map, int recip) {
+std::string tree_type(const Tree& t, int n, const std::vector<int>& map, int recip, int* slot) {
     const PNode& x = t.nodes[n];
     const std::string T = dt(x.dtype).cname;
-    auto k = [&](int i) { return tree_type(t, x.kids[i], map, recip); };
+    auto k = [&](int i) { return tree_type(t, x.kids[i], map, recip, slot); };
     const bool rdt = (x.dtype == XTG_FLOAT64 && (recip & 1)) || (x.dtype == XTG_FLOAT32 && (recip & 2));
-    if (rdt && x.op == XTG_OP_DIV && leaf_free(t, x.kids[1])) {
+    if (slot && rdt && x.op == XTG_OP_DIV && leaf_free(t, x.kids[1])) {
         const PNode& a = t.nodes[x.kids[0]];
-        if (a.op == XTG_OP_SUB && a.dtype == x.dtype && leaf_free(t, a.kids[1]))
-            return "xtg::FmaRecipSub<" + T + ", " + tree_type(t, a.kids[0], map, recip) + ", " +
-                   tree_type(t, a.kids[1], map, recip) + ", " + k(1) + ">";
-        return "xtg::MulRecip<" + T + ", " + k(0) + ", " + k(1) + ">";
+        if (a.op == XTG_OP_SUB && a.dtype == x.dtype && leaf_free(t, a.kids[1])) {
+            const std::string ta = tree_type(t, a.kids[0], map, recip, slot);
+            const std::string tm = tree_type(t, a.kids[1], map, recip, slot);
+            const std::string tb = k(1);
+            const int kr = (*slot)++, km = (*slot)++;
+            return "xtg::FmaRecipSub<" + T + ", " + ta + ", " + tm + ", " + tb + ", " + std::to_string(kr) + ", " +
+                   std::to_string(km) + ">";
+        }
+        const std::string ta = k(0), tb = k(1);
+        const int kr = (*slot)++;
+        return "xtg::MulRecip<" + T + ", " + ta + ", " + tb + ", " + std::to_string(kr) + ">";
     }
     switch (x.op) {
         case XTG_OP_LEAF:

@@ -46,8 +46,10 @@ bool is_rop(int op);
 // Type string of the subtree at node `n` (leaf indices through `leaf_map`).
 // recip_div: bit 0 float64, bit 1 float32 — divisions of that type by a
 // leaf-free (row-invariant) divisor become a multiplication by its reciprocal
-// ((a - m) / s becomes fma(a, 1/s, -(m * (1/s))); fused row kernels only).
-std::string tree_type(const Tree& t, int n, const std::vector<int>& leaf_map, int recip_div = 0);
+// ((a - m) / s becomes fma(a, 1/s, -(m * (1/s)))), whose row-invariant parts
+// take statistic slots *slot, *slot + 1, ... (fused row kernels only; slot
+// must then be given and is advanced past the slots used).
+std::string tree_type(const Tree& t, int n, const std::vector<int>& leaf_map, int recip_div = 0, int* slot = nullptr);
 // Broadcast strides of leaf `l` against the tree's shape (rank t.rank).
 void leaf_bstrides(const Tree& t, int l, int64_t* st);
 // Broadcast strides of array `a` against a target shape of rank `rank`.
