@@ -407,6 +407,7 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
         }
         p.div[x.stat] = div;
         p.rdiv[x.stat] = 1.0 / div;
+        p.vfac[x.stat] = 1.0 / ((double)row_len * div);
         p.fdiv[x.stat] = (float)div;
     }
     p.rrow_len = 1.0 / (double)row_len;

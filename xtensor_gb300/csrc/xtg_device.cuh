@@ -1411,6 +1411,50 @@ XTG_DI U192 u192_sub(U192 a, U192 b) {
     r.w2 = a.w2 - b.w2 - b1 - (t < b0 ? 1ull : 0ull);
     return r;
 }
+// (-1)^neg * q * 2^e2 rounded to nearest even, on the integer pipes (a lane
+// of a warp group runs this per row, and GB300's FP64 rate makes the usual
+// conversions + scalbn cost more than the row's elements).  Results outside
+// the normal range go through scalbn.
+XTG_DI double fix_to_double(U192 q, bool neg, int e2) {
+    int top;
+    if (q.w2) top = 191 - __clzll(q.w2);
+    else if (q.w1) top = 127 - __clzll(q.w1);
+    else if (q.w0) top = 63 - __clzll(q.w0);
+    else return neg ? -0.0 : 0.0;
+    // the 64 bits below and including the top bit, and whether anything
+    // nonzero lies under them
+    u64 m;
+    bool sticky;
+    const int sh = top - 63;
+    if (sh <= 0) {
+        m = q.w0 << (-sh);
+        sticky = false;
+    } else {
+        const int wi = sh >> 6, b = sh & 63;
+        const u64 lo = wi == 0 ? q.w0 : (wi == 1 ? q.w1 : q.w2);
+        const u64 hi = wi == 0 ? q.w1 : (wi == 1 ? q.w2 : 0ull);
+        m = b ? ((lo >> b) | (hi << (64 - b))) : lo;
+        const u64 below = b ? (lo << (64 - b)) : 0ull;
+        sticky = below != 0 || (wi >= 1 && q.w0 != 0) || (wi == 2 && q.w1 != 0);
+    }
+    u64 mant = m >> 11;  // 53 bits, leading one at bit 52
+    const bool rnd = (m >> 10) & 1;
+    sticky = sticky || (m & 0x3ffull) != 0;
+    if (rnd && (sticky || (mant & 1))) ++mant;
+    int e = top + e2;  // value = mant * 2^(e - 52)
+    if (mant >> 53) {
+        mant >>= 1;
+        ++e;
+    }
+    const int be = e + 1023;
+    if (be < 1 || be > 2046) {
+        const double r = scalbn((double)mant, e - 52);  // exact mant; scalbn rounds once at the range end
+        return neg ? -r : r;
+    }
+    const u64 bits = ((u64)neg << 63) | ((u64)be << 52) | (mant & 0xfffffffffffffull);
+    return __longlong_as_double((long long)bits);
+}
+
 // lane / group partial sums: sum X as a signed 128-bit (two's complement)
 // word pair, sum X^2 as unsigned 128-bit
 struct FixMom {
@@ -1489,8 +1533,6 @@ XTG_DI bool fixed_moments(const RG (&rg)[NV], const bool (&ok)[NV][VEC], const C
     f = group_reduce<GROUP>(f, reinterpret_cast<FixMom*>(smem));
     f = bcast_group<GROUP>(f, reinterpret_cast<FixMom*>(smem));
     const int sig = em.v - 1075;  // x = X * 2^sig
-    // |sum X| < 2^69: convert the magnitude (a negative two's-complement
-    // pair would round its low word near 2^64)
     U128 m1 = f.s1;
     const bool neg = (i64)m1.hi < 0;
     if (neg) {
@@ -1499,15 +1541,15 @@ XTG_DI bool fixed_moments(const RG (&rg)[NV], const bool (&ok)[NV][VEC], const C
         z.hi = 0;
         m1 = u128_sub(z, m1);
     }
-    // m1.hi < 2^6: the upper 70 - 32 bits are exact in a double, so the one
-    // addition below is the only rounding
-    const double mag = ((double)m1.hi * 4294967296.0 + (double)(m1.lo >> 32)) * 4294967296.0 +
-                       (double)(m1.lo & 0xffffffffull);
-    sum = scalbn(neg ? -mag : mag, sig);
+    U192 s1w;
+    s1w.w0 = m1.lo;
+    s1w.w1 = m1.hi;
+    s1w.w2 = 0;
+    sum = fix_to_double(s1w, neg, sig);
     sdev2 = 0.0;
     if (MODE >= 2) {
         // sum X^2 < 2^122, n <= 2^16: n * sum X^2 - (sum X)^2 in 192 bits
-        // (exact, >= 0)
+        // (exact, >= 0); returned as n * sum (x - mean)^2
         U192 sq = u192_mul(m1, m1.lo);
         const U192 sqh = u192_mul(m1, m1.hi);  // times 2^64
         U192 sh;
@@ -1516,8 +1558,7 @@ XTG_DI bool fixed_moments(const RG (&rg)[NV], const bool (&ok)[NV][VEC], const C
         sh.w2 = sqh.w1;
         sq = u192_add(sq, sh);
         const U192 q = u192_sub(u192_mul(f.s2, (u64)n), sq);
-        const double qd = ((double)q.w2 * 18446744073709551616.0 + (double)q.w1) * 18446744073709551616.0 + (double)q.w0;
-        sdev2 = scalbn(qd / (double)n, 2 * sig);
+        sdev2 = fix_to_double(q, false, 2 * sig);
     }
     return true;
 }
@@ -1540,7 +1581,7 @@ template <int MODE, int K, class CT> XTG_DI void put_moment(CT& c, const RowPara
     } else if (MODE == 1) {
         RowFin<double>::put(c, K, RowFin<double>::scale(sum, p, K));
     } else {
-        const double var = sdev2 * p.rdiv[K];
+        const double var = sdev2 * p.vfac[K];  // (n * sum (x - mean)^2) / (n * divisor)
         RowFin<double>::put(c, K, MODE == 3 ? m_sqrt(var) : var);
     }
     if (K < 32) c.fixmask |= 1u << K;
@@ -2022,6 +2063,19 @@ template <class T, class A, class M, class B, int KR, int KM> struct Prep<FmaRec
         const T rb = T(1) / cvt<T>(B::ev(r, 0, c));
         StatGet<T>::put(c, KR, rb);
         StatGet<T>::put(c, KM, cvt<T>(M::ev(r, 0, c)) * rb);
+    }
+};
+// float64 (a - m) / sqrt(v): 1 / sqrt(v) by CUDA's rsqrt (within 1 ulp) instead
+// of a correctly rounded sqrt and division — each lane of a warp runs this
+// once per row, at GB300's FP64 rate.
+template <class A, class M, class X, int KR, int KM> struct Prep<FmaRecipSub<double, A, M, Sqrt<double, X>, KR, KM>> {
+    template <class RG, class C> static XTG_DI void run(const RG& r, C& c) {
+        Prep<A>::run(r, c);
+        Prep<M>::run(r, c);
+        Prep<X>::run(r, c);
+        const double rb = rsqrt(cvt<double>(X::ev(r, 0, c)));
+        StatGet<double>::put(c, KR, rb);
+        StatGet<double>::put(c, KM, cvt<double>(M::ev(r, 0, c)) * rb);
     }
 };
 
