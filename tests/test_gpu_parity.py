@@ -156,6 +156,25 @@ def test_transpose_bit_exact(dt, perm):
     np.testing.assert_array_equal(out.to_numpy(), np.ascontiguousarray(x.transpose(perm)))
 
 
+@pytest.mark.parametrize("dt", ["float32", "float64", "int8", "bfloat16"])
+@pytest.mark.parametrize("perm", [(0, 2, 1), (2, 0, 1), (1, 2, 0), (2, 1, 0)])
+def test_transpose_interior_and_edge_tiles(dt, perm):
+    """Shapes with whole 64x64 (and 32x32) tiles plus ragged edges, so both
+    the unchecked interior path and the bounds-checked edge path run."""
+    g = rng(16)
+    shape = (3, 129, 257)
+    if dt == "bfloat16":
+        x = f32_to_bf16_bits(g.standard_normal(shape).astype(np.float32))
+    elif dt.startswith("float"):
+        x = g.standard_normal(shape).astype(dt)
+    else:
+        x = g.integers(-100, 100, shape).astype(dt)
+    d = dev(x, dt)
+    out = DeviceArray.empty(d.transpose(perm).shape, dt)
+    xg.assign(out, d.transpose(perm))
+    np.testing.assert_array_equal(out.to_numpy(), np.ascontiguousarray(x.transpose(perm)))
+
+
 def test_transpose_with_elementwise_and_views():
     g = rng(7)
     x = g.standard_normal((64, 48)).astype(np.float32)

@@ -1038,11 +1038,13 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
         const i64 rb = s * p.chunk;
         i64 re = rb + p.chunk;
         if (re > p.n_redv) re = p.n_redv;
-        // U vectors in flight per thread; each thread still visits its
-        // positions in increasing order
+        // two register batches of U vectors: the next batch's loads are in
+        // flight while the current one is reduced; each thread still visits
+        // its positions in increasing order
         constexpr int U = 4;
-        for (i64 r0 = rb + gtid; r0 < re; r0 += (i64)gsz * U) {
-            RG rg[U];
+        const i64 step = (i64)gsz * U;
+        RG rga[U], rgb[U];
+        auto load = [&](RG(&rg)[U], i64 r0) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const i64 r = r0 + (i64)u * gsz;
@@ -1055,6 +1057,8 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
                     LoadLeavesAt<LS>::template run<VEC>(rg[u], p.leaf, off, inner);
                 }
             }
+        };
+        auto consume = [&](const RG(&rg)[U], i64 r0) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const i64 r = r0 + (i64)u * gsz;
@@ -1063,6 +1067,15 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
                     for (int j = 0; j < VEC; ++j) acc.add(Tree::ev(rg[u], j, c), r * VEC + j);
                 }
             }
+        };
+        i64 r0 = rb + gtid;
+        if (r0 < re) load(rga, r0);
+        for (; r0 < re; r0 += 2 * step) {
+            if (r0 + step < re) load(rgb, r0 + step);
+            consume(rga, r0);
+            if (r0 + step >= re) break;
+            if (r0 + 2 * step < re) load(rga, r0 + 2 * step);
+            consume(rgb, r0 + step);
         }
         acc = group_reduce<GROUP>(acc, smem);
         if (gtid == 0) {
@@ -1236,6 +1249,29 @@ __global__ void __launch_bounds__(TILE * ROWS) k_transpose(const TransposeParams
         }
         const i64 a0 = ta * TILE, b0 = tb * TILE;
         const T0* src = reinterpret_cast<const T0*>(p.leaf[0]);
+        if (LS::N == 1 && a0 + TILE <= p.sa && b0 + TILE <= p.sb) {
+            // interior tile of a single-leaf tree: no bounds tests, and one
+            // pointer step per element instead of the 64-bit index products
+            const T0* ps = src + boff[0] + (a0 + tx) * p.la[0] + (b0 + ty) * p.lb[0];
+            const i64 sstep = (i64)ROWS * p.lb[0];
+#pragma unroll
+            for (int bb = ty; bb < TILE; bb += ROWS) {
+                tile[bb][tx] = ld1<T0>(ps);
+                ps += sstep;
+            }
+            __syncthreads();
+            OutT* pd = reinterpret_cast<OutT*>(p.out) + obo + (a0 + ty) * p.oa + (b0 + tx) * p.ob;
+            const i64 dstep = (i64)ROWS * p.oa;
+#pragma unroll
+            for (int aa = ty; aa < TILE; aa += ROWS) {
+                RG rg;
+                rg.v[0] = tile[tx][aa];
+                *pd = cvt<OutT>(Tree::ev(rg, 0, c));
+                pd += dstep;
+            }
+            __syncthreads();
+            continue;
+        }
         {
             const i64 a = a0 + tx;
 #pragma unroll

@@ -64,6 +64,9 @@ xtg_status ensure_device(DeviceInfo** info);
 
 // ---- options -----------------------------------------------------------------
 int64_t opt(const char* key, int64_t dflt);
+// Default work items a ROW reduction is split into (reduce.target_items):
+// shared by every planner of a reduction so equal calls partition alike.
+constexpr int64_t kReduceTargetItems = 2048;
 // Option "jit.dry_run": plan and compile kernels without a GPU (no launches).
 bool dry_run();
 

@@ -109,7 +109,7 @@ extern "C" xtg_status xtg_sum_f32_noalloc(const float* x, int64_t n, float* out,
     if (nv > 0xFFFFFFF0ll) return fail(XTG_ERR_UNSUPPORTED, "xtg_sum_f32_noalloc: more than 2^32 vectors");
     int64_t nsplit = 1;
     {
-        const int64_t target = opt("reduce.target_items", 8192);
+        const int64_t target = opt("reduce.target_items", kReduceTargetItems);
         const int64_t minchunk = opt("reduce.min_chunk", 512);
         nsplit = std::max<int64_t>(1, std::min<int64_t>(target, nv / minchunk));
     }

@@ -252,7 +252,7 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
     // fixed partition (depends on shapes only)
     int64_t nsplit = 1;
     if (row) {
-        const int64_t target = opt("reduce.target_items", 8192);
+        const int64_t target = opt("reduce.target_items", kReduceTargetItems);
         const int64_t minchunk = opt("reduce.min_chunk", 512);
         nsplit = std::max<int64_t>(1, std::min<int64_t>((target + n_out - 1) / n_out, p.n_redv / minchunk));
     } else {
