@@ -12,7 +12,9 @@ value      = algorithmic bytes of one step (each input read once, each output
              written once) / device time per step, GB/s, inputs resident in HBM;
 e2e        = the same metric with host buffers: pinned host->device copies of
              the inputs and device->host copies of every result inside the
-             timed region;
+             timed region (copies in, kernels and copies out on three
+             streams with two device buffer sets, so consecutive steps
+             overlap on the link);
 roofline   = the dominant kernel's algorithmic GB/s (CUDA events on its
              launching stream) over the measured HBM copy bandwidth;
 cpu_baseline = the compiled CPU port of the reference's code path
@@ -368,7 +370,7 @@ def run_gpu(args):
     # ---- end to end through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(lib, step, x32, x64, stream, max(1, min(args.steps, 5)), D)
+        e2e = run_e2e(lib, step, x32, x64, stream, max(2, min(args.steps, 10)), D)
 
     # ---- CPU baseline (rank 0, N=1)
     cpu = None
@@ -399,43 +401,76 @@ def run_gpu(args):
 
 
 def run_e2e(lib, step, x32, x64, stream, steps, D):
+    """The step end to end through the C ABI from pinned host memory: every
+    step copies both inputs in and every output back.  Copies in, kernels and
+    copies out run on three streams ordered by events, with two device buffer
+    sets, so step k's outputs stream back while step k+1's inputs stream in
+    (the link carries both directions at once)."""
     from xtensor_gb300._ffi import check
     H2D, D2H = 1, 2
-    hin, hout = [], []
-    for x, dx in zip((x32, x64), step.dev_in):
+    sets = [step, GpuStep(x32, x64, stream)]
+
+    def mkstream():
+        sp = C.c_void_p()
+        check(lib.xtg_stream_create(C.byref(sp)))
+        return sp.value
+    s_in, s_out = mkstream(), mkstream()
+    hin = []
+    for x in (x32, x64):
         p = C.c_void_p()
         check(lib.xtg_host_alloc(C.byref(p), x.nbytes))
         C.memmove(p.value, x.ctypes.data, x.nbytes)
-        hin.append((p.value, dx.ptr, x.nbytes))
-    for outs in step.dev_out:
-        for o in outs:
-            p = C.c_void_p()
-            check(lib.xtg_host_alloc(C.byref(p), o.nbytes))
-            hout.append((p.value, o.ptr, o.nbytes))
-    h2d = sum(n for _, _, n in hin)
-    d2h = sum(n for _, _, n in hout)
+        hin.append((p.value, x.nbytes))
+    hout = []
+    for o in [o for outs in step.dev_out for o in outs]:
+        p = C.c_void_p()
+        check(lib.xtg_host_alloc(C.byref(p), o.nbytes))
+        hout.append((p.value, o.nbytes))
+    h2d = sum(n for _, n in hin)
+    d2h = sum(n for _, n in hout)
+    nops = len(step.calls)
+    per = len(step.calls) // 2  # calls per input array
+    ev = [{"in": ev_create(lib, 2), "out": ev_create(lib, nops), "comp": ev_create(lib, 1)[0],
+           "d2h": ev_create(lib, 1)[0]} for _ in sets]
 
-    def one():
-        for h, d, n in hin:
-            check(lib.xtg_memcpy(d, h, n, H2D, stream))
-        step.run()
-        for h, d, n in hout:
-            check(lib.xtg_memcpy(h, d, n, D2H, stream))
+    def one(k):
+        b = k % 2
+        S, E = sets[b], ev[b]
+        if k >= 2:
+            check(lib.xtg_stream_wait_event(s_in, E["comp"]))    # inputs no longer read
+            check(lib.xtg_stream_wait_event(stream, E["d2h"]))   # outputs copied out
+        for a, (h, n) in enumerate(hin):
+            check(lib.xtg_memcpy(S.dev_in[a].ptr, h, n, H2D, s_in))
+            check(lib.xtg_event_record(E["in"][a], s_in))
+        for i, (_, _, fn) in enumerate(S.calls):
+            if i % per == 0:
+                check(lib.xtg_stream_wait_event(stream, E["in"][i // per]))
+            check(fn())
+            check(lib.xtg_event_record(E["out"][i], stream))
+        check(lib.xtg_event_record(E["comp"], stream))
+        for i in range(nops):
+            check(lib.xtg_stream_wait_event(s_out, E["out"][i]))
+            o = S.dev_out[i // per][i % per]
+            check(lib.xtg_memcpy(hout[i][0], o.ptr, o.nbytes, D2H, s_out))
+        check(lib.xtg_event_record(E["d2h"], s_out))
 
-    one()
-    check(lib.xtg_stream_sync(stream))
+    for k in range(2):
+        one(k)
+    check(lib.xtg_device_sync())
     t0, t1 = ev_create(lib, 2)
     D.barrier()
-    check(lib.xtg_event_record(t0, stream))
-    for _ in range(steps):
-        one()
-    check(lib.xtg_event_record(t1, stream))
+    check(lib.xtg_event_record(t0, s_in))
+    for k in range(steps):
+        one(k)
+    check(lib.xtg_event_record(t1, s_out))
     check(lib.xtg_event_sync(t1))
+    check(lib.xtg_device_sync())
     ms = D.max(ev_ms(lib, t0, t1) / steps)
-    for h, _, _ in hin + hout:
+    for h, _ in hin + hout:
         lib.xtg_host_free(h)
     return {"value": round(step_bytes() * D.ws / (ms / 1e3) / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "ms_per_step": round(ms, 3), "steps": steps}
+            "d2h_bytes_per_step": d2h, "ms_per_step": round(ms, 3), "steps": steps,
+            "mode": "3 streams (copy in / kernels / copy out), 2 device buffer sets"}
 
 
 def run_c3(args):

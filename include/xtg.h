@@ -216,6 +216,9 @@ xtg_status xtg_event_destroy(xtg_event ev);
 xtg_status xtg_event_record(xtg_event ev, xtg_stream stream);
 xtg_status xtg_event_sync(xtg_event ev);
 xtg_status xtg_event_elapsed_ms(xtg_event start, xtg_event end, float* ms);
+/* Work submitted to `stream` after this call waits until `ev` (as last
+ * recorded) has completed: orders copies and evaluations across streams. */
+xtg_status xtg_stream_wait_event(xtg_stream stream, xtg_event ev);
 
 /* ---- shape algebra ----------------------------------------------------------- */
 /* Broadcast shape of all leaves (right-aligned, size-1 / missing dims

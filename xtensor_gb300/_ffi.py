@@ -157,6 +157,7 @@ def _extend_signatures(L) -> None:
         "xtg_event_record": (st, [vp, vp]),
         "xtg_event_elapsed_ms": (st, [vp, vp, C.POINTER(C.c_float)]),
         "xtg_event_sync": (st, [vp]),
+        "xtg_stream_wait_event": (st, [vp, vp]),
         "xtg_last_kernels": (C.c_char_p, []),
         "xtg_sum_f32_noalloc": (st, [vp, i64, vp, vp]),
     }

@@ -366,6 +366,13 @@ xtg_status xtg_event_elapsed_ms(xtg_event start, xtg_event end, float* ms) {
     return XTG_OK;
 }
 
+xtg_status xtg_stream_wait_event(xtg_stream stream, xtg_event ev) {
+    if (!ev) return fail(XTG_ERR_INVALID, "null event");
+    if (dry_run()) return XTG_OK;
+    XTG_CUDA(cudaStreamWaitEvent((cudaStream_t)stream, (cudaEvent_t)ev, 0));
+    return XTG_OK;
+}
+
 xtg_status xtg_set_option(const char* key, int64_t value) {
     if (!key) return fail(XTG_ERR_INVALID, "null key");
     std::lock_guard<std::mutex> lk(g_opt_mu);
