@@ -26,6 +26,10 @@
  *                      include/xtensor/reducers/xnorm.hpp:397-526
  *   xtg_argreduce   <- xt::argmax / xt::argmin (arg_func_impl)
  *                      include/xtensor/misc/xsort.hpp:1158-1296
+ *   xtg_accumulate  <- xt::cumsum / cumprod / nancumsum / nancumprod
+ *                      (xt::accumulate, accumulator_impl)
+ *                      include/xtensor/reducers/xaccumulator.hpp:154-367
+ *                      include/xtensor/core/xmath.hpp:2248-2301, 2363-2391, 2592-2645
  *   xtg_batch_*     <- no counterpart (new batching layer over the same path)
  *   xtg_server_*    <- no counterpart (new request server over the same path)
  *
@@ -245,6 +249,32 @@ xtg_status xtg_reduce(const xtg_expr* e, const xtg_reduce_desc* rd,
 /* has_axis = 0: index into the flattened (row-major) expression. */
 xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis,
                          const xtg_array* out, xtg_stream stream);
+
+/* ---- accumulators ----------------------------------------------------------------------
+ * Cumulative sum / product of an expression along `axis` (has_axis = 1; the
+ * result has the expression's shape) or over its row-major flattening
+ * (has_axis = 0; the result is 1-D of the expression's size).  The element
+ * type is the accumulation type: acc_dtype (the reference's template
+ * argument T, -1 = none) or the expression's value type, combined with the
+ * value type as plus / multiplies would (short -> int, float -> float,
+ * xt::cumsum<double>(float) -> double).  Elements fold sequentially in that
+ * type; the nan variants start from NaN -> 0 / 1 and skip NaN operands.
+ * An axis outside [-rank, rank) is XTG_ERR_AXIS ("Axis larger than
+ * expression dimension in accumulator.").
+ * Order of evaluation: along a non-innermost axis, and along the innermost
+ * axis of expressions with many rows, each output element is folded in the
+ * reference's sequential order (float results bit-identical); a few long
+ * rows (and the flattened form) are scanned in fixed-size tiles whose
+ * float32 partial results carry a double-float (TwoSum / TwoProd) error
+ * term, so they stay within a few ulp of the exact prefix and are
+ * reproducible run to run. */
+typedef enum {
+    XTG_ACC_CUMSUM = 0, XTG_ACC_CUMPROD = 1, XTG_ACC_NANCUMSUM = 2, XTG_ACC_NANCUMPROD = 3
+} xtg_acc_op;
+xtg_status xtg_accumulate_shape(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis, int32_t acc_dtype,
+                                int32_t* rank, int64_t* shape, int32_t* dtype);
+xtg_status xtg_accumulate(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis, int32_t acc_dtype,
+                          const xtg_array* out, xtg_stream stream);
 
 /* ---- batching ------------------------------------------------------------------------
  * No counterpart in the reference (a new layer over the same path).  Many

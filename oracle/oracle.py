@@ -37,6 +37,8 @@ def lib():
         L.orc_reduce_result_dtype.argtypes = [P(Expr), P(ReduceDesc)]
         L.orc_last_error.restype = C.c_char_p
         L.orc_promote.argtypes = [C.c_int, C.c_int]
+        L.orc_accumulate_dtype.argtypes = [P(Expr), C.c_int, C.c_int]
+        L.orc_accumulate.argtypes = [P(Expr), C.c_int, C.c_int, C.c_int64, C.c_int, P(Array)]
         _L = L
     return _L
 
@@ -115,4 +117,27 @@ def argreduce(op, e, axis=None) -> np.ndarray:
     o = ho.xtg_array()
     code = 0 if op == "argmax" else 1
     _chk(lib().orc_argreduce(C.byref(ex), code, 0 if axis is None else 1, 0 if axis is None else axis, C.byref(o)))
+    return out
+
+
+ACC_OPS = {"cumsum": 0, "cumprod": 1, "nancumsum": 2, "nancumprod": 3}
+
+
+def accumulate(op, e, axis=None, acc_dtype=None) -> np.ndarray:
+    """xt::cumsum / cumprod / nancumsum / nancumprod of `e` over `axis` (None:
+    the row-major flattening, a 1-D result)."""
+    e = as_expr(e)
+    ex, keep = lower(e)
+    code = ACC_OPS[op]
+    acc = -1 if acc_dtype is None else dtype_code(acc_dtype)
+    dt = lib().orc_accumulate_dtype(C.byref(ex), code, acc)
+    if dt < 0:
+        _chk(-dt)
+    shape = broadcast_shape(e)
+    oshape = (int(np.prod(shape, dtype=np.int64)),) if axis is None else shape
+    out = np.zeros(oshape, dtype=np_dtype(dt))
+    ho = HostArray(out, dt)
+    o = ho.xtg_array()
+    _chk(lib().orc_accumulate(C.byref(ex), code, 0 if axis is None else 1, 0 if axis is None else int(axis), acc,
+                              C.byref(o)))
     return out

@@ -23,7 +23,11 @@
  *                    (core/xmath.hpp:1828-1858); variance = mean of squared
  *                    deviations from the evaluated mean (core/xmath.hpp:2082-2103);
  *   orc_argreduce  — arg_func_impl: strict compare, first index wins
- *                    (include/xtensor/misc/xsort.hpp:1158-1296).
+ *                    (include/xtensor/misc/xsort.hpp:1158-1296);
+ *   orc_accumulate — accumulator_impl: conversion to the accumulation type,
+ *                    then a sequential fold along the axis or over the
+ *                    row-major flattening
+ *                    (include/xtensor/reducers/xaccumulator.hpp:154-310).
  *
  * Arithmetic is carried out in the C type of each node (float ops in float,
  * integer ops wrapped to their width), with -ffp-contract=off so that no
@@ -937,6 +941,99 @@ int orc_argreduce(const xtg_expr* e, int op, int has_axis, int64_t axis, const x
         int64_t off = 0;
         for (int i = 0; i < nk; ++i) off += kidx[i] * out->strides[i];
         store(out, off, mk_u(XTG_INT64, (uint64_t)best));
+    }
+    return 0;
+}
+
+/* ---- accumulators (cumsum / cumprod / nancumsum / nancumprod) ------------------------
+ * xt::accumulate (include/xtensor/reducers/xaccumulator.hpp):
+ *  - the result type is decltype(F(init_value_type, value_type)) (:206-214,
+ *    :285-294): plus / multiplies of the template argument T (or the
+ *    expression's value type) with the value type;
+ *  - over an axis (:202-281): `result_type res = e` converts every element,
+ *    then res[.., i, ..] = F(res[.., i-1, ..], res[.., i, ..]) for i >= 1 in
+ *    that type (the nan variants first map res[.., 0, ..] through nan_init);
+ *    an axis outside the expression is std::runtime_error (:217-220), the
+ *    axis normalised by normalize_axis (include/xtensor/utils/xutils.hpp:353-357);
+ *  - flattened (:283-310): a 1-D result of e.size() elements, result[0] =
+ *    init(e_0), result[i] = F(result[i-1], e_i) in row-major order;
+ *  - nan_plus / nan_multiplies skip NaN operands, nan_init maps NaN to 0 / 1
+ *    (include/xtensor/core/xmath.hpp:2363-2391). */
+static int val_isnan(val v) { return is_float(v.t) && v.f != v.f; }
+
+int orc_accumulate_dtype(const xtg_expr* e, int op, int acc_dtype) {
+    static otree T;
+    int s = build(e, &T);
+    if (s) return -s;
+    (void)op;
+    int vt = T.type[T.root];
+    int it = acc_dtype >= 0 ? acc_dtype : vt;
+    return orc_promote(it, vt);
+}
+
+static val acc_init(int op, val x) {
+    if ((op == XTG_ACC_NANCUMSUM || op == XTG_ACC_NANCUMPROD) && val_isnan(x))
+        return cvt(mk_u(XTG_INT64, op == XTG_ACC_NANCUMSUM ? 0 : 1), x.t);
+    return x;
+}
+static val acc_step(int op, int rt, val acc, val x) {
+    if ((op == XTG_ACC_NANCUMSUM || op == XTG_ACC_NANCUMPROD) && val_isnan(x)) return acc;
+    return arith((op == XTG_ACC_CUMSUM || op == XTG_ACC_NANCUMSUM) ? XTG_OP_ADD : XTG_OP_MUL, rt, acc, x);
+}
+
+int orc_accumulate(const xtg_expr* e, int op, int has_axis, int64_t axis, int acc_dtype, const xtg_array* out) {
+    static otree T;
+    int s = build(e, &T);
+    if (s) return s;
+    int R = T.rank;
+    int vt = T.type[T.root];
+    int rt = orc_promote(acc_dtype >= 0 ? acc_dtype : vt, vt);
+    if (out->dtype != rt) return err(XTG_ERR_INVALID, "destination dtype is not the accumulation type");
+    int64_t total = 1;
+    for (int d = 0; d < R; ++d) total *= T.shape[d];
+    rowctx rc;
+    if (!has_axis) {
+        if (out->rank != 1 || out->shape[0] != total) return err(XTG_ERR_SHAPE, "flattened accumulation shape");
+        val acc = mk_u(rt, 0);
+        for (int64_t i = 0; i < total; ++i) {
+            int64_t idx[XTG_MAX_RANK];
+            unflat(i, R, T.shape, idx);
+            val x = cvt(eval(&T, T.root, idx, &rc), rt);
+            acc = i == 0 ? acc_init(op, x) : acc_step(op, rt, acc, x);
+            store(out, i * out->strides[0], acc);
+        }
+        return 0;
+    }
+    int64_t a = axis < 0 ? axis + R : axis;
+    if (a < 0 || a >= R) return err(XTG_ERR_AXIS, "Axis larger than expression dimension in accumulator.");
+    if (out->rank != R) return err(XTG_ERR_SHAPE, "accumulation shape");
+    for (int d = 0; d < R; ++d)
+        if (out->shape[d] != T.shape[d]) return err(XTG_ERR_SHAPE, "accumulation shape");
+    int ax = (int)a;
+    int64_t n = T.shape[ax];
+    int64_t n_out = n ? total / n : 0;
+    int kept[XTG_MAX_RANK], nk = 0;
+    int64_t kshape[XTG_MAX_RANK];
+    for (int d = 0; d < R; ++d)
+        if (d != ax) {
+            kshape[nk] = T.shape[d];
+            kept[nk++] = d;
+        }
+#pragma omp parallel for schedule(static)
+    for (int64_t o = 0; o < n_out; ++o) {
+        int64_t kidx[XTG_MAX_RANK], idx[XTG_MAX_RANK] = {0};
+        rowctx rc2;
+        unflat(o, nk, kshape, kidx);
+        for (int i = 0; i < nk; ++i) idx[kept[i]] = kidx[i];
+        val acc = mk_u(rt, 0);
+        for (int64_t j = 0; j < n; ++j) {
+            idx[ax] = j;
+            val x = cvt(eval(&T, T.root, idx, &rc2), rt);
+            acc = j == 0 ? acc_init(op, x) : acc_step(op, rt, acc, x);
+            int64_t off = 0;
+            for (int d = 0; d < R; ++d) off += idx[d] * out->strides[d];
+            store(out, off, acc);
+        }
     }
     return 0;
 }

@@ -207,3 +207,34 @@ def test_broadcast_rules_library_vs_oracle():
             assert ei.value.status == 2
         elif s1 or s2:
             assert xg.broadcast_shape(a + b) == want == O.broadcast_shape(a + b)
+
+
+# ---- test/test_xaccumulator.cpp, test/test_xnan_functions.cpp:152-172 -------------------------
+@pytest.mark.parametrize("name", [k[0] for k in __import__("acc_kats").KATS])
+def test_kat_accumulators(name):
+    from acc_kats import KATS
+    _, x, op, axis, expected, edt = next(k for k in KATS if k[0] == name)
+    got = O.accumulate(op, H(x), axis)
+    assert got.dtype == np.dtype(edt), (got.dtype, edt)
+    assert got.shape == expected.shape
+    np.testing.assert_array_equal(got, expected.astype(edt))
+
+
+def test_kat_nan_accumulators_and_errors():
+    from acc_kats import nan_equivalence_cases
+    a = nan_equivalence_cases()
+    for axis in (None, 0, 1, 2):
+        np.testing.assert_array_equal(O.accumulate("nancumsum", H(a), axis),
+                                      O.accumulate("cumsum", H(np.where(np.isnan(a), 0.0, a)), axis))
+        np.testing.assert_array_equal(O.accumulate("nancumprod", H(a), axis),
+                                      O.accumulate("cumprod", H(np.where(np.isnan(a), 1.0, a)), axis))
+    # xt::cumsum<double>(float) accumulates in double
+    f = np.array([[0.1, 0.2], [0.3, 0.4]], np.float32)
+    got = O.accumulate("cumsum", H(f), 1, acc_dtype="float64")
+    assert got.dtype == np.float64
+    np.testing.assert_array_equal(got, np.cumsum(f.astype(np.float64), 1))
+    # an axis outside the expression: std::runtime_error
+    for ax in (3, -4):
+        with pytest.raises(O.OracleError) as ei:
+            O.accumulate("cumsum", H(np.ones((2, 3, 4))), ax)
+        assert ei.value.status == 3

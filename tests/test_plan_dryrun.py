@@ -124,3 +124,21 @@ def test_batch_plans_and_compiles():
     ba = Batch(A0 * v0 + C0)
     ba.add(A0 * v0 + C0, fake((10, 20), "float32"))
     ba.build(autotune=False)
+
+
+@pytest.mark.parametrize("dt", ["float32", "float64", "int32"])
+def test_accumulator_plans(dt):
+    """cumsum / cumprod lower to the sequential column / row scans or the
+    tile scan, and every variant compiles."""
+    from xtensor_gb300 import ops
+    x = fake((64, 300, 33), dt)
+    for ax, fam_want in ((0, ["k_scan_col"]), (1, ["k_scan_col"]), (2, ["k_scan_rows"]),
+                         (None, ["k_scan_tile_agg", "k_scan_tile_offsets", "k_scan_tile_apply"])):
+        for op in ("cumsum", "cumprod"):
+            shape, odt = ops.accumulate_shape(op, x, ax)
+            ops.accumulate(op, x, ax, out=fake(shape, odt))
+            assert fam(last_kernels()) == fam_want, (ax, op, last_kernels())
+    # a flattened transposed view is evaluated into a temporary first
+    n = 64 * 300 * 33
+    ops.accumulate("cumsum", x.transpose((2, 0, 1)), None, out=fake((n,), ops.accumulate_shape("cumsum", x)[1]))
+    assert fam(last_kernels())[0] == "k_transpose"

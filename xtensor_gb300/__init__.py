@@ -39,5 +39,6 @@ from ._ffi import (  # noqa: F401
 from .expr import *  # noqa: F401,F403
 from .device import DeviceArray, Stream, device_sync, init  # noqa: F401
 from .ops import assign, reduce, argreduce, reduce_shape, broadcast_shape, expr_dtype  # noqa: F401
+from .ops import accumulate, cumsum, cumprod, nancumsum, nancumprod  # noqa: F401
 
 __all__ = [n for n in dir() if not n.startswith("_")]

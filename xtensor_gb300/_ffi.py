@@ -135,6 +135,9 @@ def lib() -> C.CDLL:
             "xtg_assign": (st, [C.POINTER(Expr), C.POINTER(Array), vp]),
             "xtg_reduce": (st, [C.POINTER(Expr), C.POINTER(ReduceDesc), C.POINTER(Array), vp]),
             "xtg_argreduce": (st, [C.POINTER(Expr), i32, i32, i64, C.POINTER(Array), vp]),
+            "xtg_accumulate_shape": (st, [C.POINTER(Expr), i32, i32, i64, i32, C.POINTER(i32), C.POINTER(i64),
+                                          C.POINTER(i32)]),
+            "xtg_accumulate": (st, [C.POINTER(Expr), i32, i32, i64, i32, C.POINTER(Array), vp]),
             "xtg_get_jit_stats": (st, [C.POINTER(JitStats)]),
             "xtg_set_option": (st, [C.c_char_p, i64]),
             "xtg_get_option": (st, [C.c_char_p, C.POINTER(i64)]),

@@ -487,6 +487,15 @@ template <class A> XTG_DI A shfl_xor_pod(const A& a, int m) {
     return out.a;
 }
 
+template <class A> XTG_DI A shfl_up_pod(const A& a, int d) {
+    union U { A a; u32 w[(sizeof(A) + 3) / 4]; };
+    U in, out;
+    in.a = a;
+#pragma unroll
+    for (int i = 0; i < (int)((sizeof(A) + 3) / 4); ++i) out.w[i] = __shfl_up_sync(0xffffffffu, in.w[i], d);
+    return out.a;
+}
+
 // Deterministic group reduction: warp butterfly, then warp 0 folds the
 // per-warp results in warp order.  Result valid in thread 0 of the group
 // (GROUP == 32: lane 0 of the warp; GROUP == block: thread 0).
@@ -1210,6 +1219,356 @@ __global__ void __launch_bounds__(256) k_reduce_combine(const RedParams p) {
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// K9: accumulators — cumsum / cumprod / nancumsum / nancumprod
+// (include/xtensor/reducers/xaccumulator.hpp:202-310,
+// include/xtensor/core/xmath.hpp:2248-2301, 2363-2391, 2592-2645).  Elements
+// are converted to the accumulation type RT, then folded: OP 0 plus,
+// 1 multiplies, 2 / 3 the same skipping NaN operands (the first element goes
+// through nan_init: NaN -> 0 / 1).
+template <class T> XTG_DI bool is_nan_v(T x) { return IsFloat<T>::value && !(x == x); }
+template <class RT, int OP> struct ScanOp {
+    static XTG_DI RT init(RT x) {
+        if (OP >= 2 && is_nan_v(x)) return RT(OP == 2 ? 0 : 1);
+        return x;
+    }
+    static XTG_DI RT step(RT a, RT x) {
+        if (OP >= 2 && is_nan_v(x)) return a;
+        return (OP & 1) ? RT(a * x) : RT(a + x);
+    }
+};
+
+// K9a: along a non-innermost axis.  A thread owns VEC adjacent inner
+// positions of one outer index and walks the axis in order (U positions'
+// loads in flight), so every output element is folded in the reference's
+// sequential order.
+template <class Tree, class LS, class RT, int OP, int VEC, int OKIND, int U>
+__global__ void __launch_bounds__(256) k_scan_col(const ScanParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    Ctx<0> c;
+    c.scal = p.scal;
+    const i64 nvi = p.n_inner / VEC;
+    const i64 nwork = p.n_outer * nvi;
+    for (i64 w = (i64)blockIdx.x * blockDim.x + threadIdx.x; w < nwork; w += (i64)gridDim.x * blockDim.x) {
+        const i64 o = w / nvi, iv = w - o * nvi;
+        i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
+#pragma unroll
+        for (int l = 0; l < LS::N; ++l) {
+            off[l] = o * p.lso[l] + iv * VEC * p.lsi[l];
+            inner[l] = p.lsi[l];
+        }
+        i64 oo = o * p.oso + iv * VEC * p.osi;
+        RT acc[VEC];
+        for (i64 k0 = 0; k0 < p.len; k0 += U) {
+            RG rg[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k0 + u < p.len) {
+                    i64 o2[XTG_KMAX_LEAVES];
+#pragma unroll
+                    for (int l = 0; l < LS::N; ++l) o2[l] = off[l] + (i64)u * p.lsa[l];
+                    LoadLeavesAt<LS>::template run<VEC>(rg[u], p.leaf, o2, inner);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k0 + u < p.len) {
+                    RT v[VEC];
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) {
+                        const RT x = cvt<RT>(Tree::ev(rg[u], j, c));
+                        acc[j] = (k0 + u == 0) ? ScanOp<RT, OP>::init(x) : ScanOp<RT, OP>::step(acc[j], x);
+                        v[j] = acc[j];
+                    }
+                    st_out<RT, OKIND, VEC>(reinterpret_cast<RT*>(p.out), oo + (i64)u * p.osa, p.osi, v);
+                }
+            }
+#pragma unroll
+            for (int l = 0; l < LS::N; ++l) off[l] += (i64)U * p.lsa[l];
+            oo += (i64)U * p.osa;
+        }
+    }
+}
+
+// K9b: along the innermost axis of many rows.  A warp owns 32 rows and walks
+// them in 32-column chunks: the chunk is loaded coalesced (lane = column),
+// transposed through shared memory, lane i folds row i's 32 elements in
+// order, and the chunk goes back the same way.  Sequential order per row.
+template <class Tree, class LS, class RT, int OP>
+__global__ void __launch_bounds__(128) k_scan_rows(const ScanParams p) {
+    typedef typename LS::template R<1>::type RG;
+    __shared__ RT tile[4][32][33];
+    Ctx<0> c;
+    c.scal = p.scal;
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    const i64 ngroups = (p.n_outer + 31) / 32;
+    for (i64 g = (i64)blockIdx.x * 4 + warp; g < ngroups; g += (i64)gridDim.x * 4) {
+        const i64 r0 = g * 32;
+        RT acc = RT(0);
+        for (i64 c0 = 0; c0 < p.len; c0 += 32) {
+            const i64 col = c0 + lane;
+#pragma unroll 8
+            for (int i = 0; i < 32; ++i) {
+                const i64 r = r0 + i;
+                if (r < p.n_outer && col < p.len) {
+                    i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
+#pragma unroll
+                    for (int l = 0; l < LS::N; ++l) {
+                        off[l] = r * p.lso[l] + col * p.lsa[l];
+                        inner[l] = 0;
+                    }
+                    RG rg;
+                    LoadLeavesAt<LS>::template run<1>(rg, p.leaf, off, inner);
+                    tile[warp][i][lane] = cvt<RT>(Tree::ev(rg, 0, c));
+                }
+            }
+            __syncwarp();
+            const int lim = (p.len - c0) < 32 ? (int)(p.len - c0) : 32;
+            if (r0 + lane < p.n_outer) {
+                for (int k = 0; k < lim; ++k) {
+                    const RT x = tile[warp][lane][k];
+                    acc = (c0 + k == 0) ? ScanOp<RT, OP>::init(x) : ScanOp<RT, OP>::step(acc, x);
+                    tile[warp][lane][k] = acc;
+                }
+            }
+            __syncwarp();
+#pragma unroll 8
+            for (int i = 0; i < 32; ++i) {
+                const i64 r = r0 + i;
+                if (r < p.n_outer && col < p.len) reinterpret_cast<RT*>(p.out)[r * p.oso + col * p.osa] = tile[warp][i][lane];
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// K9c: a few long rows (and the flattened form) — three launches, no
+// inter-CTA waiting: (A) every 4096-element tile's total, (B) per row, the
+// exclusive prefix of the tile totals in a fixed order, (C) every tile again,
+// scanned in a fixed structure from its prefix.  ScanState carries float32
+// values in double-float (TwoSum for sums, fma-exact TwoProd for products) so
+// the tile results are within a few ulp of the exact prefix; other types fold
+// in their own arithmetic.  The additive identity is -0 (x + -0 == x for
+// every x), so signed zeros come out as in the sequential fold.
+template <class RT, int OP> struct ScanState {
+    RT hi;
+    RT lo;
+    static XTG_DI ScanState ident() {
+        ScanState s;
+        s.hi = (OP & 1) ? RT(1) : (IsFloat<RT>::value ? RT(-0.0) : RT(0));
+        s.lo = RT(0);
+        return s;
+    }
+    XTG_DI void add(RT x) {
+        if (OP >= 2 && is_nan_v(x)) return;
+        if (OP & 1) hi = RT(hi * x);
+        else hi = RT(hi + x);
+    }
+    // partial results combine unconditionally (a NaN partial from inf - inf
+    // stays NaN, as the sequential fold's accumulator does)
+    XTG_DI void merge(const ScanState& o) {
+        if (OP & 1) hi = RT(hi * o.hi);
+        else hi = RT(hi + o.hi);
+    }
+    XTG_DI RT value() const { return hi; }
+};
+template <int OP> struct ScanState<float, OP> {
+    float hi, lo;
+    static XTG_DI ScanState ident() {
+        ScanState s;
+        s.hi = (OP & 1) ? 1.f : -0.f;
+        s.lo = 0.f;
+        return s;
+    }
+    XTG_DI void add(float x) {
+        if (OP >= 2 && !(x == x)) return;
+        if (OP & 1) {
+            const float ph = hi * x;
+            const float e = fmaf(hi, x, -ph);
+            lo = fmaf(lo, x, e);
+            hi = ph;
+        } else {
+            float s, e;
+            two_sum(hi, x, s, e);
+            hi = s;
+            lo += e;
+        }
+    }
+    XTG_DI void merge(const ScanState& o) {
+        if (OP & 1) {
+            const float ph = hi * o.hi;
+            const float e = fmaf(hi, o.hi, -ph);
+            lo = fmaf(hi, o.lo, fmaf(lo, o.hi, e));
+            hi = ph;
+        } else {
+            float s, e;
+            two_sum(hi, o.hi, s, e);
+            hi = s;
+            lo = (lo + o.lo) + e;
+        }
+    }
+    XTG_DI float value() const { return lo == 0.f ? hi : hi + lo; }
+};
+
+constexpr int XTG_SCAN_TILE = 4096;  // 256 threads x 16 elements
+constexpr int XTG_SCAN_IPT = 16;
+
+template <class Tree, class LS, class RT>
+XTG_DI RT scan_elem(const ScanParams& p, const Ctx<0>& c, i64 row, i64 k) {
+    typedef typename LS::template R<1>::type RG;
+    i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
+#pragma unroll
+    for (int l = 0; l < LS::N; ++l) {
+        off[l] = row * p.lso[l] + k * p.lsa[l];
+        inner[l] = 0;
+    }
+    RG rg;
+    LoadLeavesAt<LS>::template run<1>(rg, p.leaf, off, inner);
+    return cvt<RT>(Tree::ev(rg, 0, c));
+}
+
+template <class ST> XTG_DI ST block_reduce_state(ST s, ST* sm) {
+    // fixed order: xor butterfly in each warp, then warp totals in warp order
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+        ST o = shfl_xor_pod(s, m);
+        if ((threadIdx.x & m) == 0) s.merge(o);
+        else {
+            o.merge(s);
+            s = o;
+        }
+    }
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sm[warp] = s;
+    __syncthreads();
+    ST r = sm[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r.merge(sm[w]);
+    __syncthreads();
+    return r;
+}
+
+template <class Tree, class LS, class RT, int OP>
+__global__ void __launch_bounds__(256) k_scan_tile_agg(const ScanParams p) {
+    typedef ScanState<RT, OP> ST;
+    __shared__ ST sm[8];
+    Ctx<0> c;
+    c.scal = p.scal;
+    const i64 nitems = p.n_outer * p.ntiles;
+    for (i64 it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const i64 row = it / p.ntiles, t = it - row * p.ntiles;
+        const i64 k0 = t * XTG_SCAN_TILE;
+        // coalesced: thread th folds elements th, th + 256, ... (any fixed
+        // order will do for a tile total)
+        ST s = ST::ident();
+#pragma unroll 4
+        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+            const i64 k = k0 + (i64)i * 256 + threadIdx.x;
+            if (k < p.len) s.add(scan_elem<Tree, LS, RT>(p, c, row, k));
+        }
+        s = block_reduce_state<ST>(s, sm);
+        if (threadIdx.x == 0) reinterpret_cast<ST*>(p.agg)[it] = s;
+    }
+}
+
+// (B) one CTA per row: exclusive prefix of the tile totals, in place.
+template <class RT, int OP>
+__global__ void __launch_bounds__(256) k_scan_tile_offsets(const ScanParams p) {
+    typedef ScanState<RT, OP> ST;
+    __shared__ ST sm[256];
+    for (i64 row = blockIdx.x; row < p.n_outer; row += gridDim.x) {
+        ST* a = reinterpret_cast<ST*>(p.agg) + row * p.ntiles;
+        const i64 per = (p.ntiles + 255) / 256;
+        const i64 b = (i64)threadIdx.x * per;
+        i64 e = b + per;
+        if (e > p.ntiles) e = p.ntiles;
+        ST tot = ST::ident();
+        for (i64 i = b; i < e; ++i) tot.merge(a[i]);
+        sm[threadIdx.x] = tot;
+        __syncthreads();
+        ST pre = ST::ident();  // exclusive prefix of the thread chunks, in order
+        for (int w = 0; w < (int)threadIdx.x; ++w) pre.merge(sm[w]);
+        for (i64 i = b; i < e; ++i) {
+            const ST v = a[i];
+            a[i] = pre;
+            pre.merge(v);
+        }
+        __syncthreads();
+    }
+}
+
+// (C) every tile again: coalesced load into shared memory, thread th folds
+// its 16 elements from its prefix (tile prefix, then the totals of the
+// threads before it in order), results stored coalesced.
+template <class Tree, class LS, class RT, int OP>
+__global__ void __launch_bounds__(256) k_scan_tile_apply(const ScanParams p) {
+    typedef ScanState<RT, OP> ST;
+    __shared__ RT buf[XTG_SCAN_TILE + XTG_SCAN_TILE / 32];
+    __shared__ ST tot[8];
+    Ctx<0> c;
+    c.scal = p.scal;
+    const i64 nitems = p.n_outer * p.ntiles;
+    for (i64 it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const i64 row = it / p.ntiles, t = it - row * p.ntiles;
+        const i64 k0 = t * XTG_SCAN_TILE;
+#pragma unroll 4
+        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+            const int q = i * 256 + (int)threadIdx.x;
+            const i64 k = k0 + q;
+            if (k < p.len) buf[q + (q >> 5)] = scan_elem<Tree, LS, RT>(p, c, row, k);
+        }
+        __syncthreads();
+        ST s = ST::ident();
+        const int q0 = (int)threadIdx.x * XTG_SCAN_IPT;
+#pragma unroll
+        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+            const int q = q0 + i;
+            if (k0 + q < p.len) s.add(buf[q + (q >> 5)]);
+        }
+        // block exclusive scan of the thread totals in a fixed structure:
+        // Kogge-Stone inside each warp, then the warp totals in warp order
+        const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+        ST inc = s;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            ST y = shfl_up_pod(inc, d);
+            if (lane >= d) {
+                y.merge(inc);
+                inc = y;
+            }
+        }
+        ST lex = shfl_up_pod(inc, 1);
+        if (lane == 31) tot[warp] = inc;
+        __syncthreads();
+        ST pre = reinterpret_cast<const ST*>(p.agg)[it];
+        for (int w = 0; w < warp; ++w) pre.merge(tot[w]);
+        if (lane > 0) pre.merge(lex);
+#pragma unroll
+        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+            const int q = q0 + i;
+            const i64 k = k0 + q;
+            if (k < p.len) {
+                const RT x = buf[q + (q >> 5)];
+                if (k == 0) {
+                    pre.hi = ScanOp<RT, OP>::init(x);
+                    pre.lo = RT(0);
+                } else {
+                    pre.add(x);
+                }
+                buf[q + (q >> 5)] = pre.value();
+            }
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+            const int q = i * 256 + (int)threadIdx.x;
+            const i64 k = k0 + q;
+            if (k < p.len) reinterpret_cast<RT*>(p.out)[row * p.oso + k * p.osa] = buf[q + (q >> 5)];
+        }
+        __syncthreads();
+    }
+}
 
 // ---------------------------------------------------------------------------
 // K2: tiled transposing assignment (transpose / permuted strided_view into a

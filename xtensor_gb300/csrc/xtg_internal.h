@@ -116,6 +116,7 @@ struct Recorder {
     std::vector<RecLaunch> launches;
     size_t scratch_bytes = 0;
     int scratch_allocs = 0;
+    bool nocache = false;  // a launch holds a temporary the replay could not patch
 };
 Recorder*& recorder();  // the calling thread's active recorder (nullptr: none)
 int64_t opt_generation();  // increments whenever an option changes

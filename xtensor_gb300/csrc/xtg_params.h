@@ -105,6 +105,19 @@ struct RowParams {
     int* err;                         // set to 1 when a bounded wait gives up
 };
 
+// Accumulators (cumsum / cumprod): the expression's iteration space as
+// (outer, axis, inner), each part collapsed to one dimension.
+struct ScanParams {
+    i64 n_outer, len, n_inner;
+    const void* leaf[XTG_KMAX_LEAVES];
+    i64 lso[XTG_KMAX_LEAVES], lsa[XTG_KMAX_LEAVES], lsi[XTG_KMAX_LEAVES];  // leaf strides
+    void* out;
+    i64 oso, osa, osi;  // destination strides
+    Scalars scal;
+    i64 ntiles;         // tile scan: tiles per row
+    void* agg;          // tile scan: n_outer * ntiles partial states (16 B each)
+};
+
 // Batched evaluation: many instances of one expression shape, each a 2-D
 // (rows, cols) space with its own pointers and strides.
 struct BatchInst {

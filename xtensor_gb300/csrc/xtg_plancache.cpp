@@ -131,7 +131,7 @@ bool plan_replay(const std::vector<unsigned char>& key, cudaStream_t s, xtg_stat
 }
 
 void plan_store(std::vector<unsigned char>&& key, Recorder& rec) {
-    if (rec.scratch_allocs > 1) return;  // not expected; keep such calls uncached
+    if (rec.scratch_allocs > 1 || rec.nocache) return;  // keep such calls uncached
     auto p = std::make_shared<Plan>();
     p->key = std::move(key);
     p->launches = std::move(rec.launches);

@@ -1,6 +1,7 @@
 """Evaluation entry points: assign (xt::noalias(out) = e), reductions
 (xt::sum / mean / variance / amax / norm_l2 ... with axes, keep_dims,
-initial, evaluation type T) and arg-reductions (xt::argmax / argmin)."""
+initial, evaluation type T), arg-reductions (xt::argmax / argmin) and
+accumulators (xt::cumsum / cumprod / nancumsum / nancumprod)."""
 from __future__ import annotations
 
 import ctypes as C
@@ -133,3 +134,47 @@ def argmax(e, axis=None, **kw):
 
 def argmin(e, axis=None, **kw):
     return argreduce("argmin", e, axis, **kw)
+
+
+ACC = {"cumsum": 0, "cumprod": 1, "nancumsum": 2, "nancumprod": 3}
+
+
+def accumulate_shape(op: str, e, axis=None, acc_dtype=None):
+    ex, keep = lower(as_expr(e))
+    r = C.c_int32()
+    sh = (C.c_int64 * MAX_RANK)()
+    dt = C.c_int32()
+    check(lib().xtg_accumulate_shape(C.byref(ex), ACC[op], 0 if axis is None else 1, 0 if axis is None else int(axis),
+                                     -1 if acc_dtype is None else dtype_code(acc_dtype), C.byref(r), sh, C.byref(dt)))
+    return tuple(sh[i] for i in range(r.value)), dt.value
+
+
+def accumulate(op: str, e, axis=None, acc_dtype=None, out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
+    """xt::cumsum / cumprod / nancumsum / nancumprod of `e` along `axis` (None:
+    over the row-major flattening, a 1-D result); `acc_dtype` is the
+    reference's template argument T."""
+    e = as_expr(e)
+    shape, dt = accumulate_shape(op, e, axis, acc_dtype)
+    if out is None:
+        out = DeviceArray.empty(shape, dt, stream)
+    ex, keep = lower(e)
+    o = out.xtg_array()
+    check(lib().xtg_accumulate(C.byref(ex), ACC[op], 0 if axis is None else 1, 0 if axis is None else int(axis),
+                               -1 if acc_dtype is None else dtype_code(acc_dtype), C.byref(o), _sh(stream)))
+    return out
+
+
+def cumsum(e, axis=None, **kw):
+    return accumulate("cumsum", e, axis, **kw)
+
+
+def cumprod(e, axis=None, **kw):
+    return accumulate("cumprod", e, axis, **kw)
+
+
+def nancumsum(e, axis=None, **kw):
+    return accumulate("nancumsum", e, axis, **kw)
+
+
+def nancumprod(e, axis=None, **kw):
+    return accumulate("nancumprod", e, axis, **kw)
