@@ -570,6 +570,104 @@ def run_c3(args):
     return 0
 
 
+def run_scan(args):
+    """Accumulator workload (the scan row next to the hot path): x float32 and
+    float64 (256, 512, 1024) N(0,1) seed 1 and int32 U[-1000, 1000]:
+    cumsum along axis 2 (row scan: 131072 rows of 1024), along axis 1 (column
+    scan) and over the flattening (tile scan: one row of 2^27), through the C
+    ABI with inputs resident in HBM.  Algorithmic bytes: one read of the input
+    and one write of the result per call.  CPU baseline: the compiled port of
+    the reference's accumulate loop (oracle/xt_baseline.c bl_cumsum_*, OpenMP
+    over independent outer rows) on the same arrays."""
+    import xtensor_gb300 as xg
+    from xtensor_gb300._ffi import check
+    from xtensor_gb300.device import DeviceArray
+    from xtensor_gb300.expr import lower
+    lib = xg.lib()
+    st = C.c_void_p()
+    check(lib.xtg_stream_create(C.byref(st)))
+    stream = st.value
+    g = np.random.default_rng(1)
+    xs = {"f32": g.standard_normal(SHAPE, dtype=np.float32), "f64": g.standard_normal(SHAPE, dtype=np.float64),
+          "i32": g.integers(-1000, 1001, SHAPE, dtype=np.int32)}
+    calls, keep = [], []
+    for nm, x in xs.items():
+        dx = DeviceArray.from_numpy(x)
+        e, k = lower(dx)
+        keep += [dx, e, k]
+        for ax, tag in ((2, "rows"), (1, "cols"), (None, "flat")):
+            if nm == "i32" and tag != "cols":
+                continue
+            oshape = SHAPE if ax is not None else (N,)
+            out = DeviceArray.empty(oshape, x.dtype)
+            o = out.xtg_array()
+            keep += [out, o]
+            calls.append((f"cumsum_{tag}_{nm}", 2 * x.nbytes,
+                          lambda e=e, o=o, ax=ax: lib.xtg_accumulate(C.byref(e), 0, 0 if ax is None else 1,
+                                                                      0 if ax is None else ax, -1, C.byref(o), stream)))
+    for _ in range(args.warmup):
+        for _, _, fn in calls:
+            check(fn())
+    check(lib.xtg_stream_sync(stream))
+    evs = [ev_create(lib, len(calls) + 1) for _ in range(args.steps)]
+    clocks = Clocks(0)
+    clocks.start()
+    time.sleep(0.15)
+    l0 = xg.jit_stats()["launches"]
+    for k in range(args.steps):
+        for i, (_, _, fn) in enumerate(calls):
+            check(lib.xtg_event_record(evs[k][i], stream))
+            check(fn())
+        check(lib.xtg_event_record(evs[k][len(calls)], stream))
+    check(lib.xtg_stream_sync(stream))
+    l1 = xg.jit_stats()["launches"]
+    clk = clocks.stop()
+    per = [sum(ev_ms(lib, evs[k][i], evs[k][i + 1]) for k in range(args.steps)) / args.steps for i in range(len(calls))]
+    step_ms = sum(per)
+    total = sum(b for _, b, _ in calls)
+    peak, peak_kind = peaks()
+    per_kernel = {nm: {"ms": round(t, 4), "GB/s": round(b / (t / 1e3) / 1e9, 1), "frac": round(b / (t / 1e3) / 1e9 / peak, 3)}
+                  for (nm, b, _), t in zip(calls, per)}
+    dom = int(np.argmax(per))
+    cpu = None
+    if not args.no_cpu:
+        from oracle.oracle import SO, lib as olib  # noqa: F401
+        olib()
+        L = C.CDLL(str(SO))
+        fns = {"f32": L.bl_cumsum_f32, "f64": L.bl_cumsum_f64, "i32": L.bl_cumsum_i32}
+        t_cpu, b_cpu = 0.0, 0
+        for nm, b, _ in calls:
+            tag, dt = nm.split("_")[1], nm.split("_")[2]
+            x = xs[dt]
+            r = np.empty_like(x)
+            ax = {"rows": 2, "cols": 1, "flat": -1}[tag]
+            args_c = (x.ctypes.data_as(C.c_void_p), r.ctypes.data_as(C.c_void_p), C.c_int64(SHAPE[0]),
+                      C.c_int64(SHAPE[1]), C.c_int64(SHAPE[2]), C.c_int(ax))
+            fns[dt](*args_c)
+            t0 = time.perf_counter()
+            fns[dt](*args_c)
+            t_cpu += time.perf_counter() - t0
+            b_cpu += b
+        cpu = {"value": round(b_cpu / t_cpu / 1e9, 3), "unit": "GB/s", "cores": cores(), "kind": "port",
+               "sample": "full workload, one timed run after one warm-up (compiled port of the reference's "
+                         f"accumulate loop, OpenMP {cores()} threads over outer rows; the flattened scan is sequential)"}
+    line = {
+        "metric": "HBM GB/s (frac of roofline) of xt::cumsum through the C ABI", "unit": "GB/s",
+        "value": round(total / (step_ms / 1e3) / 1e9, 3), "higher_is_better": True, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32,f64,i32", "data": "synthetic",
+        "config": {"workload": "accumulators: cumsum of x (256,512,1024) f32/f64 along axis 2, axis 1 and flattened; "
+                               "int32 along axis 1", "algorithmic_bytes_per_step": total,
+                   "l2": "inputs larger than L2: no flush"},
+        "roofline": {"bound": "hbm", "kernel": calls[dom][0], "achieved": per_kernel[calls[dom][0]]["GB/s"],
+                     "peak": peak, "unit": "GB/s", "frac": per_kernel[calls[dom][0]]["frac"], "traffic": None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "per_kernel": per_kernel, "cpu_baseline": cpu, "e2e": None, "gpu_launches": int(l1 - l0), "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def c4_pool(n_templates, seed=4):
     """Request templates of the serving mix: kinds of the four configurations,
     element counts log-uniform in [1e3, 1e8], dtypes float32/float64/int32 at
@@ -755,9 +853,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--shape", default=None, help="profiling only: d0,d1,d2 instead of 256,512,1024")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4", "scan"],
                     help="c1: strided/axis work (default, the headline); c3: batching of uneven instances; "
-                         "c4: served Poisson request mix")
+                         "c4: served Poisson request mix; scan: cumsum along rows, columns and flattened")
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--templates", type=int, default=256)
@@ -778,6 +876,8 @@ def main():
         return run_reference(args)
     from xtensor_gb300.build import build
     build()
+    if args.workload == "scan":
+        return run_scan(args)
     return run_gpu(args)
 
 

@@ -4,7 +4,8 @@
 // xt::xtensor<T, N>, arithmetic / math operators building lazy expression
 // trees (xfunction), xt::sum / prod / amax / amin / mean / variance /
 // stddev / norm_* with axes, keep_dims, initial and evaluation_strategy,
-// xt::argmax / argmin, xt::transpose / strided views / xt::view slices,
+// xt::argmax / argmin, xt::cumsum / cumprod / nancumsum / nancumprod,
+// xt::transpose / strided views / xt::view slices,
 // xt::noalias, xt::eval.  Containers live in device memory; assigning an
 // expression lowers its template tree to the C ABI (include/xtg.h) and one
 // fused sm_103a kernel evaluates it.  Reading an element copies it back
@@ -1057,6 +1058,44 @@ template <class E> inline xarray<std::size_t> argmax(const xexpression<E>& e, st
 template <class E> inline xarray<std::size_t> argmin(const xexpression<E>& e, std::ptrdiff_t axis) {
     return detail::arg_axis(e.derived_cast(), axis, XTG_ARGMIN);
 }
+
+// ---------------------------------------------------------------------------- accumulators
+// xt::cumsum / cumprod / nancumsum / nancumprod (include/xtensor/core/xmath.hpp:
+// 2248-2301, 2592-2645): eager, like the reference's immediate accumulators;
+// the element type is decltype(T-or-value_type{} op value_type{}).
+namespace detail {
+template <class R, class E> xarray<R> accumulate_into(const E& e, int op, int has_axis, std::ptrdiff_t axis) {
+    lowering L;
+    e.lower(L);
+    int32_t r = 0, dt = 0;
+    int64_t sh[XTG_MAX_RANK];
+    check(xtg_accumulate_shape(&L.e, op, has_axis, axis, dtype_of<R>::value, &r, sh, &dt));
+    xarray<R> out(std::vector<std::size_t>(sh, sh + r));
+    xtg_array o = out.xtg_desc();
+    check(xtg_accumulate(&L.e, op, has_axis, axis, dtype_of<R>::value, &o, current_stream()));
+    return out;
+}
+template <class T, class E, int PROD> struct acc_result {
+    using V = typename std::decay_t<E>::value_type;
+    using I = std::conditional_t<std::is_void<T>::value, V, T>;
+    using type = std::conditional_t<PROD != 0, decltype(std::declval<I>() * std::declval<V>()),
+                                    decltype(std::declval<I>() + std::declval<V>())>;
+};
+}  // namespace detail
+#define XTG_ACCUMULATOR(NAME, CODE, PROD)                                                                     \
+    template <class T = void, class E>                                                                         \
+    inline auto NAME(const xexpression<E>& e, std::ptrdiff_t axis) {                                           \
+        return detail::accumulate_into<typename detail::acc_result<T, E, PROD>::type>(e.derived_cast(), CODE, 1, axis); \
+    }                                                                                                          \
+    template <class T = void, class E>                                                                         \
+    inline auto NAME(const xexpression<E>& e) {                                                                \
+        return detail::accumulate_into<typename detail::acc_result<T, E, PROD>::type>(e.derived_cast(), CODE, 0, 0); \
+    }
+XTG_ACCUMULATOR(cumsum, XTG_ACC_CUMSUM, 0)
+XTG_ACCUMULATOR(cumprod, XTG_ACC_CUMPROD, 1)
+XTG_ACCUMULATOR(nancumsum, XTG_ACC_NANCUMSUM, 0)
+XTG_ACCUMULATOR(nancumprod, XTG_ACC_NANCUMPROD, 1)
+#undef XTG_ACCUMULATOR
 
 // ---------------------------------------------------------------------------- builders
 template <class T, class S> inline xarray<T> ones(const S& s) { return xarray<T>(std::vector<std::size_t>(std::begin(s), std::end(s)), T(1)); }

@@ -27,6 +27,11 @@
  *                       (xsort.hpp:1158-1235).
  *   bl_c0_*             E = A * b + exp(-A * A); r = sum(E, {1}).
  *   bl_sum_*            full sums (sequential, as the lazy reducer).
+ *   bl_cumsum_*         xt::cumsum(x, axis) on a contiguous (d0, d1, d2) array:
+ *                       `res = x`, then res[.., i, ..] += res[.., i-1, ..]
+ *                       walking the storage with the axis stride
+ *                       (xaccumulator.hpp:233-281); axis = -1 flattens
+ *                       (:283-310).  The copy is fused into the first pass.
  */
 #include <math.h>
 #include <stdint.h>
@@ -136,3 +141,28 @@ int64_t bl_sum_i32_i64(const int32_t* x, int64_t n) {
     for (int64_t i = 0; i < n; ++i) s += x[i];
     return s;
 }
+
+
+#define DEF_CUMSUM(T, NAME)                                                                           \
+    void bl_cumsum_##NAME(const T* x, T* r, int64_t d0, int64_t d1, int64_t d2, int axis) {           \
+        if (axis < 0) {                                                                               \
+            const int64_t n = d0 * d1 * d2;                                                           \
+            T acc = 0;                                                                                \
+            for (int64_t i = 0; i < n; ++i) r[i] = acc = (i ? acc + x[i] : x[i]);                      \
+            return;                                                                                   \
+        }                                                                                             \
+        const int64_t outer = axis == 0 ? 1 : (axis == 1 ? d0 : d0 * d1);                             \
+        const int64_t len = axis == 0 ? d0 : (axis == 1 ? d1 : d2);                                   \
+        const int64_t inner = axis == 0 ? d1 * d2 : (axis == 1 ? d2 : 1);                             \
+        _Pragma("omp parallel for schedule(static)")                                                  \
+        for (int64_t o = 0; o < outer; ++o) {                                                         \
+            const T* xo = x + o * len * inner;                                                        \
+            T* ro = r + o * len * inner;                                                              \
+            for (int64_t j = 0; j < inner; ++j) ro[j] = xo[j];                                        \
+            for (int64_t i = 1; i < len; ++i)                                                         \
+                for (int64_t j = 0; j < inner; ++j) ro[i * inner + j] = ro[(i - 1) * inner + j] + xo[i * inner + j]; \
+        }                                                                                             \
+    }
+DEF_CUMSUM(float, f32)
+DEF_CUMSUM(double, f64)
+DEF_CUMSUM(int32_t, i32)

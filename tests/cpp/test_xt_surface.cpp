@@ -284,6 +284,52 @@ TEST(configs, c1_normalize_transpose_amax_argmax) {
     EXPECT_EQ(ai.shape(), (std::vector<std::size_t>{8, 1024}));
 }
 
+// test_xaccumulator.cpp:22-44, 147-178, 196-210 (cumsum / cumprod)
+TEST(xaccumulator, one_d_dim_one_cumprod_empty) {
+    xarray<int16_t> a = {int16_t(1), int16_t(2), int16_t(3), int16_t(4)};
+    auto no_axis = cumsum(a);
+    auto with_axis = cumsum(a, 0);
+    bool promotion_works = std::is_same<typename decltype(no_axis)::value_type, int>::value;
+    EXPECT_TRUE(promotion_works);
+    xarray<int> expected = {1, 3, 6, 10};
+    EXPECT_EQ(no_axis, expected);
+    EXPECT_EQ(with_axis, expected);
+
+    xarray<double> arr = {{5., 6., 7.}};
+    xarray<double> res = cumsum(arr, 0);
+    EXPECT_EQ(res, arr);
+
+    xtensor<double, 2> t = {{1, 2, 3}, {4, 5, 6}};
+    xarray<double> tres = cumsum(t, 0);
+    xarray<double> texp = {{1, 2, 3}, {5, 7, 9}};
+    EXPECT_EQ(tres, texp);
+
+    xarray<long> l = {{0, 1, 2}, {3, 4, 5}, {6, 7, 8}, {9, 10, 11}};
+    xarray<long> e0 = {{0, 1, 2}, {0, 4, 10}, {0, 28, 80}, {0, 280, 880}};
+    xarray<long> e1 = {{0, 0, 0}, {3, 12, 60}, {6, 42, 336}, {9, 90, 990}};
+    EXPECT_EQ(cumprod(l, 0), e0);
+    EXPECT_EQ(cumprod(l, 1), e1);
+    auto flat = cumprod(l);
+    EXPECT_EQ(flat.shape(), (std::vector<std::size_t>{12}));
+
+    xarray<double> z = ones<double>({3, 4, 0});
+    EXPECT_EQ(cumsum(z).shape(), (std::vector<std::size_t>{0}));
+    EXPECT_EQ(cumsum(z, 2).shape(), (std::vector<std::size_t>{3, 4, 0}));
+
+    xarray<float> f = {{0.5f, 0.25f}, {1.f, 2.f}};
+    auto fd = cumsum<double>(f, 1);
+    bool is_double = std::is_same<typename decltype(fd)::value_type, double>::value;
+    EXPECT_TRUE(is_double);
+    bool threw = false;
+    try {
+        auto bad = cumsum(f, 2);
+        (void)bad;
+    } catch (const std::runtime_error&) {
+        threw = true;
+    }
+    EXPECT_TRUE(threw);
+}
+
 int main() {
     for (auto& t : registry()) {
         const int before = g_fail;
