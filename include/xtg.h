@@ -264,10 +264,10 @@ xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_
  * Order of evaluation: along a non-innermost axis, and along the innermost
  * axis of expressions with many rows, each output element is folded in the
  * reference's sequential order (float results bit-identical); a few long
- * rows (and the flattened form) are scanned in fixed-size tiles whose
- * float32 partial results carry a double-float (TwoSum / TwoProd) error
- * term, so they stay within a few ulp of the exact prefix and are
- * reproducible run to run. */
+ * rows (and the flattened form) are cut into segments scanned from their
+ * prefixes in a fixed order (reproducible run to run); float32 partial
+ * results carry a double-float (TwoSum / TwoProd) error term, so they stay
+ * within a few ulp of the exact prefix. */
 typedef enum {
     XTG_ACC_CUMSUM = 0, XTG_ACC_CUMPROD = 1, XTG_ACC_NANCUMSUM = 2, XTG_ACC_NANCUMPROD = 3
 } xtg_acc_op;

@@ -88,7 +88,7 @@ def test_tile_scan_float32(shape, strategy):
     x = g.standard_normal(shape).astype(np.float32)
     strategy(2)
     got = ops.accumulate("cumsum", dev(x), -1).to_numpy()
-    assert last_kernels()[-1].startswith("k_scan_tile_apply")
+    assert last_kernels()[-1].startswith("k_scan_seg_apply")
     _tile_tol_check(got, x, "cumsum", "cumsum")
     # the reference's sequential float32 fold carries its own error; the tile
     # scan must sit inside that envelope
@@ -207,3 +207,20 @@ def test_large_tile_scan_reproducible_and_accurate():
     exact = np.cumsum(x.astype(np.float64))
     tol = 2.0**-23 * np.abs(exact) + 2.0**-36 * np.cumsum(np.abs(x.astype(np.float64)))
     assert (np.abs(a - exact) <= tol).all()
+
+
+def test_tile_scan_strided_and_broadcast_operands(strategy):
+    """The segmented scan over a strided view (every other column: the
+    shared-memory path) and over a broadcast expression (the vector path)."""
+    g = rng(36)
+    strategy(2)
+    x = g.integers(-50, 50, (3, 20001)).astype(np.int64)
+    d = dev(x)
+    v = d[:, ::2]
+    np.testing.assert_array_equal(ops.accumulate("cumsum", v, 1).to_numpy(), np.cumsum(x[:, ::2], 1))
+    b = g.integers(-5, 5, (20001,)).astype(np.int64)
+    e = d * dev(b) + 3
+    np.testing.assert_array_equal(ops.accumulate("cumsum", e, 1).to_numpy(), np.cumsum(x * b + 3, 1))
+    f = g.standard_normal((2, 50000)).astype(np.float32)
+    got = ops.accumulate("cumsum", dev(f)[:, ::3], 1).to_numpy()
+    _tile_tol_check(got, np.ascontiguousarray(f[:, ::3]), "cumsum", "strided float32")

@@ -133,7 +133,7 @@ def test_accumulator_plans(dt):
     from xtensor_gb300 import ops
     x = fake((64, 300, 33), dt)
     for ax, fam_want in ((0, ["k_scan_col"]), (1, ["k_scan_col"]), (2, ["k_scan_rows"]),
-                         (None, ["k_scan_tile_agg", "k_scan_tile_offsets", "k_scan_tile_apply"])):
+                         (None, ["k_scan_seg_reduce", "k_scan_seg_offsets", "k_scan_seg_apply"])):
         for op in ("cumsum", "cumprod"):
             shape, odt = ops.accumulate_shape(op, x, ax)
             ops.accumulate(op, x, ax, out=fake(shape, odt))

@@ -8,8 +8,8 @@
 //   inner > 1           -> K9a k_scan_col   (a thread walks the axis)
 //   inner == 1, many rows or short rows
 //                       -> K9b k_scan_rows  (a warp folds 32 rows in order)
-//   a few long rows     -> K9c tile scan    (tile totals, fixed-order prefix,
-//                                            rescan)
+//   a few long rows     -> K9c segmented    (segment totals, their prefix in
+//                                            order, each segment rescanned)
 // When the outer or inner dims cannot be merged into one (a flattened
 // transposed view, for instance) the expression is first evaluated into a
 // contiguous temporary of the accumulation type — which is what the
@@ -251,28 +251,73 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
     int64_t strategy = opt("scan.strategy", 0);  // 0 auto, 1 rows, 2 tiles
     if (strategy == 0) strategy = (n_outer >= 4096 || len <= 2048) ? 1 : 2;
     if (strategy == 1) {
-        std::string name = "xtg::k_scan_rows<" + tree + ", " + ls + ", " + rts + ", " + ops + ">";
+        // VEC adjacent columns per lane when the rows allow 16-byte accesses
+        int maxsz = dt(rt).size;
+        for (int l = 0; l < NL; ++l)
+            if (p.lsa[l] == 1) maxsz = std::max(maxsz, dt(t.leaves[l].dtype).size);
+        int vec = std::max(1, 16 / maxsz);
+        if (vec * dt(rt).size > 16) vec = 16 / dt(rt).size;
+        auto vec_ok = [&](int v) {
+            if (v == 1) return true;
+            if (len % v || p.osa != 1 || p.oso % v || !aligned_to(out.data, (int64_t)v * dt(rt).size)) return false;
+            for (int l = 0; l < NL; ++l)
+                if (p.lsa[l] == 1 && (p.lso[l] % v || !aligned_to(p.leaf[l], (int64_t)v * dt(t.leaves[l].dtype).size)))
+                    return false;
+            return true;
+        };
+        while (vec > 1 && !vec_ok(vec)) vec >>= 1;
+        std::vector<int> rk(NL);
+        for (int l = 0; l < NL; ++l) rk[l] = vec > 1 ? kind_of_s(p.lsa[l]) : 2;
+        std::string name = "xtg::k_scan_rows<" + tree + ", " + leafset_s(t, rk) + ", " + rts + ", " + ops + ", " +
+                           std::to_string(vec) + ">";
         Kernel* k;
-        XTG_TRY(get_kernel(name, 128, &k));
+        XTG_TRY(get_kernel(name, 64, &k));
         const int64_t groups = (n_outer + 31) / 32;
-        return launch(k, grid_of(k, (groups + 3) / 4), 128, &p, stream);
+        return launch(k, grid_of(k, (groups + 1) / 2), 64, &p, stream);
     }
-    // K9c: tiles of 4096 elements
+    // K9c: segmented reduce-then-scan; about four segments per SM overall
+    DeviceInfo* dev;
+    XTG_TRY(ensure_device(&dev));
     const int64_t ntiles = (len + 4095) / 4096;
+    const int64_t target = std::max<int64_t>(1, (int64_t)4 * dev->sm_count / std::max<int64_t>(1, n_outer));
+    const int64_t seg_tiles = std::max<int64_t>(1, (ntiles + target - 1) / target);
+    const int64_t nseg = (ntiles + seg_tiles - 1) / seg_tiles;
+    if (seg_tiles >= (1ll << 32) || nseg >= (1ll << 30)) return fail(XTG_ERR_UNSUPPORTED, "scan too long");
     p.ntiles = ntiles;
+    p.n_inner = (nseg << 32) | seg_tiles;
     void* agg = nullptr;
-    const size_t agg_bytes = (size_t)n_outer * (size_t)ntiles * 16;
-    XTG_TRY(scratch_alloc(&agg, agg_bytes, stream));
+    XTG_TRY(scratch_alloc(&agg, (size_t)n_outer * (size_t)nseg * 16, stream));
     p.agg = agg;
     const int agg_off = (int)offsetof(xtg::ScanParams, agg);
+    // 16-byte register loads / stores when every leaf is contiguous or
+    // broadcast along the rows and the destination contiguous, all aligned
+    int sv = 16 / dt(rt).size;
+    for (int l = 0; l < NL; ++l)
+        if (p.lsa[l] == 1) sv = std::min(sv, 16 / dt(t.leaves[l].dtype).size);
+    auto sv_ok = [&](int v) {
+        if (v == 1) return true;
+        if (p.osa != 1 || p.oso % v || !aligned_to(out.data, (int64_t)v * dt(rt).size)) return false;
+        for (int l = 0; l < NL; ++l) {
+            if (p.lsa[l] != 0 && p.lsa[l] != 1) return false;
+            if (p.lsa[l] == 1 && (p.lso[l] % v || !aligned_to(p.leaf[l], (int64_t)v * dt(t.leaves[l].dtype).size)))
+                return false;
+        }
+        return true;
+    };
+    while (sv > 1 && !sv_ok(sv)) sv >>= 1;
+    std::vector<int> sk(NL);
+    for (int l = 0; l < NL; ++l) sk[l] = sv > 1 ? kind_of_s(p.lsa[l]) : 2;
+    const std::string sls = leafset_s(t, sk), svs = std::to_string(sv);
     Kernel *ka, *kb, *kc;
-    xtg_status st = get_kernel("xtg::k_scan_tile_agg<" + tree + ", " + ls + ", " + rts + ", " + ops + ">", 256, &ka);
-    if (st == XTG_OK) st = get_kernel("xtg::k_scan_tile_offsets<" + rts + ", " + ops + ">", 256, &kb);
+    xtg_status st =
+        get_kernel("xtg::k_scan_seg_reduce<" + tree + ", " + sls + ", " + rts + ", " + ops + ", " + svs + ">", 256, &ka);
+    if (st == XTG_OK) st = get_kernel("xtg::k_scan_seg_offsets<" + rts + ", " + ops + ">", 256, &kb);
     if (st == XTG_OK)
-        st = get_kernel("xtg::k_scan_tile_apply<" + tree + ", " + ls + ", " + rts + ", " + ops + ">", 256, &kc);
-    if (st == XTG_OK) st = launch(ka, grid_of(ka, n_outer * ntiles), 256, &p, stream, 0, agg_off);
+        st = get_kernel("xtg::k_scan_seg_apply<" + tree + ", " + sls + ", " + rts + ", " + ops + ", " + svs + ">", 256,
+                        &kc);
+    if (st == XTG_OK) st = launch(ka, grid_of(ka, n_outer * nseg), 256, &p, stream, 0, agg_off);
     if (st == XTG_OK) st = launch(kb, grid_of(kb, n_outer), 256, &p, stream, 0, agg_off);
-    if (st == XTG_OK) st = launch(kc, grid_of(kc, n_outer * ntiles), 256, &p, stream, 0, agg_off);
+    if (st == XTG_OK) st = launch(kc, grid_of(kc, n_outer * nseg), 256, &p, stream, 0, agg_off);
     xtg_status fs = scratch_free(agg, stream);
     return st != XTG_OK ? st : fs;
 }

@@ -1292,61 +1292,81 @@ __global__ void __launch_bounds__(256) k_scan_col(const ScanParams p) {
 }
 
 // K9b: along the innermost axis of many rows.  A warp owns 32 rows and walks
-// them in 32-column chunks: the chunk is loaded coalesced (lane = column),
-// transposed through shared memory, lane i folds row i's 32 elements in
-// order, and the chunk goes back the same way.  Sequential order per row.
-template <class Tree, class LS, class RT, int OP>
-__global__ void __launch_bounds__(128) k_scan_rows(const ScanParams p) {
-    typedef typename LS::template R<1>::type RG;
-    __shared__ RT tile[4][32][33];
+// them in chunks of 32*VEC columns: each lane loads VEC adjacent columns of
+// every row (16-byte accesses, coalesced), the chunk is transposed through
+// shared memory, lane i folds row i's elements in order, and the chunk goes
+// back the same way.  Sequential order per row (bit-identical to the
+// reference's fold).  VEC > 1 needs rows whose length and starts are
+// multiples of VEC (the host checks).
+template <class Tree, class LS, class RT, int OP, int VEC>
+__global__ void __launch_bounds__(64) k_scan_rows(const ScanParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    constexpr int CW = 32 * VEC;        // columns per chunk
+    constexpr int RS = CW + VEC;        // padded row stride (keeps 16-byte rows)
+    __shared__ __align__(16) RT tile[2][32 * RS];
     Ctx<0> c;
     c.scal = p.scal;
     const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    RT* tw = tile[warp];
     const i64 ngroups = (p.n_outer + 31) / 32;
-    for (i64 g = (i64)blockIdx.x * 4 + warp; g < ngroups; g += (i64)gridDim.x * 4) {
+    for (i64 g = (i64)blockIdx.x * 2 + warp; g < ngroups; g += (i64)gridDim.x * 2) {
         const i64 r0 = g * 32;
         RT acc = RT(0);
-        for (i64 c0 = 0; c0 < p.len; c0 += 32) {
-            const i64 col = c0 + lane;
-#pragma unroll 8
+        for (i64 c0 = 0; c0 < p.len; c0 += CW) {
+            const i64 col = c0 + (i64)lane * VEC;
+#pragma unroll 4
             for (int i = 0; i < 32; ++i) {
                 const i64 r = r0 + i;
                 if (r < p.n_outer && col < p.len) {
-                    i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
+                    i64 off[XTG_KMAX_LEAVES];
 #pragma unroll
-                    for (int l = 0; l < LS::N; ++l) {
-                        off[l] = r * p.lso[l] + col * p.lsa[l];
-                        inner[l] = 0;
-                    }
+                    for (int l = 0; l < LS::N; ++l) off[l] = r * p.lso[l] + col * p.lsa[l];
                     RG rg;
-                    LoadLeavesAt<LS>::template run<1>(rg, p.leaf, off, inner);
-                    tile[warp][i][lane] = cvt<RT>(Tree::ev(rg, 0, c));
+                    LoadLeavesAt<LS>::template run<VEC>(rg, p.leaf, off, p.lsa);
+                    RT v[VEC];
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) v[j] = cvt<RT>(Tree::ev(rg, j, c));
+                    st_out<RT, K_CONTIG, VEC>(tw, (i64)i * RS + lane * VEC, 1, v);
                 }
             }
             __syncwarp();
-            const int lim = (p.len - c0) < 32 ? (int)(p.len - c0) : 32;
+            const int lim = (p.len - c0) < CW ? (int)(p.len - c0) : CW;
+            typedef typename VecT<(int)sizeof(RT) * VEC>::t VV;  // VEC * sizeof(RT) <= 16
+            union VU {
+                VV vv;
+                RT e[VEC];
+            };
             if (r0 + lane < p.n_outer) {
-                for (int k = 0; k < lim; ++k) {
-                    const RT x = tile[warp][lane][k];
-                    acc = (c0 + k == 0) ? ScanOp<RT, OP>::init(x) : ScanOp<RT, OP>::step(acc, x);
-                    tile[warp][lane][k] = acc;
+                RT* row = tw + lane * RS;
+                for (int k = 0; k < lim; k += VEC) {
+                    VU u;
+                    u.vv = *reinterpret_cast<const VV*>(row + k);
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) {
+                        acc = (c0 + k + j == 0) ? ScanOp<RT, OP>::init(u.e[j]) : ScanOp<RT, OP>::step(acc, u.e[j]);
+                        u.e[j] = acc;
+                    }
+                    *reinterpret_cast<VV*>(row + k) = u.vv;
                 }
             }
             __syncwarp();
-#pragma unroll 8
+#pragma unroll 4
             for (int i = 0; i < 32; ++i) {
                 const i64 r = r0 + i;
-                if (r < p.n_outer && col < p.len) reinterpret_cast<RT*>(p.out)[r * p.oso + col * p.osa] = tile[warp][i][lane];
+                if (r < p.n_outer && col < p.len) {
+                    VU u;
+                    u.vv = *reinterpret_cast<const VV*>(tw + i * RS + lane * VEC);
+                    st_out<RT, K_CONTIG, VEC>(reinterpret_cast<RT*>(p.out), r * p.oso + col * p.osa, p.osa, u.e);
+                }
             }
             __syncwarp();
         }
     }
 }
 
-// K9c: a few long rows (and the flattened form) — three launches, no
-// inter-CTA waiting: (A) every 4096-element tile's total, (B) per row, the
-// exclusive prefix of the tile totals in a fixed order, (C) every tile again,
-// scanned in a fixed structure from its prefix.  ScanState carries float32
+// K9c: a few long rows (and the flattened form) — segmented
+// reduce-then-scan (k_scan_seg_* below), no CTA waiting on another.
+// ScanState carries float32
 // values in double-float (TwoSum for sums, fma-exact TwoProd for products) so
 // the tile results are within a few ulp of the exact prefix; other types fold
 // in their own arithmetic.  The additive identity is -0 (x + -0 == x for
@@ -1428,145 +1448,255 @@ XTG_DI RT scan_elem(const ScanParams& p, const Ctx<0>& c, i64 row, i64 k) {
     return cvt<RT>(Tree::ev(rg, 0, c));
 }
 
-template <class ST> XTG_DI ST block_reduce_state(ST s, ST* sm) {
-    // fixed order: xor butterfly in each warp, then warp totals in warp order
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) {
-        ST o = shfl_xor_pod(s, m);
-        if ((threadIdx.x & m) == 0) s.merge(o);
-        else {
-            o.merge(s);
-            s = o;
-        }
-    }
+// In-order block scan of one state per thread (Kogge-Stone inside each warp,
+// warp totals in warp order): returns the block total and this thread's
+// exclusive prefix.  Fixed structure, so results do not depend on timing.
+template <class ST> XTG_DI ST block_inorder_scan(ST v, ST* wsum, ST& excl_in_block) {
     const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0) sm[warp] = s;
-    __syncthreads();
-    ST r = sm[0];
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r.merge(sm[w]);
-    __syncthreads();
-    return r;
-}
-
-template <class Tree, class LS, class RT, int OP>
-__global__ void __launch_bounds__(256) k_scan_tile_agg(const ScanParams p) {
-    typedef ScanState<RT, OP> ST;
-    __shared__ ST sm[8];
-    Ctx<0> c;
-    c.scal = p.scal;
-    const i64 nitems = p.n_outer * p.ntiles;
-    for (i64 it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const i64 row = it / p.ntiles, t = it - row * p.ntiles;
-        const i64 k0 = t * XTG_SCAN_TILE;
-        // coalesced: thread th folds elements th, th + 256, ... (any fixed
-        // order will do for a tile total)
-        ST s = ST::ident();
-#pragma unroll 4
-        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-            const i64 k = k0 + (i64)i * 256 + threadIdx.x;
-            if (k < p.len) s.add(scan_elem<Tree, LS, RT>(p, c, row, k));
-        }
-        s = block_reduce_state<ST>(s, sm);
-        if (threadIdx.x == 0) reinterpret_cast<ST*>(p.agg)[it] = s;
-    }
-}
-
-// (B) one CTA per row: exclusive prefix of the tile totals, in place.
-template <class RT, int OP>
-__global__ void __launch_bounds__(256) k_scan_tile_offsets(const ScanParams p) {
-    typedef ScanState<RT, OP> ST;
-    __shared__ ST sm[256];
-    for (i64 row = blockIdx.x; row < p.n_outer; row += gridDim.x) {
-        ST* a = reinterpret_cast<ST*>(p.agg) + row * p.ntiles;
-        const i64 per = (p.ntiles + 255) / 256;
-        const i64 b = (i64)threadIdx.x * per;
-        i64 e = b + per;
-        if (e > p.ntiles) e = p.ntiles;
-        ST tot = ST::ident();
-        for (i64 i = b; i < e; ++i) tot.merge(a[i]);
-        sm[threadIdx.x] = tot;
-        __syncthreads();
-        ST pre = ST::ident();  // exclusive prefix of the thread chunks, in order
-        for (int w = 0; w < (int)threadIdx.x; ++w) pre.merge(sm[w]);
-        for (i64 i = b; i < e; ++i) {
-            const ST v = a[i];
-            a[i] = pre;
-            pre.merge(v);
-        }
-        __syncthreads();
-    }
-}
-
-// (C) every tile again: coalesced load into shared memory, thread th folds
-// its 16 elements from its prefix (tile prefix, then the totals of the
-// threads before it in order), results stored coalesced.
-template <class Tree, class LS, class RT, int OP>
-__global__ void __launch_bounds__(256) k_scan_tile_apply(const ScanParams p) {
-    typedef ScanState<RT, OP> ST;
-    __shared__ RT buf[XTG_SCAN_TILE + XTG_SCAN_TILE / 32];
-    __shared__ ST tot[8];
-    Ctx<0> c;
-    c.scal = p.scal;
-    const i64 nitems = p.n_outer * p.ntiles;
-    for (i64 it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const i64 row = it / p.ntiles, t = it - row * p.ntiles;
-        const i64 k0 = t * XTG_SCAN_TILE;
-#pragma unroll 4
-        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-            const int q = i * 256 + (int)threadIdx.x;
-            const i64 k = k0 + q;
-            if (k < p.len) buf[q + (q >> 5)] = scan_elem<Tree, LS, RT>(p, c, row, k);
-        }
-        __syncthreads();
-        ST s = ST::ident();
-        const int q0 = (int)threadIdx.x * XTG_SCAN_IPT;
+    ST inc = v;
 #pragma unroll
-        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-            const int q = q0 + i;
-            if (k0 + q < p.len) s.add(buf[q + (q >> 5)]);
+    for (int d = 1; d < 32; d <<= 1) {
+        ST y = shfl_up_pod(inc, d);
+        if (lane >= d) {
+            y.merge(inc);
+            inc = y;
         }
-        // block exclusive scan of the thread totals in a fixed structure:
-        // Kogge-Stone inside each warp, then the warp totals in warp order
-        const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
-        ST inc = s;
+    }
+    const ST lex = shfl_up_pod(inc, 1);
+    __syncthreads();
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    // warp 0 scans the warp totals in order: wsum[w] becomes the exclusive
+    // prefix of warp w, wsum[nw] the block total
+    const int nw = (int)(blockDim.x >> 5);
+    if (warp == 0) {
+        ST v2 = lane < nw ? wsum[lane] : ST::ident();
+        ST i2 = v2;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
-            ST y = shfl_up_pod(inc, d);
+            ST y = shfl_up_pod(i2, d);
             if (lane >= d) {
-                y.merge(inc);
-                inc = y;
+                y.merge(i2);
+                i2 = y;
             }
         }
-        ST lex = shfl_up_pod(inc, 1);
-        if (lane == 31) tot[warp] = inc;
-        __syncthreads();
-        ST pre = reinterpret_cast<const ST*>(p.agg)[it];
-        for (int w = 0; w < warp; ++w) pre.merge(tot[w]);
-        if (lane > 0) pre.merge(lex);
+        const ST e2 = shfl_up_pod(i2, 1);
+        __syncwarp();
+        if (lane < nw) wsum[lane] = lane == 0 ? ST::ident() : e2;
+        if (lane == nw - 1) wsum[nw] = i2;
+    }
+    __syncthreads();
+    ST pre = wsum[warp];
+    if (lane > 0) pre.merge(lex);
+    excl_in_block = pre;
+    return wsum[nw];
+}
+
+// Segmented reduce-then-scan (no CTA ever waits on another): a row is cut
+// into segments of seg_tiles tiles (about four segments per SM over the
+// launch); (A) each segment's total, (B) per row, the exclusive prefix of
+// the segment totals in order, (C) each segment again, tile by tile, from
+// its prefix with the running total carried inside the CTA.
+// ScanParams.ntiles = tiles per row; segments per row and tiles per segment
+// ride in n_inner (unused for these rows) as nseg * 2^32 + seg_tiles.
+XTG_DI i64 seg_tiles_of(const ScanParams& p) { return p.n_inner & 0xffffffffll; }
+XTG_DI i64 nseg_of(const ScanParams& p) { return p.n_inner >> 32; }
+
+// A thread's 16 consecutive elements of a tile into registers: VEC-wide
+// loads when all 16 lie before `ke` (VEC > 1: every leaf contiguous or
+// broadcast along the row, rows VEC-aligned — the host checks), else one by
+// one.
+template <class Tree, class LS, class RT, int VEC>
+XTG_DI void scan_load16(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kt, i64 ke, RT (&v)[XTG_SCAN_IPT]) {
+    if (VEC > 1 && kt + XTG_SCAN_IPT <= ke) {
+        typedef typename LS::template R<VEC>::type RG;
 #pragma unroll
-        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-            const int q = q0 + i;
-            const i64 k = k0 + q;
-            if (k < p.len) {
-                const RT x = buf[q + (q >> 5)];
-                if (k == 0) {
-                    pre.hi = ScanOp<RT, OP>::init(x);
-                    pre.lo = RT(0);
-                } else {
-                    pre.add(x);
+        for (int m = 0; m < XTG_SCAN_IPT / VEC; ++m) {
+            i64 off[XTG_KMAX_LEAVES];
+#pragma unroll
+            for (int l = 0; l < LS::N; ++l) off[l] = row * p.lso[l] + (kt + m * VEC) * p.lsa[l];
+            RG rg;
+            LoadLeavesAt<LS>::template run<VEC>(rg, p.leaf, off, p.lsa);
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) v[m * VEC + j] = cvt<RT>(Tree::ev(rg, j, c));
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < XTG_SCAN_IPT; ++i) v[i] = kt + i < ke ? scan_elem<Tree, LS, RT>(p, c, row, kt + i) : RT(0);
+    }
+}
+
+template <class Tree, class LS, class RT, int OP, int VEC>
+__global__ void __launch_bounds__(256) k_scan_seg_reduce(const ScanParams p) {
+    typedef ScanState<RT, OP> ST;
+    __shared__ ST wsum[9];
+    Ctx<0> c;
+    c.scal = p.scal;
+    const i64 nseg = nseg_of(p), st = seg_tiles_of(p);
+    const i64 nitems = p.n_outer * nseg;
+    for (i64 it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const i64 row = it / nseg, sg = it - row * nseg;
+        i64 kb = sg * st * XTG_SCAN_TILE;
+        i64 ke = kb + st * XTG_SCAN_TILE;
+        if (ke > p.len) ke = p.len;
+        ST s = ST::ident();
+        for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_TILE) {
+            RT v[XTG_SCAN_IPT];
+            if (VEC > 1) {
+                // each thread its 16 consecutive elements (vector loads)
+                const i64 kt = k0 + (i64)threadIdx.x * XTG_SCAN_IPT;
+                scan_load16<Tree, LS, RT, VEC>(p, c, row, kt, ke, v);
+#pragma unroll
+                for (int i = 0; i < XTG_SCAN_IPT; ++i)
+                    if (kt + i < ke) s.add(v[i]);
+            } else {
+                // coalesced scalar loads: thread th takes th, th + 256, ...
+#pragma unroll
+                for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+                    const i64 k = k0 + (i64)i * 256 + threadIdx.x;
+                    v[i] = k < ke ? scan_elem<Tree, LS, RT>(p, c, row, k) : RT(0);
                 }
-                buf[q + (q >> 5)] = pre.value();
+#pragma unroll
+                for (int i = 0; i < XTG_SCAN_IPT; ++i)
+                    if (k0 + (i64)i * 256 + threadIdx.x < ke) s.add(v[i]);
             }
         }
-        __syncthreads();
-#pragma unroll 4
-        for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-            const int q = i * 256 + (int)threadIdx.x;
-            const i64 k = k0 + q;
-            if (k < p.len) reinterpret_cast<RT*>(p.out)[row * p.oso + k * p.osa] = buf[q + (q >> 5)];
+        ST unused;
+        const ST tot = block_inorder_scan(s, wsum, unused);
+        if (threadIdx.x == 0) reinterpret_cast<ST*>(p.agg)[it] = tot;
+    }
+}
+
+// (B) one CTA per row: exclusive prefixes of the row's segment totals, in place
+template <class RT, int OP>
+__global__ void __launch_bounds__(256) k_scan_seg_offsets(const ScanParams p) {
+    typedef ScanState<RT, OP> ST;
+    __shared__ ST wsum[9];
+    const i64 nseg = nseg_of(p);
+    for (i64 row = blockIdx.x; row < p.n_outer; row += gridDim.x) {
+        ST* a = reinterpret_cast<ST*>(p.agg) + row * nseg;
+        ST carry = ST::ident();
+        for (i64 b = 0; b < nseg; b += 256) {
+            const i64 i = b + threadIdx.x;
+            const ST v = i < nseg ? a[i] : ST::ident();
+            ST ex;
+            const ST tot = block_inorder_scan(v, wsum, ex);
+            ST pre = carry;
+            pre.merge(ex);
+            if (i < nseg) a[i] = pre;
+            carry.merge(tot);
+            __syncthreads();
         }
-        __syncthreads();
+    }
+}
+
+// (C) each segment, tile by tile: coalesced loads into shared memory, thread
+// th folds 16 consecutive elements from (carry, then the threads before it),
+// coalesced stores; the tile total joins the carry
+template <class Tree, class LS, class RT, int OP, int VEC>
+__global__ void __launch_bounds__(256) k_scan_seg_apply(const ScanParams p) {
+    typedef ScanState<RT, OP> ST;
+    __shared__ RT buf[VEC > 1 ? 1 : XTG_SCAN_TILE + XTG_SCAN_TILE / 32];
+    __shared__ ST wsum[9];
+    Ctx<0> c;
+    c.scal = p.scal;
+    const i64 nseg = nseg_of(p), st = seg_tiles_of(p);
+    const i64 nitems = p.n_outer * nseg;
+    const int q0 = (int)threadIdx.x * XTG_SCAN_IPT;
+    for (i64 it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const i64 row = it / nseg, sg = it - row * nseg;
+        const i64 kb = sg * st * XTG_SCAN_TILE;
+        i64 ke = kb + st * XTG_SCAN_TILE;
+        if (ke > p.len) ke = p.len;
+        ST carry = reinterpret_cast<const ST*>(p.agg)[it];
+        if constexpr (VEC > 1) {
+            // registers only: each thread its 16 consecutive elements
+            for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_TILE) {
+                const i64 kt = k0 + q0;
+                RT v[XTG_SCAN_IPT];
+                scan_load16<Tree, LS, RT, VEC>(p, c, row, kt, ke, v);
+                ST s = ST::ident();
+#pragma unroll
+                for (int i = 0; i < XTG_SCAN_IPT; ++i)
+                    if (kt + i < ke) s.add(v[i]);
+                ST thr_excl;
+                const ST tile_tot = block_inorder_scan(s, wsum, thr_excl);
+                ST pre = carry;
+                pre.merge(thr_excl);
+#pragma unroll
+                for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+                    const i64 k = kt + i;
+                    if (k < ke) {
+                        if (k == 0) {
+                            pre.hi = ScanOp<RT, OP>::init(v[i]);
+                            pre.lo = RT(0);
+                        } else {
+                            pre.add(v[i]);
+                        }
+                        v[i] = pre.value();
+                    }
+                }
+                RT* o = reinterpret_cast<RT*>(p.out) + row * p.oso;
+                if (kt + XTG_SCAN_IPT <= ke) {
+#pragma unroll
+                    for (int m = 0; m < XTG_SCAN_IPT / VEC; ++m) {
+                        RT w[VEC];
+#pragma unroll
+                        for (int j = 0; j < VEC; ++j) w[j] = v[m * VEC + j];
+                        st_out<RT, K_CONTIG, VEC>(o, kt + m * VEC, 1, w);
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < XTG_SCAN_IPT; ++i)
+                        if (kt + i < ke) o[kt + i] = v[i];
+                }
+                carry.merge(tile_tot);
+            }
+            continue;
+        }
+        for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_TILE) {
+#pragma unroll
+            for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+                const int q = i * 256 + (int)threadIdx.x;
+                const i64 k = k0 + q;
+                if (k < ke) buf[q + (q >> 5)] = scan_elem<Tree, LS, RT>(p, c, row, k);
+            }
+            __syncthreads();
+            ST s = ST::ident();
+#pragma unroll
+            for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+                const int q = q0 + i;
+                if (k0 + q < ke) s.add(buf[q + (q >> 5)]);
+            }
+            ST thr_excl;
+            const ST tile_tot = block_inorder_scan(s, wsum, thr_excl);
+            ST pre = carry;
+            pre.merge(thr_excl);
+#pragma unroll
+            for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+                const int q = q0 + i;
+                const i64 k = k0 + q;
+                if (k < ke) {
+                    const RT x = buf[q + (q >> 5)];
+                    if (k == 0) {
+                        pre.hi = ScanOp<RT, OP>::init(x);
+                        pre.lo = RT(0);
+                    } else {
+                        pre.add(x);
+                    }
+                    buf[q + (q >> 5)] = pre.value();
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+                const int q = i * 256 + (int)threadIdx.x;
+                const i64 k = k0 + q;
+                if (k < ke) reinterpret_cast<RT*>(p.out)[row * p.oso + k * p.osa] = buf[q + (q >> 5)];
+            }
+            carry.merge(tile_tot);
+            __syncthreads();
+        }
     }
 }
 

@@ -114,8 +114,8 @@ struct ScanParams {
     void* out;
     i64 oso, osa, osi;  // destination strides
     Scalars scal;
-    i64 ntiles;         // tile scan: tiles per row
-    void* agg;          // tile scan: n_outer * ntiles partial states (16 B each)
+    i64 ntiles;         // segmented scan: tiles per row
+    void* agg;          // segmented scan: one partial state (16 B) per segment
 };
 
 // Batched evaluation: many instances of one expression shape, each a 2-D
