@@ -30,6 +30,11 @@
  *                      (xt::accumulate, accumulator_impl)
  *                      include/xtensor/reducers/xaccumulator.hpp:154-367
  *                      include/xtensor/core/xmath.hpp:2248-2301, 2363-2391, 2592-2645
+ *   xtg_gather / xtg_scatter, xtg_filter* , xtg_masked_assign
+ *                   <- reading and assigning through xt::index_view / filter /
+ *                      filtration / masked_view
+ *                      include/xtensor/views/xindex_view.hpp:54-206, 786-850
+ *                      include/xtensor/views/xmasked_view.hpp:63-240
  *   xtg_batch_*     <- no counterpart (new batching layer over the same path)
  *   xtg_server_*    <- no counterpart (new request server over the same path)
  *
@@ -208,9 +213,10 @@ xtg_status xtg_stream_destroy(xtg_stream stream);
 xtg_status xtg_stream_sync(xtg_stream stream);
 xtg_status xtg_device_sync(void);
 size_t xtg_dtype_size(int32_t dtype);
-/* Kernels never trap: a bounded wait that gives up sets a device error word
- * and the kernel returns.  This synchronises the device, reads and clears
- * the word: XTG_ERR_TIMEOUT if it was set. */
+/* Kernels never trap: a bounded wait that gives up, or an index-view
+ * coordinate outside its array, sets a device error word and the kernel
+ * skips the work.  This synchronises the device, reads and clears the word:
+ * XTG_ERR_TIMEOUT (a wait gave up) or XTG_ERR_OUT_OF_RANGE (a coordinate). */
 xtg_status xtg_check_device_errors(void);
 
 /* CUDA events (timing on the launching stream). */
@@ -275,6 +281,38 @@ xtg_status xtg_accumulate_shape(const xtg_expr* e, int32_t op, int32_t has_axis,
                                 int32_t* rank, int64_t* shape, int32_t* dtype);
 xtg_status xtg_accumulate(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis, int32_t acc_dtype,
                           const xtg_array* out, xtg_stream stream);
+
+/* ---- index, filter and masked views ----------------------------------------------------
+ * Assignment operators for writes through a view: dst = op(dst, value). */
+typedef enum {
+    XTG_SET = 0, XTG_SET_ADD = 1, XTG_SET_SUB = 2, XTG_SET_MUL = 3, XTG_SET_DIV = 4
+} xtg_set_op;
+/* out[k] = e[indices[k]] — reading an xt::index_view(e, indices).  indices:
+ * device int64, n rows of rank(e) coordinates; out 1-D of n elements.
+ * Coordinates outside e's shape are not read: the element is left as is and
+ * the device error word is set (xtg_check_device_errors). */
+xtg_status xtg_gather(const xtg_expr* e, const int64_t* indices, int64_t n, const xtg_array* out,
+                      xtg_stream stream);
+/* dst[indices[k]] = op(dst[indices[k]], src[k]) — assigning through an
+ * index_view.  src is 1-D of n elements or broadcast to it (a scalar).
+ * Repeated coordinates: each write happens, their order is unspecified. */
+xtg_status xtg_scatter(const xtg_expr* src, const int64_t* indices, int64_t n, int32_t op, const xtg_array* dst,
+                       xtg_stream stream);
+/* Number of true elements of cond (synchronises the stream). */
+xtg_status xtg_filter_count(const xtg_expr* cond, int64_t* count, xtg_stream stream);
+/* out[k] = e[i_k], i_k the k-th position (row-major) where cond is true —
+ * xt::filter(e, cond).  cond is broadcast to e's shape; out 1-D of
+ * xtg_filter_count(cond) elements. */
+xtg_status xtg_filter(const xtg_expr* e, const xtg_expr* cond, const xtg_array* out, xtg_stream stream);
+/* dst[i_k] = op(dst[i_k], src[k]) — assigning through filter(dst, cond)
+ * (src 1-D of the selected count) or through filtration(dst, cond) (src a
+ * scalar). */
+xtg_status xtg_filter_assign(const xtg_expr* src, const xtg_expr* cond, int32_t op, const xtg_array* dst,
+                             xtg_stream stream);
+/* dst[i] = mask[i] ? op(dst[i], src[i]) : dst[i] — assigning through
+ * xt::masked_view(dst, mask); src and mask broadcast to dst's shape. */
+xtg_status xtg_masked_assign(const xtg_expr* src, const xtg_expr* mask, int32_t op, const xtg_array* dst,
+                             xtg_stream stream);
 
 /* ---- batching ------------------------------------------------------------------------
  * No counterpart in the reference (a new layer over the same path).  Many

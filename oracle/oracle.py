@@ -141,3 +141,80 @@ def accumulate(op, e, axis=None, acc_dtype=None) -> np.ndarray:
     _chk(lib().orc_accumulate(C.byref(ex), code, 0 if axis is None else 1, 0 if axis is None else int(axis), acc,
                               C.byref(o)))
     return out
+
+
+# ---- index, filter and masked views ---------------------------------------------------------
+# Restatements of the reference's view semantics, over values the C oracle
+# evaluates (orc_assign), with the C++ conversions of `dst op= value`
+# (computed in the promoted type, stored as the destination type):
+#  * index_view read: v(i) = e[indices[i]] (include/xtensor/views/xindex_view.hpp:398-488);
+#  * index_view assignment: element by element in index order through the
+#    view's stepper (xview_semantic), so a repeated coordinate is written
+#    once per occurrence, in order;
+#  * filter(e, cond) = index_view(e, argwhere(cond)), argwhere in row-major
+#    order (xindex_view.hpp:821-826); filtration(e, cond) op= scalar applies
+#    `cond ? op(e, scalar) : e` element by element (:763-767);
+#  * masked_view(dst, mask) = e copies e through the view's iterator, which
+#    skips masked elements (include/xtensor/views/xmasked_view.hpp:577-594).
+def _set_apply(op, a, b, ct, dt):
+    a = a.astype(ct)
+    b = np.asarray(b).astype(ct)
+    if op == "=":
+        r = b
+    elif op == "+=":
+        r = a + b
+    elif op == "-=":
+        r = a - b
+    elif op == "*=":
+        r = a * b
+    elif np.issubdtype(ct, np.floating):
+        r = a / b
+    else:
+        # C++ integer division truncates toward zero
+        bb = np.where(b == 0, 1, b)
+        q = np.abs(a) // np.abs(bb)
+        r = np.where(b != 0, np.where((a < 0) != (bb < 0), -q, q), 0).astype(ct)
+    return r.astype(dt)
+
+
+def index_view(e, indices) -> np.ndarray:
+    v = assign(e)
+    idx = np.asarray(indices, dtype=np.int64).reshape(-1, v.ndim)
+    return np.array([v[tuple(ix)] for ix in idx], dtype=v.dtype)
+
+
+def index_assign(dst: np.ndarray, indices, src, op="=") -> np.ndarray:
+    """dst (numpy, modified and returned) through index_view(dst, indices)."""
+    idx = np.asarray(indices, dtype=np.int64).reshape(-1, dst.ndim)
+    s = assign(src) if not np.isscalar(src) else np.asarray(src)
+    s = np.broadcast_to(s, (len(idx),))
+    ct = np_dtype(lib().orc_promote(dtype_code(dst.dtype), dtype_code(s.dtype)))
+    for k, ix in enumerate(idx):
+        dst[tuple(ix)] = _set_apply(op, np.asarray(dst[tuple(ix)]), s[k], ct, dst.dtype)
+    return dst
+
+
+def filter(e, cond) -> np.ndarray:  # noqa: A001
+    v = assign(e)
+    c = assign(cond).astype(bool)
+    return np.array([v[tuple(ix)] for ix in np.argwhere(c)], dtype=v.dtype)
+
+
+def filter_assign(dst: np.ndarray, cond, src, op="=") -> np.ndarray:
+    c = assign(cond).astype(bool)
+    pos = np.argwhere(c)
+    s = assign(src) if not np.isscalar(src) else np.asarray(src)
+    s = np.broadcast_to(s, (len(pos),))
+    ct = np_dtype(lib().orc_promote(dtype_code(dst.dtype), dtype_code(s.dtype)))
+    for k, ix in enumerate(pos):
+        dst[tuple(ix)] = _set_apply(op, np.asarray(dst[tuple(ix)]), s[k], ct, dst.dtype)
+    return dst
+
+
+def masked_assign(dst: np.ndarray, mask, src, op="=") -> np.ndarray:
+    m = np.broadcast_to(assign(mask).astype(bool), dst.shape)
+    s = np.broadcast_to(assign(src) if not np.isscalar(src) else np.asarray(src), dst.shape)
+    ct = np_dtype(lib().orc_promote(dtype_code(dst.dtype), dtype_code(s.dtype)))
+    for ix in np.argwhere(m):
+        dst[tuple(ix)] = _set_apply(op, np.asarray(dst[tuple(ix)]), s[tuple(ix)], ct, dst.dtype)
+    return dst

@@ -142,3 +142,28 @@ def test_accumulator_plans(dt):
     n = 64 * 300 * 33
     ops.accumulate("cumsum", x.transpose((2, 0, 1)), None, out=fake((n,), ops.accumulate_shape("cumsum", x)[1]))
     assert fam(last_kernels())[0] == "k_transpose"
+
+
+def test_view_plans():
+    """Masked writes lower to the elementwise kernel, index views to the
+    indexed kernel, filters to the accumulator (positions) + indexed kernel;
+    everything compiles."""
+    from xtensor_gb300 import ops
+    a = fake((64, 300), "float32")
+    m = fake((64, 300), "bool")
+    ops.masked_assign(a, m, a * 2, "+=")
+    assert fam(last_kernels()) == ["k_assign"]
+    idx = fake((100, 2), "int64")
+    ops.index_view(a, idx, out=fake((100,), "float32"))
+    assert fam(last_kernels()) == ["k_indexed"]
+    ops.index_assign(a, idx, fake((100,), "float64"), "*=")
+    assert fam(last_kernels()) == ["k_indexed"]
+    ops.filter(a, a > 0, out=fake((0,), "float32"))
+    ks = fam(last_kernels())
+    assert ks[-1] == "k_indexed" and "k_scan_rows" in ks or "k_scan_seg_apply" in ks, ks
+    ops.filter_assign(a, a > 0, 1.5, "=")
+    assert fam(last_kernels())[-1] == "k_indexed"
+    # a write through a transposed view of itself goes through a temporary
+    sq = fake((64, 64), "float32")
+    xg.assign(sq, sq.transpose((1, 0)))
+    assert fam(last_kernels()) == ["k_transpose", "k_assign"]

@@ -40,5 +40,6 @@ from .expr import *  # noqa: F401,F403
 from .device import DeviceArray, Stream, device_sync, init  # noqa: F401
 from .ops import assign, reduce, argreduce, reduce_shape, broadcast_shape, expr_dtype  # noqa: F401
 from .ops import accumulate, cumsum, cumprod, nancumsum, nancumprod  # noqa: F401
+from .ops import index_view, index_assign, filter_count, filter, filter_assign, masked_assign  # noqa: F401,A004
 
 __all__ = [n for n in dir() if not n.startswith("_")]

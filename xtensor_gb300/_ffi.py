@@ -138,6 +138,12 @@ def lib() -> C.CDLL:
             "xtg_accumulate_shape": (st, [C.POINTER(Expr), i32, i32, i64, i32, C.POINTER(i32), C.POINTER(i64),
                                           C.POINTER(i32)]),
             "xtg_accumulate": (st, [C.POINTER(Expr), i32, i32, i64, i32, C.POINTER(Array), vp]),
+            "xtg_gather": (st, [C.POINTER(Expr), vp, i64, C.POINTER(Array), vp]),
+            "xtg_scatter": (st, [C.POINTER(Expr), vp, i64, i32, C.POINTER(Array), vp]),
+            "xtg_filter_count": (st, [C.POINTER(Expr), C.POINTER(i64), vp]),
+            "xtg_filter": (st, [C.POINTER(Expr), C.POINTER(Expr), C.POINTER(Array), vp]),
+            "xtg_filter_assign": (st, [C.POINTER(Expr), C.POINTER(Expr), i32, C.POINTER(Array), vp]),
+            "xtg_masked_assign": (st, [C.POINTER(Expr), C.POINTER(Expr), i32, C.POINTER(Array), vp]),
             "xtg_get_jit_stats": (st, [C.POINTER(JitStats)]),
             "xtg_set_option": (st, [C.c_char_p, i64]),
             "xtg_get_option": (st, [C.c_char_p, C.POINTER(i64)]),

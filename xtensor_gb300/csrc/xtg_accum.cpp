@@ -324,6 +324,11 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
 
 }  // namespace
 
+xtg_status accumulate_call(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis, int32_t acc_dtype,
+                           const xtg_array* out, cudaStream_t stream) {
+    return accumulate_impl(e, op, has_axis, axis, acc_dtype, out, stream);
+}
+
 }  // namespace xtgh
 
 using namespace xtgh;

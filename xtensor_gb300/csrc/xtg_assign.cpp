@@ -460,6 +460,76 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
     return launch(kr, grid_for(kr, need), block, &p, stream);
 }
 
+// Memory hazards: a leaf sharing memory with the destination but read at
+// other positions than the ones being written (a transposed, shifted or
+// reinterpreted view of the destination).  Such assignments evaluate into a
+// temporary first — what the reference's `a = e` does for every call
+// (include/xtensor/core/xsemantic.hpp:620-690).
+static void byte_range(const xtg_array& a, int64_t& lo, int64_t& hi) {
+    lo = hi = 0;
+    for (int d = 0; d < a.rank; ++d) {
+        if (a.shape[d] == 0) {
+            lo = 1;
+            hi = 0;  // empty
+            return;
+        }
+        const int64_t ext = (a.shape[d] - 1) * a.strides[d];
+        if (ext < 0) lo += ext;
+        else hi += ext;
+    }
+    const int64_t sz = dt(a.dtype).size;
+    lo = (int64_t)(uintptr_t)a.data + lo * sz;
+    hi = (int64_t)(uintptr_t)a.data + hi * sz + sz;
+}
+
+bool assign_hazard(const Tree& t, const xtg_array& out) {
+    int64_t olo, ohi;
+    byte_range(out, olo, ohi);
+    if (olo >= ohi) return false;
+    for (const xtg_array& l : t.leaves) {
+        int64_t llo, lhi;
+        byte_range(l, llo, lhi);
+        if (llo >= lhi || lhi <= olo || llo >= ohi) continue;
+        if (l.data != out.data || l.dtype != out.dtype || l.rank > out.rank) return true;
+        int64_t st[XTG_MAX_RANK];
+        bstrides_to(l, out.rank, out.shape, st);
+        for (int d = 0; d < out.rank; ++d)
+            if (out.shape[d] > 1 && st[d] != out.strides[d]) return true;
+    }
+    return false;
+}
+
+xtg_status assign_guarded(const Tree& t, const xtg_array* out, cudaStream_t stream) {
+    if (!assign_hazard(t, *out)) return assign_tree(t, out, stream);
+    if (recorder()) recorder()->nocache = true;  // the temporary's address is baked into the launches
+    int64_t n = 1;
+    for (int d = 0; d < out->rank; ++d) n *= out->shape[d];
+    void* tmp = nullptr;
+    XTG_TRY(scratch_alloc(&tmp, (size_t)std::max<int64_t>(n, 1) * dt(out->dtype).size + 16, stream));
+    xtg_array ta = *out;
+    ta.data = tmp;
+    int64_t m = 1;
+    for (int d = out->rank - 1; d >= 0; --d) {
+        ta.strides[d] = m;
+        m *= out->shape[d];
+    }
+    xtg_status st = assign_tree(t, &ta, stream);
+    if (st == XTG_OK) {
+        xtg_expr le;
+        memset(&le, 0, sizeof le);
+        le.n_nodes = 1;
+        le.nodes[0].op = XTG_OP_LEAF;
+        le.nodes[0].dtype = out->dtype;
+        le.n_leaves = 1;
+        le.leaves[0] = ta;
+        Tree t2;
+        st = build_tree(&le, false, t2);
+        if (st == XTG_OK) st = assign_tree(t2, out, stream);
+    }
+    xtg_status fs = scratch_free(tmp, stream);
+    return st != XTG_OK ? st : fs;
+}
+
 }  // namespace xtgh
 
 using namespace xtgh;
@@ -473,6 +543,6 @@ extern "C" xtg_status xtg_assign(const xtg_expr* e, const xtg_array* out, xtg_st
         Tree t;
         const bool demote = opt("fp32_compute", 1) != 0 && out->dtype != XTG_FLOAT64;
         XTG_TRY(build_tree(e, demote, t));
-        return assign_tree(t, out, (cudaStream_t)stream);
+        return assign_guarded(t, out, (cudaStream_t)stream);
     });
 }

@@ -1701,6 +1701,72 @@ __global__ void __launch_bounds__(256) k_scan_seg_apply(const ScanParams p) {
 }
 
 // ---------------------------------------------------------------------------
+// K10: indexed evaluation — reads and writes through xt::index_view, filter
+// and filtration (include/xtensor/views/xindex_view.hpp:54-206, 786-850).
+// VT: value type of the evaluated tree; DT: destination type; CT: the type
+// `dst op value` computes in (C++ conversions); OP: xtg_set_op.
+template <class Tree, class LS, class VT, class DT, class CT, int MODE, int R, int OP>
+__global__ void __launch_bounds__(256) k_indexed(const IndexParams p) {
+    typedef typename LS::template R<1>::type RG;
+    Ctx<0> c;
+    c.scal = p.scal;
+    for (i64 k = (i64)blockIdx.x * blockDim.x + threadIdx.x; k < p.n; k += (i64)gridDim.x * blockDim.x) {
+        i64 ix[R > 0 ? R : 1];
+        i64 j = 0;  // 1-D position in the out (0, 2) or src (1, 3) space
+        if (MODE <= 1) {
+            bool ok = true;
+#pragma unroll
+            for (int d = 0; d < R; ++d) {
+                ix[d] = p.idx[k * R + d];
+                if (ix[d] < 0 || ix[d] >= p.shape[d]) ok = false;
+            }
+            if (!ok) {
+                atomicExch(p.err, 2);  // reported as XTG_ERR_OUT_OF_RANGE
+                continue;
+            }
+            j = k;
+        } else {
+            const long long cur = p.idx[k];
+            const long long prev = k ? p.idx[k - 1] : 0;
+            if (cur == prev) continue;  // not selected
+            j = cur - 1;
+            decode_dims<R, true>(p.shape, p.fd, k, ix);
+        }
+        i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
+#pragma unroll
+        for (int l = 0; l < LS::N; ++l) {
+            inner[l] = 0;
+            if (MODE == 0 || MODE == 2) {
+                i64 o = 0;
+#pragma unroll
+                for (int d = 0; d < R; ++d) o += ix[d] * p.ls[l][d];
+                off[l] = o;
+            } else {
+                off[l] = j * p.ls[l][0];
+            }
+        }
+        RG rg;
+        LoadLeavesAt<LS>::template run<1>(rg, p.leaf, off, inner);
+        const VT v = cvt<VT>(Tree::ev(rg, 0, c));
+        DT* dst = reinterpret_cast<DT*>(p.dst);
+        if (MODE == 0 || MODE == 2) {
+            dst[j * p.ds[0]] = cvt<DT>(v);
+        } else {
+            i64 o = 0;
+#pragma unroll
+            for (int d = 0; d < R; ++d) o += ix[d] * p.ds[d];
+            if (OP == 0) {
+                dst[o] = cvt<DT>(v);
+            } else {
+                const CT a = cvt<CT>(dst[o]), b = cvt<CT>(v);
+                const CT r = OP == 1 ? CT(a + b) : OP == 2 ? CT(a - b) : OP == 3 ? CT(a * b) : CT(a / b);
+                dst[o] = cvt<DT>(r);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // K2: tiled transposing assignment (transpose / permuted strided_view into a
 // contiguous destination — the case xtensor sends to the scalar
 // stepper_assigner, include/xtensor/core/xassign.hpp:1087, 1341).

@@ -118,6 +118,25 @@ struct ScanParams {
     void* agg;          // segmented scan: one partial state (16 B) per segment
 };
 
+// Indexed evaluation through index_view / filter (gathers and scatters).
+// MODE 0 gather (out[k] = e[idx row k]), 1 scatter (dst[idx row k] op= src[k]),
+// 2 filter gather (out[P[i]-1] = e[i] where selected), 3 filter assign
+// (dst[i] op= src[P[i]-1] where selected); P = inclusive count of the
+// condition in row-major order.
+struct IndexParams {
+    i64 n;                                      // index rows (0, 1) or flat positions (2, 3)
+    int rank;
+    i64 shape[XTG_KMAX_RANK];                   // the indexed space (e: 0, 2; dst: 1, 3)
+    FastDiv fd[XTG_KMAX_RANK];                  // row-major decode of flat positions (2, 3)
+    const long long* idx;                       // n x rank coordinates (0, 1) or P (2, 3)
+    const void* leaf[XTG_KMAX_LEAVES];
+    i64 ls[XTG_KMAX_LEAVES][XTG_KMAX_RANK];     // value-tree leaf strides (0, 2: indexed space; 1, 3: dim 0)
+    void* dst;
+    i64 ds[XTG_KMAX_RANK];                      // out stride in ds[0] (0, 2) or dst strides (1, 3)
+    Scalars scal;
+    int* err;                                   // set when a coordinate is outside the shape
+};
+
 // Batched evaluation: many instances of one expression shape, each a 2-D
 // (rows, cols) space with its own pointers and strides.
 struct BatchInst {

@@ -75,6 +75,12 @@ struct ScratchSpec {
 xtg_status reduce_impl(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, cudaStream_t stream,
                        const ScratchSpec* scratch);
 xtg_status assign_tree(const Tree& t, const xtg_array* out, cudaStream_t stream);
+// xtg_accumulate without the plan cache (used by the filter views).
+xtg_status accumulate_call(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis, int32_t acc_dtype,
+                           const xtg_array* out, cudaStream_t stream);
+// assign_tree, through a temporary when a leaf shares memory with `out` but
+// is read at other positions than the ones written.
+xtg_status assign_guarded(const Tree& t, const xtg_array* out, cudaStream_t stream);
 
 // Accumulator type string, post-operation and initial values of a reduction.
 struct AccChoice {

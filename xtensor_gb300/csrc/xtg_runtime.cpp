@@ -331,6 +331,7 @@ xtg_status xtg_check_device_errors(void) {
     XTG_CUDA(cudaMemcpy(&v, g_err_word, sizeof v, cudaMemcpyDeviceToHost));
     if (v) {
         XTG_CUDA(cudaMemset(g_err_word, 0, sizeof v));
+        if (v == 2) return fail(XTG_ERR_OUT_OF_RANGE, "an index view coordinate was outside the array (element skipped)");
         return fail(XTG_ERR_TIMEOUT, "a kernel's bounded wait gave up (device error word was set)");
     }
     return XTG_OK;

@@ -178,3 +178,80 @@ def nancumsum(e, axis=None, **kw):
 
 def nancumprod(e, axis=None, **kw):
     return accumulate("nancumprod", e, axis, **kw)
+
+
+# ---- index, filter and masked views -------------------------------------------------------
+SET_OPS = {"=": 0, "+=": 1, "-=": 2, "*=": 3, "/=": 4}
+
+
+def _indices(indices, rank: int, stream=None) -> DeviceArray:
+    import numpy as np
+    if isinstance(indices, DeviceArray):
+        return indices
+    a = np.ascontiguousarray(np.asarray(indices, dtype=np.int64).reshape(-1, rank))
+    return DeviceArray.from_numpy(a, None, stream)
+
+
+def index_view(e, indices, out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
+    """Read xt::index_view(e, indices): out[k] = e[indices[k]] (indices: n
+    coordinate rows of rank(e))."""
+    e = as_expr(e)
+    rank = len(broadcast_shape(e))
+    idx = _indices(indices, rank, stream)
+    n = idx.shape[0] if idx.ndim else 0
+    if out is None:
+        out = DeviceArray.empty((n,), expr_dtype(e), stream)
+    ex, keep = lower(e)
+    o = out.xtg_array()
+    check(lib().xtg_gather(C.byref(ex), C.c_void_p(idx.ptr), n, C.byref(o), _sh(stream)))
+    return out
+
+
+def index_assign(dst: DeviceArray, indices, src, op: str = "=", stream=None) -> DeviceArray:
+    """Assign through xt::index_view(dst, indices): dst[indices[k]] op= src[k]."""
+    idx = _indices(indices, dst.ndim, stream)
+    n = idx.shape[0]
+    ex, keep = lower(as_expr(src))
+    o = dst.xtg_array()
+    check(lib().xtg_scatter(C.byref(ex), C.c_void_p(idx.ptr), n, SET_OPS[op], C.byref(o), _sh(stream)))
+    return dst
+
+
+def filter_count(cond, stream=None) -> int:
+    ex, keep = lower(as_expr(cond))
+    c = C.c_int64()
+    check(lib().xtg_filter_count(C.byref(ex), C.byref(c), _sh(stream)))
+    return c.value
+
+
+def filter(e, cond, out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:  # noqa: A001
+    """Read xt::filter(e, cond): the elements of e where cond holds, in
+    row-major order (1-D)."""
+    e, cond = as_expr(e), as_expr(cond)
+    if out is None:
+        out = DeviceArray.empty((filter_count(cond, stream),), expr_dtype(e), stream)
+    ex, k1 = lower(e)
+    cx, k2 = lower(cond)
+    o = out.xtg_array()
+    check(lib().xtg_filter(C.byref(ex), C.byref(cx), C.byref(o), _sh(stream)))
+    return out
+
+
+def filter_assign(dst: DeviceArray, cond, src, op: str = "=", stream=None) -> DeviceArray:
+    """Assign through xt::filter(dst, cond) (src 1-D of the selected count)
+    or xt::filtration(dst, cond) (src a scalar)."""
+    sx, k1 = lower(as_expr(src))
+    cx, k2 = lower(as_expr(cond))
+    o = dst.xtg_array()
+    check(lib().xtg_filter_assign(C.byref(sx), C.byref(cx), SET_OPS[op], C.byref(o), _sh(stream)))
+    return dst
+
+
+def masked_assign(dst: DeviceArray, mask, src, op: str = "=", stream=None) -> DeviceArray:
+    """Assign through xt::masked_view(dst, mask): where mask holds,
+    dst op= src (src and mask broadcast to dst)."""
+    sx, k1 = lower(as_expr(src))
+    mx, k2 = lower(as_expr(mask))
+    o = dst.xtg_array()
+    check(lib().xtg_masked_assign(C.byref(sx), C.byref(mx), SET_OPS[op], C.byref(o), _sh(stream)))
+    return dst
