@@ -668,6 +668,72 @@ def run_scan(args):
     return 0
 
 
+def run_views(args):
+    """Writes and reads through views on x float32 (256, 512, 1024) N(0,1)
+    seed 1, through the C ABI with operands resident in HBM:
+    masked_view(x, m) += 1.5 (m bool, ~50% true); filter(y, y > 1) (read,
+    1-D result); filtration(z, y > 1) *= 0.5; index_view(x, idx) read and
+    += 1 for 2^24 random distinct coordinates.  Algorithmic bytes: what the
+    call must read and write (the mask, the selected elements, the
+    coordinates and the gathered values; the filter reads x once for the
+    condition and once for the values)."""
+    import xtensor_gb300 as xg
+    from xtensor_gb300 import ops
+    from xtensor_gb300._ffi import check
+    from xtensor_gb300.device import DeviceArray
+    lib = xg.lib()
+    g = np.random.default_rng(1)
+    x = g.standard_normal(SHAPE, dtype=np.float32)
+    m = g.random(SHAPE) < 0.5
+    nidx = 1 << 24
+    flat = g.choice(N, nidx, replace=False)
+    idx = np.stack(np.unravel_index(flat, SHAPE), 1).astype(np.int64)
+    dx, dm, di = DeviceArray.from_numpy(x), DeviceArray.from_numpy(m), DeviceArray.from_numpy(idx)
+    # the filters select on y (never written), so the selected count is fixed
+    dy, dz = DeviceArray.from_numpy(x), DeviceArray.from_numpy(x)
+    sel = int((x > 1).sum())
+    gout = DeviceArray.empty((nidx,), "float32")
+    fout = DeviceArray.empty((sel,), "float32")
+    calls = [
+        ("masked_add", N * 4 * 2 + N, lambda: ops.masked_assign(dx, dm, 1.5, "+=")),
+        ("filter_read", 2 * N * 4 + sel * 4, lambda: ops.filter(dy, dy > 1, out=fout)),
+        ("filtration_mul", N * 4 + 2 * sel * 4, lambda: ops.filter_assign(dz, dy > 1, 0.5, "*=")),
+        ("index_read", nidx * 24 + 2 * nidx * 4, lambda: ops.index_view(dx, di, out=gout)),
+        ("index_add", nidx * 24 + 2 * nidx * 4, lambda: ops.index_assign(dx, di, 1.0, "+=")),
+    ]
+    for _ in range(args.warmup):
+        for _, _, fn in calls:
+            fn()
+    check(lib.xtg_device_sync())
+    evs = [ev_create(lib, len(calls) + 1) for _ in range(args.steps)]
+    for k in range(args.steps):
+        for i, (_, _, fn) in enumerate(calls):
+            check(lib.xtg_event_record(evs[k][i], None))
+            fn()
+        check(lib.xtg_event_record(evs[k][len(calls)], None))
+    check(lib.xtg_device_sync())
+    per = [sum(ev_ms(lib, evs[k][i], evs[k][i + 1]) for k in range(args.steps)) / args.steps for i in range(len(calls))]
+    peak, peak_kind = peaks()
+    total = sum(b for _, b, _ in calls)
+    step_ms = sum(per)
+    per_kernel = {nm: {"ms": round(t, 4), "GB/s": round(b / (t / 1e3) / 1e9, 1), "frac": round(b / (t / 1e3) / 1e9 / peak, 3)}
+                  for (nm, b, _), t in zip(calls, per)}
+    dom = int(np.argmax(per))
+    print(json.dumps({
+        "metric": "HBM GB/s (frac of roofline) of reads and writes through index / filter / masked views",
+        "unit": "GB/s", "value": round(total / (step_ms / 1e3) / 1e9, 3), "higher_is_better": True, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4), "dtype": "f32",
+        "data": "synthetic", "config": {"workload": "views on x f32 (256,512,1024): masked +=, filter, filtration *=, "
+                                                    "index_view read / += over 2^24 coordinates",
+                                        "algorithmic_bytes_per_step": total, "selected": sel},
+        "roofline": {"bound": "hbm", "kernel": calls[dom][0], "achieved": per_kernel[calls[dom][0]]["GB/s"],
+                     "peak": peak, "unit": "GB/s", "frac": per_kernel[calls[dom][0]]["frac"],
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "per_kernel": per_kernel,
+    }))
+    return 0
+
+
 def c4_pool(n_templates, seed=4):
     """Request templates of the serving mix: kinds of the four configurations,
     element counts log-uniform in [1e3, 1e8], dtypes float32/float64/int32 at
@@ -853,7 +919,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--shape", default=None, help="profiling only: d0,d1,d2 instead of 256,512,1024")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4", "scan"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4", "scan", "views"],
                     help="c1: strided/axis work (default, the headline); c3: batching of uneven instances; "
                          "c4: served Poisson request mix; scan: cumsum along rows, columns and flattened")
     ap.add_argument("--instances", type=int, default=4096)
@@ -878,6 +944,8 @@ def main():
     build()
     if args.workload == "scan":
         return run_scan(args)
+    if args.workload == "views":
+        return run_views(args)
     return run_gpu(args)
 
 

@@ -5,6 +5,7 @@
 // trees (xfunction), xt::sum / prod / amax / amin / mean / variance /
 // stddev / norm_* with axes, keep_dims, initial and evaluation_strategy,
 // xt::argmax / argmin, xt::cumsum / cumprod / nancumsum / nancumprod,
+// xt::index_view / filter / filtration / masked_view (read and write),
 // xt::transpose / strided views / xt::view slices,
 // xt::noalias, xt::eval.  Containers live in device memory; assigning an
 // expression lowers its template tree to the C ABI (include/xtg.h) and one
@@ -474,18 +475,31 @@ public:
 
     // host copies
     std::vector<T> to_host() const {
-        std::vector<T> h(m_size);
-        if (m_size) {
-            detail::check(xtg_memcpy(h.data(), data(), m_size * sizeof(T), XTG_MEMCPY_D2H, detail::current_stream()));
-            detail::check(xtg_stream_sync(detail::current_stream()));
+        if constexpr (std::is_same<T, bool>::value) {  // std::vector<bool> packs bits: go through bytes
+            std::vector<unsigned char> b(m_size);
+            if (m_size) {
+                detail::check(xtg_memcpy(b.data(), data(), m_size, XTG_MEMCPY_D2H, detail::current_stream()));
+                detail::check(xtg_stream_sync(detail::current_stream()));
+            }
+            return std::vector<bool>(b.begin(), b.end());
+        } else {
+            std::vector<T> h(m_size);
+            if (m_size) {
+                detail::check(xtg_memcpy(h.data(), data(), m_size * sizeof(T), XTG_MEMCPY_D2H, detail::current_stream()));
+                detail::check(xtg_stream_sync(detail::current_stream()));
+            }
+            return h;
         }
-        return h;
     }
     void upload(const std::vector<T>& h) {
-        if (m_size) {
+        if (!m_size) return;
+        if constexpr (std::is_same<T, bool>::value) {
+            std::vector<unsigned char> b(h.begin(), h.end());
+            detail::check(xtg_memcpy(data(), b.data(), m_size, XTG_MEMCPY_H2D, detail::current_stream()));
+        } else {
             detail::check(xtg_memcpy(data(), h.data(), m_size * sizeof(T), XTG_MEMCPY_H2D, detail::current_stream()));
-            detail::check(xtg_stream_sync(detail::current_stream()));
         }
+        detail::check(xtg_stream_sync(detail::current_stream()));
     }
 
     // evaluation entry points used by the free functions
@@ -1096,6 +1110,175 @@ XTG_ACCUMULATOR(cumprod, XTG_ACC_CUMPROD, 1)
 XTG_ACCUMULATOR(nancumsum, XTG_ACC_NANCUMSUM, 0)
 XTG_ACCUMULATOR(nancumprod, XTG_ACC_NANCUMPROD, 1)
 #undef XTG_ACCUMULATOR
+
+// ---------------------------------------------------------------------------- index / filter / masked views
+// xt::index_view, xt::filter, xt::filtration, xt::masked_view
+// (include/xtensor/views/xindex_view.hpp, views/xmasked_view.hpp).  Reading a
+// view evaluates it (a gather); writing through it (=, +=, -=, *=, /= with an
+// expression or a scalar) writes the selected elements of the underlying
+// container or strided view.
+namespace detail {
+// an lvalue operand is referenced, a temporary expression kept by value
+template <class E> using view_closure_t = std::conditional_t<std::is_lvalue_reference<E>::value, E, std::decay_t<E>>;
+inline std::shared_ptr<device_buffer> upload_indices(const std::vector<std::vector<std::size_t>>& idx, std::size_t rank) {
+    std::vector<int64_t> h;
+    h.reserve(idx.size() * rank);
+    for (const auto& r : idx) {
+        if (r.size() != rank) throw std::out_of_range("index_view: coordinate rank differs from the expression's");
+        for (auto v : r) h.push_back((int64_t)v);
+    }
+    auto b = std::make_shared<device_buffer>(h.size() * sizeof(int64_t));
+    if (!h.empty()) check(xtg_memcpy(b->ptr, h.data(), h.size() * sizeof(int64_t), XTG_MEMCPY_H2D, current_stream()));
+    return b;
+}
+template <class V> struct rhs_lowering {
+    lowering L;
+    std::shared_ptr<void> keep;
+    template <class E, std::enable_if_t<is_xexpression<E>::value, int> = 0> explicit rhs_lowering(const E& e) { e.lower(L); }
+    template <class S, std::enable_if_t<std::is_arithmetic<S>::value, int> = 0> explicit rhs_lowering(S v) {
+        xscalar<V>((V)v).lower(L);
+    }
+};
+template <class E> int32_t rank_of(const E& e) {
+    lowering L;
+    e.lower(L);
+    int32_t r = 0;
+    int64_t sh[XTG_MAX_RANK];
+    check(xtg_broadcast_shape(&L.e, &r, sh));
+    return r;
+}
+}  // namespace detail
+
+template <class CT> class xindex_view {
+public:
+    using expression_type = std::decay_t<CT>;
+    using value_type = typename expression_type::value_type;
+    template <class E> xindex_view(E&& e, std::vector<std::vector<std::size_t>> idx) : m_e(std::forward<E>(e)) {
+        m_rank = (std::size_t)detail::rank_of(m_e);
+        m_n = idx.size();
+        m_idx = detail::upload_indices(idx, m_rank);
+    }
+    std::vector<std::size_t> shape() const { return {m_n}; }
+    std::size_t size() const { return m_n; }
+    xarray<value_type> eval() const {
+        detail::lowering L;
+        m_e.lower(L);
+        xarray<value_type> out(std::vector<std::size_t>{m_n});
+        xtg_array o = out.xtg_desc();
+        detail::check(xtg_gather(&L.e, (const int64_t*)m_idx->ptr, (int64_t)m_n, &o, detail::current_stream()));
+        return out;
+    }
+    operator xarray<value_type>() const { return eval(); }
+    value_type operator()(std::size_t i) const { return eval()(i); }
+    template <class R> xindex_view& operator=(const R& r) { return apply(r, XTG_SET); }
+    template <class R> xindex_view& operator+=(const R& r) { return apply(r, XTG_SET_ADD); }
+    template <class R> xindex_view& operator-=(const R& r) { return apply(r, XTG_SET_SUB); }
+    template <class R> xindex_view& operator*=(const R& r) { return apply(r, XTG_SET_MUL); }
+    template <class R> xindex_view& operator/=(const R& r) { return apply(r, XTG_SET_DIV); }
+
+private:
+    template <class R> xindex_view& apply(const R& r, int op) {
+        if constexpr (!is_xexpression<R>::value && !std::is_arithmetic<R>::value) {
+            auto v = r.eval();  // another view on the right: evaluate it first
+            return apply(v, op);
+        } else {
+            detail::rhs_lowering<value_type> rl(r);
+            xtg_array d = m_e.xtg_desc();
+            detail::check(
+                xtg_scatter(&rl.L.e, (const int64_t*)m_idx->ptr, (int64_t)m_n, op, &d, detail::current_stream()));
+            return *this;
+        }
+    }
+    CT m_e;
+    std::size_t m_rank = 0, m_n = 0;
+    std::shared_ptr<detail::device_buffer> m_idx;
+};
+template <class E> inline auto index_view(E&& e, std::vector<std::vector<std::size_t>> idx) {
+    return xindex_view<detail::view_closure_t<E>>(std::forward<E>(e), std::move(idx));
+}
+
+// filter(e, cond): a 1-D view of the elements where cond holds (row-major)
+template <class CT, class CC> class xfilter_view {
+public:
+    using expression_type = std::decay_t<CT>;
+    using value_type = typename expression_type::value_type;
+    template <class E, class C> xfilter_view(E&& e, C&& c) : m_e(std::forward<E>(e)), m_c(std::forward<C>(c)) {}
+    std::size_t size() const {
+        detail::lowering C;
+        m_c.lower(C);
+        int64_t n = 0;
+        detail::check(xtg_filter_count(&C.e, &n, detail::current_stream()));
+        return (std::size_t)n;
+    }
+    xarray<value_type> eval() const {
+        detail::lowering L, C;
+        m_e.lower(L);
+        m_c.lower(C);
+        xarray<value_type> out(std::vector<std::size_t>{size()});
+        xtg_array o = out.xtg_desc();
+        detail::check(xtg_filter(&L.e, &C.e, &o, detail::current_stream()));
+        return out;
+    }
+    operator xarray<value_type>() const { return eval(); }
+    value_type operator()(std::size_t i) const { return eval()(i); }
+    template <class R> xfilter_view& operator=(const R& r) { return apply(r, XTG_SET); }
+    template <class R> xfilter_view& operator+=(const R& r) { return apply(r, XTG_SET_ADD); }
+    template <class R> xfilter_view& operator-=(const R& r) { return apply(r, XTG_SET_SUB); }
+    template <class R> xfilter_view& operator*=(const R& r) { return apply(r, XTG_SET_MUL); }
+    template <class R> xfilter_view& operator/=(const R& r) { return apply(r, XTG_SET_DIV); }
+    void fill(value_type v) { apply(v, XTG_SET); }
+
+private:
+    template <class R> xfilter_view& apply(const R& r, int op) {
+        if constexpr (!is_xexpression<R>::value && !std::is_arithmetic<R>::value) {
+            auto v = r.eval();  // another view on the right: evaluate it first
+            return apply(v, op);
+        } else {
+            detail::rhs_lowering<value_type> rl(r);
+            detail::lowering C;
+            m_c.lower(C);
+            xtg_array d = m_e.xtg_desc();
+            detail::check(xtg_filter_assign(&rl.L.e, &C.e, op, &d, detail::current_stream()));
+            return *this;
+        }
+    }
+    CT m_e;
+    CC m_c;
+};
+template <class E, class C> inline auto filter(E&& e, C&& c) {
+    return xfilter_view<detail::view_closure_t<E>, detail::view_closure_t<C>>(std::forward<E>(e), std::forward<C>(c));
+}
+// filtration(e, cond): scalar and computed scalar assignment to the selected elements
+template <class E, class C> inline auto filtration(E&& e, C&& c) { return filter(std::forward<E>(e), std::forward<C>(c)); }
+
+template <class CT, class CM> class xmasked_view {
+public:
+    using expression_type = std::decay_t<CT>;
+    using value_type = typename expression_type::value_type;
+    template <class E, class M> xmasked_view(E&& e, M&& m) : m_e(std::forward<E>(e)), m_m(std::forward<M>(m)) {}
+    template <class R> xmasked_view& operator=(const R& r) { return apply(r, XTG_SET); }
+    template <class R> xmasked_view& operator+=(const R& r) { return apply(r, XTG_SET_ADD); }
+    template <class R> xmasked_view& operator-=(const R& r) { return apply(r, XTG_SET_SUB); }
+    template <class R> xmasked_view& operator*=(const R& r) { return apply(r, XTG_SET_MUL); }
+    template <class R> xmasked_view& operator/=(const R& r) { return apply(r, XTG_SET_DIV); }
+    void fill(value_type v) { apply(v, XTG_SET); }
+
+private:
+    template <class R> xmasked_view& apply(const R& r, int op) {
+        static_assert(is_xexpression<R>::value || std::is_arithmetic<R>::value, "masked_view: assign an expression or a scalar");
+        detail::rhs_lowering<value_type> rl(r);
+        detail::lowering M;
+        m_m.lower(M);
+        xtg_array d = m_e.xtg_desc();
+        detail::check(xtg_masked_assign(&rl.L.e, &M.e, op, &d, detail::current_stream()));
+        return *this;
+    }
+    CT m_e;
+    CM m_m;
+};
+template <class E, class M> inline auto masked_view(E&& e, M&& m) {
+    return xmasked_view<detail::view_closure_t<E>, detail::view_closure_t<M>>(std::forward<E>(e), std::forward<M>(m));
+}
 
 // ---------------------------------------------------------------------------- builders
 template <class T, class S> inline xarray<T> ones(const S& s) { return xarray<T>(std::vector<std::size_t>(std::begin(s), std::end(s)), T(1)); }

@@ -330,6 +330,48 @@ TEST(xaccumulator, one_d_dim_one_cumprod_empty) {
     EXPECT_TRUE(threw);
 }
 
+// test_xindex_view.cpp:24-57, 68-86, 140-165 and test_xmasked_view.cpp:189-256
+TEST(xviews, index_filter_masked) {
+    xarray<double> e = {{0., 1., 2.}, {3., 4., 5.}, {6., 7., 8.}};
+    auto v = index_view(e, {{1, 1}, {1, 2}, {2, 2}});
+    EXPECT_EQ(v(0), 4.);
+    v += 3;
+    EXPECT_EQ((double)e(1, 1), 7.);
+    v = 123.;
+    EXPECT_EQ((double)e(1, 2), 123.);
+    xarray<double> as = {3, 3, 3};
+    v = as;
+    EXPECT_EQ((double)e(2, 2), 3.);
+
+    xarray<double> f = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    auto fv = filter(f, f > 0.);
+    EXPECT_EQ(fv(0), 1.);
+    fv += 2;
+    EXPECT_EQ((double)f(1, 1), 3.);
+    fv += xarray<double>{1, 2, 3};
+    EXPECT_EQ((double)f(1, 1), 5.);
+    EXPECT_EQ((double)f(2, 2), 6.);
+
+    xarray<double> a = {{1, 5, 3}, {4, 5, 6}};
+    filtration(a, a >= 5.) += 2;
+    xarray<double> ea = {{1, 7, 3}, {4, 7, 8}};
+    EXPECT_EQ(a, ea);
+    xarray<double> a2 = {{1, 5, 3}, {4, 5, 6}};
+    const xarray<double> b = {{1, 5, 3}, {4, 5, 6}};
+    filter(a2, a2 > 3.) += filter(b, b > 3.);
+    xarray<double> ea2 = {{1, 10, 3}, {8, 10, 12}};
+    EXPECT_EQ(a2, ea2);
+
+    xarray<double> data = {{1., -2., 3.}, {4., 5., -6.}, {7., 8., -9.}};
+    xarray<bool> mask = {{true, true, true}, {true, false, false}, {true, false, true}};
+    masked_view(data, mask) = 3.65;
+    xarray<double> e1 = {{3.65, 3.65, 3.65}, {3.65, 5., -6.}, {3.65, 8., 3.65}};
+    EXPECT_EQ(data, e1);
+    masked_view(data, mask) += 3.;
+    xarray<double> e2 = {{6.65, 6.65, 6.65}, {6.65, 5., -6.}, {6.65, 8., 6.65}};
+    EXPECT_EQ(data, e2);
+}
+
 int main() {
     for (auto& t : registry()) {
         const int before = g_fail;
