@@ -1725,12 +1725,6 @@ __global__ void __launch_bounds__(256) k_indexed(const IndexParams p) {
                 continue;
             }
             j = k;
-        } else {
-            const long long cur = p.idx[k];
-            const long long prev = k ? p.idx[k - 1] : 0;
-            if (cur == prev) continue;  // not selected
-            j = cur - 1;
-            decode_dims<R, true>(p.shape, p.fd, k, ix);
         }
         i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
 #pragma unroll
@@ -1763,6 +1757,139 @@ __global__ void __launch_bounds__(256) k_indexed(const IndexParams p) {
                 dst[o] = cvt<DT>(r);
             }
         }
+    }
+}
+
+// K11: filters — xt::filter(e, cond) reads and filter / filtration writes
+// (include/xtensor/views/xindex_view.hpp:786-850).  Thread th of a tile owns
+// the 16 consecutive positions t*4096 + 16 th .. + 15, so the selected
+// elements come out in row-major order: (A) count per tile, (B) an
+// inclusive scan of the counts (the accumulator kernels), (C) every tile
+// again, each selected element to tile offset + its rank in the tile.
+template <class Tree, class LS, int R, bool BIG>
+XTG_DI bool filter_cond(const FilterParams& p, const Ctx<0>& c, i64 k, i64 (&ix)[R]) {
+    typedef typename LS::template R<1>::type RG;
+    decode_dims<R, BIG>(p.shape, p.fd, k, ix);
+    i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
+#pragma unroll
+    for (int l = 0; l < LS::N; ++l) {
+        i64 o = 0;
+#pragma unroll
+        for (int d = 0; d < R; ++d) o += ix[d] * p.cls[l][d];
+        off[l] = o;
+        inner[l] = 0;
+    }
+    RG rg;
+    LoadLeavesAt<LS>::template run<1>(rg, p.cleaf, off, inner);
+    return Tree::ev(rg, 0, c) != typename Tree::type(0);
+}
+
+template <class CTree, class CLS, int R, bool BIG>
+__global__ void __launch_bounds__(256) k_filter_count(const FilterParams p) {
+    __shared__ int ws[8];
+    Ctx<0> c;
+    c.scal = p.cscal;
+    const i64 ntiles = (p.n + 4095) / 4096;
+    for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        int cnt = 0;
+        const i64 k0 = t * 4096 + (i64)threadIdx.x * 16;
+#pragma unroll 4
+        for (int i = 0; i < 16; ++i) {
+            const i64 k = k0 + i;
+            i64 ix[R];
+            if (k < p.n && filter_cond<CTree, CLS, R, BIG>(p, c, k, ix)) ++cnt;
+        }
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int s = 0;
+            for (int w = 0; w < 8; ++w) s += ws[w];
+            p.tcount[t] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// MODE 0: out[j] = e[position]; MODE 1: dst[position] = dst op src[j]
+template <class CTree, class CLS, class VTree, class VLS, class VT, class DT, class CT, int MODE, int R, int OP, bool BIG>
+__global__ void __launch_bounds__(256) k_filter_tile(const FilterParams p) {
+    typedef typename VLS::template R<1>::type VRG;
+    __shared__ int ws[9];
+    Ctx<0> cc, vc;
+    cc.scal = p.cscal;
+    vc.scal = p.vscal;
+    const i64 ntiles = (p.n + 4095) / 4096;
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const i64 k0 = t * 4096 + (i64)threadIdx.x * 16;
+        unsigned flags = 0;
+#pragma unroll 4
+        for (int i = 0; i < 16; ++i) {
+            const i64 k = k0 + i;
+            i64 ix[R];
+            if (k < p.n && filter_cond<CTree, CLS, R, BIG>(p, cc, k, ix)) flags |= 1u << i;
+        }
+        // exclusive prefix of the thread counts in thread order
+        const int cnt = __popc(flags);
+        int inc = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, d);
+            if (lane >= d) inc += y;
+        }
+        if (lane == 31) ws[warp] = inc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int s = 0;
+            for (int w = 0; w < 8; ++w) {
+                const int v = ws[w];
+                ws[w] = s;
+                s += v;
+            }
+        }
+        __syncthreads();
+        i64 j = (t ? (i64)p.tincl[t - 1] : 0) + ws[warp] + (inc - cnt);
+        while (flags) {
+            const int i = __ffs(flags) - 1;
+            flags &= flags - 1;
+            const i64 k = k0 + i;
+            i64 ix[R];
+            decode_dims<R, BIG>(p.shape, p.fd, k, ix);
+            i64 off[XTG_KMAX_LEAVES], inner[XTG_KMAX_LEAVES];
+#pragma unroll
+            for (int l = 0; l < VLS::N; ++l) {
+                inner[l] = 0;
+                if (MODE == 0) {
+                    i64 o = 0;
+#pragma unroll
+                    for (int d = 0; d < R; ++d) o += ix[d] * p.vls[l][d];
+                    off[l] = o;
+                } else {
+                    off[l] = j * p.vls[l][0];
+                }
+            }
+            VRG rg;
+            LoadLeavesAt<VLS>::template run<1>(rg, p.vleaf, off, inner);
+            const VT v = cvt<VT>(VTree::ev(rg, 0, vc));
+            DT* dst = reinterpret_cast<DT*>(p.dst);
+            if (MODE == 0) {
+                dst[j * p.ds[0]] = cvt<DT>(v);
+            } else {
+                i64 o = 0;
+#pragma unroll
+                for (int d = 0; d < R; ++d) o += ix[d] * p.ds[d];
+                if (OP == 0) {
+                    dst[o] = cvt<DT>(v);
+                } else {
+                    const CT a = cvt<CT>(dst[o]), b = cvt<CT>(v);
+                    const CT r = OP == 1 ? CT(a + b) : OP == 2 ? CT(a - b) : OP == 3 ? CT(a * b) : CT(a / b);
+                    dst[o] = cvt<DT>(r);
+                }
+            }
+            ++j;
+        }
+        __syncthreads();
     }
 }
 

@@ -137,6 +137,24 @@ struct IndexParams {
     int* err;                                   // set when a coordinate is outside the shape
 };
 
+// Filters by tiles of 4096 row-major positions: the condition tree (c*) and
+// the value tree (v*: the filtered expression, or the 1-D values assigned)
+// with their own leaves and scalars.
+struct FilterParams {
+    i64 n;                                      // positions in the filtered shape
+    i64 shape[XTG_KMAX_RANK];
+    FastDiv fd[XTG_KMAX_RANK];
+    const void* cleaf[XTG_KMAX_LEAVES];
+    i64 cls[XTG_KMAX_LEAVES][XTG_KMAX_RANK];    // condition leaf strides over the shape
+    const void* vleaf[XTG_KMAX_LEAVES];
+    i64 vls[XTG_KMAX_LEAVES][XTG_KMAX_RANK];    // value leaves: over the shape (read) or dim 0 (assign)
+    void* dst;
+    i64 ds[XTG_KMAX_RANK];                      // out stride in ds[0] (read) or dst strides (assign)
+    Scalars cscal, vscal;
+    int* tcount;                                // selected per tile
+    const long long* tincl;                     // inclusive selected count per tile
+};
+
 // Batched evaluation: many instances of one expression shape, each a 2-D
 // (rows, cols) space with its own pointers and strides.
 struct BatchInst {

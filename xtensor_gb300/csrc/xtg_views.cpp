@@ -8,10 +8,10 @@
 //    and written at the same positions);
 //  * index_view reads are a gather and writes a scatter over a device list of
 //    coordinates (K10 k_indexed, coordinates checked on the device);
-//  * filter(e, cond) and filtration(dst, cond) take P = the inclusive count
-//    of cond in row-major order (a cumsum of the condition as int64, the
-//    accumulator kernels), then element i is selected when P[i] > P[i-1] and
-//    lands at P[i] - 1 — the order of argwhere (xindex_view.hpp:821-826).
+//  * filter(e, cond) and filtration(dst, cond) run by tiles of 4096
+//    row-major positions: per-tile counts of cond, their inclusive scan, then
+//    each tile's selected elements go to the tile's offset plus their rank
+//    in the tile — the order of argwhere (xindex_view.hpp:821-826).
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -94,55 +94,112 @@ bool same_shape(const Tree& t, const xtg_array& a) {
     return true;
 }
 
-// the inclusive count of cond over `shape` (row-major) into a temporary
-xtg_status positions(const xtg_expr* cond, int rank, const int64_t* shape, void** P, int64_t* total,
-                     cudaStream_t stream) {
+// Filters run by tiles of 4096 row-major positions: per-tile counts of the
+// condition (K11 k_filter_count), their inclusive scan (the accumulator
+// kernels, int64), then the compaction / write kernel.  FilterRun holds the
+// scratch (counts + scan) and the condition's part of the parameters.
+struct FilterRun {
+    xtg::FilterParams p;
     Tree tc;
-    XTG_TRY(build_tree(cond, false, tc));
-    if (tc.rank != rank) return fail(XTG_ERR_SHAPE, "condition shape differs from the filtered expression's");
+    void* scratch = nullptr;
+    int64_t ntiles = 0;
+    bool big = false;
+    std::string ctree, cls;
+};
+
+xtg_status filter_prepare(const xtg_expr* cond, int rank, const int64_t* shape, FilterRun& F, cudaStream_t stream) {
+    XTG_TRY(build_tree(cond, false, F.tc));
+    if (F.tc.n_rstats) return fail(XTG_ERR_UNSUPPORTED, "row statistics inside a filter condition");
+    if (F.tc.rank != rank) return fail(XTG_ERR_SHAPE, "condition shape differs from the filtered expression's");
     for (int d = 0; d < rank; ++d)
-        if (tc.shape[d] != shape[d]) return fail(XTG_ERR_SHAPE, "condition shape differs from the filtered expression's");
+        if (F.tc.shape[d] != shape[d]) return fail(XTG_ERR_SHAPE, "condition shape differs from the filtered expression's");
+    memset(&F.p, 0, sizeof F.p);
     int64_t n = 1;
-    for (int d = 0; d < rank; ++d) n *= shape[d];
-    *total = n;
-    xtg_expr c64;
-    memset(&c64, 0, sizeof c64);
-    XTG_TRY(append_expr(c64, cond));
-    {
-        // cast(cond != 0, int64)
-        xtg_node z;
-        memset(&z, 0, sizeof z);
-        z.op = XTG_OP_SCALAR;
-        z.dtype = XTG_INT32;
-        z.imm.i = 0;
-        if (c64.n_nodes + 3 > XTG_MAX_NODES) return fail(XTG_ERR_UNSUPPORTED, "condition expression is too large");
-        c64.nodes[c64.n_nodes++] = z;
-        XTG_TRY(push_op(c64, XTG_OP_NE));
-        XTG_TRY(push_op(c64, XTG_OP_CAST, XTG_INT64));
+    for (int d = 0; d < rank; ++d) {
+        n *= shape[d];
+        F.p.shape[d] = shape[d];
+        F.p.fd[d] = make_fd((uint64_t)std::max<int64_t>(shape[d], 1));
     }
-    XTG_TRY(scratch_alloc(P, (size_t)std::max<int64_t>(n, 1) * 8, stream));
-    xtg_array pa;
-    memset(&pa, 0, sizeof pa);
-    pa.data = *P;
-    pa.dtype = XTG_INT64;
-    pa.rank = 1;
-    pa.shape[0] = n;
-    pa.strides[0] = 1;
-    xtg_status st = n ? accumulate_call(&c64, XTG_ACC_CUMSUM, 0, 0, XTG_INT64, &pa, stream) : XTG_OK;
-    if (st != XTG_OK) scratch_free(*P, stream);
-    return st;
+    F.p.n = n;
+    F.big = n > 0xFFFFFFF0ll;
+    const int NL = (int)F.tc.leaves.size();
+    for (int l = 0; l < NL; ++l) {
+        F.p.cleaf[l] = F.tc.leaves[l].data;
+        bstrides_to(F.tc.leaves[l], rank, shape, reinterpret_cast<int64_t*>(F.p.cls[l]));
+    }
+    for (size_t i = 0; i < F.tc.scalars.size(); ++i) F.p.cscal.v[i] = F.tc.scalars[i];
+    std::vector<int> map(NL);
+    for (int l = 0; l < NL; ++l) map[l] = l;
+    F.ctree = tree_type(F.tc, F.tc.root, map);
+    F.cls = leafset_of(F.tc);
+    F.ntiles = (n + 4095) / 4096;
+    if (F.ntiles == 0) return XTG_OK;
+    // scratch: int32 counts, then int64 inclusive counts
+    const size_t cbytes = (size_t)((F.ntiles * 4 + 15) / 16 * 16);
+    XTG_TRY(scratch_alloc(&F.scratch, cbytes + (size_t)F.ntiles * 8, stream));
+    F.p.tcount = (int*)F.scratch;
+    F.p.tincl = (const long long*)((char*)F.scratch + cbytes);
+    if (recorder()) recorder()->nocache = true;  // scratch addresses are baked into several parameter blocks
+    Kernel* k;
+    XTG_TRY(get_kernel("xtg::k_filter_count<" + F.ctree + ", " + F.cls + ", " + std::to_string(rank) + ", " +
+                           (F.big ? "true" : "false") + ">",
+                       256, &k));
+    XTG_TRY(launch(k, grid_n(k, F.ntiles * 256), 256, &F.p, stream));
+    // inclusive scan of the int32 counts into int64
+    xtg_expr ce;
+    memset(&ce, 0, sizeof ce);
+    xtg_array ca;
+    memset(&ca, 0, sizeof ca);
+    ca.data = F.scratch;
+    ca.dtype = XTG_INT32;
+    ca.rank = 1;
+    ca.shape[0] = F.ntiles;
+    ca.strides[0] = 1;
+    XTG_TRY(push_leaf(ce, ca));
+    xtg_array ia = ca;
+    ia.data = (void*)F.p.tincl;
+    ia.dtype = XTG_INT64;
+    return accumulate_call(&ce, XTG_ACC_CUMSUM, 0, 0, XTG_INT64, &ia, stream);
 }
 
-xtg_status count_of(void* P, int64_t n, int64_t* count, cudaStream_t stream) {
-    if (n == 0 || dry_run()) {
+xtg_status filter_total(const FilterRun& F, int64_t* count, cudaStream_t stream) {
+    if (F.ntiles == 0 || dry_run()) {
         *count = 0;
         return XTG_OK;
     }
     long long c = 0;
-    XTG_CUDA(cudaMemcpyAsync(&c, (const long long*)P + (n - 1), 8, cudaMemcpyDeviceToHost, stream));
+    XTG_CUDA(cudaMemcpyAsync(&c, F.p.tincl + (F.ntiles - 1), 8, cudaMemcpyDeviceToHost, stream));
     XTG_CUDA(cudaStreamSynchronize(stream));
     *count = c;
     return XTG_OK;
+}
+
+xtg_status filter_launch(FilterRun& F, const Tree& tv, int mode, int op, int rank, const xtg_array& dst,
+                         cudaStream_t stream) {
+    const int NL = (int)tv.leaves.size();
+    for (int l = 0; l < NL; ++l) {
+        F.p.vleaf[l] = tv.leaves[l].data;
+        if (mode == 0) {
+            bstrides_to(tv.leaves[l], rank, reinterpret_cast<const int64_t*>(F.p.shape), reinterpret_cast<int64_t*>(F.p.vls[l]));
+        } else {
+            int64_t one = std::max<int64_t>(1, tv.rank ? tv.shape[0] : 1);
+            bstrides_to(tv.leaves[l], 1, &one, reinterpret_cast<int64_t*>(F.p.vls[l]));
+        }
+    }
+    for (size_t i = 0; i < tv.scalars.size(); ++i) F.p.vscal.v[i] = tv.scalars[i];
+    F.p.dst = dst.data;
+    for (int d = 0; d < dst.rank; ++d) F.p.ds[d] = dst.strides[d];
+    std::vector<int> map(NL);
+    for (int l = 0; l < NL; ++l) map[l] = l;
+    const int vt = tv.nodes[tv.root].dtype;
+    const int ct = promote(dst.dtype, vt);
+    std::string name = "xtg::k_filter_tile<" + F.ctree + ", " + F.cls + ", " + tree_type(tv, tv.root, map) + ", " +
+                       leafset_of(tv) + ", " + dt(vt).cname + ", " + dt(dst.dtype).cname + ", " + dt(ct).cname + ", " +
+                       std::to_string(mode) + ", " + std::to_string(rank) + ", " + std::to_string(op) + ", " +
+                       (F.big ? "true" : "false") + ">";
+    Kernel* k;
+    XTG_TRY(get_kernel(name, 256, &k));
+    return launch(k, grid_n(k, F.ntiles * 256), 256, &F.p, stream);
 }
 
 // K10 launch
@@ -250,11 +307,10 @@ xtg_status xtg_filter_count(const xtg_expr* cond, int64_t* count, xtg_stream str
     if (!count) return fail(XTG_ERR_INVALID, "null argument");
     Tree tc;
     XTG_TRY(build_tree(cond, false, tc));
-    void* P = nullptr;
-    int64_t n = 0;
-    XTG_TRY(positions(cond, tc.rank, tc.shape, &P, &n, (cudaStream_t)stream));
-    xtg_status st = count_of(P, n, count, (cudaStream_t)stream);
-    xtg_status fs = scratch_free(P, (cudaStream_t)stream);
+    FilterRun F;
+    xtg_status st = filter_prepare(cond, tc.rank, tc.shape, F, (cudaStream_t)stream);
+    if (st == XTG_OK) st = filter_total(F, count, (cudaStream_t)stream);
+    xtg_status fs = F.scratch ? scratch_free(F.scratch, (cudaStream_t)stream) : XTG_OK;
     return st != XTG_OK ? st : fs;
 }
 
@@ -265,14 +321,15 @@ xtg_status xtg_filter(const xtg_expr* e, const xtg_expr* cond, const xtg_array* 
     XTG_TRY(build_tree(e, opt("fp32_compute", 1) != 0 && out->dtype != XTG_FLOAT64, t));
     if (t.n_rstats) return fail(XTG_ERR_UNSUPPORTED, "row statistics inside a filter");
     if (t.rank < 1) return fail(XTG_ERR_INVALID, "filter of a 0-d expression");
-    void* P = nullptr;
-    int64_t n = 0, count = 0;
-    XTG_TRY(positions(cond, t.rank, t.shape, &P, &n, (cudaStream_t)stream));
-    xtg_status st = count_of(P, n, &count, (cudaStream_t)stream);
-    if (st == XTG_OK && !dry_run() && (out->rank != 1 || out->shape[0] != count))
+    if (out->rank != 1) return fail(XTG_ERR_SHAPE, "filter result must be 1-D");
+    FilterRun F;
+    xtg_status st = filter_prepare(cond, t.rank, t.shape, F, (cudaStream_t)stream);
+    int64_t count = 0;
+    if (st == XTG_OK) st = filter_total(F, &count, (cudaStream_t)stream);
+    if (st == XTG_OK && !dry_run() && out->shape[0] != count)
         st = fail(XTG_ERR_SHAPE, "filter result must be 1-D of xtg_filter_count elements");
-    if (st == XTG_OK && n) st = launch_indexed(t, 2, 0, t.rank, t.shape, (const long long*)P, n, *out, (cudaStream_t)stream);
-    xtg_status fs = scratch_free(P, (cudaStream_t)stream);
+    if (st == XTG_OK && F.ntiles) st = filter_launch(F, t, 0, 0, t.rank, *out, (cudaStream_t)stream);
+    xtg_status fs = F.scratch ? scratch_free(F.scratch, (cudaStream_t)stream) : XTG_OK;
     return st != XTG_OK ? st : fs;
 }
 
@@ -286,18 +343,16 @@ xtg_status xtg_filter_assign(const xtg_expr* src, const xtg_expr* cond, int32_t 
     if (t.n_rstats) return fail(XTG_ERR_UNSUPPORTED, "row statistics inside a filter");
     if (t.rank > 1) return fail(XTG_ERR_BROADCAST, "values assigned through a filter must be 1-D or a scalar");
     if (dst->rank < 1) return fail(XTG_ERR_INVALID, "filter of a 0-d array");
-    void* P = nullptr;
-    int64_t n = 0, count = 0;
-    XTG_TRY(positions(cond, dst->rank, dst->shape, &P, &n, (cudaStream_t)stream));
-    xtg_status st = XTG_OK;
-    if (t.rank == 1 && t.shape[0] != 1) {
-        st = count_of(P, n, &count, (cudaStream_t)stream);
+    FilterRun F;
+    xtg_status st = filter_prepare(cond, dst->rank, dst->shape, F, (cudaStream_t)stream);
+    if (st == XTG_OK && t.rank == 1 && t.shape[0] != 1) {
+        int64_t count = 0;
+        st = filter_total(F, &count, (cudaStream_t)stream);
         if (st == XTG_OK && !dry_run() && t.shape[0] != count)
             st = fail(XTG_ERR_BROADCAST, "assigned values do not match the filter's length");
     }
-    if (st == XTG_OK && n)
-        st = launch_indexed(t, 3, op, dst->rank, dst->shape, (const long long*)P, n, *dst, (cudaStream_t)stream);
-    xtg_status fs = scratch_free(P, (cudaStream_t)stream);
+    if (st == XTG_OK && F.ntiles) st = filter_launch(F, t, 1, op, dst->rank, *dst, (cudaStream_t)stream);
+    xtg_status fs = F.scratch ? scratch_free(F.scratch, (cudaStream_t)stream) : XTG_OK;
     return st != XTG_OK ? st : fs;
 }
 
