@@ -910,6 +910,169 @@ def run_c4(args):
     return 0
 
 
+def _npy_dir(need: int) -> str:
+    import shutil
+    import tempfile
+    for d in ("/dev/shm", tempfile.gettempdir()):
+        try:
+            if os.path.isdir(d) and shutil.disk_usage(d).free > 3 * need:
+                return tempfile.mkdtemp(prefix="xtg_npy_", dir=d)
+        except OSError:
+            continue
+    return tempfile.mkdtemp(prefix="xtg_npy_")
+
+
+def run_npy(args):
+    """.npy I/O workload (xt::dump_npy / xt::load_npy): x float32
+    (256, 512, 1024) N(0,1) seed 1, 512 MiB.  Per step: dump_npy(path, x)
+    from device memory; load_npy(path) into a row-major device array; the same
+    values in a Fortran-order file loaded into a row-major array (reordered on
+    the device); load_npy of the in-memory file image (pageable bytes).  The
+    files sit in the page cache (tmpfs when it has room).  Bytes per call: the
+    array's 512 MiB.  Timer: host wall clock (each call returns once the
+    bytes have landed).  The link bound beside it: one cudaMemcpyAsync of the
+    same bytes from / to pinned host memory, timed here.  CPU baseline: the
+    reference's own load / dump path (one read into a heap buffer / one
+    write), compiled port in oracle/xt_baseline.c, single thread as the
+    reference's stream I/O."""
+    import shutil
+    import xtensor_gb300 as xg
+    from xtensor_gb300 import ops
+    from xtensor_gb300._ffi import check
+    from xtensor_gb300.device import DeviceArray
+    lib = xg.lib()
+    g = np.random.default_rng(1)
+    x = g.standard_normal(SHAPE, dtype=np.float32)
+    nb = x.nbytes
+    d = _npy_dir(2 * nb)
+    fc, ff = os.path.join(d, "x_c.npy"), os.path.join(d, "x_f.npy")
+    try:
+        dx = DeviceArray.from_numpy(x)
+        np.save(ff, np.asfortranarray(x))
+        out = DeviceArray.empty(SHAPE, "float32")
+        ops.dump_npy(fc, dx)
+        img = open(fc, "rb").read()
+        calls = [
+            ("dump_npy_file", lambda: ops.dump_npy(fc, dx)),
+            ("load_npy_file", lambda: ops.load_npy(fc, "float32", out=out)),
+            ("load_npy_fortran_file", lambda: ops.load_npy(ff, "float32", out=out)),
+            ("load_npy_image", lambda: ops.load_npy(img, "float32", out=out)),
+        ]
+        for _ in range(args.warmup):
+            for _, fn in calls:
+                fn()
+        check(lib.xtg_device_sync())
+        # link bound: pinned host memory <-> device, same bytes
+        hp = C.c_void_p()
+        check(lib.xtg_host_alloc(C.byref(hp), nb))
+        link = {}
+        for nm, kind, dst, src in (("h2d", 1, out.ptr, hp.value), ("d2h", 2, hp.value, dx.ptr)):
+            ts = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                check(lib.xtg_memcpy(dst, src, nb, kind, None))
+                check(lib.xtg_stream_sync(None))
+                ts.append(time.perf_counter() - t0)
+            link[nm] = nb / min(ts) / 1e9
+        check(lib.xtg_host_free(hp))
+        # host ceiling of the load side: 8 threads reading the file from the
+        # page cache into host memory, no device copy (os.preadv drops the GIL)
+        from concurrent.futures import ThreadPoolExecutor
+        hb = np.ones(nb, dtype=np.uint8)
+        fd = os.open(fc, os.O_RDONLY)
+        try:
+            ch = 8 << 20
+            offs = list(range(0, nb, ch))
+
+            def rd(o):
+                os.preadv(fd, [memoryview(hb)[o:o + min(ch, nb - o)]], 128 + o)
+            with ThreadPoolExecutor(8) as ex:
+                ts = []
+                for _ in range(3):
+                    t0 = time.perf_counter()
+                    list(ex.map(rd, offs))
+                    ts.append(time.perf_counter() - t0)
+            host_read = nb / min(ts) / 1e9
+        finally:
+            os.close(fd)
+        del hb
+        clocks = Clocks(0)
+        clocks.start()
+        time.sleep(0.15)
+        l0 = xg.jit_stats()["launches"]
+        per = {nm: [] for nm, _ in calls}
+        for _ in range(args.steps):
+            for nm, fn in calls:
+                t0 = time.perf_counter()
+                fn()
+                per[nm].append(time.perf_counter() - t0)
+        check(lib.xtg_device_sync())
+        l1 = xg.jit_stats()["launches"]
+        clk = clocks.stop()
+        np.testing.assert_array_equal(out.to_numpy()[::7, ::5, ::3], x[::7, ::5, ::3])
+        med = {nm: statistics.median(v) for nm, v in per.items()}
+        step_s = sum(med.values())
+        per_call = {}
+        for nm, t in med.items():
+            bound = link["d2h"] if nm.startswith("dump") else link["h2d"]
+            per_call[nm] = {"ms": round(t * 1e3, 2), "GB/s": round(nb / t / 1e9, 2),
+                            "frac_of_link": round(nb / t / 1e9 / bound, 3)}
+            if nm.startswith("load"):
+                per_call[nm]["frac_of_host_read"] = round(nb / t / 1e9 / host_read, 3)
+        dom = max(med, key=med.get)
+        cpu = None
+        if not args.no_cpu:
+            from oracle.oracle import SO, lib as olib
+            olib()
+            L = C.CDLL(str(SO))
+            L.bl_npy_load.restype = C.c_int64
+            L.bl_npy_load.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+            L.bl_npy_save.argtypes = [C.c_char_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
+            L.bl_free.argtypes = [C.c_void_p]
+            hdr = ops.npy_format_header("float32", SHAPE)
+            t_load, t_save = [], []
+            for _ in range(3):
+                p = C.c_void_p()
+                t0 = time.perf_counter()
+                n = L.bl_npy_load(fc.encode(), C.byref(p))
+                t_load.append(time.perf_counter() - t0)
+                assert n == nb
+                t0 = time.perf_counter()
+                assert L.bl_npy_save(fc.encode(), hdr, len(hdr), p, nb) == 0
+                t_save.append(time.perf_counter() - t0)
+                L.bl_free(p)
+            tl, tsv = statistics.median(t_load), statistics.median(t_save)
+            cpu = {"value": round(2 * nb / (tl + tsv) / 1e9, 3), "unit": "GB/s", "cores": 1, "kind": "port",
+                   "sample": "full 512 MiB file, median of 3 (port of the reference's load_npy read into a heap "
+                             f"buffer: {nb / tl / 1e9:.2f} GB/s; dump_npy write: {nb / tsv / 1e9:.2f} GB/s)"}
+        gbs = len(calls) * nb / step_s / 1e9
+        line = {
+            "metric": "GB/s of array bytes through xt::dump_npy / xt::load_npy (file or host image <-> device)",
+            "unit": "GB/s", "value": round(gbs, 3), "higher_is_better": True, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 3), "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "npy: dump_npy and load_npy of x f32 (256,512,1024) (C-order file, Fortran-order "
+                                   "file into a row-major array, in-memory image)", "bytes_per_call": nb,
+                       "files": "page cache (" + d.rsplit("/", 1)[0] + ")", "timer": "host wall clock, median"},
+            "roofline": {"bound": "link", "kernel": dom, "achieved": per_call[dom]["GB/s"],
+                         "peak": round(link["d2h"] if dom.startswith("dump") else link["h2d"], 1), "unit": "GB/s",
+                         "frac": per_call[dom]["frac_of_link"], "traffic": None,
+                         "peak_source": "measured here: one cudaMemcpyAsync of the same bytes to / from pinned host "
+                                        f"memory (h2d {link['h2d']:.1f} GB/s, d2h {link['d2h']:.1f} GB/s)",
+                         "host_read_gbs": round(host_read, 1),
+                         "host_read_source": "8 threads pread of the same file from the page cache into host memory, "
+                                             "no device copy (the load side's ceiling below the link)"},
+            "per_call": per_call, "cpu_baseline": cpu,
+            "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 3 * nb, "d2h_bytes_per_step": nb,
+                    "note": "the path is itself host <-> device: value and e2e are the same calls"},
+            "gpu_launches": int(l1 - l0), "clocks": clk,
+        }
+        print(json.dumps(line))
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -919,7 +1082,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--shape", default=None, help="profiling only: d0,d1,d2 instead of 256,512,1024")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4", "scan", "views"],
+    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4", "scan", "views", "npy"],
                     help="c1: strided/axis work (default, the headline); c3: batching of uneven instances; "
                          "c4: served Poisson request mix; scan: cumsum along rows, columns and flattened")
     ap.add_argument("--instances", type=int, default=4096)
@@ -946,6 +1109,8 @@ def main():
         return run_scan(args)
     if args.workload == "views":
         return run_views(args)
+    if args.workload == "npy":
+        return run_npy(args)
     return run_gpu(args)
 
 

@@ -28,6 +28,8 @@
 #include <cstdint>
 #include <cstring>
 #include <initializer_list>
+#include <istream>
+#include <iterator>
 #include <memory>
 #include <numeric>
 #include <ostream>
@@ -1278,6 +1280,48 @@ private:
 };
 template <class E, class M> inline auto masked_view(E&& e, M&& m) {
     return xmasked_view<detail::view_closure_t<E>, detail::view_closure_t<M>>(std::forward<E>(e), std::forward<M>(m));
+}
+
+// ---------------------------------------------------------------------------- .npy files
+// xt::load_npy<T, L> / xt::dump_npy (include/xtensor/io/xnpy.hpp:674-800):
+// the file streams through libxtg's pinned staging ring straight into the
+// device container (a Fortran-order file is reordered on the device; the
+// container keeps its row-major strides).
+#ifndef XTG_HAVE_LAYOUT_TYPE
+#define XTG_HAVE_LAYOUT_TYPE
+enum class layout_type { dynamic = 0x00, any = 0xFF, row_major = 0x01, column_major = 0x02 };
+#endif
+
+template <class T, layout_type L = layout_type::dynamic> inline xarray<T> load_npy(const std::string& filename) {
+    xtg_npy_header h;
+    detail::check(xtg_npy_info(filename.c_str(), &h));
+    xarray<T> out(std::vector<std::size_t>(h.shape, h.shape + h.rank));
+    const xtg_array a = out.xtg_desc();
+    detail::check(xtg_npy_load(filename.c_str(), &a, (int32_t)L, detail::current_stream()));
+    return out;
+}
+template <class T, layout_type L = layout_type::dynamic> inline xarray<T> load_npy(std::istream& stream) {
+    const std::string buf((std::istreambuf_iterator<char>(stream)), std::istreambuf_iterator<char>());
+    xtg_npy_header h;
+    detail::check(xtg_npy_info_buffer(buf.data(), buf.size(), &h));
+    xarray<T> out(std::vector<std::size_t>(h.shape, h.shape + h.rank));
+    const xtg_array a = out.xtg_desc();
+    detail::check(xtg_npy_load_buffer(buf.data(), buf.size(), &a, (int32_t)L, detail::current_stream()));
+    return out;
+}
+template <class E> inline void dump_npy(const std::string& filename, const xexpression<E>& e) {
+    const auto& ev = xt::eval(e.derived_cast());
+    const xtg_array a = ev.xtg_desc();
+    detail::check(xtg_npy_save(filename.c_str(), &a, detail::current_stream()));
+}
+template <class E> inline std::string dump_npy(const xexpression<E>& e) {
+    const auto& ev = xt::eval(e.derived_cast());
+    const xtg_array a = ev.xtg_desc();
+    std::size_t n = 0;
+    detail::check(xtg_npy_save_buffer(&a, nullptr, 0, &n, detail::current_stream()));
+    std::string out(n, '\0');
+    detail::check(xtg_npy_save_buffer(&a, &out[0], n, &n, detail::current_stream()));
+    return out;
 }
 
 // ---------------------------------------------------------------------------- builders

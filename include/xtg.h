@@ -30,6 +30,8 @@
  *                      (xt::accumulate, accumulator_impl)
  *                      include/xtensor/reducers/xaccumulator.hpp:154-367
  *                      include/xtensor/core/xmath.hpp:2248-2301, 2363-2391, 2592-2645
+ *   xtg_npy_*       <- xt::load_npy / xt::dump_npy (include/xtensor/io/xnpy.hpp:
+ *                      237-450, 674-800)
  *   xtg_gather / xtg_scatter, xtg_filter* , xtg_masked_assign
  *                   <- reading and assigning through xt::index_view / filter /
  *                      filtration / masked_view
@@ -281,6 +283,54 @@ xtg_status xtg_accumulate_shape(const xtg_expr* e, int32_t op, int32_t has_axis,
                                 int32_t* rank, int64_t* shape, int32_t* dtype);
 xtg_status xtg_accumulate(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis, int32_t acc_dtype,
                           const xtg_array* out, xtg_stream stream);
+
+/* ---- .npy files ----------------------------------------------------------------------------
+ * The NumPy format of the reference's load_npy / dump_npy: versions 1.0 and
+ * 2.0, typestrings |b1 |i1 |u1 <i2 <u2 <i4 <u4 <i8 <u8 <f4 <f8 on a
+ * little-endian host, C or Fortran order.  Data streams between the file (or
+ * a host buffer) and device memory through pinned staging buffers, several
+ * host threads each reading / writing its own chunks while the previous
+ * chunk is in flight over the link.
+ * Errors carry the reference's messages: XTG_ERR_INVALID for
+ * "io error: failed to open a file.", "this file do not have a valid npy
+ * format.", "unsupported file format version", "invalid header",
+ * "missing 'descr' key", "invalid typestring", "invalid shape", "Cast error:
+ * formats not matching <file> vs <requested>", "Cast error: layout mismatch
+ * between npy file and requested layout."; XTG_ERR_SHAPE for a destination
+ * whose shape differs from the file's; XTG_ERR_UNSUPPORTED for bfloat16
+ * (no NumPy typestring) and rank > XTG_MAX_RANK. */
+typedef struct {
+    char descr[16];        /* the typestring as written, e.g. "<f8" */
+    int32_t dtype;         /* the xtg_dtype written with that typestring here, -1 if none */
+    int32_t fortran_order;
+    int32_t version;       /* 1 or 2 */
+    int32_t rank;
+    int64_t shape[XTG_MAX_RANK];
+    int64_t data_offset;   /* bytes of magic, version, length and header */
+    int64_t data_bytes;    /* product of the shape times the item size */
+} xtg_npy_header;
+typedef enum { XTG_LAYOUT_DYNAMIC = 0, XTG_LAYOUT_ROW_MAJOR = 1, XTG_LAYOUT_COLUMN_MAJOR = 2 } xtg_layout;
+
+xtg_status xtg_npy_info(const char* path, xtg_npy_header* h);
+/* The header bytes dump_npy writes before the data (host only; *len gets
+ * the size, nothing written when buf is NULL). */
+xtg_status xtg_npy_format_header(int32_t dtype, int32_t fortran_order, int32_t rank, const int64_t* shape,
+                                 char* buf, size_t cap, size_t* len);
+xtg_status xtg_npy_info_buffer(const void* buf, size_t len, xtg_npy_header* h);
+/* Reads the file into `out` (device memory, the file's shape, any strides).
+ * The type check and the `layout` check are load_npy<T, L>'s, T being
+ * out->dtype. */
+xtg_status xtg_npy_load(const char* path, const xtg_array* out, int32_t layout, xtg_stream stream);
+xtg_status xtg_npy_load_buffer(const void* buf, size_t len, const xtg_array* out, int32_t layout, xtg_stream stream);
+/* Writes `in` with dump_npy's header and padding: a C-order file of its
+ * dtype and shape, or a Fortran-order one when `in` is column-major
+ * contiguous with rank > 1 and not also row-major contiguous; any other
+ * strided `in` is evaluated into a row-major copy first.  Both return after
+ * the bytes are in the file / buffer. */
+xtg_status xtg_npy_save(const char* path, const xtg_array* in, xtg_stream stream);
+/* *len receives the size of the whole file image; nothing is written when
+ * buf is NULL; cap < *len is XTG_ERR_INVALID. */
+xtg_status xtg_npy_save_buffer(const xtg_array* in, void* buf, size_t cap, size_t* len, xtg_stream stream);
 
 /* ---- index, filter and masked views ----------------------------------------------------
  * Assignment operators for writes through a view: dst = op(dst, value). */

@@ -32,9 +32,18 @@
  *                       walking the storage with the axis stride
  *                       (xaccumulator.hpp:233-281); axis = -1 flattens
  *                       (:283-310).  The copy is fused into the first pass.
+ *   bl_npy_load         xt::load_npy<T>(filename): read the magic and version,
+ *                       the header length and the header, take the word
+ *                       size from 'descr' and the shape from 'shape', then
+ *                       read the whole data block into one heap buffer with
+ *                       one read (xnpy.hpp:674-705, 540-566).
+ *   bl_npy_save         xt::dump_npy(filename, e) of an evaluated container:
+ *                       write the header, then the data with one write
+ *                       (xnpy.hpp:707-742).
  */
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -166,3 +175,63 @@ int64_t bl_sum_i32_i64(const int32_t* x, int64_t n) {
 DEF_CUMSUM(float, f32)
 DEF_CUMSUM(double, f64)
 DEF_CUMSUM(int32_t, i32)
+
+
+/* Returns the data bytes read into *out (malloc'd; free with bl_free), -1 on error. */
+int64_t bl_npy_load(const char* path, void** out) {
+    FILE* f = fopen(path, "rb");
+    if (!f) return -1;
+    unsigned char pre[8];
+    int64_t res = -1;
+    char* header = NULL;
+    if (fread(pre, 1, 8, f) != 8 || memcmp(pre, "\x93NUMPY", 6) != 0) goto done;
+    unsigned char lb[4] = {0, 0, 0, 0};
+    const size_t nl = pre[6] == 1 ? 2 : 4;
+    if (fread(lb, 1, nl, f) != nl) goto done;
+    const size_t hl = (size_t)lb[0] | (size_t)lb[1] << 8 | (size_t)lb[2] << 16 | (size_t)lb[3] << 24;
+    header = (char*)malloc(hl + 1);
+    if (!header || fread(header, 1, hl, f) != hl) goto done;
+    header[hl] = 0;
+    const char* d = strstr(header, "'descr'");
+    const char* sh = strstr(header, "'shape'");
+    if (!d || !sh) goto done;
+    d = strchr(d + 7, '\'');
+    if (!d) goto done;
+    const int64_t word = strtoll(d + 3, NULL, 10);
+    const char* p = strchr(sh, '(');
+    if (!p) goto done;
+    int64_t n = 1;
+    for (++p; *p && *p != ')';) {
+        char* e;
+        const long long v = strtoll(p, &e, 10);
+        if (e == p) {
+            ++p;
+            continue;
+        }
+        n *= v;
+        p = e;
+    }
+    const int64_t bytes = n * word;
+    void* buf = malloc(bytes > 0 ? (size_t)bytes : 1);
+    if (!buf) goto done;
+    if ((int64_t)fread(buf, 1, (size_t)bytes, f) != bytes) {
+        free(buf);
+        goto done;
+    }
+    *out = buf;
+    res = bytes;
+done:
+    free(header);
+    fclose(f);
+    return res;
+}
+
+int bl_npy_save(const char* path, const void* header, int64_t hlen, const void* data, int64_t nbytes) {
+    FILE* f = fopen(path, "wb");
+    if (!f) return -1;
+    int ok = fwrite(header, 1, (size_t)hlen, f) == (size_t)hlen && fwrite(data, 1, (size_t)nbytes, f) == (size_t)nbytes;
+    ok = (fclose(f) == 0) && ok;
+    return ok ? 0 : -1;
+}
+
+void bl_free(void* p) { free(p); }

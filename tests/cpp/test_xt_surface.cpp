@@ -4,7 +4,10 @@
 // the bodies are the same xtensor calls, evaluated on the GPU.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
+#include <fstream>
 #include <functional>
+#include <iterator>
 #include <string>
 #include <vector>
 
@@ -12,6 +15,7 @@
 #include "xtensor/containers/xtensor.hpp"
 #include "xtensor/core/xmath.hpp"
 #include "xtensor/core/xnoalias.hpp"
+#include "xtensor/io/xnpy.hpp"
 #include "xtensor/misc/xmanipulation.hpp"
 #include "xtensor/misc/xsort.hpp"
 #include "xtensor/reducers/xnorm.hpp"
@@ -370,6 +374,61 @@ TEST(xviews, index_filter_masked) {
     masked_view(data, mask) += 3.;
     xarray<double> e2 = {{6.65, 6.65, 6.65}, {6.65, 5., -6.}, {6.65, 8., 6.65}};
     EXPECT_EQ(data, e2);
+}
+
+// test_xnpy.cpp:39-83 (load), 125-170 (dump) on the reference's fixtures
+static std::string npy_file(const std::string& stem) {
+    const char* d = std::getenv("XTG_NPY_DIR");
+    return std::string(d ? d : "tests/golden/npy") + "/" + stem + ".le.npy";
+}
+static std::string read_bytes(const std::string& name) {
+    std::ifstream f(name, std::ios::binary);
+    return std::string((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+}
+TEST(xnpy, load_dump) {
+    xarray<double> darr = {{{0.29731723, 0.04380157, 0.94748308}, {0.85020643, 0.52958618, 0.0598172},
+                            {0.77253259, 0.47564231, 0.70274005}},
+                           {{0.85998447, 0.61160158, 0.44432939}, {0.25506765, 0.97420976, 0.15455842},
+                            {0.05873659, 0.66191764, 0.01448838}},
+                           {{0.175919, 0.13850365, 0.94059426}, {0.79941809, 0.5124432, 0.51364796},
+                            {0.25721979, 0.41608858, 0.06255319}}};
+    xarray<bool> barr = {{{0, 0, 1}, {1, 1, 0}, {1, 0, 1}}, {{1, 1, 0}, {0, 1, 0}, {0, 1, 0}},
+                         {{0, 0, 1}, {1, 1, 1}, {0, 0, 0}}};
+    xarray<int> iarr1d = {3, 4, 5, 6, 7};
+
+    auto darr_loaded = load_npy<double>(npy_file("double"));
+    EXPECT_TRUE(allclose(darr, darr_loaded));
+    std::ifstream dstream(npy_file("double"), std::ios::binary);
+    auto darr_loaded_stream = load_npy<double>(dstream);
+    EXPECT_TRUE(allclose(darr, darr_loaded_stream));
+    auto barr_loaded = load_npy<bool>(npy_file("bool"));
+    EXPECT_EQ(barr, barr_loaded);
+    auto dfarr_loaded = load_npy<double, layout_type::column_major>(npy_file("double_fortran"));
+    EXPECT_TRUE(allclose(darr, dfarr_loaded));
+    auto iarr1d_loaded = load_npy<int>(npy_file("int"));
+    EXPECT_EQ(iarr1d, iarr1d_loaded);
+    EXPECT_THROW(load_npy<float>(npy_file("double")), std::runtime_error);
+    EXPECT_THROW((load_npy<double, layout_type::row_major>(npy_file("double_fortran"))), std::runtime_error);
+    EXPECT_THROW(load_npy<double>(std::string("no/such/file.npy")), std::runtime_error);
+
+    EXPECT_TRUE(dump_npy(barr) == read_bytes(npy_file("bool")));
+    xtensor<uint64_t, 1> ularr = {12ul, 14ul, 16ul, 18ul, 1234321ul};
+    const std::string fn = "test_dump_1.npy";
+    dump_npy(fn, ularr);
+    auto ularrcpy = load_npy<uint64_t>(fn);
+    EXPECT_TRUE(allclose(ularr, ularrcpy));
+    EXPECT_TRUE(read_bytes(fn) == read_bytes(npy_file("unsignedlong")));
+    EXPECT_TRUE(dump_npy(ularr) == read_bytes(npy_file("unsignedlong")));
+    std::remove(fn.c_str());
+    // an expression is evaluated before it is written
+    auto twice = load_npy<double>([&] {
+        std::ofstream o("test_dump_2.npy", std::ios::binary);
+        o << dump_npy(darr * 2.);
+        o.close();
+        return std::string("test_dump_2.npy");
+    }());
+    EXPECT_TRUE(allclose(twice, darr * 2.));
+    std::remove("test_dump_2.npy");
 }
 
 int main() {

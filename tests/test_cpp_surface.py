@@ -3,6 +3,7 @@ reference's own tests) compile against include/xtensor/... and run on the GPU
 through libxtg."""
 from __future__ import annotations
 
+import os
 import subprocess
 from pathlib import Path
 
@@ -28,7 +29,8 @@ def test_cpp_call_sites_compile(tmp_path):
 def test_cpp_call_sites_run_on_gpu(tmp_path):
     exe = tmp_path / "test_xt"
     _compile(exe)
-    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600, cwd=tmp_path,
+                       env={**os.environ, "XTG_NPY_DIR": str(ROOT / "tests" / "golden" / "npy")})
     print(r.stdout[-6000:])
     assert r.returncode == 0, r.stdout[-6000:] + r.stderr[-2000:]
     assert "0 failed checks" in r.stdout

@@ -85,6 +85,15 @@ class ReduceDesc(C.Structure):
                 ("acc_dtype", C.c_int32), ("precision", C.c_int32), ("ddof", C.c_int64)]
 
 
+class NpyHeader(C.Structure):
+    _fields_ = [("descr", C.c_char * 16), ("dtype", C.c_int32), ("fortran_order", C.c_int32),
+                ("version", C.c_int32), ("rank", C.c_int32), ("shape", C.c_int64 * MAX_RANK),
+                ("data_offset", C.c_int64), ("data_bytes", C.c_int64)]
+
+
+LAYOUTS = {"dynamic": 0, "row_major": 1, "column_major": 2}
+
+
 class JitStats(C.Structure):
     _fields_ = [("compiles", C.c_int64), ("disk_hits", C.c_int64), ("memory_hits", C.c_int64),
                 ("compile_seconds", C.c_double), ("launches", C.c_int64)]
@@ -144,6 +153,13 @@ def lib() -> C.CDLL:
             "xtg_filter": (st, [C.POINTER(Expr), C.POINTER(Expr), C.POINTER(Array), vp]),
             "xtg_filter_assign": (st, [C.POINTER(Expr), C.POINTER(Expr), i32, C.POINTER(Array), vp]),
             "xtg_masked_assign": (st, [C.POINTER(Expr), C.POINTER(Expr), i32, C.POINTER(Array), vp]),
+            "xtg_npy_info": (st, [C.c_char_p, C.POINTER(NpyHeader)]),
+            "xtg_npy_info_buffer": (st, [vp, sz, C.POINTER(NpyHeader)]),
+            "xtg_npy_format_header": (st, [i32, i32, i32, C.POINTER(i64), vp, sz, C.POINTER(sz)]),
+            "xtg_npy_load": (st, [C.c_char_p, C.POINTER(Array), i32, vp]),
+            "xtg_npy_load_buffer": (st, [vp, sz, C.POINTER(Array), i32, vp]),
+            "xtg_npy_save": (st, [C.c_char_p, C.POINTER(Array), vp]),
+            "xtg_npy_save_buffer": (st, [C.POINTER(Array), vp, sz, C.POINTER(sz), vp]),
             "xtg_get_jit_stats": (st, [C.POINTER(JitStats)]),
             "xtg_set_option": (st, [C.c_char_p, i64]),
             "xtg_get_option": (st, [C.c_char_p, C.POINTER(i64)]),

@@ -1,11 +1,14 @@
 """Evaluation entry points: assign (xt::noalias(out) = e), reductions
 (xt::sum / mean / variance / amax / norm_l2 ... with axes, keep_dims,
 initial, evaluation type T), arg-reductions (xt::argmax / argmin) and
-accumulators (xt::cumsum / cumprod / nancumsum / nancumprod)."""
+accumulators (xt::cumsum / cumprod / nancumsum / nancumprod), index / filter /
+masked views and .npy files (xt::load_npy / dump_npy)."""
 from __future__ import annotations
 
 import ctypes as C
 from typing import Iterable, Optional
+
+import numpy as np
 
 from ._ffi import ARG_MAX, ARG_MIN, RED, MAX_RANK, ReduceDesc, check, dtype_code, lib
 from .device import DeviceArray, _sh
@@ -255,3 +258,112 @@ def masked_assign(dst: DeviceArray, mask, src, op: str = "=", stream=None) -> De
     o = dst.xtg_array()
     check(lib().xtg_masked_assign(C.byref(sx), C.byref(mx), SET_OPS[op], C.byref(o), _sh(stream)))
     return dst
+
+
+# ---- .npy files (xt::load_npy / xt::dump_npy, io/xnpy.hpp) ----------------------------
+
+def _npy_source(src):
+    """(path bytes, None) for a file name, (None, buffer) for a file image."""
+    import os
+    if isinstance(src, (str, os.PathLike)):
+        return os.fsencode(src), None
+    mv = memoryview(src)
+    if not mv.c_contiguous:
+        raise ValueError("npy buffer must be contiguous")
+    return None, mv.cast("B")
+
+
+def npy_header(src) -> dict:
+    """The header of a .npy file (path) or file image (bytes-like)."""
+    from ._ffi import NpyHeader
+    h = NpyHeader()
+    path, mv = _npy_source(src)
+    if path is not None:
+        check(lib().xtg_npy_info(path, C.byref(h)))
+    else:
+        a = np.frombuffer(mv, dtype=np.uint8)  # no copy of the image
+        check(lib().xtg_npy_info_buffer(a.ctypes.data, a.nbytes, C.byref(h)))
+    return {"descr": h.descr.decode(), "dtype": h.dtype, "fortran_order": bool(h.fortran_order),
+            "version": h.version, "shape": tuple(h.shape[i] for i in range(h.rank)),
+            "data_offset": h.data_offset, "data_bytes": h.data_bytes}
+
+
+def load_npy(src, dtype=None, layout: str = "dynamic", out: Optional[DeviceArray] = None,
+             stream=None) -> DeviceArray:
+    """xt::load_npy<T, L>(filename) / load_npy<T, L>(std::istream&) into
+    device memory.  ``src`` is a path or a bytes-like file image; ``dtype`` is
+    T (default: the file's own type); ``layout`` is L ("dynamic",
+    "row_major", "column_major").  A Fortran-order file loads into a
+    column-major array, as the reference's dynamic-layout result."""
+    from ._ffi import LAYOUTS, XtgError
+    h = npy_header(src)
+    if out is None:
+        if dtype is None:
+            if h["dtype"] < 0:
+                raise XtgError(1, f"Cast error: formats not matching {h['descr']} vs (no device type)")
+            code = h["dtype"]
+        else:
+            code = dtype_code(dtype)
+        shape = h["shape"]
+        n = int(np.prod(shape)) if shape else 1
+        buf = DeviceArray.empty((n,), code, stream)
+        if h["fortran_order"]:
+            st, acc = [], 1
+            for d in shape:
+                st.append(acc)
+                acc *= max(int(d), 1)
+            out = DeviceArray(shape, code, buf.ptr, st, base=buf)
+        else:
+            out = DeviceArray(shape, code, buf.ptr, base=buf)
+    o = out.xtg_array()
+    path, mv = _npy_source(src)
+    if path is not None:
+        check(lib().xtg_npy_load(path, C.byref(o), LAYOUTS[layout], _sh(stream)))
+    else:
+        a = np.frombuffer(mv, dtype=np.uint8)
+        check(lib().xtg_npy_load_buffer(a.ctypes.data, a.nbytes, C.byref(o), LAYOUTS[layout], _sh(stream)))
+    return out
+
+
+def _npy_device_source(e, stream):
+    if isinstance(e, DeviceArray):
+        return e
+    from .expr import as_expr
+    ex = as_expr(e)
+    t = DeviceArray.empty(broadcast_shape(ex), expr_dtype(ex), stream)
+    return assign(t, ex, stream)
+
+
+def dump_npy(*args, stream=None):
+    """xt::dump_npy(filename, e) writes a file; xt::dump_npy(e) returns the
+    file image as bytes.  ``e`` is a device array or an expression (evaluated
+    first, as the reference's eval)."""
+    import os
+    # `src` holds an evaluated temporary alive until the bytes are out
+    if len(args) == 2:
+        path, e = args
+        src = _npy_device_source(e, stream)
+        a = src.xtg_array()
+        check(lib().xtg_npy_save(os.fsencode(path), C.byref(a), _sh(stream)))
+        return None
+    (e,) = args
+    src = _npy_device_source(e, stream)
+    a = src.xtg_array()
+    n = C.c_size_t()
+    check(lib().xtg_npy_save_buffer(C.byref(a), None, 0, C.byref(n), _sh(stream)))
+    out = bytearray(n.value)
+    buf = (C.c_char * n.value).from_buffer(out)
+    check(lib().xtg_npy_save_buffer(C.byref(a), buf, n.value, C.byref(n), _sh(stream)))
+    return bytes(out)
+
+
+def npy_format_header(dtype, shape, fortran_order: bool = False) -> bytes:
+    """The header bytes dump_npy writes before the data (host only)."""
+    shp = (C.c_int64 * MAX_RANK)(*[int(s) for s in shape])
+    n = C.c_size_t()
+    code = dtype_code(dtype)
+    check(lib().xtg_npy_format_header(code, int(fortran_order), len(shape), shp, None, 0, C.byref(n)))
+    out = bytearray(n.value)
+    buf = (C.c_char * n.value).from_buffer(out)
+    check(lib().xtg_npy_format_header(code, int(fortran_order), len(shape), shp, buf, n.value, C.byref(n)))
+    return bytes(out)
