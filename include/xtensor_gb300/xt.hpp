@@ -431,7 +431,10 @@ public:
     const T* data() const noexcept { return m_buf ? (const T*)m_buf->ptr : nullptr; }
     template <class S> void resize(const S& s) {
         auto ns = to_shape(s);
-        if (std::vector<std::size_t>(ns.begin(), ns.end()) != std::vector<std::size_t>(m_shape.begin(), m_shape.end()))
+        // a container built from an expression has no storage yet, even when
+        // its (default, 0-d) shape already matches
+        if (!m_buf ||
+            std::vector<std::size_t>(ns.begin(), ns.end()) != std::vector<std::size_t>(m_shape.begin(), m_shape.end()))
             set_shape(ns);
     }
     template <class S> void reshape(const S& s) {
@@ -933,6 +936,16 @@ XTG_XT_REDUCER(norm_linf, XTG_RED_NORM_LINF)
     template <class T = void, class E, class I, std::enable_if_t<std::is_integral<I>::value, int> = 0>              \
     inline auto NAME(E&& e, I axis, reducer_options o = {}) {                                                      \
         return detail::make_reducer<OP, T>(std::forward<E>(e), {(std::ptrdiff_t)axis}, false, o);                   \
+    }                                                                                                              \
+    template <class T = void, class E, class X,                                                                   \
+              std::enable_if_t<!std::is_integral<std::decay_t<X>>::value && !std::is_base_of<reducer_options, std::decay_t<X>>::value, int> = 0> \
+    inline auto NAME(E&& e, const X& axes, reducer_options o = {}) {                                               \
+        return detail::make_reducer<OP, T>(std::forward<E>(e), detail::axes_vec(axes), false, o);                   \
+    }                                                                                                              \
+    template <class T = void, class E, class X, class D,                                                           \
+              std::enable_if_t<!std::is_integral<std::decay_t<X>>::value && std::is_integral<D>::value, int> = 0>   \
+    inline auto NAME(E&& e, const X& axes, D ddof, reducer_options o = {}) {                                       \
+        return detail::make_reducer<OP, T>(std::forward<E>(e), detail::axes_vec(axes), false, o, (int64_t)ddof);    \
     }
 XTG_XT_MOMENT(variance, XTG_RED_VARIANCE)
 XTG_XT_MOMENT(stddev, XTG_RED_STDDEV)
@@ -1112,6 +1125,134 @@ XTG_ACCUMULATOR(cumprod, XTG_ACC_CUMPROD, 1)
 XTG_ACCUMULATOR(nancumsum, XTG_ACC_NANCUMSUM, 0)
 XTG_ACCUMULATOR(nancumprod, XTG_ACC_NANCUMPROD, 1)
 #undef XTG_ACCUMULATOR
+
+// ---------------------------------------------------------------------------- blockwise reducers
+// xt::blockwise::<op>(e, block_shape, axes, options)
+// (include/xtensor/reducers/xblockwise_reducer.hpp:269-533): the reducer's
+// shape(), dimension() and assign_to(result) as the reference's; the work is
+// libxtg's slab-streamed blockwise reduction.  `e` is a device expression
+// (evaluated first) or an xt::host_array<T> — a dense host buffer, possibly
+// larger than device memory, streamed through in slabs of whole blocks.
+template <class T> struct host_array {
+    using value_type = T;
+    const T* data;
+    std::vector<std::size_t> shape;
+    std::vector<std::ptrdiff_t> strides;
+};
+template <class T, class S> inline host_array<T> adapt_host(const T* data, const S& shape) {
+    host_array<T> h{data, std::vector<std::size_t>(std::begin(shape), std::end(shape)), {}};
+    h.strides = detail::row_major_strides(h.shape);
+    return h;
+}
+template <class T> inline host_array<T> adapt_host(const T* data, std::initializer_list<std::size_t> shape) {
+    return adapt_host(data, std::vector<std::size_t>(shape));
+}
+
+template <int OP, class R> class xblockwise_reducer {
+public:
+    using value_type = R;
+    template <class E, class BS, class X>
+    xblockwise_reducer(const E& e, const BS& block_shape, const X& axes, bool all_axes, reducer_options o, double p)
+        : m_p(p) {
+        bind(e);
+        m_block.assign(std::begin(block_shape), std::end(block_shape));
+        std::memset(&m_rd, 0, sizeof m_rd);
+        m_rd.op = OP;
+        m_rd.n_axes = all_axes ? -1 : 0;
+        if (!all_axes)
+            for (auto a : axes) m_rd.axes[m_rd.n_axes++] = (int64_t)a;
+        m_rd.keep_dims = o.keep_dims;
+        m_rd.has_initial = o.has_initial;
+        m_rd.acc_dtype = detail::dtype_of<R>::value;
+        if (OP == XTG_RED_AMAX || OP == XTG_RED_AMIN || OP >= XTG_RED_NORM_L0) m_rd.acc_dtype = -1;
+        int32_t r = 0, dt = 0;
+        int64_t sh[XTG_MAX_RANK];
+        detail::check(xtg_blockwise_shape(&m_in, &m_rd, &r, sh, &dt));
+        m_shape.assign(sh, sh + r);
+    }
+    const std::vector<std::size_t>& shape() const { return m_shape; }
+    std::size_t dimension() const { return m_shape.size(); }
+    template <class D> void assign_to(D& result) const {
+        const xtg_array o = result.xtg_desc();
+        detail::check(xtg_blockwise_reduce(&m_in, m_block.data(), &m_rd, m_p, &o, detail::current_stream()));
+    }
+
+private:
+    template <class T> void bind(const host_array<T>& h) {
+        std::memset(&m_in, 0, sizeof m_in);
+        m_in.data = const_cast<T*>(h.data);
+        m_in.dtype = detail::dtype_of<T>::value;
+        m_in.rank = (int32_t)h.shape.size();
+        for (std::size_t i = 0; i < h.shape.size(); ++i) {
+            m_in.shape[i] = (int64_t)h.shape[i];
+            m_in.strides[i] = (int64_t)h.strides[i];
+        }
+    }
+    template <class E> void bind(const E& e) {
+        using V = typename std::decay_t<E>::value_type;
+        auto ev = std::make_shared<xarray<V>>(xt::eval(e));
+        m_keep = ev;
+        m_in = ev->xtg_desc();
+    }
+    xtg_array m_in;
+    std::shared_ptr<void> m_keep;
+    std::vector<int64_t> m_block;
+    xtg_reduce_desc m_rd;
+    double m_p;
+    std::vector<std::size_t> m_shape;
+};
+
+namespace blockwise {
+namespace detail {
+template <class E> struct value_of { using type = typename std::decay_t<E>::value_type; };
+}  // namespace detail
+#define XTG_BLOCKWISE(NAME, CODE)                                                                                  \
+    template <class T = void, class E, class BS, class X,                                                           \
+              std::enable_if_t<!std::is_integral<X>::value && !std::is_base_of<reducer_options, X>::value, int> = 0> \
+    inline auto NAME(const E& e, const BS& block_shape, const X& axes, reducer_options o = {}) {                    \
+        using R = typename xt::detail::red_result<CODE, typename detail::value_of<E>::type, T>::type;              \
+        return xblockwise_reducer<CODE, R>(e, block_shape, axes, false, o, 0.0);                                    \
+    }                                                                                                               \
+    template <class T = void, class E, class BS>                                                                    \
+    inline auto NAME(const E& e, const BS& block_shape, std::initializer_list<std::size_t> axes,                    \
+                     reducer_options o = {}) {                                                                      \
+        return NAME<T>(e, block_shape, std::vector<std::size_t>(axes), o);                                          \
+    }                                                                                                               \
+    template <class T = void, class E, class BS, class I, std::enable_if_t<std::is_integral<I>::value, int> = 0>    \
+    inline auto NAME(const E& e, const BS& block_shape, I axis, reducer_options o = {}) {                           \
+        return NAME<T>(e, block_shape, std::vector<std::size_t>{(std::size_t)axis}, o);                             \
+    }                                                                                                               \
+    template <class T = void, class E, class BS>                                                                    \
+    inline auto NAME(const E& e, const BS& block_shape, reducer_options o = {}) {                                   \
+        using R = typename xt::detail::red_result<CODE, typename detail::value_of<E>::type, T>::type;              \
+        return xblockwise_reducer<CODE, R>(e, block_shape, std::vector<std::size_t>{}, true, o, 0.0);               \
+    }
+XTG_BLOCKWISE(sum, XTG_RED_SUM)
+XTG_BLOCKWISE(prod, XTG_RED_PROD)
+XTG_BLOCKWISE(amin, XTG_RED_AMIN)
+XTG_BLOCKWISE(amax, XTG_RED_AMAX)
+XTG_BLOCKWISE(mean, XTG_RED_MEAN)
+XTG_BLOCKWISE(variance, XTG_RED_VARIANCE)
+XTG_BLOCKWISE(stddev, XTG_RED_STDDEV)
+XTG_BLOCKWISE(norm_l0, XTG_RED_NORM_L0)
+XTG_BLOCKWISE(norm_l1, XTG_RED_NORM_L1)
+XTG_BLOCKWISE(norm_l2, XTG_RED_NORM_L2)
+XTG_BLOCKWISE(norm_sq, XTG_RED_NORM_SQ)
+XTG_BLOCKWISE(norm_linf, XTG_RED_NORM_LINF)
+#undef XTG_BLOCKWISE
+#define XTG_BLOCKWISE_P(NAME, CODE)                                                                                \
+    template <class E, class BS, class X, std::enable_if_t<!std::is_base_of<reducer_options, X>::value, int> = 0>   \
+    inline auto NAME(const E& e, const BS& block_shape, double p, const X& axes, reducer_options o = {}) {          \
+        return xblockwise_reducer<CODE, double>(e, block_shape, axes, false, o, p);                                 \
+    }                                                                                                               \
+    template <class E, class BS>                                                                                    \
+    inline auto NAME(const E& e, const BS& block_shape, double p, reducer_options o = {}) {                         \
+        return xblockwise_reducer<CODE, double>(e, block_shape, std::vector<std::size_t>{}, true, o, p);            \
+    }
+XTG_BLOCKWISE_P(norm_lp_to_p, XTG_RED_NORM_LP_TO_P)
+XTG_BLOCKWISE_P(norm_lp, XTG_RED_NORM_LP)
+#undef XTG_BLOCKWISE_P
+}  // namespace blockwise
 
 // ---------------------------------------------------------------------------- index / filter / masked views
 // xt::index_view, xt::filter, xt::filtration, xt::masked_view

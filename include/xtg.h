@@ -32,6 +32,7 @@
  *                      include/xtensor/core/xmath.hpp:2248-2301, 2363-2391, 2592-2645
  *   xtg_npy_*       <- xt::load_npy / xt::dump_npy (include/xtensor/io/xnpy.hpp:
  *                      237-450, 674-800)
+ *   xtg_blockwise_* <- xt::blockwise::* (include/xtensor/reducers/xblockwise_reducer.hpp:269-533)
  *   xtg_gather / xtg_scatter, xtg_filter* , xtg_masked_assign
  *                   <- reading and assigning through xt::index_view / filter /
  *                      filtration / masked_view
@@ -169,7 +170,10 @@ typedef struct {
 typedef enum {
     XTG_RED_SUM = 0, XTG_RED_PROD, XTG_RED_AMAX, XTG_RED_AMIN, XTG_RED_MEAN,
     XTG_RED_VARIANCE, XTG_RED_STDDEV, XTG_RED_NORM_L0, XTG_RED_NORM_L1,
-    XTG_RED_NORM_SQ, XTG_RED_NORM_L2, XTG_RED_NORM_LINF
+    XTG_RED_NORM_SQ, XTG_RED_NORM_L2, XTG_RED_NORM_LINF,
+    /* xtg_blockwise_reduce only (the blockwise norm_lp_to_p / norm_lp, which
+     * take the exponent p): */
+    XTG_RED_NORM_LP_TO_P, XTG_RED_NORM_LP
 } xtg_reduce_op;
 
 typedef enum {
@@ -331,6 +335,25 @@ xtg_status xtg_npy_save(const char* path, const xtg_array* in, xtg_stream stream
 /* *len receives the size of the whole file image; nothing is written when
  * buf is NULL; cap < *len is XTG_ERR_INVALID. */
 xtg_status xtg_npy_save_buffer(const xtg_array* in, void* buf, size_t cap, size_t* len, xtg_stream stream);
+
+/* ---- blockwise reducers ---------------------------------------------------------------------
+ * xt::blockwise::sum / prod / amin / amax / mean / variance / stddev / norm_l0 /
+ * norm_l1 / norm_l2 / norm_sq / norm_linf / norm_lp_to_p / norm_lp
+ * (reducers/xblockwise_reducer.hpp:269-533, xblockwise_reducer_functors.hpp):
+ * per-block results merged in block order (+=, *=, minimum / maximum, the
+ * pairwise mean / variance update), then finalized (mean / factor, sqrt,
+ * pow(., 1/p)).  `in` may be in device memory, or in host memory (pinned or
+ * pageable, any dense strides) and larger than HBM: it streams through two
+ * device buffers in slabs of whole blocks along its outermost dimension, the
+ * copy of slab k+1 overlapping the reduction of slab k.  `out` (device) has
+ * xtg_reduce_shape's shape and type; `p` is read by the lp ops only.
+ * Unsupported: xt::initial and ddof (the reference's blockwise functors
+ * take neither).  Returns once the host input is no longer read. */
+xtg_status xtg_blockwise_reduce(const xtg_array* in, const int64_t* block_shape, const xtg_reduce_desc* rd, double p,
+                                const xtg_array* out, xtg_stream stream);
+/* Shape and type of that result. */
+xtg_status xtg_blockwise_shape(const xtg_array* in, const xtg_reduce_desc* rd, int32_t* rank, int64_t* shape,
+                               int32_t* out_dtype);
 
 /* ---- index, filter and masked views ----------------------------------------------------
  * Assignment operators for writes through a view: dst = op(dst, value). */

@@ -32,6 +32,14 @@
  *                       walking the storage with the axis stride
  *                       (xaccumulator.hpp:233-281); axis = -1 flattens
  *                       (:283-310).  The copy is fused into the first pass.
+ *   bl_blockwise_sum_axis0_f32 / bl_blockwise_mean_12_f32
+ *                       xt::blockwise::sum(x, {b0, b1, b2}, {0}) and
+ *                       blockwise::mean(x, blocks, {1, 2}) on a contiguous
+ *                       (d0, d1, d2) float array: each block summed in the
+ *                       plain reducer's order, block results folded in grid
+ *                       order, the mean divided at the end
+ *                       (xblockwise_reducer.hpp:129-194, functors :38-160);
+ *                       OpenMP over independent outputs.
  *   bl_npy_load         xt::load_npy<T>(filename): read the magic and version,
  *                       the header length and the header, take the word
  *                       size from 'descr' and the shape from 'shape', then
@@ -235,3 +243,38 @@ int bl_npy_save(const char* path, const void* header, int64_t hlen, const void* 
 }
 
 void bl_free(void* p) { free(p); }
+
+void bl_blockwise_sum_axis0_f32(const float* x, float* out, int64_t d0, int64_t d1, int64_t d2, int64_t b0) {
+    const int64_t m = d1 * d2;
+    _Pragma("omp parallel for schedule(static)")
+    for (int64_t j0 = 0; j0 < m; j0 += 4096) {
+        const int64_t j1 = j0 + 4096 < m ? j0 + 4096 : m;
+        float part[4096];
+        for (int64_t i0 = 0; i0 < d0; i0 += b0) {
+            const int64_t i1 = i0 + b0 < d0 ? i0 + b0 : d0;
+            for (int64_t j = j0; j < j1; ++j) part[j - j0] = x[i0 * m + j];
+            for (int64_t i = i0 + 1; i < i1; ++i)
+                for (int64_t j = j0; j < j1; ++j) part[j - j0] += x[i * m + j];
+            for (int64_t j = j0; j < j1; ++j) out[j] = i0 == 0 ? part[j - j0] : out[j] + part[j - j0];
+        }
+    }
+}
+
+void bl_blockwise_mean_12_f32(const float* x, double* out, int64_t d0, int64_t d1, int64_t d2, int64_t b1, int64_t b2) {
+    _Pragma("omp parallel for schedule(static)")
+    for (int64_t i = 0; i < d0; ++i) {
+        const float* r = x + i * d1 * d2;
+        double acc = 0;
+        int first = 1;
+        for (int64_t k0 = 0; k0 < d1; k0 += b1)
+            for (int64_t l0 = 0; l0 < d2; l0 += b2) {
+                const int64_t k1 = k0 + b1 < d1 ? k0 + b1 : d1, l1 = l0 + b2 < d2 ? l0 + b2 : d2;
+                double s = 0;
+                for (int64_t k = k0; k < k1; ++k)
+                    for (int64_t l = l0; l < l1; ++l) s += r[k * d2 + l];
+                acc = first ? s : acc + s;
+                first = 0;
+            }
+        out[i] = acc / (double)(d1 * d2);
+    }
+}

@@ -8,6 +8,7 @@
 #include <fstream>
 #include <functional>
 #include <iterator>
+#include <numeric>
 #include <string>
 #include <vector>
 
@@ -18,6 +19,7 @@
 #include "xtensor/io/xnpy.hpp"
 #include "xtensor/misc/xmanipulation.hpp"
 #include "xtensor/misc/xsort.hpp"
+#include "xtensor/reducers/xblockwise_reducer.hpp"
 #include "xtensor/reducers/xnorm.hpp"
 #include "xtensor/reducers/xreducer.hpp"
 #include "xtensor/views/xview.hpp"
@@ -429,6 +431,48 @@ TEST(xnpy, load_dump) {
     }());
     EXPECT_TRUE(allclose(twice, darr * 2.));
     std::remove("test_dump_2.npy");
+}
+
+// test_xblockwise_reducer.cpp:95-140: blockwise::op equals the plain reducer
+template <class BR, class PR> static void check_blockwise(BR reducer, PR should_reducer, bool close) {
+    auto should = xt::eval(should_reducer);
+    EXPECT_EQ(reducer.dimension(), should.dimension());
+    EXPECT_TRUE(std::vector<std::size_t>(reducer.shape().begin(), reducer.shape().end()) ==
+                std::vector<std::size_t>(should.shape().begin(), should.shape().end()));
+    auto result = xarray<typename BR::value_type>::from_shape(reducer.shape());
+    reducer.assign_to(result);
+    if (close) EXPECT_TRUE(allclose(result, should));
+    else EXPECT_TRUE(result == should);
+}
+TEST(xreducer, explicit_all_axes_to_fresh_container) {
+    xarray<int> a = {{1, 2}, {3, 4}};
+    xarray<int> s = xt::sum(a, std::vector<std::size_t>{0, 1});  // 0-d, built from the expression
+    EXPECT_EQ(s.dimension(), 0u);
+    EXPECT_EQ(s(), 10);
+}
+TEST(xblockwise_reducer, test_values) {
+    const std::vector<std::size_t> shape = {21, 10, 5}, chunk_shape = {5, 4, 2};
+    std::vector<int> h(21 * 10 * 5);
+    std::iota(h.begin(), h.end(), -5);
+    for (std::size_t i = 0; i < h.size(); ++i)
+        if (i % 2) h[i] += 10;
+    xarray<int> input_exp(shape);
+    input_exp.upload(h);
+    const std::vector<std::vector<std::size_t>> axes_vec = {{0}, {1}, {2}, {0, 1}, {0, 2}, {0, 1, 2}};
+    for (const auto& axes : axes_vec) {
+        check_blockwise(blockwise::sum(input_exp, chunk_shape, axes, keep_dims), xt::sum(input_exp, axes, keep_dims), false);
+        check_blockwise(blockwise::prod(input_exp, chunk_shape, axes), xt::prod(input_exp, axes), false);
+        check_blockwise(blockwise::amin(input_exp, chunk_shape, axes, keep_dims), xt::amin(input_exp, axes, keep_dims), false);
+        check_blockwise(blockwise::amax(input_exp, chunk_shape, axes), xt::amax(input_exp, axes), false);
+        check_blockwise(blockwise::mean(input_exp, chunk_shape, axes, keep_dims), xt::mean(input_exp, axes, keep_dims), false);
+        check_blockwise(blockwise::variance(input_exp, chunk_shape, axes), xt::variance(input_exp, axes), true);
+        check_blockwise(blockwise::stddev(input_exp, chunk_shape, axes, keep_dims), xt::stddev(input_exp, axes, keep_dims), true);
+        check_blockwise(blockwise::norm_l1(input_exp, chunk_shape, axes), xt::norm_l1(input_exp, axes), false);
+        check_blockwise(blockwise::norm_linf(input_exp, chunk_shape, axes, keep_dims), xt::norm_linf(input_exp, axes, keep_dims), false);
+        check_blockwise(blockwise::norm_lp(input_exp, chunk_shape, 2.0, axes), xt::norm_l2(input_exp, axes), true);
+        // the same input from host memory, streamed by slabs
+        check_blockwise(blockwise::sum(adapt_host(h.data(), shape), chunk_shape, axes), xt::sum(input_exp, axes), false);
+    }
 }
 
 int main() {

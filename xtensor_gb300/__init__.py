@@ -42,5 +42,6 @@ from .ops import assign, reduce, argreduce, reduce_shape, broadcast_shape, expr_
 from .ops import accumulate, cumsum, cumprod, nancumsum, nancumprod  # noqa: F401
 from .ops import index_view, index_assign, filter_count, filter, filter_assign, masked_assign  # noqa: F401,A004
 from .ops import load_npy, dump_npy, npy_header, npy_format_header  # noqa: F401
+from .ops import blockwise, blockwise_shape  # noqa: F401
 
 __all__ = [n for n in dir() if not n.startswith("_")]

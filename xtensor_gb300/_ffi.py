@@ -33,7 +33,8 @@ OP = dict(
     RSUM=80, RMEAN=81, RVAR=82, RSTD=83, RMAX=84, RMIN=85,
 )
 RED = dict(sum=0, prod=1, amax=2, amin=3, mean=4, variance=5, stddev=6,
-           norm_l0=7, norm_l1=8, norm_sq=9, norm_l2=10, norm_linf=11)
+           norm_l0=7, norm_l1=8, norm_sq=9, norm_l2=10, norm_linf=11,
+           norm_lp_to_p=12, norm_lp=13)  # the last two: blockwise only
 ARG_MAX, ARG_MIN = 0, 1
 PREC_COMPENSATED, PREC_PLAIN = 0, 1
 
@@ -160,6 +161,10 @@ def lib() -> C.CDLL:
             "xtg_npy_load_buffer": (st, [vp, sz, C.POINTER(Array), i32, vp]),
             "xtg_npy_save": (st, [C.c_char_p, C.POINTER(Array), vp]),
             "xtg_npy_save_buffer": (st, [C.POINTER(Array), vp, sz, C.POINTER(sz), vp]),
+            "xtg_blockwise_reduce": (st, [C.POINTER(Array), C.POINTER(i64), C.POINTER(ReduceDesc), C.c_double,
+                                          C.POINTER(Array), vp]),
+            "xtg_blockwise_shape": (st, [C.POINTER(Array), C.POINTER(ReduceDesc), C.POINTER(i32), C.POINTER(i64),
+                                         C.POINTER(i32)]),
             "xtg_get_jit_stats": (st, [C.POINTER(JitStats)]),
             "xtg_set_option": (st, [C.c_char_p, i64]),
             "xtg_get_option": (st, [C.c_char_p, C.POINTER(i64)]),

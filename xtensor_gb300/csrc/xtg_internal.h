@@ -126,6 +126,12 @@ void count_launch();
 // Resets the per-thread record of launched kernels (start of an API call).
 void begin_call();
 
+// ---- pinned staging ring (xtg_npy.cpp) ---------------------------------------------
+// Copies `bytes` of pageable host memory to device memory through the pinned
+// staging ring (several host threads, one CUDA stream each); the copies start
+// after `wait_for` (non-null) and have landed when the call returns.
+xtg_status ring_h2d(void* dev, const void* host, size_t bytes, cudaEvent_t wait_for);
+
 // ---- scratch ---------------------------------------------------------------------
 xtg_status scratch_alloc(void** p, size_t bytes, cudaStream_t s);
 xtg_status scratch_free(void* p, cudaStream_t s);

@@ -319,7 +319,8 @@ struct Job {
     size_t chunk = 0;
     int nworkers = 1;
     int device = 0;
-    cudaEvent_t after = nullptr;  // the caller's stream reached this point
+    cudaEvent_t after = nullptr;  // the copies start after this event
+    cudaEvent_t wait_for = nullptr;  // if set: the event to start after (else the caller's stream now)
     std::atomic<int> status{XTG_OK};
     std::string msg;
     std::mutex msg_mu;
@@ -408,8 +409,8 @@ xtg_status run_job(Job& j, cudaStream_t stream) {
     j.nworkers = nw;
     cudaEvent_t after;
     XTG_CUDA(cudaEventCreateWithFlags(&after, cudaEventDisableTiming));
-    j.after = after;
-    cudaError_t e = cudaEventRecord(after, stream);
+    j.after = j.wait_for ? j.wait_for : after;
+    cudaError_t e = j.wait_for ? cudaSuccess : cudaEventRecord(after, stream);
     if (e == cudaSuccess) {
         std::vector<std::thread> th;
         for (int i = 1; i < nw; ++i) th.emplace_back(run_worker, std::ref(j), std::ref(st.w[i]), i);
@@ -627,6 +628,19 @@ bool host_pinned(const void* p) {
 }
 
 }  // namespace
+
+xtg_status ring_h2d(void* dev, const void* host, size_t bytes, cudaEvent_t wait_for) {
+    Src src;
+    src.mem = (const unsigned char*)host;
+    src.mem_len = bytes;
+    Job j;
+    j.to_device = true;
+    j.src = &src;
+    j.dev = (unsigned char*)dev;
+    j.bytes = bytes;
+    j.wait_for = wait_for;
+    return run_job(j, nullptr);
+}
 
 }  // namespace xtgh
 

@@ -414,6 +414,7 @@ static bool out_matches(const xtg_array& out, int rank, const int64_t* shape) {
 xtg_status reduce_impl(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, cudaStream_t stream,
                        const ScratchSpec* scratch) {
     if (!rd || !out) return fail(XTG_ERR_INVALID, "null argument");
+    if (rd->op < XTG_RED_SUM || rd->op > XTG_RED_NORM_LINF) return fail(XTG_ERR_INVALID, "unknown reduction op");
     Tree t;
     XTG_TRY(build_tree(e, opt("fp32_compute", 1) != 0, t));
     if (t.n_rstats) return fail(XTG_ERR_UNSUPPORTED, "row statistics inside a reduction operand");
@@ -513,6 +514,7 @@ extern "C" {
 xtg_status xtg_reduce_shape(const xtg_expr* e, const xtg_reduce_desc* rd, int32_t* rank, int64_t* shape,
                             int32_t* out_dtype) {
     if (!rd) return fail(XTG_ERR_INVALID, "null reduce descriptor");
+    if (rd->op < XTG_RED_SUM || rd->op > XTG_RED_NORM_LINF) return fail(XTG_ERR_INVALID, "unknown reduction op");
     Tree t;
     XTG_TRY(build_tree(e, false, t));
     RedShape S;

@@ -367,3 +367,46 @@ def npy_format_header(dtype, shape, fortran_order: bool = False) -> bytes:
     buf = (C.c_char * n.value).from_buffer(out)
     check(lib().xtg_npy_format_header(code, int(fortran_order), len(shape), shp, buf, n.value, C.byref(n)))
     return bytes(out)
+
+
+# ---- blockwise reducers (xt::blockwise::*, reducers/xblockwise_reducer.hpp) -----------
+
+def _blockwise_array(x):
+    """(xtg_array, keepalive) for a device array or a host numpy array."""
+    from .device import HostArray
+    if isinstance(x, DeviceArray):
+        return x.xtg_array(), x
+    if isinstance(x, np.ndarray):
+        h = HostArray(x)
+        return h.xtg_array(), h
+    raise TypeError("blockwise input must be a DeviceArray or a host numpy array")
+
+
+def blockwise_shape(op: str, x, axes=None, keep_dims=False, acc_dtype=None):
+    a, keep = _blockwise_array(x)
+    rd = make_desc(op, axes, keep_dims, acc_dtype=acc_dtype)
+    r = C.c_int32()
+    sh = (C.c_int64 * MAX_RANK)()
+    dt = C.c_int32()
+    check(lib().xtg_blockwise_shape(C.byref(a), C.byref(rd), C.byref(r), sh, C.byref(dt)))
+    return tuple(sh[i] for i in range(r.value)), dt.value
+
+
+def blockwise(op: str, x, block_shape, axes=None, keep_dims=False, p: float = 2.0, acc_dtype=None,
+              out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
+    """xt::blockwise::<op>(x, block_shape, axes, options) evaluated into a
+    device array (``reducer.assign_to(result)``).  ``x`` is a device array or
+    a host numpy array (pageable or pinned; it may be larger than device
+    memory: it streams through in slabs of whole blocks).  ``p`` is the
+    exponent of norm_lp_to_p / norm_lp."""
+    a, keep = _blockwise_array(x)
+    rd = make_desc(op, axes, keep_dims, acc_dtype=acc_dtype)
+    if out is None:
+        shape, dt = blockwise_shape(op, x, axes, keep_dims, acc_dtype)
+        out = DeviceArray.empty(shape, dt, stream)
+    bs = (C.c_int64 * MAX_RANK)(*[int(b) for b in block_shape])
+    if len(block_shape) != len(a.shape[:a.rank]):
+        raise ValueError("block_shape must have one extent per dimension")
+    o = out.xtg_array()
+    check(lib().xtg_blockwise_reduce(C.byref(a), bs, C.byref(rd), float(p), C.byref(o), _sh(stream)))
+    return out
