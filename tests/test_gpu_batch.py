@@ -102,6 +102,79 @@ def test_batched_int_sums_and_autotune_cache(tmp_path, monkeypatch):
     assert (tmp_path / "autotune.txt").exists()
 
 
+@pytest.fixture
+def batch_vec():
+    def set_(v):
+        xg.set_option("batch.vec", v)
+    yield set_
+    xg.set_option("batch.vec", 1)
+
+
+@pytest.mark.parametrize("vec", [0, 1])
+def test_vector_and_strided_forms(vec, batch_vec):
+    """The vector form (16-byte loads where a row's leaves share alignment,
+    scalar loads where they do not, scalar head and tail) and the strided
+    form: row sums within the compensated bound of FP64, integer sums and
+    maxima exact, over ragged widths, rows starting at every alignment
+    phase (views offset by one element) and broadcast leaves."""
+    batch_vec(vec)
+    xg.init(0)
+    g = np.random.default_rng(7)
+    shapes = [(int(g.integers(1, 90)), int(g.integers(1, 300))) for _ in range(40)] + [(3, 1), (5, 2), (2, 3), (1, 5)]
+    # float32: A is a view one element into a wider buffer, so its rows start
+    # at other phases than C's
+    data, keep = [], []
+    for r, c in shapes:
+        Abig = g.uniform(-1, 1, (r, c + 3)).astype(np.float32)
+        v = g.standard_normal(c).astype(np.float32)
+        Cm = g.uniform(-1, 1, (r, c)).astype(np.float32)
+        dAbig = DeviceArray.from_numpy(Abig)
+        dev = (dAbig[:, 1:c + 1], DeviceArray.from_numpy(v), DeviceArray.from_numpy(Cm))
+        keep.append(dAbig)
+        data.append((Abig[:, 1:c + 1], v, Cm, dev))
+    outs = [DeviceArray.empty((r,), "float32") for r, _ in shapes]
+    b = Batch(data[0][3][0] * data[0][3][1] + data[0][3][2], reduce="sum")
+    for (_, _, _, (dA, dv, dC)), o in zip(data, outs):
+        b.add(dA * dv + dC, o)
+    b.build(autotune=False)
+    b.run()
+    for (A, v, Cm, _), o in zip(data, outs):
+        E = A.astype(np.float64) * v + Cm
+        assert (np.abs(o.to_numpy() - E.sum(1)) <= 1e-6 * np.abs(E).sum(1) + 1e-30).all()
+    # float64 means (two elements per vector)
+    xs = [g.standard_normal(sh) for sh in shapes]
+    dx = [DeviceArray.from_numpy(x) for x in xs]
+    om = [DeviceArray.empty((sh[0],), "float64") for sh in shapes]
+    bm = Batch(dx[0], reduce="mean")
+    for d, o in zip(dx, om):
+        bm.add(d, o)
+    bm.build(autotune=False)
+    bm.run()
+    for x, o in zip(xs, om):
+        np.testing.assert_allclose(o.to_numpy(), x.mean(1), rtol=1e-13, atol=1e-15)
+    # int32 maxima and uint8 sums (sixteen elements per vector): exact
+    ints = [g.integers(-10**6, 10**6, sh).astype(np.int32) for sh in shapes]
+    di = [DeviceArray.from_numpy(x) for x in ints]
+    oi = [DeviceArray.empty((sh[0],), "int32") for sh in shapes]
+    bi = Batch(di[0], reduce="amax")
+    for d, o in zip(di, oi):
+        bi.add(d, o)
+    bi.build(autotune=False)
+    bi.run()
+    for x, o in zip(ints, oi):
+        np.testing.assert_array_equal(o.to_numpy(), x.max(1))
+    u8 = [g.integers(0, 256, sh).astype(np.uint8) for sh in shapes]
+    du = [DeviceArray.from_numpy(x) for x in u8]
+    ou = [DeviceArray.empty((sh[0],), "uint64") for sh in shapes]
+    bu = Batch(du[0], reduce="sum", acc_dtype="uint64")
+    for d, o in zip(du, ou):
+        bu.add(d, o)
+    bu.build(autotune=False)
+    bu.run()
+    for x, o in zip(u8, ou):
+        np.testing.assert_array_equal(o.to_numpy(), x.astype(np.uint64).sum(1))
+
+
 def test_fill_random_is_seeded():
     xg.init(0)
     a = fill_random(DeviceArray.empty((1 << 20,), "float32"), "normal", 0.0, 1.0, 7).to_numpy()

@@ -47,6 +47,7 @@ struct xtg_batch {
     cudaStream_t stream = nullptr;  // stream of the last allocation / launch
     // configuration
     int gl = 32, unroll = 4, cpsm = 4;
+    int vec = 1;  // reductions: elements per vector load (1: the strided form)
     int64_t tile_elems = 32768;
     int tuned = 0;
     std::string kname;  // kernel name for the current group width
@@ -163,7 +164,8 @@ std::string kernel_name(xtg_batch* b, const Tree& t, int gl, const AccChoice* ch
     const std::string tree = tree_type(t, t.root, map);
     if (b->reduce)
         return "xtg::k_batch_rowreduce<" + tree + ", " + ls + ", " + ch->acc + ", " + dt(b->out_dtype).cname + ", " +
-               std::to_string(ch->post) + ", " + std::to_string(gl) + ", " + std::to_string(b->unroll) + ">";
+               std::to_string(ch->post) + ", " + std::to_string(gl) + ", " +
+               std::to_string(b->vec > 1 ? 2 : b->unroll) + ", " + std::to_string(b->vec) + ">";
     return "xtg::k_batch_assign<" + tree + ", " + ls + ", " + dt(b->out_dtype).cname + ", " + std::to_string(gl) + ", " +
            std::to_string(b->unroll) + ">";
 }
@@ -299,6 +301,17 @@ xtg_status xtg_batch_build(xtg_batch* b, int32_t autotune, xtg_stream stream) {
         b->params.has_initial = ch.has_initial;
         b->params.initial_f = ch.initial_f;
         b->params.initial_i = ch.initial_i;
+    }
+    // vector form of the row reduction: every leaf of every instance
+    // contiguous or broadcast along its rows, all leaves of one element size
+    b->vec = 1;
+    if (b->reduce && !t.leaves.empty() && opt("batch.vec", 1)) {
+        const int esz = dt(t.leaves[0].dtype).size;
+        bool ok = esz >= 1 && esz <= 8 && 16 % esz == 0;
+        for (auto& L : t.leaves) ok = ok && dt(L.dtype).size == esz;
+        for (auto& I : b->inst)
+            for (size_t l = 0; ok && l < t.leaves.size(); ++l) ok = I.cs[l] == 0 || I.cs[l] == 1;
+        if (ok) b->vec = 16 / esz;
     }
     // shape class for the tuning cache
     std::vector<int64_t> cols, rows;

@@ -2643,7 +2643,111 @@ template <class T, class A, class B, int KR> struct Prep<MulRecip<T, A, B, KR>> 
 // counter until the list is exhausted; a sub-warp group of GL lanes owns a
 // row.  Row reductions: each row's result is produced by one group in a fixed
 // order, so results do not depend on which CTA took the tile.
-template <class Tree, class LS, class Acc, class Out, int POST, int GL, int U>
+// Row loads for the vector form of K8: per leaf a 2-bit mode for the row —
+// 3: contiguous and 16-byte aligned at the row's vector start (one vector
+// load), 1: contiguous but differently aligned (VEC scalar loads), 0:
+// broadcast along the row (one load).  The modes are uniform over a row, so
+// the branches do not diverge.
+template <int I, int VEC, class... S> struct LoadRowV;
+template <int I, int VEC> struct LoadRowV<I, VEC> {
+    template <class RG> static XTG_DI void run(RG&, const void* const*, i64, unsigned) {}
+};
+template <int I, int VEC, class S0, class... S> struct LoadRowV<I, VEC, S0, S...> {
+    template <class RG> static XTG_DI void run(RG& rg, const void* const* ptr, i64 col, unsigned modes) {
+        typedef typename S0::type T;
+        const T* b = reinterpret_cast<const T*>(ptr[I]);
+        const unsigned m = (modes >> (2 * I)) & 3u;
+        if (VEC > 1 && m == 3u) {
+            ld_contig<T, VEC>(rg.v, b + col);
+        } else if (m != 0u) {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) rg.v[j] = ld1<T>(b + col + j);
+        } else {
+            const T v = ld1<T>(b);
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) rg.v[j] = v;
+        }
+        LoadRowV<I + 1, VEC, S...>::run(rg.rest, ptr, col, modes);
+    }
+};
+template <class LS> struct LoadRowVec;
+template <class... S> struct LoadRowVec<LeafSet<S...>> {
+    template <int VEC, class RG> static XTG_DI void run(RG& rg, const void* const* ptr, i64 col, unsigned modes) {
+        LoadRowV<0, VEC, S...>::run(rg, ptr, col, modes);
+    }
+};
+
+// K8 vector form: every leaf of every instance is contiguous (column stride
+// 1) or broadcast (0) along a row, all of one element size E = 16 / VEC.  A
+// group of GL lanes owns a row: a scalar head up to the first 16-byte
+// boundary of the row's first contiguous leaf, then VEC-wide vectors (16-byte
+// loads for the leaves aligned like it, scalar loads for the others), then a
+// scalar tail; U vectors per lane in flight.  Each lane folds its columns in
+// order; lanes merge by the fixed butterfly, so a row's result does not
+// depend on the tile's CTA.
+template <class Tree, class LS, class Acc, class Out, int POST, int GL, int U, int VEC>
+XTG_DI void batch_row_vec(const BatchInst* I, i64 row, int gl, Acc& acc, Ctx<0>& c) {
+    typedef typename LS::template R<VEC>::type RGV;
+    typedef typename LS::template R<1>::type RG1;
+    const i64 cols = I->cols;
+    const void* rp[XTG_KMAX_LEAVES];
+    unsigned modes = 0;
+    int prim = -1;
+#pragma unroll
+    for (int l = 0; l < LS::N; ++l) {
+        rp[l] = reinterpret_cast<const char*>(I->leaf[l]) + row * I->rs[l] * (16 / VEC);
+        if (I->cs[l] != 0) {
+            modes |= 1u << (2 * l);
+            if (prim < 0) prim = l;
+        }
+    }
+    i64 head = 0;
+    if (prim >= 0) {
+        const unsigned mis = (unsigned)((unsigned long long)rp[prim] & 15u) / (16 / VEC);
+        head = mis ? (i64)(VEC - mis) : 0;
+        if (head > cols) head = cols;
+#pragma unroll
+        for (int l = 0; l < LS::N; ++l)
+            if (I->cs[l] != 0 && (((unsigned long long)rp[l] + (unsigned long long)head * (16 / VEC)) & 15u) == 0) modes |= 2u << (2 * l);
+    }
+    if (NeedsShift<Acc>::value && cols > 0) {
+        RG1 r1;
+        LoadRowVec<LS>::template run<1>(r1, rp, 0, modes & 0x55555555u);
+        Shift<Acc>::set(acc, Tree::ev(r1, 0, c));
+    }
+    // head (fewer than VEC columns)
+    if (gl < head) {
+        RG1 r1;
+        LoadRowVec<LS>::template run<1>(r1, rp, gl, modes & 0x55555555u);
+        acc.add(Tree::ev(r1, 0, c), (i64)gl);
+    }
+    const i64 nv = (cols - head) / VEC;
+    for (i64 v0 = gl; v0 < nv; v0 += (i64)GL * U) {
+        RGV rg[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const i64 v = v0 + (i64)u * GL;
+            if (v < nv) LoadRowVec<LS>::template run<VEC>(rg[u], rp, head + v * VEC, modes);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const i64 v = v0 + (i64)u * GL;
+            if (v < nv) {
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) acc.add(Tree::ev(rg[u], j, c), head + v * VEC + j);
+            }
+        }
+    }
+    // tail
+    const i64 t0 = head + nv * VEC;
+    if (t0 + gl < cols) {
+        RG1 r1;
+        LoadRowVec<LS>::template run<1>(r1, rp, t0 + gl, modes & 0x55555555u);
+        acc.add(Tree::ev(r1, 0, c), t0 + gl);
+    }
+}
+
+template <class Tree, class LS, class Acc, class Out, int POST, int GL, int U, int VEC = 1>
 __global__ void __launch_bounds__(256) k_batch_rowreduce(const BatchParams p) {
     typedef typename LS::template R<1>::type RG;
     __shared__ i64 s_tile;
@@ -2679,7 +2783,9 @@ __global__ void __launch_bounds__(256) k_batch_rowreduce(const BatchParams p) {
             const i64 row = tl.row0 + r;
             Acc acc;
             acc.init(fp);
-            if (active) {
+            if (VEC > 1) {
+                if (active) batch_row_vec<Tree, LS, Acc, Out, POST, GL, U, VEC>(I, row, gl, acc, c);
+            } else if (active) {
                 i64 base[XTG_KMAX_LEAVES];
 #pragma unroll
                 for (int l = 0; l < LS::N; ++l) base[l] = row * rsv[l];
