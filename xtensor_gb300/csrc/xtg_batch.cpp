@@ -45,6 +45,8 @@ struct xtg_batch {
     size_t tiles_cap = 0;
     std::vector<std::vector<xtg::BatchTile>> h_tiles;
     cudaStream_t stream = nullptr;  // stream of the last allocation / launch
+    cudaEvent_t last = nullptr;     // recorded after every upload and launch: destroy waits on it,
+                                    // never on the stream (which may be gone by then)
     // configuration
     int gl = 32, unroll = 4, cpsm = 4;
     int vec = 1;  // reductions: elements per vector load (1: the strided form)
@@ -165,9 +167,17 @@ std::string kernel_name(xtg_batch* b, const Tree& t, int gl, const AccChoice* ch
     if (b->reduce)
         return "xtg::k_batch_rowreduce<" + tree + ", " + ls + ", " + ch->acc + ", " + dt(b->out_dtype).cname + ", " +
                std::to_string(ch->post) + ", " + std::to_string(gl) + ", " +
-               std::to_string(b->vec > 1 ? 2 : b->unroll) + ", " + std::to_string(b->vec) + ">";
+               std::to_string(b->vec > 1 ? (int)opt("batch.vec_unroll", 2) : b->unroll) + ", " + std::to_string(b->vec) +
+               ", " + std::to_string(b->vec > 1 ? (int)opt("batch.vec_minblocks", 3) : 1) + ">";
     return "xtg::k_batch_assign<" + tree + ", " + ls + ", " + dt(b->out_dtype).cname + ", " + std::to_string(gl) + ", " +
            std::to_string(b->unroll) + ">";
+}
+
+xtg_status mark(xtg_batch* b, cudaStream_t s) {
+    if (dry_run()) return XTG_OK;
+    if (!b->last) XTG_CUDA(cudaEventCreateWithFlags(&b->last, cudaEventDisableTiming));
+    XTG_CUDA(cudaEventRecord(b->last, s));
+    return XTG_OK;
 }
 
 xtg_status launch_once(xtg_batch* b, cudaStream_t s) {
@@ -177,7 +187,8 @@ xtg_status launch_once(xtg_batch* b, cudaStream_t s) {
     b->stream = s;
     int64_t cap = (int64_t)std::min(b->k->max_blocks_per_sm, b->cpsm) * dev->sm_count;
     unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(b->ntiles, cap));
-    return launch(b->k, grid, 256, &b->params, s);
+    XTG_TRY(launch(b->k, grid, 256, &b->params, s));
+    return mark(b, s);
 }
 
 }  // namespace
@@ -436,6 +447,7 @@ xtg_status xtg_batch_capture(xtg_batch* b, xtg_stream stream) {
 xtg_status xtg_batch_replay(xtg_batch* b, xtg_stream stream) {
     if (!b || !b->exec) return fail(XTG_ERR_INVALID, "no captured graph");
     XTG_CUDA(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+    XTG_TRY(mark(b, (cudaStream_t)stream));
     count_launch();
     return XTG_OK;
 }
@@ -461,10 +473,17 @@ xtg_status xtg_batch_destroy(xtg_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (!dry_run()) {
-        // stream-ordered: the frees wait for the batch's last launch
-        if (b->d_inst) cudaFreeAsync(b->d_inst, b->stream);
-        if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->stream);
-        if (b->d_counter) cudaFreeAsync(b->d_counter, b->stream);
+        // wait for the batch's last upload / launch, then free without a
+        // stream: the caller may have destroyed the stream it used
+        if (b->last) {
+            cudaEventSynchronize(b->last);
+            cudaEventDestroy(b->last);
+        } else if (b->stream) {
+            cudaDeviceSynchronize();
+        }
+        if (b->d_inst) cudaFree(b->d_inst);
+        if (b->d_tiles) cudaFree(b->d_tiles);
+        if (b->d_counter) cudaFree(b->d_counter);
     }
     delete b;
     return XTG_OK;

@@ -2692,18 +2692,18 @@ XTG_DI void batch_row_vec(const BatchInst* I, i64 row, int gl, Acc& acc, Ctx<0>&
     const i64 cols = I->cols;
     const void* rp[XTG_KMAX_LEAVES];
     unsigned modes = 0;
-    int prim = -1;
+    unsigned long long prim = ~0ull;  // address of the first contiguous leaf's row
 #pragma unroll
     for (int l = 0; l < LS::N; ++l) {
         rp[l] = reinterpret_cast<const char*>(I->leaf[l]) + row * I->rs[l] * (16 / VEC);
         if (I->cs[l] != 0) {
             modes |= 1u << (2 * l);
-            if (prim < 0) prim = l;
+            if (prim == ~0ull) prim = (unsigned long long)rp[l];
         }
     }
     i64 head = 0;
-    if (prim >= 0) {
-        const unsigned mis = (unsigned)((unsigned long long)rp[prim] & 15u) / (16 / VEC);
+    if (prim != ~0ull) {
+        const unsigned mis = (unsigned)(prim & 15u) / (16 / VEC);
         head = mis ? (i64)(VEC - mis) : 0;
         if (head > cols) head = cols;
 #pragma unroll
@@ -2747,13 +2747,18 @@ XTG_DI void batch_row_vec(const BatchInst* I, i64 row, int gl, Acc& acc, Ctx<0>&
     }
 }
 
-template <class Tree, class LS, class Acc, class Out, int POST, int GL, int U, int VEC = 1>
-__global__ void __launch_bounds__(256) k_batch_rowreduce(const BatchParams p) {
+template <class Tree, class LS, class Acc, class Out, int POST, int GL, int U, int VEC = 1, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) k_batch_rowreduce(const BatchParams p) {
     typedef typename LS::template R<1>::type RG;
     __shared__ i64 s_tile;
     Ctx<0> c;
     c.scal = p.scal;
-    const int g = (int)threadIdx.x / GL, gl = (int)threadIdx.x % GL, ngroups = (int)blockDim.x / GL;
+    // the vector form takes tiles per warp (no block barrier between tiles);
+    // the strided form per block
+    constexpr bool WT = VEC > 1;
+    const int lane32 = (int)threadIdx.x & 31;
+    const int g = WT ? lane32 / GL : (int)threadIdx.x / GL, gl = (int)threadIdx.x % GL;
+    const int ngroups = WT ? 32 / GL : (int)blockDim.x / GL;
     FinP fp;
     fp.init_f = p.init_f;
     fp.init_i = p.init_i;
@@ -2761,10 +2766,17 @@ __global__ void __launch_bounds__(256) k_batch_rowreduce(const BatchParams p) {
     fp.initial_f = p.initial_f;
     fp.initial_i = p.initial_i;
     for (;;) {
-        __syncthreads();
-        if (threadIdx.x == 0) s_tile = (i64)atomicAdd(p.counter, 1);
-        __syncthreads();
-        const i64 t = s_tile;
+        i64 t;
+        if (WT) {
+            int tt = 0;
+            if (lane32 == 0) tt = atomicAdd(p.counter, 1);
+            t = (i64)__shfl_sync(0xffffffffu, tt, 0);
+        } else {
+            __syncthreads();
+            if (threadIdx.x == 0) s_tile = (i64)atomicAdd(p.counter, 1);
+            __syncthreads();
+            t = s_tile;
+        }
         if (t >= p.ntiles) break;
         const BatchTile tl = p.tiles[t];
         const BatchInst* I = p.inst + tl.inst;
