@@ -1102,12 +1102,64 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
     }
 }
 
+// Asynchronous global -> shared copies of 4, 8 or 16 bytes (cp.async): the
+// copies are in flight without holding registers; a thread's own copies are
+// visible to it after cp.async.wait_group.
+XTG_DI unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+template <int B> XTG_DI void cp_async(void* dst, const void* src) {
+    if (B == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+    else if (B == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+XTG_DI void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> XTG_DI void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Per-leaf ring slots of the COL kernel: slot (stage, leaf, thread) is 16
+// bytes at ((stage * NL + leaf) * blockDim + thread) * 16.
+template <int I, int VEC, class... S> struct RingAt;
+template <int I, int VEC> struct RingAt<I, VEC> {
+    static XTG_DI void issue(unsigned char*, int, const void* const*, const i64*) {}
+    template <class RG> static XTG_DI void read(RG&, const unsigned char*, int) {}
+};
+template <int I, int VEC, class S0, class... S> struct RingAt<I, VEC, S0, S...> {
+    typedef typename S0::type T;
+    static XTG_DI void issue(unsigned char* slot0, int lstride, const void* const* ptr, const i64* off) {
+        cp_async<(int)sizeof(T) * VEC>(slot0 + (size_t)I * lstride, reinterpret_cast<const T*>(ptr[I]) + off[I]);
+        RingAt<I + 1, VEC, S...>::issue(slot0, lstride, ptr, off);
+    }
+    template <class RG> static XTG_DI void read(RG& rg, const unsigned char* slot0, int lstride) {
+        constexpr int B = (int)sizeof(T) * VEC;
+        typedef typename VecT<B>::t V;
+        union { V v; T e[VEC]; } u;
+        u.v = *reinterpret_cast<const V*>(slot0 + (size_t)I * lstride);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) rg.v[j] = u.e[j];
+        RingAt<I + 1, VEC, S...>::read(rg.rest, slot0, lstride);
+    }
+};
+template <class LS, int VEC> struct Ring;
+template <class... S, int VEC> struct Ring<LeafSet<S...>, VEC> {
+    static XTG_DI void issue(unsigned char* slot0, int lstride, const void* const* ptr, const i64* off) {
+        RingAt<0, VEC, S...>::issue(slot0, lstride, ptr, off);
+    }
+    template <class RG> static XTG_DI void read(RG& rg, const unsigned char* slot0, int lstride) {
+        RingAt<0, VEC, S...>::read(rg, slot0, lstride);
+    }
+};
+
 // K4: COL strategy — the innermost kept dim is contiguous; each thread owns
 // VEC consecutive outputs and walks the reduced space (U loads in flight).
+// With RS > 0 (every leaf contiguous along the outputs, VEC * size of 4, 8
+// or 16 bytes) the loads are asynchronous copies into a per-thread ring of
+// RS stages in shared memory: RS - 1 rows in flight without registers.
 // Work items: w = s * n_outv + ov (consecutive threads -> consecutive outputs).
-template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int U, bool BIG>
+template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int U, bool BIG, int RS = 0>
 __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
     typedef typename LS::template R<VEC>::type RG;
+    extern __shared__ __align__(16) unsigned char col_ring[];
     Ctx<0> c;
     c.scal = p.scal;
     const i64 nwork = p.n_outv * p.nsplit;
@@ -1137,6 +1189,37 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
         const i64 rb = s * p.chunk;
         i64 re = rb + p.chunk;
         if (re > p.n_redv) re = p.n_redv;
+        if constexpr (RS > 0) {
+            const int lstride = (int)blockDim.x * 16;
+            const int sstride = LS::N * lstride;
+            unsigned char* mine = col_ring + (size_t)threadIdx.x * 16;
+            auto issue = [&](i64 r, int st) {
+                i64 ri[RR];
+                decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);
+                i64 off[XTG_KMAX_LEAVES];
+                red_offsets<LS::N, RO, RR>(p, ko, ri, off);
+                Ring<LS, VEC>::issue(mine + (size_t)st * sstride, lstride, p.leaf, off);
+            };
+#pragma unroll
+            for (int k = 0; k < RS - 1; ++k) {
+                if (rb + k < re) issue(rb + k, k);
+                cp_async_commit();
+            }
+            int st = 0;
+            for (i64 r = rb; r < re; ++r) {
+                cp_async_wait<RS - 2>();  // row r's copies have landed
+                RG rg;
+                Ring<LS, VEC>::read(rg, mine + (size_t)st * sstride, lstride);
+                // refill the slot row r - 1 used (read in the previous step)
+                const int sf = st == 0 ? RS - 1 : st - 1;
+                if (r + RS - 1 < re) issue(r + RS - 1, sf);
+                cp_async_commit();
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) acc[j].add(Tree::ev(rg, j, c), r);
+                st = st == RS - 1 ? 0 : st + 1;
+            }
+            cp_async_wait<0>();
+        } else {
         for (i64 r = rb; r < re; r += U) {
             RG rg[U];
 #pragma unroll
@@ -1156,6 +1239,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
                     for (int j = 0; j < VEC; ++j) acc[j].add(Tree::ev(rg[u], j, c), r + u);
                 }
             }
+        }
         }
         // flat output index of the first of the VEC outputs
         i64 ofl = 0;

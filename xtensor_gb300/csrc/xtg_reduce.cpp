@@ -308,13 +308,27 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         }
     } else {
         const int U = (int)opt("reduce.col_unroll", 4);
+        // asynchronous-copy ring when every leaf is contiguous along the
+        // outputs with 4-, 8- or 16-byte vectors: 8 / leaves stages
+        int rs = 0;
+        {
+            bool ok = opt("reduce.col_async", 1) != 0;
+            for (int l = 0; ok && l < NL; ++l) {
+                const int b = vec * dt(t.leaves[l].dtype).size;
+                ok = kinds[l] == 0 && (b == 4 || b == 8 || b == 16);
+            }
+            if (ok) rs = (int)std::max<int64_t>(2, std::min<int64_t>(opt("reduce.col_stages", 8), 8 / std::max(NL, 1)));
+            if (ok && NL > 4) rs = 0;
+        }
+        const size_t ring = (size_t)rs * (size_t)NL * 256 * 16;
         std::string name = "xtg::k_reduce_col<" + tree + ", " + ls + ", " + accname + ", " + outc + ", " +
                            std::to_string(post) + ", " + std::to_string(vec) + ", " + std::to_string(RO) + ", " +
-                           std::to_string(RR) + ", " + std::to_string(U) + ", " + (big ? "true" : "false") + ">";
-        st = get_kernel(name, 256, &k);
+                           std::to_string(RR) + ", " + std::to_string(U) + ", " + (big ? "true" : "false") + ", " +
+                           std::to_string(rs) + ">";
+        st = get_kernel(name, 256, &k, ring);
         if (st == XTG_OK) {
             int64_t need = (p.n_outv * nsplit + 255) / 256;
-            st = launch(k, grid_cap(k, need), 256, &p, stream, 0, part_off);
+            st = launch(k, grid_cap(k, need), 256, &p, stream, ring, part_off);
         }
     }
     if (st == XTG_OK && nsplit > 1) {
