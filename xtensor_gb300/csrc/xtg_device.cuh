@@ -1009,6 +1009,54 @@ template <class S0, class... S> struct LoadRest<LeafSet<S0, S...>> {
     }
 };
 
+// Asynchronous global -> shared copies of 4, 8 or 16 bytes (cp.async): the
+// copies are in flight without holding registers; a thread's own copies are
+// visible to it after cp.async.wait_group.
+XTG_DI unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+template <int B> XTG_DI void cp_async(void* dst, const void* src) {
+    if (B == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+    else if (B == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+XTG_DI void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> XTG_DI void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Per-leaf ring slots of the COL kernel: slot (stage, leaf, thread) is 16
+// bytes at ((stage * NL + leaf) * blockDim + thread) * 16.
+template <int I, int VEC, class... S> struct RingAt;
+template <int I, int VEC> struct RingAt<I, VEC> {
+    static XTG_DI void issue(unsigned char*, int, const void* const*, const i64*) {}
+    template <class RG> static XTG_DI void read(RG&, const unsigned char*, int) {}
+};
+template <int I, int VEC, class S0, class... S> struct RingAt<I, VEC, S0, S...> {
+    typedef typename S0::type T;
+    static XTG_DI void issue(unsigned char* slot0, int lstride, const void* const* ptr, const i64* off) {
+        cp_async<(int)sizeof(T) * VEC>(slot0 + (size_t)I * lstride, reinterpret_cast<const T*>(ptr[I]) + off[I]);
+        RingAt<I + 1, VEC, S...>::issue(slot0, lstride, ptr, off);
+    }
+    template <class RG> static XTG_DI void read(RG& rg, const unsigned char* slot0, int lstride) {
+        constexpr int B = (int)sizeof(T) * VEC;
+        typedef typename VecT<B>::t V;
+        union { V v; T e[VEC]; } u;
+        u.v = *reinterpret_cast<const V*>(slot0 + (size_t)I * lstride);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) rg.v[j] = u.e[j];
+        RingAt<I + 1, VEC, S...>::read(rg.rest, slot0, lstride);
+    }
+};
+template <class LS, int VEC> struct Ring;
+template <class... S, int VEC> struct Ring<LeafSet<S...>, VEC> {
+    static XTG_DI void issue(unsigned char* slot0, int lstride, const void* const* ptr, const i64* off) {
+        RingAt<0, VEC, S...>::issue(slot0, lstride, ptr, off);
+    }
+    template <class RG> static XTG_DI void read(RG& rg, const unsigned char* slot0, int lstride) {
+        RingAt<0, VEC, S...>::read(rg, slot0, lstride);
+    }
+};
+
 // K3/K5: ROW strategy — the reduced run is contiguous (or broadcast) for the
 // leaves; a group (warp or CTA) owns one (output, split) work item and strides
 // over its vectors.  Work items: w = o * nsplit + s.
@@ -1101,54 +1149,6 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
         if (GROUP > 32) __syncthreads();
     }
 }
-
-// Asynchronous global -> shared copies of 4, 8 or 16 bytes (cp.async): the
-// copies are in flight without holding registers; a thread's own copies are
-// visible to it after cp.async.wait_group.
-XTG_DI unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-template <int B> XTG_DI void cp_async(void* dst, const void* src) {
-    if (B == 16)
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-    else if (B == 8)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-XTG_DI void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N> XTG_DI void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// Per-leaf ring slots of the COL kernel: slot (stage, leaf, thread) is 16
-// bytes at ((stage * NL + leaf) * blockDim + thread) * 16.
-template <int I, int VEC, class... S> struct RingAt;
-template <int I, int VEC> struct RingAt<I, VEC> {
-    static XTG_DI void issue(unsigned char*, int, const void* const*, const i64*) {}
-    template <class RG> static XTG_DI void read(RG&, const unsigned char*, int) {}
-};
-template <int I, int VEC, class S0, class... S> struct RingAt<I, VEC, S0, S...> {
-    typedef typename S0::type T;
-    static XTG_DI void issue(unsigned char* slot0, int lstride, const void* const* ptr, const i64* off) {
-        cp_async<(int)sizeof(T) * VEC>(slot0 + (size_t)I * lstride, reinterpret_cast<const T*>(ptr[I]) + off[I]);
-        RingAt<I + 1, VEC, S...>::issue(slot0, lstride, ptr, off);
-    }
-    template <class RG> static XTG_DI void read(RG& rg, const unsigned char* slot0, int lstride) {
-        constexpr int B = (int)sizeof(T) * VEC;
-        typedef typename VecT<B>::t V;
-        union { V v; T e[VEC]; } u;
-        u.v = *reinterpret_cast<const V*>(slot0 + (size_t)I * lstride);
-#pragma unroll
-        for (int j = 0; j < VEC; ++j) rg.v[j] = u.e[j];
-        RingAt<I + 1, VEC, S...>::read(rg.rest, slot0, lstride);
-    }
-};
-template <class LS, int VEC> struct Ring;
-template <class... S, int VEC> struct Ring<LeafSet<S...>, VEC> {
-    static XTG_DI void issue(unsigned char* slot0, int lstride, const void* const* ptr, const i64* off) {
-        RingAt<0, VEC, S...>::issue(slot0, lstride, ptr, off);
-    }
-    template <class RG> static XTG_DI void read(RG& rg, const unsigned char* slot0, int lstride) {
-        RingAt<0, VEC, S...>::read(rg, slot0, lstride);
-    }
-};
 
 // K4: COL strategy — the innermost kept dim is contiguous; each thread owns
 // VEC consecutive outputs and walks the reduced space (U loads in flight).

@@ -145,6 +145,18 @@ static void lim_max(int t, double& f, int64_t& i) {
     }
 }
 
+// Stages of the column kernel's asynchronous-copy ring (0: register loads): used
+// when every leaf is contiguous along the vectorised dimension with 4-, 8-
+// or 16-byte vectors; 8 / leaves stages (at least 2), at most 4 leaves.
+static int async_stages(const Tree& t, const std::vector<int>& kinds, int NL, int vec, const char* on_key, const char* stages_key) {
+    if (!opt(on_key, 1) || NL < 1 || NL > 4) return 0;
+    for (int l = 0; l < NL; ++l) {
+        const int b = vec * dt(t.leaves[l].dtype).size;
+        if (kinds[l] != 0 || !(b == 4 || b == 8 || b == 16)) return 0;
+    }
+    return (int)std::max<int64_t>(2, std::min<int64_t>(opt(stages_key, 8), 8 / NL));
+}
+
 static unsigned grid_cap(Kernel* k, int64_t need) {
     DeviceInfo* dev;
     ensure_device(&dev);
@@ -297,6 +309,8 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
     xtg_status st;
     if (row) {
         const int group = (chunk >= opt("reduce.cta_chunk", 2048)) ? 256 : 32;
+        // (a copy ring as in the column kernel measured slower here: these
+        // loops are instruction-bound once two register batches are in flight)
         std::string name = "xtg::k_reduce_row<" + tree + ", " + ls + ", " + accname + ", " + outc + ", " +
                            std::to_string(post) + ", " + std::to_string(vec) + ", " + std::to_string(RO) + ", " +
                            std::to_string(RR) + ", " + std::to_string(group) + ", " + (big ? "true" : "false") + ">";
@@ -308,18 +322,7 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         }
     } else {
         const int U = (int)opt("reduce.col_unroll", 4);
-        // asynchronous-copy ring when every leaf is contiguous along the
-        // outputs with 4-, 8- or 16-byte vectors: 8 / leaves stages
-        int rs = 0;
-        {
-            bool ok = opt("reduce.col_async", 1) != 0;
-            for (int l = 0; ok && l < NL; ++l) {
-                const int b = vec * dt(t.leaves[l].dtype).size;
-                ok = kinds[l] == 0 && (b == 4 || b == 8 || b == 16);
-            }
-            if (ok) rs = (int)std::max<int64_t>(2, std::min<int64_t>(opt("reduce.col_stages", 8), 8 / std::max(NL, 1)));
-            if (ok && NL > 4) rs = 0;
-        }
+        const int rs = async_stages(t, kinds, NL, vec, "reduce.col_async", "reduce.col_stages");
         const size_t ring = (size_t)rs * (size_t)NL * 256 * 16;
         std::string name = "xtg::k_reduce_col<" + tree + ", " + ls + ", " + accname + ", " + outc + ", " +
                            std::to_string(post) + ", " + std::to_string(vec) + ", " + std::to_string(RO) + ", " +
