@@ -70,6 +70,7 @@ def test_results_same_alone_and_in_the_mix():
     reqs = make_requests()
     ref = [alone(q) for q in reqs]
     srv = Server(streams=6, max_inflight=32, batch_min_group=3)
+    xg.set_option("server.compile_inline", 1)  # the burst batches on its first wave
     outs, ids = [], []
     # hold admissions while the first half arrives (a burst the scheduler
     # admits together), then let the rest arrive while those run
@@ -94,6 +95,7 @@ def test_results_same_alone_and_in_the_mix():
     st = srv.stats()
     assert st["completed"] == len(reqs) and st["inflight"] == 0 and st["hbm_reserved"] == 0
     assert st["batch_launches"] >= 1, st
+    xg.set_option("server.compile_inline", 0)
     for q, o, r, res in zip(reqs, outs, ref, results):
         kind, op, e, axes, shape, A, v, Cm = q
         got = o.to_numpy()

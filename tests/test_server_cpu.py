@@ -56,6 +56,7 @@ def test_rejection_when_larger_than_budget():
 
 def test_cancel_timeout_and_grouped_wave():
     s = Server(batch_min_group=4)
+    xg.set_option("server.compile_inline", 1)  # batch on the first wave (this test counts launches)
     xg.set_option("server.paused", 1)
     ids = [s.submit_reduce("sum", fake((32, 64)) + fake((64,)), fake((32,)), axes=[-1]) for _ in range(10)]
     victim = s.submit_assign(fake((8, 8)), fake((8, 8)) * 3)
@@ -73,6 +74,33 @@ def test_cancel_timeout_and_grouped_wave():
         assert s.wait(rid, 5000)["status"] == 0
     st = s.stats()
     assert st["batch_launches"] >= 1 and st["batched_requests"] >= 10 and st["cancelled"] == 1
+    xg.set_option("server.compile_inline", 0)
+    s.close()
+
+
+def test_batch_kernels_compile_off_the_scheduler():
+    """A group whose batch kernel is not loaded runs one request at a time
+    while the kernel builds on another thread; a later group batches."""
+    import time
+    s = Server(batch_min_group=3)
+
+    def wave(n, rows):
+        xg.set_option("server.paused", 1)
+        ids = [s.submit_reduce("sum", fake((rows, 96)) * fake((96,)), fake((rows,)), axes=[-1]) for _ in range(n)]
+        xg.set_option("server.paused", 0)
+        kick = s.submit_assign(fake((4,)), fake((4,)) + 1)
+        for rid in ids + [kick]:
+            assert s.wait(rid, 20000)["status"] == 0
+
+    wave(6, 33)
+    first = s.stats()
+    assert first["batch_launches"] == 0  # the kernel was not loaded yet
+    for _ in range(200):  # its background build finishes
+        time.sleep(0.05)
+        wave(6, 33)
+        if s.stats()["batch_launches"] >= 1:
+            break
+    assert s.stats()["batch_launches"] >= 1
     s.close()
 
 

@@ -191,7 +191,53 @@ xtg_status launch_once(xtg_batch* b, cudaStream_t s) {
     return mark(b, s);
 }
 
+// The parts of a build that decide the kernel: the tree, the accumulator,
+// the vector form and the default group width.
+xtg_status plan_kernel(xtg_batch* b, Tree& t, AccChoice& ch, int& gl_default, std::vector<int64_t>& cols,
+                       std::vector<int64_t>& rows) {
+    const bool demote = opt("fp32_compute", 1) != 0 && b->out_dtype != XTG_FLOAT64;
+    XTG_TRY(build_tree(&b->templ, demote, t, false));
+    if (b->reduce) {
+        XTG_TRY(choose_acc(t, &b->rd, ch));
+        if (ch.result_dtype != b->out_dtype)
+            return fail(XTG_ERR_INVALID, "batch output dtype differs from the reduction's result type");
+    }
+    // vector form of the row reduction: every leaf of every instance
+    // contiguous or broadcast along its rows, all leaves of one element size
+    b->vec = 1;
+    if (b->reduce && !t.leaves.empty() && opt("batch.vec", 1)) {
+        const int esz = dt(t.leaves[0].dtype).size;
+        bool ok = esz >= 1 && esz <= 8 && 16 % esz == 0;
+        for (auto& L : t.leaves) ok = ok && dt(L.dtype).size == esz;
+        for (auto& I : b->inst)
+            for (size_t l = 0; ok && l < t.leaves.size(); ++l) ok = I.cs[l] == 0 || I.cs[l] == 1;
+        if (ok) b->vec = 16 / esz;
+    }
+    cols.clear();
+    rows.clear();
+    for (auto& I : b->inst) {
+        cols.push_back(I.cols);
+        rows.push_back(I.rows);
+    }
+    std::sort(cols.begin(), cols.end());
+    std::sort(rows.begin(), rows.end());
+    gl_default = (int)opt("batch.group_lanes", -1);
+    if (gl_default < 0) gl_default = cols[cols.size() / 2] >= 512 ? 32 : (cols[cols.size() / 2] >= 128 ? 16 : 8);
+    return XTG_OK;
+}
+
 }  // namespace
+
+xtg_status xtgh::batch_planned_kernel(xtg_batch* b, std::string* name) {
+    if (!b || b->inst.empty()) return fail(XTG_ERR_INVALID, "empty batch");
+    Tree t;
+    AccChoice ch;
+    int gl;
+    std::vector<int64_t> cols, rows;
+    XTG_TRY(plan_kernel(b, t, ch, gl, cols, rows));
+    *name = kernel_name(b, t, gl, b->reduce ? &ch : nullptr);
+    return XTG_OK;
+}
 
 extern "C" {
 
@@ -285,15 +331,11 @@ xtg_status xtg_batch_build(xtg_batch* b, int32_t autotune, xtg_stream stream) {
     DeviceInfo* dev;
     XTG_TRY(ensure_device(&dev));
     cudaStream_t s = (cudaStream_t)stream;
-    const bool demote = opt("fp32_compute", 1) != 0 && b->out_dtype != XTG_FLOAT64;
     Tree t;
-    XTG_TRY(build_tree(&b->templ, demote, t, false));
     AccChoice ch;
-    if (b->reduce) {
-        XTG_TRY(choose_acc(t, &b->rd, ch));
-        if (ch.result_dtype != b->out_dtype)
-            return fail(XTG_ERR_INVALID, "batch output dtype differs from the reduction's result type");
-    }
+    int gl_default;
+    std::vector<int64_t> cols, rows;
+    XTG_TRY(plan_kernel(b, t, ch, gl_default, cols, rows));
     // device work list
     if (!dry_run()) {
         if (!b->d_inst) XTG_CUDA(cudaMallocAsync((void**)&b->d_inst, b->inst.size() * sizeof(xtg::BatchInst), s));
@@ -313,25 +355,7 @@ xtg_status xtg_batch_build(xtg_batch* b, int32_t autotune, xtg_stream stream) {
         b->params.initial_f = ch.initial_f;
         b->params.initial_i = ch.initial_i;
     }
-    // vector form of the row reduction: every leaf of every instance
-    // contiguous or broadcast along its rows, all leaves of one element size
-    b->vec = 1;
-    if (b->reduce && !t.leaves.empty() && opt("batch.vec", 1)) {
-        const int esz = dt(t.leaves[0].dtype).size;
-        bool ok = esz >= 1 && esz <= 8 && 16 % esz == 0;
-        for (auto& L : t.leaves) ok = ok && dt(L.dtype).size == esz;
-        for (auto& I : b->inst)
-            for (size_t l = 0; ok && l < t.leaves.size(); ++l) ok = I.cs[l] == 0 || I.cs[l] == 1;
-        if (ok) b->vec = 16 / esz;
-    }
     // shape class for the tuning cache
-    std::vector<int64_t> cols, rows;
-    for (auto& I : b->inst) {
-        cols.push_back(I.cols);
-        rows.push_back(I.rows);
-    }
-    std::sort(cols.begin(), cols.end());
-    std::sort(rows.begin(), rows.end());
     const std::string base = kernel_name(b, t, 0, b->reduce ? &ch : nullptr);
     char cls[160];
     snprintf(cls, sizeof cls, "|n%d|c%d|r%d|e%d|sm%d", ilog2((int64_t)b->inst.size()), ilog2(cols[cols.size() / 2]),
@@ -340,9 +364,8 @@ xtg_status xtg_batch_build(xtg_batch* b, int32_t autotune, xtg_stream stream) {
     for (char c : base + cls)
         if (c != ' ') key += c;
 
-    int gl = (int)opt("batch.group_lanes", -1), cpsm = (int)opt("batch.ctas_per_sm", 4);
+    int gl = gl_default, cpsm = (int)opt("batch.ctas_per_sm", 4);
     int64_t te = opt("batch.tile_elems", 32768);
-    if (gl < 0) gl = cols[cols.size() / 2] >= 512 ? 32 : (cols[cols.size() / 2] >= 128 ? 16 : 8);
     b->tuned = 0;
     if (autotune && !dry_run()) {
         int tg, tc;
@@ -409,6 +432,7 @@ xtg_status xtg_batch_build(xtg_batch* b, int32_t autotune, xtg_stream stream) {
     b->kname = kernel_name(b, t, gl, b->reduce ? &ch : nullptr);
     XTG_TRY(get_kernel(b->kname, 256, &b->k));
     b->built = true;
+    XTG_TRY(mark(b, s));  // the uploads are ordered before the event destroy waits on
     return XTG_OK;
 }
 
@@ -473,17 +497,19 @@ xtg_status xtg_batch_destroy(xtg_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (!dry_run()) {
-        // wait for the batch's last upload / launch, then free without a
-        // stream: the caller may have destroyed the stream it used
+        // wait for the batch's last upload / launch (its own event: the
+        // caller may have destroyed the stream it used), then free on the
+        // per-thread stream — cudaFree would synchronise the whole device,
+        // stalling a server that destroys batches while others run
         if (b->last) {
             cudaEventSynchronize(b->last);
             cudaEventDestroy(b->last);
         } else if (b->stream) {
             cudaDeviceSynchronize();
         }
-        if (b->d_inst) cudaFree(b->d_inst);
-        if (b->d_tiles) cudaFree(b->d_tiles);
-        if (b->d_counter) cudaFree(b->d_counter);
+        if (b->d_inst) cudaFreeAsync(b->d_inst, cudaStreamPerThread);
+        if (b->d_tiles) cudaFreeAsync(b->d_tiles, cudaStreamPerThread);
+        if (b->d_counter) cudaFreeAsync(b->d_counter, cudaStreamPerThread);
     }
     delete b;
     return XTG_OK;

@@ -93,6 +93,13 @@ struct Kernel {
 // (e.g. "xtg::k_assign<...>").  `block` / `dyn_smem` are used for the
 // occupancy query (and dyn_smem > 48 KiB raises the kernel's limit).
 xtg_status get_kernel(const std::string& expr, int block, Kernel** k, size_t dyn_smem = 0);
+// Whether `expr` is compiled and loaded in this process (no compile).
+bool kernel_ready(const std::string& expr);
+// Compiles and loads `expr` on a background thread (no-op when it is ready
+// or being built); callers that must not wait use their other path meanwhile.
+void compile_async(const std::string& expr, int block, size_t dyn_smem = 0);
+// Waits (bounded) until no background compile is running.
+void wait_background_compiles(int64_t timeout_ms);
 // Launch with a parameter block of `psize` bytes.  scratch_off >= 0: byte
 // offset of a pointer to the call's split-reduction scratch inside the
 // block (patched when a cached plan is replayed with fresh scratch).
@@ -125,6 +132,10 @@ xtg_status device_error_word(int** p);
 void count_launch();
 // Resets the per-thread record of launched kernels (start of an API call).
 void begin_call();
+
+// ---- batches (xtg_batch.cpp) -----------------------------------------------------------
+// The kernel xtg_batch_build would launch without autotuning (no device work).
+xtg_status batch_planned_kernel(xtg_batch* b, std::string* name);
 
 // ---- pinned staging ring (xtg_npy.cpp) ---------------------------------------------
 // Copies `bytes` of pageable host memory to device memory through the pinned

@@ -14,10 +14,13 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <condition_variable>
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <unordered_map>
+#include <unordered_set>
 
 #include <sys/stat.h>
 #include <unistd.h>
@@ -31,12 +34,15 @@ namespace {
 
 struct JitState {
     std::mutex mu;
+    std::condition_variable cv;  // a kernel another thread was building is ready
     std::unordered_map<std::string, std::unique_ptr<Kernel>> kernels;
+    std::unordered_set<std::string> building;  // compiled / loaded right now, outside the lock
+    int background = 0;                        // compile_async threads still running
     xtg_jit_stats st{};
 };
 JitState& js() {
-    static JitState s;
-    return s;
+    static JitState* s = new JitState();  // never destroyed: a background compile may outlive main()
+    return *s;
 }
 std::atomic<int64_t> g_launches{0};
 
@@ -145,19 +151,92 @@ static xtg_status configure(Kernel* k, int block, size_t dyn_smem) {
     return XTG_OK;
 }
 
+xtg_status build_kernel(const std::string& expr, DeviceInfo* dev, std::unique_ptr<Kernel>& k, bool& compiled,
+                        bool& from_disk, double& secs);
+
+// The cache lock is not held while a kernel is compiled or loaded: other
+// threads keep launching cached kernels meanwhile; a second request for a
+// kernel that is being built waits for it instead of compiling it again.
 xtg_status get_kernel(const std::string& expr, int block, Kernel** out, size_t dyn_smem) {
     DeviceInfo* dev;
     XTG_TRY(ensure_device(&dev));
     JitState& S = js();
-    std::lock_guard<std::mutex> lk(S.mu);
     // dry-run kernels have no function handle: keep them apart
     const std::string key = dry_run() ? "dry:" + expr : expr;
-    auto it = S.kernels.find(key);
-    if (it != S.kernels.end()) {
-        S.st.memory_hits++;
-        *out = it->second.get();
-        return configure(*out, block, dyn_smem);
+    {
+        std::unique_lock<std::mutex> lk(S.mu);
+        for (;;) {
+            auto it = S.kernels.find(key);
+            if (it != S.kernels.end()) {
+                S.st.memory_hits++;
+                *out = it->second.get();
+                return configure(*out, block, dyn_smem);
+            }
+            if (!S.building.count(key)) break;
+            S.cv.wait(lk);
+        }
+        S.building.insert(key);
     }
+    struct Done {
+        JitState& S;
+        const std::string& key;
+        ~Done() {
+            std::lock_guard<std::mutex> lk(S.mu);
+            S.building.erase(key);
+            S.cv.notify_all();
+        }
+    } done{S, key};
+    std::unique_ptr<Kernel> k;
+    bool compiled = false, disk = false;
+    double secs = 0;
+    XTG_TRY(build_kernel(expr, dev, k, compiled, disk, secs));
+    std::lock_guard<std::mutex> lk(S.mu);
+    if (compiled) {
+        S.st.compiles++;
+        S.st.compile_seconds += secs;
+    }
+    if (disk) S.st.disk_hits++;
+    Kernel* kp = k.get();
+    S.kernels.emplace(key, std::move(k));
+    *out = kp;
+    if (dry_run()) return XTG_OK;
+    return configure(kp, block, dyn_smem);
+}
+
+bool kernel_ready(const std::string& expr) {
+    JitState& S = js();
+    std::lock_guard<std::mutex> lk(S.mu);
+    return S.kernels.count(dry_run() ? "dry:" + expr : expr) > 0;
+}
+
+void compile_async(const std::string& expr, int block, size_t dyn_smem) {
+    JitState& S = js();
+    {
+        std::lock_guard<std::mutex> lk(S.mu);
+        const std::string key = dry_run() ? "dry:" + expr : expr;
+        if (S.kernels.count(key) || S.building.count(key)) return;
+        S.background++;
+    }
+    std::thread([expr, block, dyn_smem]() {
+        Kernel* k = nullptr;
+        get_kernel(expr, block, &k, dyn_smem);
+        clear_error();
+        JitState& S = js();
+        std::lock_guard<std::mutex> lk(S.mu);
+        S.background--;
+        S.cv.notify_all();
+    }).detach();
+}
+
+void wait_background_compiles(int64_t timeout_ms) {
+    JitState& S = js();
+    std::unique_lock<std::mutex> lk(S.mu);
+    S.cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return S.background == 0; });
+}
+
+// Compiles (or reads from the disk cache) and loads one kernel; no shared state.
+xtg_status build_kernel(const std::string& expr, DeviceInfo* dev, std::unique_ptr<Kernel>& k, bool& compiled,
+                        bool& from_disk, double& secs) {
     char arch[32];
     snprintf(arch, sizeof arch, "sm_%d%da", dev->cc_major, dev->cc_minor);
     int vmaj = 0, vmin = 0;
@@ -170,7 +249,8 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out, size_t d
     const std::string path = dir + "/" + hex + ".cubin";
 
     std::string blob, cubin, lowered;
-    bool from_disk = false;
+    from_disk = false;
+    compiled = false;
     if (read_file(path, blob) && blob.size() > 8) {
         uint32_t nl = 0;
         memcpy(&nl, blob.data(), 4);
@@ -184,23 +264,19 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out, size_t d
         auto t0 = std::chrono::steady_clock::now();
         XTG_TRY(compile(expr, arch, cubin, lowered));
         auto t1 = std::chrono::steady_clock::now();
-        S.st.compiles++;
-        S.st.compile_seconds += std::chrono::duration<double>(t1 - t0).count();
+        compiled = true;
+        secs = std::chrono::duration<double>(t1 - t0).count();
         mkdirs(dir);
         uint32_t nl = (uint32_t)lowered.size();
         std::string b(4, '\0');
         memcpy(&b[0], &nl, 4);
         write_file_atomic(path, b + lowered + cubin);
-    } else {
-        S.st.disk_hits++;
     }
+    k.reset(new Kernel);
+    k->name = expr;
     if (dry_run()) {
-        std::unique_ptr<Kernel> k(new Kernel);
-        k->name = expr;
-        k->block = block;
+        k->block = 256;
         k->max_blocks_per_sm = 4;
-        *out = k.get();
-        S.kernels.emplace(key, std::move(k));
         return XTG_OK;
     }
     CUmodule mod;
@@ -209,13 +285,8 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out, size_t d
         if (from_disk) unlink(path.c_str());
         return cu_fail(cr, "cuModuleLoadData");
     }
-    std::unique_ptr<Kernel> k(new Kernel);
     XTG_CU(drv().ModuleGetFunction(&k->fn, mod, lowered.c_str()));
-    k->name = expr;
     k->max_blocks_per_sm = 0;
-    XTG_TRY(configure(k.get(), block, dyn_smem));
-    *out = k.get();
-    S.kernels.emplace(key, std::move(k));
     return XTG_OK;
 }
 

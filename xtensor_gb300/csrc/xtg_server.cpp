@@ -191,6 +191,17 @@ void dispatch(xtg_server* s, std::vector<Req*>& admitted) {
         int rc = xtg_batch_create(&f->r.expr, f->r.kind == XTG_REQ_REDUCE ? &f->r.rd : nullptr, &b);
         for (size_t i = 0; rc == XTG_OK && i < kv.second.size(); ++i)
             rc = xtg_batch_add(b, kv.second[i]->r.expr.leaves, kv.second[i]->r.expr.n_leaves, &kv.second[i]->r.out);
+        if (rc == XTG_OK) {
+            // never compile on the scheduler: a batch kernel that is not
+            // loaded yet is built in the background while this group runs
+            // one request at a time
+            std::string kname;
+            rc = batch_planned_kernel(b, &kname);
+            if (rc == XTG_OK && !kernel_ready(kname) && !opt("server.compile_inline", 0)) {
+                compile_async(kname, 256);
+                rc = XTG_ERR_UNSUPPORTED;
+            }
+        }
         if (rc == XTG_OK) rc = xtg_batch_build(b, 0, st);
         if (rc == XTG_OK) rc = xtg_batch_run(b, st);
         if (rc != XTG_OK) {
@@ -450,6 +461,7 @@ xtg_status xtg_server_destroy(xtg_server* s) {
         s->cv_sched.notify_all();
     }
     if (s->sched.joinable()) s->sched.join();
+    wait_background_compiles(60000);  // batch kernels it started building
     for (cudaStream_t st : s->streams) {
         if (!st) continue;
         cudaStreamSynchronize(st);
