@@ -268,8 +268,13 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
         while (vec > 1 && !vec_ok(vec)) vec >>= 1;
         std::vector<int> rk(NL);
         for (int l = 0; l < NL; ++l) rk[l] = vec > 1 ? kind_of_s(p.lsa[l]) : 2;
+        // a plain contiguous operand of the accumulation type goes into the
+        // shared-memory tile by asynchronous copies (all 32 rows in flight)
+        const int vb = vec * dt(rt).size;
+        const bool raw = opt("scan.async", 1) && NL == 1 && t.nodes[t.root].op == XTG_OP_LEAF &&
+                         t.leaves[0].dtype == rt && p.lsa[0] == 1 && (vb == 4 || vb == 8 || vb == 16);
         std::string name = "xtg::k_scan_rows<" + tree + ", " + leafset_s(t, rk) + ", " + rts + ", " + ops + ", " +
-                           std::to_string(vec) + ">";
+                           std::to_string(vec) + ", " + (raw ? "true" : "false") + ">";
         Kernel* k;
         XTG_TRY(get_kernel(name, 64, &k));
         const int64_t groups = (n_outer + 31) / 32;

@@ -1382,7 +1382,7 @@ __global__ void __launch_bounds__(256) k_scan_col(const ScanParams p) {
 // back the same way.  Sequential order per row (bit-identical to the
 // reference's fold).  VEC > 1 needs rows whose length and starts are
 // multiples of VEC (the host checks).
-template <class Tree, class LS, class RT, int OP, int VEC>
+template <class Tree, class LS, class RT, int OP, int VEC, bool RAW = false>
 __global__ void __launch_bounds__(64) k_scan_rows(const ScanParams p) {
     typedef typename LS::template R<VEC>::type RG;
     constexpr int CW = 32 * VEC;        // columns per chunk
@@ -1398,6 +1398,19 @@ __global__ void __launch_bounds__(64) k_scan_rows(const ScanParams p) {
         RT acc = RT(0);
         for (i64 c0 = 0; c0 < p.len; c0 += CW) {
             const i64 col = c0 + (i64)lane * VEC;
+            if constexpr (RAW) {
+                // the operand is the accumulation type, contiguous along the
+                // rows: copy it into the tile, every row's vector in flight
+                const RT* src = reinterpret_cast<const RT*>(p.leaf[0]);
+#pragma unroll 8
+                for (int i = 0; i < 32; ++i) {
+                    const i64 r = r0 + i;
+                    if (r < p.n_outer && col < p.len)
+                        cp_async<(int)sizeof(RT) * VEC>(tw + (i64)i * RS + lane * VEC, src + r * p.lso[0] + col);
+                }
+                cp_async_commit();
+                cp_async_wait<0>();
+            } else {
 #pragma unroll 4
             for (int i = 0; i < 32; ++i) {
                 const i64 r = r0 + i;
@@ -1412,6 +1425,7 @@ __global__ void __launch_bounds__(64) k_scan_rows(const ScanParams p) {
                     for (int j = 0; j < VEC; ++j) v[j] = cvt<RT>(Tree::ev(rg, j, c));
                     st_out<RT, K_CONTIG, VEC>(tw, (i64)i * RS + lane * VEC, 1, v);
                 }
+            }
             }
             __syncwarp();
             const int lim = (p.len - c0) < CW ? (int)(p.len - c0) : CW;
