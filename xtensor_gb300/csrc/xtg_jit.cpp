@@ -199,7 +199,10 @@ xtg_status get_kernel(const std::string& expr, int block, Kernel** out, size_t d
     Kernel* kp = k.get();
     S.kernels.emplace(key, std::move(k));
     *out = kp;
-    if (dry_run()) return XTG_OK;
+    if (dry_run()) {
+        kp->block = block;
+        return XTG_OK;
+    }
     return configure(kp, block, dyn_smem);
 }
 
@@ -275,7 +278,6 @@ xtg_status build_kernel(const std::string& expr, DeviceInfo* dev, std::unique_pt
     k.reset(new Kernel);
     k->name = expr;
     if (dry_run()) {
-        k->block = 256;
         k->max_blocks_per_sm = 4;
         return XTG_OK;
     }
