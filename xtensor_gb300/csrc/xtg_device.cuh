@@ -1882,21 +1882,67 @@ XTG_DI bool filter_cond(const FilterParams& p, const Ctx<0>& c, i64 k, i64 (&ix)
     return Tree::ev(rg, 0, c) != typename Tree::type(0);
 }
 
-template <class CTree, class CLS, int R, bool BIG>
+// One flat dim (R == 1), every condition leaf contiguous (stride 1, 16-byte
+// aligned) or broadcast (stride 0): the 16 consecutive positions of a
+// thread are read with 16-byte loads.
+template <int I, class... S> struct LoadFlat16;
+template <int I> struct LoadFlat16<I> {
+    template <class RG> static XTG_DI void run(RG&, const void* const*, i64, const i64 (*)[XTG_KMAX_RANK]) {}
+};
+template <int I, class S0, class... S> struct LoadFlat16<I, S0, S...> {
+    template <class RG> static XTG_DI void run(RG& rg, const void* const* ptr, i64 k0, const i64 (*st)[XTG_KMAX_RANK]) {
+        typedef typename S0::type T;
+        const T* b = reinterpret_cast<const T*>(ptr[I]);
+        if (st[I][0] != 0) {
+            constexpr int NV = (int)sizeof(T) * 16 / 16;  // 16-byte vectors for 16 elements
+            union { uint4 v[NV]; T e[16]; } u;
+#pragma unroll
+            for (int q = 0; q < NV; ++q) u.v[q] = __ldg(reinterpret_cast<const uint4*>(b + k0) + q);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) rg.v[j] = u.e[j];
+        } else {
+            const T v = ld1<T>(b);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) rg.v[j] = v;
+        }
+        LoadFlat16<I + 1, S...>::run(rg.rest, ptr, k0, st);
+    }
+};
+template <class LS> struct CondFlat16;
+template <class... S> struct CondFlat16<LeafSet<S...>> {
+    template <class Tree> static XTG_DI unsigned run(const FilterParams& p, const Ctx<0>& c, i64 k0) {
+        typename LeafSet<S...>::template R<16>::type rg;
+        LoadFlat16<0, S...>::run(rg, p.cleaf, k0, p.cls);
+        unsigned f = 0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (Tree::ev(rg, j, c) != typename Tree::type(0)) f |= 1u << j;
+        return f;
+    }
+};
+// The condition flags of positions k0 .. k0 + 15 (bit i: position k0 + i).
+template <class CTree, class CLS, int R, bool BIG, bool V16>
+XTG_DI unsigned filter_flags16(const FilterParams& p, const Ctx<0>& c, i64 k0) {
+    if (V16 && k0 + 16 <= p.n) return CondFlat16<CLS>::template run<CTree>(p, c, k0);
+    unsigned flags = 0;
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+        const i64 k = k0 + i;
+        i64 ix[R];
+        if (k < p.n && filter_cond<CTree, CLS, R, BIG>(p, c, k, ix)) flags |= 1u << i;
+    }
+    return flags;
+}
+
+template <class CTree, class CLS, int R, bool BIG, bool V16 = false>
 __global__ void __launch_bounds__(256) k_filter_count(const FilterParams p) {
     __shared__ int ws[8];
     Ctx<0> c;
     c.scal = p.cscal;
     const i64 ntiles = (p.n + 4095) / 4096;
     for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        int cnt = 0;
         const i64 k0 = t * 4096 + (i64)threadIdx.x * 16;
-#pragma unroll 4
-        for (int i = 0; i < 16; ++i) {
-            const i64 k = k0 + i;
-            i64 ix[R];
-            if (k < p.n && filter_cond<CTree, CLS, R, BIG>(p, c, k, ix)) ++cnt;
-        }
+        int cnt = __popc(filter_flags16<CTree, CLS, R, BIG, V16>(p, c, k0));
         cnt = __reduce_add_sync(0xffffffffu, cnt);
         if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
         __syncthreads();
@@ -1910,7 +1956,8 @@ __global__ void __launch_bounds__(256) k_filter_count(const FilterParams p) {
 }
 
 // MODE 0: out[j] = e[position]; MODE 1: dst[position] = dst op src[j]
-template <class CTree, class CLS, class VTree, class VLS, class VT, class DT, class CT, int MODE, int R, int OP, bool BIG>
+template <class CTree, class CLS, class VTree, class VLS, class VT, class DT, class CT, int MODE, int R, int OP, bool BIG,
+          bool V16 = false>
 __global__ void __launch_bounds__(256) k_filter_tile(const FilterParams p) {
     typedef typename VLS::template R<1>::type VRG;
     __shared__ int ws[9];
@@ -1921,13 +1968,7 @@ __global__ void __launch_bounds__(256) k_filter_tile(const FilterParams p) {
     const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
     for (i64 t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const i64 k0 = t * 4096 + (i64)threadIdx.x * 16;
-        unsigned flags = 0;
-#pragma unroll 4
-        for (int i = 0; i < 16; ++i) {
-            const i64 k = k0 + i;
-            i64 ix[R];
-            if (k < p.n && filter_cond<CTree, CLS, R, BIG>(p, cc, k, ix)) flags |= 1u << i;
-        }
+        unsigned flags = filter_flags16<CTree, CLS, R, BIG, V16>(p, cc, k0);
         // exclusive prefix of the thread counts in thread order
         const int cnt = __popc(flags);
         int inc = cnt;

@@ -104,10 +104,18 @@ struct FilterRun {
     void* scratch = nullptr;
     int64_t ntiles = 0;
     bool big = false;
+    bool v16 = false;  // one flat dim, condition leaves contiguous (aligned) or broadcast: 16-byte loads
+    int rank = 1;  // of the position space after merging dims that are contiguous for every array
     std::string ctree, cls;
+    std::vector<std::array<int64_t, XTG_MAX_RANK>> extra;  // the callers' position strides, merged alike
 };
 
-xtg_status filter_prepare(const xtg_expr* cond, int rank, const int64_t* shape, FilterRun& F, cudaStream_t stream) {
+// `extra`: strides over the filtered shape of the other arrays the tile pass
+// addresses by position (the value leaves of a read, the destination of an
+// assignment).  Dims that are contiguous for the condition and all of them
+// merge (row-major order is kept), so a contiguous filter walks one flat dim.
+xtg_status filter_prepare(const xtg_expr* cond, int rank, const int64_t* shape, FilterRun& F, cudaStream_t stream,
+                          const std::vector<std::array<int64_t, XTG_MAX_RANK>>& extra = {}) {
     XTG_TRY(build_tree(cond, false, F.tc));
     if (F.tc.n_rstats) return fail(XTG_ERR_UNSUPPORTED, "row statistics inside a filter condition");
     if (F.tc.rank != rank) return fail(XTG_ERR_SHAPE, "condition shape differs from the filtered expression's");
@@ -115,17 +123,39 @@ xtg_status filter_prepare(const xtg_expr* cond, int rank, const int64_t* shape, 
         if (F.tc.shape[d] != shape[d]) return fail(XTG_ERR_SHAPE, "condition shape differs from the filtered expression's");
     memset(&F.p, 0, sizeof F.p);
     int64_t n = 1;
-    for (int d = 0; d < rank; ++d) {
-        n *= shape[d];
-        F.p.shape[d] = shape[d];
-        F.p.fd[d] = make_fd((uint64_t)std::max<int64_t>(shape[d], 1));
-    }
+    for (int d = 0; d < rank; ++d) n *= shape[d];
     F.p.n = n;
     F.big = n > 0xFFFFFFF0ll;
     const int NL = (int)F.tc.leaves.size();
+    Dims D;
+    D.R = rank;
+    for (int d = 0; d < rank; ++d) D.shape[d] = shape[d];
+    D.st.resize(NL + extra.size());
     for (int l = 0; l < NL; ++l) {
         F.p.cleaf[l] = F.tc.leaves[l].data;
-        bstrides_to(F.tc.leaves[l], rank, shape, reinterpret_cast<int64_t*>(F.p.cls[l]));
+        D.st[l].fill(0);
+        bstrides_to(F.tc.leaves[l], rank, shape, D.st[l].data());
+    }
+    for (size_t e = 0; e < extra.size(); ++e) D.st[NL + e] = extra[e];
+    if (D.st.empty()) D.st.resize(1);
+    collapse(D);
+    if (D.R == 0) {  // every extent 1: one position
+        D.R = 1;
+        D.shape[0] = 1;
+        for (auto& st : D.st) st[0] = 0;
+    }
+    F.rank = D.R;
+    for (int d = 0; d < D.R; ++d) {
+        F.p.shape[d] = D.shape[d];
+        F.p.fd[d] = make_fd((uint64_t)std::max<int64_t>(D.shape[d], 1));
+    }
+    for (int l = 0; l < NL; ++l)
+        for (int d = 0; d < D.R; ++d) F.p.cls[l][d] = D.st[l][d];
+    F.extra.assign(D.st.begin() + NL, D.st.begin() + NL + extra.size());
+    F.v16 = F.rank == 1;
+    for (int l = 0; F.v16 && l < NL; ++l) {
+        const int64_t st = F.p.cls[l][0];
+        F.v16 = st == 0 || (st == 1 && ((uintptr_t)F.tc.leaves[l].data % 16) == 0);
     }
     for (size_t i = 0; i < F.tc.scalars.size(); ++i) F.p.cscal.v[i] = F.tc.scalars[i];
     std::vector<int> map(NL);
@@ -141,8 +171,8 @@ xtg_status filter_prepare(const xtg_expr* cond, int rank, const int64_t* shape, 
     F.p.tincl = (const long long*)((char*)F.scratch + cbytes);
     if (recorder()) recorder()->nocache = true;  // scratch addresses are baked into several parameter blocks
     Kernel* k;
-    XTG_TRY(get_kernel("xtg::k_filter_count<" + F.ctree + ", " + F.cls + ", " + std::to_string(rank) + ", " +
-                           (F.big ? "true" : "false") + ">",
+    XTG_TRY(get_kernel("xtg::k_filter_count<" + F.ctree + ", " + F.cls + ", " + std::to_string(F.rank) + ", " +
+                           (F.big ? "true" : "false") + ", " + (F.v16 ? "true" : "false") + ">",
                        256, &k));
     XTG_TRY(launch(k, grid_n(k, F.ntiles * 256), 256, &F.p, stream));
     // inclusive scan of the int32 counts into int64
@@ -174,13 +204,31 @@ xtg_status filter_total(const FilterRun& F, int64_t* count, cudaStream_t stream)
     return XTG_OK;
 }
 
-xtg_status filter_launch(FilterRun& F, const Tree& tv, int mode, int op, int rank, const xtg_array& dst,
-                         cudaStream_t stream) {
+// The strides the tile pass addresses by position, before merging: the
+// value leaves of a read (mode 0) or the destination of an assignment.
+std::vector<std::array<int64_t, XTG_MAX_RANK>> filter_extra(const Tree& tv, int mode, int rank, const int64_t* shape,
+                                                            const xtg_array& dst) {
+    std::vector<std::array<int64_t, XTG_MAX_RANK>> ex;
+    if (mode == 0) {
+        for (const auto& L : tv.leaves) {
+            ex.emplace_back();
+            ex.back().fill(0);
+            bstrides_to(L, rank, shape, ex.back().data());
+        }
+    } else {
+        ex.emplace_back();
+        ex.back().fill(0);
+        for (int d = 0; d < dst.rank; ++d) ex.back()[d] = dst.shape[d] == 1 ? 0 : dst.strides[d];
+    }
+    return ex;
+}
+
+xtg_status filter_launch(FilterRun& F, const Tree& tv, int mode, int op, const xtg_array& dst, cudaStream_t stream) {
     const int NL = (int)tv.leaves.size();
     for (int l = 0; l < NL; ++l) {
         F.p.vleaf[l] = tv.leaves[l].data;
         if (mode == 0) {
-            bstrides_to(tv.leaves[l], rank, reinterpret_cast<const int64_t*>(F.p.shape), reinterpret_cast<int64_t*>(F.p.vls[l]));
+            for (int d = 0; d < F.rank; ++d) F.p.vls[l][d] = F.extra[l][d];
         } else {
             int64_t one = std::max<int64_t>(1, tv.rank ? tv.shape[0] : 1);
             bstrides_to(tv.leaves[l], 1, &one, reinterpret_cast<int64_t*>(F.p.vls[l]));
@@ -188,7 +236,12 @@ xtg_status filter_launch(FilterRun& F, const Tree& tv, int mode, int op, int ran
     }
     for (size_t i = 0; i < tv.scalars.size(); ++i) F.p.vscal.v[i] = tv.scalars[i];
     F.p.dst = dst.data;
-    for (int d = 0; d < dst.rank; ++d) F.p.ds[d] = dst.strides[d];
+    if (mode == 0) {
+        F.p.ds[0] = dst.strides[0];  // the 1-D compacted result
+    } else {
+        for (int d = 0; d < F.rank; ++d) F.p.ds[d] = F.extra[0][d];
+    }
+    const int rank = F.rank;
     std::vector<int> map(NL);
     for (int l = 0; l < NL; ++l) map[l] = l;
     const int vt = tv.nodes[tv.root].dtype;
@@ -196,7 +249,7 @@ xtg_status filter_launch(FilterRun& F, const Tree& tv, int mode, int op, int ran
     std::string name = "xtg::k_filter_tile<" + F.ctree + ", " + F.cls + ", " + tree_type(tv, tv.root, map) + ", " +
                        leafset_of(tv) + ", " + dt(vt).cname + ", " + dt(dst.dtype).cname + ", " + dt(ct).cname + ", " +
                        std::to_string(mode) + ", " + std::to_string(rank) + ", " + std::to_string(op) + ", " +
-                       (F.big ? "true" : "false") + ">";
+                       (F.big ? "true" : "false") + ", " + (F.v16 ? "true" : "false") + ">";
     Kernel* k;
     XTG_TRY(get_kernel(name, 256, &k));
     return launch(k, grid_n(k, F.ntiles * 256), 256, &F.p, stream);
@@ -323,12 +376,12 @@ xtg_status xtg_filter(const xtg_expr* e, const xtg_expr* cond, const xtg_array* 
     if (t.rank < 1) return fail(XTG_ERR_INVALID, "filter of a 0-d expression");
     if (out->rank != 1) return fail(XTG_ERR_SHAPE, "filter result must be 1-D");
     FilterRun F;
-    xtg_status st = filter_prepare(cond, t.rank, t.shape, F, (cudaStream_t)stream);
+    xtg_status st = filter_prepare(cond, t.rank, t.shape, F, (cudaStream_t)stream, filter_extra(t, 0, t.rank, t.shape, *out));
     int64_t count = 0;
     if (st == XTG_OK) st = filter_total(F, &count, (cudaStream_t)stream);
     if (st == XTG_OK && !dry_run() && out->shape[0] != count)
         st = fail(XTG_ERR_SHAPE, "filter result must be 1-D of xtg_filter_count elements");
-    if (st == XTG_OK && F.ntiles) st = filter_launch(F, t, 0, 0, t.rank, *out, (cudaStream_t)stream);
+    if (st == XTG_OK && F.ntiles) st = filter_launch(F, t, 0, 0, *out, (cudaStream_t)stream);
     xtg_status fs = F.scratch ? scratch_free(F.scratch, (cudaStream_t)stream) : XTG_OK;
     return st != XTG_OK ? st : fs;
 }
@@ -344,14 +397,15 @@ xtg_status xtg_filter_assign(const xtg_expr* src, const xtg_expr* cond, int32_t 
     if (t.rank > 1) return fail(XTG_ERR_BROADCAST, "values assigned through a filter must be 1-D or a scalar");
     if (dst->rank < 1) return fail(XTG_ERR_INVALID, "filter of a 0-d array");
     FilterRun F;
-    xtg_status st = filter_prepare(cond, dst->rank, dst->shape, F, (cudaStream_t)stream);
+    xtg_status st = filter_prepare(cond, dst->rank, dst->shape, F, (cudaStream_t)stream,
+                                   filter_extra(t, 1, dst->rank, dst->shape, *dst));
     if (st == XTG_OK && t.rank == 1 && t.shape[0] != 1) {
         int64_t count = 0;
         st = filter_total(F, &count, (cudaStream_t)stream);
         if (st == XTG_OK && !dry_run() && t.shape[0] != count)
             st = fail(XTG_ERR_BROADCAST, "assigned values do not match the filter's length");
     }
-    if (st == XTG_OK && F.ntiles) st = filter_launch(F, t, 1, op, dst->rank, *dst, (cudaStream_t)stream);
+    if (st == XTG_OK && F.ntiles) st = filter_launch(F, t, 1, op, *dst, (cudaStream_t)stream);
     xtg_status fs = F.scratch ? scratch_free(F.scratch, (cudaStream_t)stream) : XTG_OK;
     return st != XTG_OK ? st : fs;
 }
