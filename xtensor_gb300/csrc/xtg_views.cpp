@@ -270,7 +270,7 @@ xtg_status launch_indexed(const Tree& t, int mode, int op, int rank, const int64
     p.idx = idx;
     for (int l = 0; l < NL; ++l) {
         p.leaf[l] = t.leaves[l].data;
-        if (mode == 0 || mode == 2) {
+        if (mode == 0) {
             bstrides_to(t.leaves[l], rank, shape, reinterpret_cast<int64_t*>(p.ls[l]));
         } else {
             int64_t one = n;  // the value tree runs over a 1-D space of n (or count) elements
