@@ -1638,16 +1638,31 @@ __global__ void __launch_bounds__(256) k_scan_seg_reduce(const ScanParams p) {
         i64 ke = kb + st * XTG_SCAN_TILE;
         if (ke > p.len) ke = p.len;
         ST s = ST::ident();
-        for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_TILE) {
-            RT v[XTG_SCAN_IPT];
-            if (VEC > 1) {
-                // each thread its 16 consecutive elements (vector loads)
-                const i64 kt = k0 + (i64)threadIdx.x * XTG_SCAN_IPT;
-                scan_load16<Tree, LS, RT, VEC>(p, c, row, kt, ke, v);
+        if constexpr (VEC > 1) {
+            // each thread its 16 consecutive elements (vector loads); the
+            // next tile's loads are in flight while this one is added (the
+            // additions keep their order)
+            RT va[XTG_SCAN_IPT], vb[XTG_SCAN_IPT];
+            const i64 tofs = (i64)threadIdx.x * XTG_SCAN_IPT;
+            auto add = [&](const RT(&v)[XTG_SCAN_IPT], i64 k0) {
+                const i64 kt = k0 + tofs;
 #pragma unroll
                 for (int i = 0; i < XTG_SCAN_IPT; ++i)
                     if (kt + i < ke) s.add(v[i]);
-            } else {
+            };
+            if (kb < ke) scan_load16<Tree, LS, RT, VEC>(p, c, row, kb + tofs, ke, va);
+            for (i64 k0 = kb; k0 < ke; k0 += 2 * XTG_SCAN_TILE) {
+                if (k0 + XTG_SCAN_TILE < ke) scan_load16<Tree, LS, RT, VEC>(p, c, row, k0 + XTG_SCAN_TILE + tofs, ke, vb);
+                add(va, k0);
+                if (k0 + XTG_SCAN_TILE >= ke) break;
+                if (k0 + 2 * XTG_SCAN_TILE < ke)
+                    scan_load16<Tree, LS, RT, VEC>(p, c, row, k0 + 2 * XTG_SCAN_TILE + tofs, ke, va);
+                add(vb, k0 + XTG_SCAN_TILE);
+            }
+        } else
+        for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_TILE) {
+            RT v[XTG_SCAN_IPT];
+            {
                 // coalesced scalar loads: thread th takes th, th + 256, ...
 #pragma unroll
                 for (int i = 0; i < XTG_SCAN_IPT; ++i) {
@@ -1708,11 +1723,10 @@ __global__ void __launch_bounds__(256) k_scan_seg_apply(const ScanParams p) {
         if (ke > p.len) ke = p.len;
         ST carry = reinterpret_cast<const ST*>(p.agg)[it];
         if constexpr (VEC > 1) {
-            // registers only: each thread its 16 consecutive elements
-            for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_TILE) {
+            // registers only: each thread its 16 consecutive elements; the
+            // next tile's loads are issued before this tile's block scan
+            auto tile = [&](RT(&v)[XTG_SCAN_IPT], i64 k0) {
                 const i64 kt = k0 + q0;
-                RT v[XTG_SCAN_IPT];
-                scan_load16<Tree, LS, RT, VEC>(p, c, row, kt, ke, v);
                 ST s = ST::ident();
 #pragma unroll
                 for (int i = 0; i < XTG_SCAN_IPT; ++i)
@@ -1749,6 +1763,16 @@ __global__ void __launch_bounds__(256) k_scan_seg_apply(const ScanParams p) {
                         if (kt + i < ke) o[kt + i] = v[i];
                 }
                 carry.merge(tile_tot);
+            };
+            RT va[XTG_SCAN_IPT], vb[XTG_SCAN_IPT];
+            if (kb < ke) scan_load16<Tree, LS, RT, VEC>(p, c, row, kb + q0, ke, va);
+            for (i64 k0 = kb; k0 < ke; k0 += 2 * XTG_SCAN_TILE) {
+                if (k0 + XTG_SCAN_TILE < ke) scan_load16<Tree, LS, RT, VEC>(p, c, row, k0 + XTG_SCAN_TILE + q0, ke, vb);
+                tile(va, k0);
+                if (k0 + XTG_SCAN_TILE >= ke) break;
+                if (k0 + 2 * XTG_SCAN_TILE < ke)
+                    scan_load16<Tree, LS, RT, VEC>(p, c, row, k0 + 2 * XTG_SCAN_TILE + q0, ke, va);
+                tile(vb, k0 + XTG_SCAN_TILE);
             }
             continue;
         }
