@@ -975,8 +975,9 @@ def run_npy(args):
                 ts.append(time.perf_counter() - t0)
             link[nm] = nb / min(ts) / 1e9
         check(lib.xtg_host_free(hp))
-        # host ceiling of the load side: 8 threads reading the file from the
-        # page cache into host memory, no device copy (os.preadv drops the GIL)
+        # host ceiling of the load side: 16 threads (as the library's ring)
+        # reading the file from the page cache into host memory, no device
+        # copy (os.preadv drops the GIL)
         from concurrent.futures import ThreadPoolExecutor
         hb = np.ones(nb, dtype=np.uint8)
         fd = os.open(fc, os.O_RDONLY)
@@ -986,7 +987,7 @@ def run_npy(args):
 
             def rd(o):
                 os.preadv(fd, [memoryview(hb)[o:o + min(ch, nb - o)]], 128 + o)
-            with ThreadPoolExecutor(8) as ex:
+            with ThreadPoolExecutor(16) as ex:
                 ts = []
                 for _ in range(3):
                     t0 = time.perf_counter()
@@ -1060,7 +1061,7 @@ def run_npy(args):
                          "peak_source": "measured here: one cudaMemcpyAsync of the same bytes to / from pinned host "
                                         f"memory (h2d {link['h2d']:.1f} GB/s, d2h {link['d2h']:.1f} GB/s)",
                          "host_read_gbs": round(host_read, 1),
-                         "host_read_source": "8 threads pread of the same file from the page cache into host memory, "
+                         "host_read_source": "16 threads pread of the same file from the page cache into host memory, "
                                              "no device copy (the load side's ceiling below the link)"},
             "per_call": per_call, "cpu_baseline": cpu,
             "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 3 * nb, "d2h_bytes_per_step": nb,

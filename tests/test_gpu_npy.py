@@ -39,8 +39,8 @@ def chunk():
         if threads is not None:
             xg.set_option("npy.threads", threads)
     yield set_
-    xg.set_option("npy.chunk_bytes", 8 << 20)
-    xg.set_option("npy.threads", 8)
+    xg.set_option("npy.chunk_bytes", -1)
+    xg.set_option("npy.threads", -1)
 
 
 def _bits(a: np.ndarray) -> np.ndarray:

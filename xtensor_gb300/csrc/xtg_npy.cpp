@@ -8,7 +8,8 @@
 //   data starts on a 64-byte boundary, then the raw elements.
 //
 // Data path: the header is parsed on the calling thread; the data moves in
-// chunks through pinned staging buffers.  Each of W host threads owns a CUDA
+// 4 MiB chunks through pinned staging buffers.  Each of W host threads (up to
+// 16) owns a CUDA
 // stream and two buffers: it reads chunk k (pread from the file, or memcpy
 // from a pageable host buffer) into one buffer while the copy of chunk k-1
 // from the other is in flight, so the file read, the staging copy and the
@@ -399,8 +400,10 @@ xtg_status run_job(Job& j, cudaStream_t stream) {
     DeviceInfo* info;
     XTG_TRY(ensure_device(&info));
     j.device = info->device;
-    const size_t chunk = (size_t)std::max<int64_t>(opt("npy.chunk_bytes", 8 << 20), 1 << 16) & ~(size_t)4095;
-    int nw = (int)opt("npy.threads", std::min(8u, std::max(1u, std::thread::hardware_concurrency())));
+    // 4 MiB chunks on up to 16 threads: measured on the GB300's Grace host,
+    // loads from the page cache ran 74 GB/s with 8 threads and 89 with 16
+    const size_t chunk = (size_t)std::max<int64_t>(opt("npy.chunk_bytes", 4 << 20), 1 << 16) & ~(size_t)4095;
+    int nw = (int)opt("npy.threads", std::min(16u, std::max(1u, std::thread::hardware_concurrency())));
     nw = std::max(1, std::min<int>(std::min(nw, j.max_workers), (int)((j.bytes + chunk - 1) / chunk)));
     Staging& st = staging();
     std::lock_guard<std::mutex> g(st.mu);
