@@ -385,6 +385,35 @@ def test_float64_selection_prefilter_edges():
         np.testing.assert_array_equal(ops.argreduce(op, dev(y), 1).to_numpy(), O.argreduce(op, H(y), 1))
 
 
+@pytest.mark.parametrize("dt", ["float32", "float64"])
+def test_long_row_selection_specials(dt):
+    """amax / amin over long rows (split work items, block-wide groups): the
+    position-free first pass hands over to the exact pass with positions
+    whenever a group meets a zero at the extreme, a NaN or (float64) another
+    special value — the signed zero that wins is the one the fold visits
+    last, a trailing NaN wins."""
+    g = rng(22)
+    n = 1 << 20
+    x = -np.abs(g.standard_normal((6, n))).astype(dt) - 1
+    x[0, 1000] = 0.0
+    x[0, n - 5000] = -0.0  # the later zero: -0
+    x[1, 7] = -0.0
+    x[1, n - 1] = 0.0  # +0 last
+    x[2, n // 2] = np.nan
+    x[2, n - 1] = np.nan  # a trailing NaN: the fold ends on it
+    x[3] = g.standard_normal(n).astype(dt)  # no specials: the fast pass alone
+    x[4, 123] = -np.inf
+    x[5, 99] = np.inf
+    for op in ("amax", "amin"):
+        y = -x if op == "amin" else x
+        got = ops.reduce(op, dev(y), [1]).to_numpy()
+        ref = O.reduce(op, H(y), [1])
+        # (a NaN result is a NaN; float64 selection returns it as a canonical NaN)
+        num = ~np.isnan(ref)
+        np.testing.assert_array_equal(np.signbit(got[num]), np.signbit(ref[num]), err_msg=op)
+        np.testing.assert_array_equal(got, ref, err_msg=op)
+
+
 # ------------------------------------------------------------------------------- arg
 @pytest.mark.parametrize("dt", ["float32", "float64", "int32"])
 def test_argmax_argmin(dt):

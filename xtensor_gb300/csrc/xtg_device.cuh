@@ -675,6 +675,55 @@ template <int MAXOP> struct AccSel<double, MAXOP> {
     XTG_DI double dval() const { return value(); }
 };
 
+// Position-free selection for the row kernel's first pass.  Positions only
+// decide between values that compare equal with different bits (+0 / -0) and
+// around NaNs; a pass that met neither keeps the plain best value (equal
+// values then have equal bits, so any merge order gives the same result).
+// A pass that met a NaN, or ends on a zero (float) / a key64 special value
+// (double), asks for the exact pass with positions.
+template <class A, int MAXOP> struct AccSelFast {
+    A v;
+    bool odd;
+    template <class P> XTG_DI void init(const P& p) {
+        v = IsFloat<A>::value ? (A)p.init_f : (A)p.init_i;
+        odd = false;
+    }
+    template <class X> XTG_DI void add(X x, i64) {
+        const A a = cvt<A>(x);
+        if (IsFloat<A>::value) odd |= !(a == a);
+        const bool keep = MAXOP ? Cmp<A>::gt(v, a) : Cmp<A>::lt(v, a);
+        if (!keep) v = a;
+    }
+    XTG_DI bool exact() const { return odd || (IsFloat<A>::value && v == A(0)); }
+    XTG_DI void to(AccSel<A, MAXOP>& s) const {
+        s.v = v;
+        s.pos = -1;
+    }
+};
+template <int MAXOP> struct AccSelFast<double, MAXOP> {
+    i64 kv;
+    bool odd;
+    template <class P> XTG_DI void init(const P& p) {
+        AccSel<double, MAXOP> s;
+        s.start(p.init_f);
+        kv = s.kv;
+        odd = f64_special(__double_as_longlong(p.init_f));
+    }
+    template <class X> XTG_DI void add(X x, i64) {
+        const i64 b = __double_as_longlong(cvt<double>(x));
+        odd |= f64_special(b);
+        const i64 ka = key64(b);
+        if (MAXOP ? (ka >= kv) : (ka <= kv)) kv = ka;
+    }
+    XTG_DI bool exact() const { return odd; }
+    XTG_DI void to(AccSel<double, MAXOP>& s) const {
+        s.kv = kv;
+        s.pos = -1;
+    }
+};
+template <class A> struct FastSel { enum { value = 0 }; typedef A F; };
+template <class A, int M> struct FastSel<AccSel<A, M>> { enum { value = 1 }; typedef AccSelFast<A, M> F; };
+
 // Moments for mean / variance / stddev.  Data are shifted by k (the first
 // element of the output's reduction set), then sum(d) and sum(d*d) are
 // accumulated — in double-float for float32/bf16 data (TwoSum + exact
@@ -1115,25 +1164,44 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
                 }
             }
         };
-        auto consume = [&](const RG(&rg)[U], i64 r0) {
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const i64 r = r0 + (i64)u * gsz;
-                if (r < re) {
-#pragma unroll
-                    for (int j = 0; j < VEC; ++j) acc.add(Tree::ev(rg[u], j, c), r * VEC + j);
-                }
-            }
-        };
-        i64 r0 = rb + gtid;
-        if (r0 < re) load(rga, r0);
-        for (; r0 < re; r0 += 2 * step) {
-            if (r0 + step < re) load(rgb, r0 + step);
-            consume(rga, r0);
-            if (r0 + step >= re) break;
-            if (r0 + 2 * step < re) load(rga, r0 + 2 * step);
-            consume(rgb, r0 + step);
+// the reduction pass over the work item, folding into accumulator A
+#define XTG_ROW_PASS(A)                                                                \
+    {                                                                                  \
+        auto consume = [&](const RG(&rg)[U], i64 r0) {                                 \
+            _Pragma("unroll") for (int u = 0; u < U; ++u) {                            \
+                const i64 r = r0 + (i64)u * gsz;                                       \
+                if (r < re) {                                                          \
+                    _Pragma("unroll") for (int j = 0; j < VEC; ++j)                    \
+                        A.add(Tree::ev(rg[u], j, c), r * VEC + j);                     \
+                }                                                                      \
+            }                                                                          \
+        };                                                                             \
+        i64 r0 = rb + gtid;                                                            \
+        if (r0 < re) load(rga, r0);                                                    \
+        for (; r0 < re; r0 += 2 * step) {                                              \
+            if (r0 + step < re) load(rgb, r0 + step);                                  \
+            consume(rga, r0);                                                          \
+            if (r0 + step >= re) break;                                                \
+            if (r0 + 2 * step < re) load(rga, r0 + 2 * step);                          \
+            consume(rgb, r0 + step);                                                   \
+        }                                                                              \
+    }
+        if constexpr (FastSel<Acc>::value) {
+            // amax / amin: a position-free pass; the exact pass with
+            // positions only when some thread of the group met a NaN, a zero
+            // or (float64) another special value
+            typename FastSel<Acc>::F fa;
+            fa.init(p);
+            XTG_ROW_PASS(fa)
+            bool ex = fa.exact();
+            if (GROUP <= 32) ex = __any_sync(0xffffffffu, ex);
+            else ex = __syncthreads_or(ex) != 0;
+            if (ex) XTG_ROW_PASS(acc)
+            else fa.to(acc);
+        } else {
+            XTG_ROW_PASS(acc)
         }
+#undef XTG_ROW_PASS
         acc = group_reduce<GROUP>(acc, smem);
         if (gtid == 0) {
             if (p.nsplit > 1) {
