@@ -1109,7 +1109,7 @@ template <class... S, int VEC> struct Ring<LeafSet<S...>, VEC> {
 // K3/K5: ROW strategy — the reduced run is contiguous (or broadcast) for the
 // leaves; a group (warp or CTA) owns one (output, split) work item and strides
 // over its vectors.  Work items: w = o * nsplit + s.
-template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int GROUP, bool BIG>
+template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int GROUP, bool BIG, int UR = 4>
 __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
     typedef typename LS::template R<VEC>::type RG;
     __shared__ Acc smem[32];
@@ -1147,7 +1147,7 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
         // two register batches of U vectors: the next batch's loads are in
         // flight while the current one is reduced; each thread still visits
         // its positions in increasing order
-        constexpr int U = 4;
+        constexpr int U = UR;
         const i64 step = (i64)gsz * U;
         RG rga[U], rgb[U];
         auto load = [&](RG(&rg)[U], i64 r0) {

@@ -313,7 +313,8 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         // loops are instruction-bound once two register batches are in flight)
         std::string name = "xtg::k_reduce_row<" + tree + ", " + ls + ", " + accname + ", " + outc + ", " +
                            std::to_string(post) + ", " + std::to_string(vec) + ", " + std::to_string(RO) + ", " +
-                           std::to_string(RR) + ", " + std::to_string(group) + ", " + (big ? "true" : "false") + ">";
+                           std::to_string(RR) + ", " + std::to_string(group) + ", " + (big ? "true" : "false") + ", " +
+                           std::to_string(opt("reduce.row_unroll", 4)) + ">";
         st = get_kernel(name, 256, &k);
         if (st == XTG_OK) {
             int64_t items = n_out * nsplit;
