@@ -436,6 +436,26 @@ def test_argmax_nan_rules(dt):
             np.testing.assert_array_equal(ops.argreduce(op, dev(x), axis).to_numpy(), O.argreduce(op, H(x), axis))
 
 
+@pytest.mark.parametrize("dt", ["float32", "int32", "float64"])
+def test_argmax_column_walk_split_starts(dt):
+    """Column arg-reductions split the reduced axis (here 64 splits of 64
+    rows): a thread's first rows may hold NaN (skipped unless at position 0),
+    -inf or ties; the compare-only update starts once every column holds a
+    value.  Bit-exact against the plain fold."""
+    g = rng(23)
+    x = g.integers(-3, 4, (4, 4096, 64)).astype(dt)
+    if dt != "int32":
+        x[:, 64, :8] = np.nan        # first row of split 1
+        x[:, 64:70, 8:12] = np.nan   # several leading rows
+        x[:, 0, 12:14] = np.nan      # position 0: the NaN is the result
+        x[:, 128, 14:16] = -np.inf
+        x[:, 192:256, 16:18] = np.nan  # a whole split of NaN
+    x[:, 4000, 20] = 9  # a late unique maximum
+    for op in ("argmax", "argmin"):
+        got = ops.argreduce(op, dev(x), 1).to_numpy()
+        np.testing.assert_array_equal(got, O.argreduce(op, H(x), 1), err_msg=op)
+
+
 def test_reference_argmax_kats():
     a = np.array([[5, 3, 1], [4, 4, 4]], np.float64)
     assert ops.argreduce("argmax", dev(a)).to_numpy() == 0

@@ -700,6 +700,25 @@ template <class A, int MAXOP> struct AccSelFast {
         s.pos = -1;
     }
 };
+// float: one NaN-propagating max / min per element (PTX max.NaN / min.NaN):
+// the running value turns NaN at the first NaN and stays NaN, which asks for
+// the exact pass; otherwise it is the plain fold's value.
+XTG_DI float fsel_nan(float a, float b, int maxop) {
+    float r;
+    if (maxop) asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    else asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+template <int MAXOP> struct AccSelFast<float, MAXOP> {
+    float v;
+    template <class P> XTG_DI void init(const P& p) { v = (float)p.init_f; }
+    template <class X> XTG_DI void add(X x, i64) { v = fsel_nan(v, cvt<float>(x), MAXOP); }
+    XTG_DI bool exact() const { return !(v == v) || v == 0.f; }
+    XTG_DI void to(AccSel<float, MAXOP>& s) const {
+        s.v = v;
+        s.pos = -1;
+    }
+};
 template <int MAXOP> struct AccSelFast<double, MAXOP> {
     i64 kv;
     bool odd;
@@ -810,6 +829,15 @@ template <class A, int MAXOP> struct AccArg {
             idx = ps;
         }
     }
+    // add() once a value is held (idx >= 0): the compare and the selects only
+    template <class X> XTG_DI void add_held(X x, i64 ps) {
+        A a = cvt<A>(x);
+        if (MAXOP ? Cmp<A>::gt(a, v) : Cmp<A>::lt(a, v)) {
+            v = a;
+            idx = ps;
+        }
+    }
+    XTG_DI bool held() const { return idx >= 0; }
     XTG_DI void merge(const AccArg& o) {
         if (o.idx < 0) return;
         if (idx < 0) { v = o.v; idx = o.idx; return; }
@@ -917,6 +945,36 @@ template <int MODE> struct Shift<AccMom<double, MODE>> {
 template <class A> struct NeedsShift { enum { value = 0 }; };
 template <int MODE> struct NeedsShift<AccMom<float, MODE>> { enum { value = MODE != 0 }; };
 template <int MODE> struct NeedsShift<AccMom<double, MODE>> { enum { value = MODE != 0 }; };
+// arg-reductions whose update has a cheaper form once a value is held
+// (float64 keeps its key path)
+template <class A> struct HeldFast { enum { value = 0 }; };
+template <class A, int M> struct HeldFast<AccArg<A, M>> { enum { value = 1 }; };
+template <int M> struct HeldFast<AccArg<double, M>> { enum { value = 0 }; };
+// one step of a column walk: VEC accumulators take row r of their columns.
+// Until every one of them holds a value the full update runs; after that
+// (held == true) the compare-and-select form.
+template <class Tree, class Acc, int VEC> struct ColStep {
+    template <class RG, class C>
+    static XTG_DI void run(Acc (&acc)[VEC], const RG& rg, i64 r, const C& c, bool& held) {
+        if constexpr (HeldFast<Acc>::value) {
+            if (held) {
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) acc[j].add_held(Tree::ev(rg, j, c), r);
+                return;
+            }
+            bool h = true;
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                acc[j].add(Tree::ev(rg, j, c), r);
+                h = h && acc[j].held();
+            }
+            held = h;
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) acc[j].add(Tree::ev(rg, j, c), r);
+        }
+    }
+};
 
 // Finalisation: accumulator state -> output element (merging xt::initial
 // last, as xreducer_stepper::aggregate does, xreducer.hpp:1778-1799).
@@ -1257,6 +1315,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
         const i64 rb = s * p.chunk;
         i64 re = rb + p.chunk;
         if (re > p.n_redv) re = p.n_redv;
+        bool held = false;
         if constexpr (RS > 0) {
             const int lstride = (int)blockDim.x * 16;
             const int sstride = LS::N * lstride;
@@ -1282,8 +1341,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
                 const int sf = st == 0 ? RS - 1 : st - 1;
                 if (r + RS - 1 < re) issue(r + RS - 1, sf);
                 cp_async_commit();
-#pragma unroll
-                for (int j = 0; j < VEC; ++j) acc[j].add(Tree::ev(rg, j, c), r);
+                ColStep<Tree, Acc, VEC>::run(acc, rg, r, c, held);
                 st = st == RS - 1 ? 0 : st + 1;
             }
             cp_async_wait<0>();
@@ -1302,10 +1360,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                if (r + u < re) {
-#pragma unroll
-                    for (int j = 0; j < VEC; ++j) acc[j].add(Tree::ev(rg[u], j, c), r + u);
-                }
+                if (r + u < re) ColStep<Tree, Acc, VEC>::run(acc, rg[u], r + u, c, held);
             }
         }
         }
