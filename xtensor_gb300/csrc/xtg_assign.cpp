@@ -435,14 +435,25 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
         }
     }
     const int tma_block = 128;
-    const size_t dyn = (size_t)buf_bytes * 2 * (tma_block / 32);
+    // One buffer per warp by default (refilled once the row is in registers),
+    // and a register cap that leaves room for 4 blocks per SM when a lane's
+    // share of the row takes at most 64 registers (float64 rows of 1024: 389
+    // us per 2^27 elements against 519 us uncapped with two buffers, 422 us
+    // at 3 blocks).  Without a cap the compiler spends ~210 registers.
+    const int nbuf = opt("row.tma_buffers", 1) == 2 ? 2 : 1;
+    int64_t row_regs = 0;
+    for (int l = 0; l < NL; ++l) row_regs += (int64_t)nv * vec * dt(t.leaves[l].dtype).size / 4;
+    const int64_t minb_auto = row_regs <= 64 ? 4 : (row_regs <= 96 ? 3 : 2);
+    const int minb = (int)std::max<int64_t>(1, std::min<int64_t>(opt("row.tma_min_blocks", minb_auto), 16));
+    const size_t dyn = (size_t)buf_bytes * nbuf * (tma_block / 32);
     if (tma && dyn > 200 * 1024) tma = false;
     if (tma) {
         p.buf_bytes = buf_bytes;
         XTG_TRY(device_error_word(&p.err));
         std::string name = "xtg::k_rowfused_tma<" + tree + ", " + sl + ", " + leafset(t, order, kinds) + ", " +
                            dt(out.dtype).cname + ", " + std::to_string(vec) + ", " + std::to_string(nv) + ", " +
-                           std::to_string(D.R) + ", " + std::to_string(nstat) + ", " + std::to_string(full) + ">";
+                           std::to_string(D.R) + ", " + std::to_string(nstat) + ", " + std::to_string(full) + ", " +
+                           std::to_string(nbuf) + ", " + std::to_string(minb) + ">";
         Kernel* kr;
         XTG_TRY(get_kernel(name, tma_block, &kr, dyn));
         int64_t need = (n_rows + 3) / 4;

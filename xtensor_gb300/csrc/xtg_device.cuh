@@ -2817,8 +2817,12 @@ template <class... S> struct LoadRowSmem<LeafSet<S...>> {
     }
 };
 
-template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int RO, int NSTAT, int FULL>
-__global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
+// NB = 2: a double buffer per warp, row i + 1 copied while row i is reduced
+// from shared memory.  NB = 1: one buffer per warp, refilled with row i + 1
+// as soon as row i sits in registers (half the shared memory, so more warps
+// per SM).  MINB: the launch-bounds minimum of resident blocks per SM.
+template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int RO, int NSTAT, int FULL, int NB = 2, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) k_rowfused_tma(const RowParams p) {
     typedef typename LS::template R<VEC>::type RG;
     extern __shared__ __align__(128) unsigned char dsmem[];
     __shared__ __align__(16) unsigned char red_smem[32 * 48];
@@ -2826,7 +2830,7 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
     const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
     const int nw = (int)blockDim.x >> 5;
     u64* mybar = bars + 2 * warp;
-    unsigned char* const buf0 = dsmem + (size_t)(2 * warp) * p.buf_bytes;  // buffer b at buf0 + b * buf_bytes
+    unsigned char* const buf0 = dsmem + (size_t)(NB * warp) * p.buf_bytes;  // buffer b at buf0 + b * buf_bytes
     if (lane == 0) {
         mbar_init(&mybar[0], 1);
         mbar_init(&mybar[1], 1);
@@ -2855,9 +2859,9 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
     int it = 0;
     if (gid < p.n_rows) issue(gid, 0);
     for (i64 row = gid; row < p.n_rows; row += ng, ++it) {
-        const int b = it & 1;
-        if (row + ng < p.n_rows) issue(row + ng, b ^ 1);
-        const unsigned parity = (unsigned)(it >> 1) & 1u;
+        const int b = NB == 2 ? (it & 1) : 0;
+        if (NB == 2 && row + ng < p.n_rows) issue(row + ng, b ^ 1);
+        const unsigned parity = NB == 2 ? ((unsigned)(it >> 1) & 1u) : ((unsigned)it & 1u);
         bool done = false;
         for (int k = 0; k < (1 << 22); ++k) {
             if (mbar_try_wait(&mybar[b], parity)) {
@@ -2869,7 +2873,7 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
             // give up: flag it, wait (bounded) for the copy into the other
             // buffer if one was issued, and leave
             if (lane == 0) atomicExch(p.err, 1);
-            if (row + ng < p.n_rows) {
+            if (NB == 2 && row + ng < p.n_rows) {
                 const unsigned par2 = (unsigned)((it + 1) >> 1) & 1u;
                 for (int k = 0; k < (1 << 22); ++k)
                     if (mbar_try_wait(&mybar[b ^ 1], par2)) break;
@@ -2884,6 +2888,12 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
 #pragma unroll
             for (int j = 0; j < VEC; ++j) ok[n][j] = FULL || (e0 + j) < p.row_len;
             if (FULL || e0 < p.row_len) LoadRowSmem<LS>::template run<VEC>(rg[n], buf0 + (size_t)b * p.buf_bytes, p.loff, e0);
+        }
+        if (NB == 1) {
+            // the row is in registers: refill the buffer with the next one
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (row + ng < p.n_rows) issue(row + ng, 0);
         }
         c.fixmask = 0;
         Stats<SL>::template run<32, VEC, NV>(rg, ok, c, p, (void*)red_smem);
@@ -2903,9 +2913,11 @@ __global__ void __launch_bounds__(128) k_rowfused_tma(const RowParams p) {
                 st_out<OutT, K_CONTIG, VEC>(reinterpret_cast<OutT*>(p.out), ob + e0, 1, v);
             }
         }
-        // all lanes are done reading buffer b before it is refilled
-        fence_proxy_async_smem();
-        __syncwarp();
+        if (NB == 2) {
+            // all lanes are done reading buffer b before it is refilled
+            fence_proxy_async_smem();
+            __syncwarp();
+        }
     }
 }
 
