@@ -436,14 +436,15 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
     }
     const int tma_block = 128;
     // One buffer per warp by default (refilled once the row is in registers),
-    // and a register cap that leaves room for 4 blocks per SM when a lane's
-    // share of the row takes at most 64 registers (float64 rows of 1024: 389
-    // us per 2^27 elements against 519 us uncapped with two buffers, 422 us
-    // at 3 blocks).  Without a cap the compiler spends ~210 registers.
+    // and a register cap that leaves room for 5 blocks per SM when a lane's
+    // share of the row takes at most 64 registers (float64 rows of 1024: 376
+    // us per 2^27 elements with 96 registers; 388 at 4 blocks, 422 at 3,
+    // 519 uncapped with two buffers — the compiler then spends ~210
+    // registers; 6 blocks spill).
     const int nbuf = opt("row.tma_buffers", 1) == 2 ? 2 : 1;
     int64_t row_regs = 0;
     for (int l = 0; l < NL; ++l) row_regs += (int64_t)nv * vec * dt(t.leaves[l].dtype).size / 4;
-    const int64_t minb_auto = row_regs <= 64 ? 4 : (row_regs <= 96 ? 3 : 2);
+    const int64_t minb_auto = row_regs <= 64 ? 5 : (row_regs <= 96 ? 3 : 2);
     const int minb = (int)std::max<int64_t>(1, std::min<int64_t>(opt("row.tma_min_blocks", minb_auto), 16));
     const size_t dyn = (size_t)buf_bytes * nbuf * (tma_block / 32);
     if (tma && dyn > 200 * 1024) tma = false;

@@ -2356,8 +2356,8 @@ template <> struct RowFin<float> {  // float32 rows: double-float sums rounded o
 // which is exact for the elements in the top binade; smaller ones are
 // rounded to the top binade's ulp (so a row sum is within n/2 of that ulp
 // plus one final rounding).  From there on everything is exact:  Each lane (at most 256 elements)
-// keeps sum X and sum X^2 exactly in 64-bit words (X = Xh * 2^27 + Xl, so
-// X^2 = Xh^2 2^54 + 2 Xh Xl 2^27 + Xl^2 as three sums of 32x32-bit
+// keeps sum X and sum X^2 exactly in 64-bit words (|X| = Xh * 2^27 + Xl, so
+// X^2 = Xh^2 2^54 + 2 Xh Xl 2^27 + Xl^2 as three sums of unsigned 32x32-bit
 // products); lanes combine in 128-bit, and
 //   n * sum (X - mean)^2 = n * sum X^2 - (sum X)^2
 // is evaluated in 192-bit integers, so no cancellation can occur whatever the
@@ -2472,20 +2472,15 @@ struct FixMom {
         s2 = u128_add(s2, o.s2);
     }
 };
-XTG_DI int exp_field(double x) {
-    const int e = (__double2hiint(x) >> 20) & 0x7ff;
-    return e ? e : 1;  // subnormals scale like exponent field 1
-}
-XTG_DI i64 to_fixed(double x, int ef_max) {
-    const int hi = __double2hiint(x);
-    const unsigned lo = (unsigned)__double2loint(x);
+// |X| for the element with words (hi, lo): twice the significand (< 2^54),
+// shifted down to the row's scale, then one add and one shift round it half
+// away from zero.  The sign is the sign bit of hi.
+XTG_DI u64 fixed_mag(int hi, unsigned lo, int ef_max) {
     const int e = (hi >> 20) & 0x7ff;
-    // twice the significand (< 2^54), so that one shift and one add round
     const u64 m2 = (((u64)(unsigned)((hi & 0xfffff) | (e ? 0x100000 : 0)) << 32) | lo) << 1;
-    int sh = ef_max - (e ? e : 1);
+    int sh = ef_max - (e ? e : 1);  // subnormals scale like exponent field 1
     sh = sh < 63 ? sh : 63;
-    const i64 v = (i64)(((m2 >> sh) + 1) >> 1);  // significand / 2^sh, rounded half away from zero
-    return hi < 0 ? -v : v;
+    return ((m2 >> sh) + 1) >> 1;
 }
 
 template <int GROUP, int VEC, int NV, int MODE, class Sub, class RG, class CT>
@@ -2493,34 +2488,41 @@ XTG_DI bool fixed_moments(const RG (&rg)[NV], const bool (&ok)[NV][VEC], const C
                           double& sum, double& sdev2) {
     static_assert(NV * VEC <= 256, "per-lane 64-bit sums hold at most 256 elements");
     const i64 n = p.row_len;
-    IMaxI em;
-    em.v = 1;
+    // the largest exponent field: the high words with the sign cleared order
+    // like their exponent fields
+    unsigned mh = 0;
 #pragma unroll
     for (int i = 0; i < NV; ++i)
 #pragma unroll
         for (int j = 0; j < VEC; ++j)
             if (ok[i][j]) {
-                const int e = exp_field(cvt<double>(Sub::ev(rg[i], j, c)));
-                em.v = em.v > e ? em.v : e;
+                const unsigned h = (unsigned)__double2hiint(cvt<double>(Sub::ev(rg[i], j, c))) & 0x7fffffffu;
+                mh = mh > h ? mh : h;
             }
+    IMaxI em;
+    em.v = (int)(mh >> 20);
+    em.v = em.v > 1 ? em.v : 1;
     em = group_reduce<GROUP>(em, reinterpret_cast<IMaxI*>(smem));
     em = bcast_group<GROUP>(em, reinterpret_cast<IMaxI*>(smem));
     if (em.v >= 0x7ff || n > 65536) return false;
-    i64 s1 = 0, a = 0, b = 0;
-    u64 cc = 0;
+    i64 s1 = 0;
+    u64 a = 0, b = 0, cc = 0;
 #pragma unroll
     for (int i = 0; i < NV; ++i)
 #pragma unroll
         for (int j = 0; j < VEC; ++j)
             if (ok[i][j]) {
-                const i64 x = to_fixed(cvt<double>(Sub::ev(rg[i], j, c)), em.v);
-                s1 += x;
+                const double xd = cvt<double>(Sub::ev(rg[i], j, c));
+                const int hi = __double2hiint(xd);
+                const u64 v = fixed_mag(hi, (unsigned)__double2loint(xd), em.v);  // |X| < 2^53
+                if (hi < 0) s1 -= (i64)v;
+                else s1 += (i64)v;
                 if (MODE >= 2) {
-                    const int xh = (int)(x >> 27);                      // |xh| <= 2^26
-                    const int xl = (int)((unsigned)x & 0x7ffffffu);     // 0 <= xl < 2^27
-                    a += (i64)xh * xh;
-                    b += (i64)xh * xl;
-                    cc += (u64)(unsigned)xl * (unsigned)xl;
+                    const unsigned xh = (unsigned)(v >> 27);   // < 2^26
+                    const unsigned xl = (unsigned)v & 0x7ffffffu;  // < 2^27
+                    a += (u64)xh * xh;
+                    b += (u64)xh * xl;
+                    cc += (u64)xl * xl;
                 }
             }
     FixMom f;
@@ -2529,10 +2531,9 @@ XTG_DI bool fixed_moments(const RG (&rg)[NV], const bool (&ok)[NV][VEC], const C
     f.s2.lo = 0;
     f.s2.hi = 0;
     if (MODE >= 2) {
-        // lane sum X^2 = a 2^54 + b 2^28 + cc  (>= 0, < 2^116)
-        U128 t = u128_shl((u64)a, 54);
-        const U128 bt = u128_shl((u64)(b < 0 ? -b : b), 28);
-        t = b < 0 ? u128_sub(t, bt) : u128_add(t, bt);
+        // lane sum X^2 = a 2^54 + b 2^28 + cc  (< 2^116)
+        U128 t = u128_shl(a, 54);
+        t = u128_add(t, u128_shl(b, 28));
         U128 ct;
         ct.lo = cc;
         ct.hi = 0;
