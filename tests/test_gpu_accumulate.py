@@ -209,6 +209,28 @@ def test_large_tile_scan_reproducible_and_accurate():
     assert (np.abs(a - exact) <= tol).all()
 
 
+def test_tile_scan_long_products():
+    """float32 cumprod over 4.2M elements (one row cut into segments): the
+    double-float states are renormalised before two of them multiply — the
+    per-element chain lets lo drift to ~1e-3 of hi, and a product of two
+    such states that drops lo * lo was 4.8e-4 off at the end of this row.
+    Within 4 ulp of the exact prefix product; nancumprod skips NaNs."""
+    g = rng(37)
+    n = (1 << 22) + 12345
+    y = (1.0 + 1e-5 * g.standard_normal(n)).astype(np.float32)
+    got = ops.accumulate("cumprod", dev(y), None).to_numpy()
+    assert last_kernels()[-1].startswith("k_scan_seg_apply")
+    _tile_tol_check(got[None, :], y[None, :], "cumprod", "long cumprod")
+    y[[5, n // 3]] = np.nan
+    got = ops.accumulate("nancumprod", dev(y), None).to_numpy()
+    _tile_tol_check(got[None, :], np.where(np.isnan(y), np.float32(1), y)[None, :], "cumprod", "long nancumprod")
+    # the same row as (1, n) along axis 1 with the segmented strategy
+    g2 = rng(38)
+    z = (1.0 + 1e-5 * g2.standard_normal((1, n))).astype(np.float32)
+    got = ops.accumulate("cumprod", dev(z), 1).to_numpy()
+    _tile_tol_check(got, z, "cumprod", "long cumprod axis 1")
+
+
 def test_tile_scan_strided_and_broadcast_operands(strategy):
     """The segmented scan over a strided view (every other column: the
     shared-memory path) and over a broadcast expression (the vector path)."""

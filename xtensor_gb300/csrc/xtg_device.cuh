@@ -1636,11 +1636,29 @@ template <int OP> struct ScanState<float, OP> {
             lo += e;
         }
     }
+    // (hi, lo) with |lo| <= ulp(hi) / 2 (Fast2Sum; |hi| >= |lo| holds for
+    // these states).  add() leaves lo to grow (its rounding errors of hi * x
+    // drift one way over long runs, to ~1e-3 of hi after 10^5 products),
+    // which is harmless along one chain but not in a product of two states,
+    // where lo * o.lo is dropped.  Non-finite states stay as they are.
+    static XTG_DI void norm2(float h, float l, float& nh, float& nl) {
+        const float s = h + l;
+        if (s - s == 0.f) {  // finite
+            nh = s;
+            nl = l - (s - h);
+        } else {
+            nh = h;
+            nl = l;
+        }
+    }
     XTG_DI void merge(const ScanState& o) {
         if (OP & 1) {
-            const float ph = hi * o.hi;
-            const float e = fmaf(hi, o.hi, -ph);
-            lo = fmaf(hi, o.lo, fmaf(lo, o.hi, e));
+            float ah, al, bh, bl;
+            norm2(hi, lo, ah, al);
+            norm2(o.hi, o.lo, bh, bl);
+            const float ph = ah * bh;
+            const float e = fmaf(ah, bh, -ph);
+            lo = fmaf(ah, bl, fmaf(al, bh, e));
             hi = ph;
         } else {
             float s, e;
