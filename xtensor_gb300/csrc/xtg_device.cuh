@@ -875,18 +875,27 @@ template <int MAXOP> struct AccArg<double, MAXOP> {
         kv = MAXOP ? XTG_KEY_MIN : XTG_KEY_MAX;
     }
     XTG_DI double value() const { return unkey64(kv); }
+    // The key compare comes first, non-strict: wherever key order and IEEE
+    // order differ for an incoming value a (a = +0 after -0 for argmax, -0
+    // after +0 for argmin, a NaN whose key sits at the far end or equals the
+    // empty state's end key), a is a candidate by key and special, so the
+    // exact path decides.  A NaN whose key sits below the held key is never
+    // taken, as the fold never takes a NaN after the first element.  Equal
+    // keys of ordinary values keep the first (strict order).
     template <class X> XTG_DI void add(X x, i64 ps) {
         const i64 b = __double_as_longlong(cvt<double>(x));
-        if (f64_special(b)) {
-            const KeyPos r = arg_special<MAXOP>(kv, idx, __longlong_as_double(b), ps);
-            kv = r.k;
-            idx = r.p;
-            return;
-        }
         const i64 ka = key64(b);
-        if (MAXOP ? (ka > kv) : (ka < kv)) {  // strict: the first of equal values stays
-            kv = ka;
-            idx = ps;
+        if (MAXOP ? (ka >= kv) : (ka <= kv)) {
+            if (f64_special(b)) {
+                const KeyPos r = arg_special<MAXOP>(kv, idx, __longlong_as_double(b), ps);
+                kv = r.k;
+                idx = r.p;
+                return;
+            }
+            if (ka != kv) {
+                kv = ka;
+                idx = ps;
+            }
         }
     }
     XTG_DI void merge(const AccArg& o) {
