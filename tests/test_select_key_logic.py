@@ -1,0 +1,82 @@
+"""The float64 arg-reduction update of the device code (key compare first,
+the special-value path only for candidates; `AccArg<double>` in
+xtensor_gb300/csrc/xtg_device.cuh), restated step for step on the host and
+checked against the oracle's sequential fold on short sequences rich in
+signed zeros, infinities, subnormals and NaNs of every bit pattern that
+matters (including the all-ones patterns whose keys equal the empty state's
+end keys).  CPU only: this pins the logic; the GPU tests pin the kernels."""
+from __future__ import annotations
+
+import struct
+
+import numpy as np
+
+from oracle import oracle as O
+from xtensor_gb300.device import HostArray as H
+
+M64 = (1 << 64) - 1
+KMIN, KMAX = -(1 << 63), (1 << 63) - 1
+
+
+def _s64(u):
+    return u - (1 << 64) if u >= (1 << 63) else u
+
+
+def _bits(d):
+    return _s64(struct.unpack("<Q", struct.pack("<d", d))[0])
+
+
+def _unbits(b):
+    return struct.unpack("<d", struct.pack("<Q", b & M64))[0]
+
+
+def _key64(b):
+    return b ^ (0x7FFFFFFFFFFFFFFF if b < 0 else 0)
+
+
+def _special(b):
+    hi = (b >> 32) & 0xFFFFFFFF
+    return (((hi & 0x7FFFFFFF) - 1) & 0xFFFFFFFF) >= 0x7FEFFFFF
+
+
+def _isnan_bits(b):
+    return (b & 0x7FFFFFFFFFFFFFFF) > 0x7FF0000000000000
+
+
+def _arg_special(maxop, kv, idx, a, ps):
+    b = _bits(a)
+    nan = _isnan_bits(b)
+    if idx < 0:
+        take = (not nan) or ps == 0
+    else:
+        v = _unbits(_key64(kv))
+        take = (a > v) if maxop else (a < v)
+    if take:
+        return ((KMAX if maxop else KMIN) if nan else _key64(b)), ps
+    return kv, idx
+
+
+def _device_fold(xs, maxop):
+    kv, idx = (KMIN if maxop else KMAX), -1
+    for ps, a in enumerate(xs):
+        b = _bits(a)
+        ka = _key64(b)
+        if (ka >= kv) if maxop else (ka <= kv):
+            if _special(b):
+                kv, idx = _arg_special(maxop, kv, idx, a, ps)
+                continue
+            if ka != kv:
+                kv, idx = ka, ps
+    return idx
+
+
+def test_key_first_update_matches_the_fold():
+    g = np.random.default_rng(7)
+    specials = [0.0, -0.0, np.inf, -np.inf, np.nan, -np.nan, 5e-324, -5e-324, 2.2250738585072014e-308,
+                _unbits(-1), _unbits(0x7FFFFFFFFFFFFFFF), _unbits(0x7FF0000000000001), _unbits(0xFFF0000000000001)]
+    for _ in range(6000):
+        n = int(g.integers(1, 12))
+        xs = [specials[g.integers(len(specials))] if g.random() < 0.4 else float(g.integers(-3, 4)) for _ in range(n)]
+        a = np.array(xs, dtype=np.float64)
+        for op, mx in (("argmax", 1), ("argmin", 0)):
+            assert _device_fold(xs, mx) == int(O.argreduce(op, H(a), None)), (op, [hex(_bits(v) & M64) for v in xs])
