@@ -167,8 +167,8 @@ std::string kernel_name(xtg_batch* b, const Tree& t, int gl, const AccChoice* ch
     if (b->reduce)
         return "xtg::k_batch_rowreduce<" + tree + ", " + ls + ", " + ch->acc + ", " + dt(b->out_dtype).cname + ", " +
                std::to_string(ch->post) + ", " + std::to_string(gl) + ", " +
-               std::to_string(b->vec > 1 ? (int)opt("batch.vec_unroll", 2) : b->unroll) + ", " + std::to_string(b->vec) +
-               ", " + std::to_string(b->vec > 1 ? (int)opt("batch.vec_minblocks", 3) : 1) + ">";
+               std::to_string(b->vec > 1 ? (int)opt("batch.vec_unroll", 3) : b->unroll) + ", " + std::to_string(b->vec) +
+               ", " + std::to_string(b->vec > 1 ? (int)opt("batch.vec_minblocks", 4) : 1) + ">";
     return "xtg::k_batch_assign<" + tree + ", " + ls + ", " + dt(b->out_dtype).cname + ", " + std::to_string(gl) + ", " +
            std::to_string(b->unroll) + ">";
 }
