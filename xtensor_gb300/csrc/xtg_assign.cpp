@@ -15,6 +15,7 @@
 //   K7 k_rowfused   — trees containing keep-dims statistics over trailing
 //                     axes, evaluated in one pass.
 #include <algorithm>
+#include <cmath>
 #include <array>
 #include <cstring>
 #include <string>
@@ -408,6 +409,13 @@ static xtg_status assign_rowfused(const Tree& t, const xtg_array& out, int R, co
         p.div[x.stat] = div;
         p.rdiv[x.stat] = 1.0 / div;
         p.vfac[x.stat] = 1.0 / ((double)row_len * div);
+        auto e2 = [](double f) {
+            int k;
+            const double m = std::frexp(f, &k);  // f = m * 2^k, m in [0.5, 1)
+            return (m == 0.5 && k - 1 > -1000 && k - 1 < 1000) ? k - 1 + 100000 : 0;
+        };
+        p.rdiv_e2[x.stat] = e2(p.rdiv[x.stat]);
+        p.vfac_e2[x.stat] = e2(p.vfac[x.stat]);
         p.fdiv[x.stat] = (float)div;
     }
     p.rrow_len = 1.0 / (double)row_len;

@@ -2611,13 +2611,25 @@ template <class Sub, int K2, int M2, class C2, class S2, class... R> struct Same
         value = rest > mine ? rest : mine
     };
 };
+// v * f where f = 2^k when e2 = k + 100000 (else e2 = 0): the exponent field
+// moves on the integer pipes when v and the result are normal (the product is
+// exact then, as the multiplication's would be); otherwise the FP64 multiply.
+XTG_DI double mul_pow2(double v, double f, int e2) {
+    if (e2) {
+        const long long b = __double_as_longlong(v);
+        const int e = (int)((b >> 52) & 0x7ff) + (e2 - 100000);
+        if (((b >> 52) & 0x7ff) != 0 && e >= 1 && e <= 2046)
+            return __longlong_as_double(b + ((long long)(e2 - 100000) << 52));
+    }
+    return v * f;
+}
 template <int MODE, int K, class CT> XTG_DI void put_moment(CT& c, const RowParams& p, double sum, double sdev2) {
     if (MODE == 0) {
         RowFin<double>::put(c, K, sum);
     } else if (MODE == 1) {
-        RowFin<double>::put(c, K, RowFin<double>::scale(sum, p, K));
+        RowFin<double>::put(c, K, mul_pow2(sum, p.rdiv[K], p.rdiv_e2[K]));
     } else {
-        const double var = sdev2 * p.vfac[K];  // (n * sum (x - mean)^2) / (n * divisor)
+        const double var = mul_pow2(sdev2, p.vfac[K], p.vfac_e2[K]);  // (n * sum (x - mean)^2) / (n * divisor)
         RowFin<double>::put(c, K, MODE == 3 ? m_sqrt(var) : var);
     }
     if (K < 32) c.fixmask |= 1u << K;

@@ -95,6 +95,8 @@ struct RowParams {
     double div[XTG_KMAX_SCAL];  // per statistic divisor (mean: n, var: n - ddof)
     double rdiv[XTG_KMAX_SCAL]; // 1 / div (float64 rows multiply)
     double vfac[XTG_KMAX_SCAL]; // 1 / (row_len * div): float64 variance from n * sum of squared deviations
+    int rdiv_e2[XTG_KMAX_SCAL]; // rdiv == 2^k: k + 100000, else 0 (float64 rows scale by the exponent)
+    int vfac_e2[XTG_KMAX_SCAL]; // the same for vfac
     float fdiv[XTG_KMAX_SCAL];  // div as float (float32 rows divide in FP32)
     double rrow_len;            // 1 / row_len
     float frow_len;             // row_len as float
