@@ -2795,11 +2795,12 @@ __global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
 
 // ---------------------------------------------------------------------------
 // K7 with bulk copies.  Each warp owns rows; the rows of every leaf stream
-// into a per-warp double buffer in shared memory with one cp.async.bulk per
-// leaf per row (the TMA engine's 1-D bulk copy, completion counted in bytes
-// on an mbarrier), issued one row ahead, so HBM reads of row i+1 overlap the
-// statistics and the stores of row i.  Requires every leaf to be contiguous
-// along the row, rows 16-byte aligned and a multiple of 16 bytes.
+// into a per-warp buffer in shared memory (one, or a double buffer) with one
+// cp.async.bulk per leaf per row (the TMA engine's 1-D bulk copy, completion
+// counted in bytes on an mbarrier), issued one row ahead, so HBM reads of row
+// i+1 overlap the statistics and the stores of row i.  Requires every leaf to
+// be contiguous along the row, rows 16-byte aligned and a multiple of 16
+// bytes.
 XTG_DI unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 XTG_DI void mbar_init(u64* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
