@@ -549,6 +549,34 @@ def test_row_moments_float64(n):
     np.testing.assert_array_equal(got[~np.isnan(got)], y.mean(-1)[~np.isnan(got)])
 
 
+@pytest.mark.parametrize("n", [1024, 1000])
+def test_row_moments_float64_overflowing_variance(n):
+    """Finite float64 rows whose squared deviations overflow (|x| ~ 1e200):
+    the fixed-point moments round the variance to infinity, and the scaling
+    by 1/n (by the exponent field when n is a power of two, else a multiply)
+    keeps it infinite, as numpy's and the reference's float64 arithmetic do;
+    the normalised row is then all zeros.  Rows near the bottom of the range
+    (|x| ~ 1e-200) give a variance that underflows to 0."""
+    g = rng(24)
+    x = np.stack([g.standard_normal(n) * 1e200, g.standard_normal(n) * 1e-200])
+    d = dev(x)
+    with np.errstate(over="ignore", under="ignore"):
+        want_var = x.var(-1)
+        want_mean = x.mean(-1)
+    assert np.isinf(want_var[0]) and want_var[1] == 0.0
+    o = DeviceArray.empty(x.shape, "float64")
+    xg.assign(o, xg.rvar(d) + 0.0 * d)
+    got_var = o.to_numpy()[:, 0]
+    assert np.isposinf(got_var[0]) and got_var[1] == 0.0, got_var
+    xg.assign(o, xg.rmean(d) + 0.0 * d)
+    np.testing.assert_allclose(o.to_numpy()[:, 0], want_mean, rtol=1e-14, atol=0)
+    xg.assign(o, (d - xg.rmean(d)) / xg.sqrt(xg.rvar(d) + 1e-5))
+    y = o.to_numpy()
+    np.testing.assert_array_equal(y[0], np.zeros(n))
+    exact = (x[1] - want_mean[1]) / np.sqrt(1e-5)
+    np.testing.assert_allclose(y[1], exact, rtol=1e-12, atol=1e-300)
+
+
 def test_row_stats_other_modes():
     g = rng(15)
     x = g.standard_normal((6, 7, 33)).astype(np.float32)

@@ -2613,12 +2613,15 @@ template <class Sub, int K2, int M2, class C2, class S2, class... R> struct Same
 };
 // v * f where f = 2^k when e2 = k + 100000 (else e2 = 0): the exponent field
 // moves on the integer pipes when v and the result are normal (the product is
-// exact then, as the multiplication's would be); otherwise the FP64 multiply.
+// exact then, as the multiplication's would be); zeros, subnormals,
+// infinities, NaNs and results outside the normal range take the FP64
+// multiply.
 XTG_DI double mul_pow2(double v, double f, int e2) {
     if (e2) {
         const long long b = __double_as_longlong(v);
-        const int e = (int)((b >> 52) & 0x7ff) + (e2 - 100000);
-        if (((b >> 52) & 0x7ff) != 0 && e >= 1 && e <= 2046)
+        const int ef = (int)((b >> 52) & 0x7ff);
+        const int e = ef + (e2 - 100000);
+        if (ef != 0 && ef != 0x7ff && e >= 1 && e <= 2046)
             return __longlong_as_double(b + ((long long)(e2 - 100000) << 52));
     }
     return v * f;
