@@ -80,3 +80,40 @@ def test_key_first_update_matches_the_fold():
         a = np.array(xs, dtype=np.float64)
         for op, mx in (("argmax", 1), ("argmin", 0)):
             assert _device_fold(xs, mx) == int(O.argreduce(op, H(a), None)), (op, [hex(_bits(v) & M64) for v in xs])
+
+
+def test_position_free_float64_pass_matches_the_fold_when_it_stands():
+    """The position-free first pass of float64 amax / amin (`AccSelFast<double>`):
+    the best key and the largest high-word magnitude; when it does not ask
+    for the exact pass (no infinity or NaN seen, best key not a zero's),
+    its value is the fold's value bit for bit; and it does ask whenever a
+    NaN is present."""
+    g = np.random.default_rng(8)
+    specials = [0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -5e-324, 2.2250738585072014e-308,
+                -2.2250738585072014e-308, 1.7976931348623157e308, -1.7976931348623157e308]
+    lowest, highest = -1.7976931348623157e308, 1.7976931348623157e308
+    asked = 0
+    for _ in range(6000):
+        n = int(g.integers(1, 12))
+        xs = [specials[g.integers(len(specials))] if g.random() < 0.4 else float(g.integers(-3, 4)) * 0.5
+              for _ in range(n)]
+        a = np.array(xs, dtype=np.float64)
+        for op, mx in (("amax", 1), ("amin", 0)):
+            kv = _key64(_bits(lowest if mx else highest))
+            mh = 0
+            for v in xs:
+                b = _bits(v)
+                mh = max(mh, (b >> 32) & 0x7FFFFFFF)
+                ka = _key64(b)
+                if (ka >= kv) if mx else (ka <= kv):
+                    kv = ka
+            exact = mh >= 0x7FF00000 or kv in (0, -1)
+            want = O.reduce(op, H(a), None)
+            if np.isnan(a).any():
+                assert exact
+            if exact:
+                asked += 1
+                continue
+            got = _unbits(_key64(kv))
+            assert np.array(got).view(np.int64) == np.array(want, np.float64).view(np.int64), (op, xs)
+    assert asked < 12000

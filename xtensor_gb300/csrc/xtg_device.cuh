@@ -719,22 +719,29 @@ template <int MAXOP> struct AccSelFast<float, MAXOP> {
         s.pos = -1;
     }
 };
+// double: the key order is the IEEE order except for NaNs and for -0 / +0,
+// so the pass keeps the largest high word magnitude (an infinity or NaN
+// anywhere asks for the exact pass) and asks for it too when the best key is
+// a zero's (0: +0, -1: -0), where the fold's last-visited rule decides.
 template <int MAXOP> struct AccSelFast<double, MAXOP> {
     i64 kv;
+    unsigned mh;  // largest (high word & 0x7fffffff) seen
     bool odd;
     template <class P> XTG_DI void init(const P& p) {
         AccSel<double, MAXOP> s;
         s.start(p.init_f);
         kv = s.kv;
+        mh = 0;
         odd = f64_special(__double_as_longlong(p.init_f));
     }
     template <class X> XTG_DI void add(X x, i64) {
         const i64 b = __double_as_longlong(cvt<double>(x));
-        odd |= f64_special(b);
+        const unsigned h = (unsigned)(b >> 32) & 0x7fffffffu;
+        mh = mh > h ? mh : h;
         const i64 ka = key64(b);
         if (MAXOP ? (ka >= kv) : (ka <= kv)) kv = ka;
     }
-    XTG_DI bool exact() const { return odd; }
+    XTG_DI bool exact() const { return odd || mh >= 0x7ff00000u || kv == 0 || kv == -1; }
     XTG_DI void to(AccSel<double, MAXOP>& s) const {
         s.kv = kv;
         s.pos = -1;
