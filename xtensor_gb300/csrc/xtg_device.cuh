@@ -2455,8 +2455,9 @@ XTG_DI U192 u192_sub(U192 a, U192 b) {
 }
 // (-1)^neg * q * 2^e2 rounded to nearest even, on the integer pipes (a lane
 // of a warp group runs this per row, and GB300's FP64 rate makes the usual
-// conversions + scalbn cost more than the row's elements).  Results outside
-// the normal range go through scalbn.
+// conversions + scalbn cost more than the row's elements).  One rounding in
+// every range: results below the normal range round the 64-bit window
+// directly to the subnormal grid, results above it are infinities.
 XTG_DI double fix_to_double(U192 q, bool neg, int e2) {
     int top;
     if (q.w2) top = 191 - __clzll(q.w2);
@@ -2479,6 +2480,29 @@ XTG_DI double fix_to_double(U192 q, bool neg, int e2) {
         const u64 below = b ? (lo << (64 - b)) : 0ull;
         sticky = below != 0 || (wi >= 1 && q.w0 != 0) || (wi == 2 && q.w1 != 0);
     }
+    if (top + e2 + 1023 < 1) {
+        // below the normal range: round the window (and what lies under it)
+        // once, straight to the subnormal grid of 2^-1074; a carry into
+        // 2^52 is the smallest normal number's bit pattern
+        const int r = -(top - 63 + e2 + 1074);  // bits of the window to drop, >= 12
+        u64 qv;
+        bool rb, st;
+        if (r >= 65) {
+            qv = 0;
+            rb = false;
+            st = true;
+        } else if (r == 64) {
+            qv = 0;
+            rb = (m >> 63) & 1;
+            st = sticky || (m << 1) != 0;
+        } else {
+            qv = m >> r;
+            rb = (m >> (r - 1)) & 1;
+            st = sticky || (m << (65 - r)) != 0;
+        }
+        if (rb && (st || (qv & 1))) ++qv;
+        return __longlong_as_double((long long)(((u64)neg << 63) | qv));
+    }
     u64 mant = m >> 11;  // 53 bits, leading one at bit 52
     const bool rnd = (m >> 10) & 1;
     sticky = sticky || (m & 0x3ffull) != 0;
@@ -2489,10 +2513,7 @@ XTG_DI double fix_to_double(U192 q, bool neg, int e2) {
         ++e;
     }
     const int be = e + 1023;
-    if (be < 1 || be > 2046) {
-        const double r = scalbn((double)mant, e - 52);  // exact mant; scalbn rounds once at the range end
-        return neg ? -r : r;
-    }
+    if (be > 2046) return neg ? -__longlong_as_double(0x7ff0000000000000ll) : __longlong_as_double(0x7ff0000000000000ll);
     const u64 bits = ((u64)neg << 63) | ((u64)be << 52) | (mant & 0xfffffffffffffull);
     return __longlong_as_double((long long)bits);
 }
