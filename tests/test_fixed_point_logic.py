@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import math
 import random
+import struct
 from fractions import Fraction
 
 M64 = (1 << 64) - 1
@@ -85,3 +86,44 @@ def test_subnormal_edges():
             if q == 0:
                 continue
             assert _fix_to_double(q, False, -1074 - 64) == _exact(q, False, -1074 - 64), (base, frac)
+
+
+def _fixed_mag(x: float, ef_max: int) -> int:
+    """`fixed_mag`: |X| = |x| * 2^(1075 - ef_max) rounded half away from zero
+    (twice the significand shifted down, plus one, halved)."""
+    b = struct.unpack("<Q", struct.pack("<d", x))[0]
+    hi, lo = b >> 32, b & 0xFFFFFFFF
+    e = (hi >> 20) & 0x7FF
+    m2 = ((((hi & 0xFFFFF) | (0x100000 if e else 0)) << 32) | lo) << 1
+    sh = min(ef_max - (e if e else 1), 63)
+    return ((m2 >> sh) + 1) >> 1
+
+
+def test_fixed_point_elements_and_square_sums():
+    """Each element becomes X = round(x * 2^(1075 - Ef)) (exact in the top
+    binade, half away from zero below it), and a lane's sum of X^2 split as
+    Xh^2 2^54 + 2 Xh Xl 2^27 + Xl^2 (|X| = Xh 2^27 + Xl, unsigned 32x32-bit
+    products) is exact."""
+    rnd = random.Random(5)
+    for _ in range(3000):
+        ef = rnd.randint(2, 2046)
+        xs = []
+        for _ in range(64):
+            e = rnd.randint(max(0, ef - 70), ef)
+            mant = rnd.getrandbits(52)
+            sign = rnd.random() < 0.5
+            b = (int(sign) << 63) | (e << 52) | mant
+            xs.append(struct.unpack("<d", struct.pack("<Q", b))[0])
+        a = bb = cc = 0
+        for x in xs:
+            v = _fixed_mag(x, ef)
+            exact = abs(Fraction(x)) * Fraction(2) ** (1075 - ef)
+            fl = math.floor(exact)
+            want = fl + 1 if exact - fl >= Fraction(1, 2) else fl
+            assert v == want and v < (1 << 53), (x, ef, v, want)
+            xh, xl = v >> 27, v & 0x7FFFFFF
+            a += xh * xh
+            bb += xh * xl
+            cc += xl * xl
+        assert (a << 54) + (bb << 28) + cc == sum(_fixed_mag(x, ef) ** 2 for x in xs)
+        assert a < (1 << 64) and bb < (1 << 64) and cc < (1 << 64)
