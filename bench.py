@@ -43,6 +43,8 @@ sys.path.insert(0, str(ROOT))
 
 SHAPE = (256, 512, 1024)
 N = SHAPE[0] * SHAPE[1] * SHAPE[2]
+NOMINAL_HBM_GBS = 8000.0  # GB300 HBM3e, nominal
+
 METRIC = "HBM GB/s (frac of roofline) assign+reduce; served p50/p99 ms vs plain"
 WORKLOAD = ("strided/axis work: x float32+float64 (256,512,1024) N(0,1) seed 1; transpose {2,0,1} to contiguous; "
             "y=(x-mean(x,{2},kd))/sqrt(var(x,{2},kd)+1e-5); amax {0,2}; int32 argmax axis 1")
@@ -364,7 +366,9 @@ def run_gpu(args):
         except Exception:
             traffic = None
     per_kernel = {names[i]: {"ms": round(avg[i], 4), "GB/s": round(op_bytes(step.calls[i][1])[step.calls[i][0]] / (avg[i] / 1e3) / 1e9, 1),
-                             "frac": round(op_bytes(step.calls[i][1])[step.calls[i][0]] / (avg[i] / 1e3) / 1e9 / peak, 3)}
+                             "frac": round(op_bytes(step.calls[i][1])[step.calls[i][0]] / (avg[i] / 1e3) / 1e9 / peak, 3),
+                             "frac_nominal": round(op_bytes(step.calls[i][1])[step.calls[i][0]] / (avg[i] / 1e3) / 1e9
+                                                   / NOMINAL_HBM_GBS, 3)}
                   for i in range(nops)}
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -391,6 +395,9 @@ def run_gpu(args):
                          "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6800 GB/s"},
             "per_kernel": per_kernel,
+            # the same throughputs against the nominal 8000 GB/s HBM3e figure
+            "vs_nominal_hbm": {"peak": NOMINAL_HBM_GBS, "step_frac": round(value / D.ws / NOMINAL_HBM_GBS, 4),
+                               "kernel_frac": round(achieved / NOMINAL_HBM_GBS, 4)},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(l1 - l0),
