@@ -56,8 +56,19 @@ def test_c1_strided_axis(dt):
     y = fake((256, 512, 1024), dt)
     xg.assign(y, (x - xg.rmean(x)) / xg.sqrt(xg.rvar(x) + 1e-5))
     ks = last_kernels()
-    # rows of 1024 contiguous elements: the bulk-copy (TMA) double-buffered variant
+    # rows of 1024 contiguous elements: the bulk-copy (TMA) variant with one
+    # buffer per warp and a register bound of 5 blocks per SM (a lane holds
+    # 64 registers of the row at most)
     assert fam(ks) == ["k_rowfused_tma"] and "RStat<0, 1" in ks[0] and "RStat<1, 2" in ks[0]
+    assert ks[0].endswith(", 1, 5>"), ks[0]
+    xg.set_option("row.tma_buffers", 2)
+    xg.set_option("row.tma_min_blocks", 3)
+    try:
+        xg.assign(y, (x - xg.rmean(x)) / xg.sqrt(xg.rvar(x) + 1e-5))
+        assert last_kernels()[0].endswith(", 2, 3>")
+    finally:
+        xg.set_option("row.tma_buffers", -1)
+        xg.set_option("row.tma_min_blocks", -1)
     if dt == "float64":
         assert "FmaRecipSub<double" in ks[0]
     am = fake((512,), dt)
