@@ -117,3 +117,39 @@ def test_position_free_float64_pass_matches_the_fold_when_it_stands():
             got = _unbits(_key64(kv))
             assert np.array(got).view(np.int64) == np.array(want, np.float64).view(np.int64), (op, xs)
     assert asked < 12000
+
+
+def test_position_free_float32_pass_matches_the_fold_when_it_stands():
+    """The float32 amax / amin position-free pass (`AccSelFast<float>`): one
+    NaN-propagating max / min per element (PTX max.NaN / min.NaN); it asks
+    for the exact pass when the result is a NaN or a zero, and otherwise its
+    value is the fold's, bit for bit."""
+    g = np.random.default_rng(9)
+    f32 = np.float32
+    specials = [f32(0.0), f32(-0.0), f32(np.inf), f32(-np.inf), f32(np.nan), f32(1e-45), f32(-1e-45),
+                f32(3.4028235e38), f32(-3.4028235e38)]
+    lowest, highest = f32(-3.4028235e38), f32(3.4028235e38)
+
+    def sel_nan(a, b, mx):
+        if np.isnan(a) or np.isnan(b):
+            return f32(np.nan)
+        if a == b:  # +0 / -0: either is fine here, a zero result asks for the exact pass
+            return a
+        return max(a, b) if mx else min(a, b)
+
+    for _ in range(6000):
+        n = int(g.integers(1, 12))
+        xs = [specials[g.integers(len(specials))] if g.random() < 0.4 else f32(g.integers(-3, 4) * 0.5)
+              for _ in range(n)]
+        a = np.array(xs, dtype=np.float32)
+        for op, mx in (("amax", 1), ("amin", 0)):
+            v = lowest if mx else highest
+            for x in xs:
+                v = sel_nan(v, x, mx)
+            exact = bool(np.isnan(v)) or v == 0
+            if np.isnan(a).any():
+                assert exact
+            if exact:
+                continue
+            want = O.reduce(op, H(a), None)
+            assert np.array(v, np.float32).view(np.int32) == np.array(want, np.float32).view(np.int32), (op, xs)
