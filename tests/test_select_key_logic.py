@@ -153,3 +153,40 @@ def test_position_free_float32_pass_matches_the_fold_when_it_stands():
                 continue
             want = O.reduce(op, H(a), None)
             assert np.array(v, np.float32).view(np.int32) == np.array(want, np.float32).view(np.int32), (op, xs)
+
+
+def test_held_arg_update_equals_the_full_update():
+    """Column arg-reductions (`ColStep` with `AccArg<float>`): once a column
+    holds a value (idx >= 0) the update is compare-and-select only.  Along
+    any chain of positions (a split need not start at position 0) the state
+    is the same as with the full update at every element."""
+    g = np.random.default_rng(10)
+    f32 = np.float32
+    vals = [f32(np.nan), f32(np.inf), f32(-np.inf), f32(0.0), f32(-0.0), f32(1.0), f32(-1.0), f32(2.0)]
+
+    def full(state, a, ps, mx):
+        v, idx = state
+        if idx < 0:
+            return (a, ps) if (a == a or ps == 0) else state
+        return (a, ps) if ((a > v) if mx else (a < v)) else state
+
+    def held(state, a, ps, mx):
+        v, idx = state
+        return (a, ps) if ((a > v) if mx else (a < v)) else state
+
+    for _ in range(5000):
+        p0 = int(g.integers(0, 3))
+        xs = [vals[g.integers(len(vals))] for _ in range(int(g.integers(1, 10)))]
+        for mx in (1, 0):
+            s_full = s_fast = (f32(0), -1)
+            is_held = False
+            for k, a in enumerate(xs):
+                ps = p0 + k
+                s_full = full(s_full, a, ps, mx)
+                if is_held:
+                    s_fast = held(s_fast, a, ps, mx)
+                else:
+                    s_fast = full(s_fast, a, ps, mx)
+                    is_held = s_fast[1] >= 0
+            assert s_full[1] == s_fast[1], (p0, xs, mx)
+            assert np.array(s_full[0], np.float32).view(np.int32) == np.array(s_fast[0], np.float32).view(np.int32)
