@@ -64,6 +64,12 @@ def step_bytes() -> int:
     return sum(op_bytes(4).values()) + sum(op_bytes(8).values())
 
 
+def c1_config() -> dict:
+    """The workload description both arms print (identical keys and values)."""
+    return {"workload": WORKLOAD, "elements": N, "algorithmic_bytes_per_step": step_bytes(),
+            "l2": "inputs (512 MiB f32, 1 GiB f64) larger than L2 (129 MB): no flush"}
+
+
 def peaks() -> tuple[float, str]:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -295,7 +301,7 @@ def run_reference(args):
         "metric": METRIC, "value": round(val, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(sec * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32,f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": WORKLOAD, "elements": N, "algorithmic_bytes_per_step": total},
+        "config": c1_config(),
         "cpu_baseline": {"value": round(val, 3), "unit": "GB/s", "cores": cores(), "kind": "port",
                          "sample": "full workload per step (compiled C port of the reference's loops, OpenMP)"},
         "e2e": {"value": round(val, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -388,9 +394,7 @@ def run_gpu(args):
             "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": D.ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32,f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "elements": N, "algorithmic_bytes_per_step": step_bytes(),
-                       "l2": "inputs (512 MiB f32, 1 GiB f64) larger than L2 (129 MB): no flush",
-                       "parallelism": f"replicas x{D.ws}", "kernel_ms_per_step": round(kern_ms, 4)},
+            "config": c1_config(), "parallelism": f"replicas x{D.ws}", "kernel_ms_per_step": round(kern_ms, 4),
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6800 GB/s"},

@@ -9,7 +9,7 @@ path to tests/golden/*.json, so that the tests (and the GPU machine, which has no
 copy of the reference) can pin the oracle and the GPU path to them.
 
 Run (in the build container, where the reference is mounted):
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 """
 from __future__ import annotations
 
@@ -85,4 +85,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])

@@ -9,7 +9,7 @@ this script copies them next to the tests and checks, with numpy, that each
 holds the arrays test_xnpy.cpp expects.
 
 Run (in the build container, where the reference is mounted):
-    python tests/golden/make_npy_golden.py /root/reference
+    python tests/golden/make_npy_golden.py <reference checkout>
 """
 from __future__ import annotations
 
@@ -62,4 +62,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python {sys.argv[0]} <path of the reference checkout>")
+    main(sys.argv[1])
