@@ -1,8 +1,10 @@
 /*
  * xt_baseline.c — compiled CPU port of the reference's code path for the
  * benchmark workloads.  TEST / BASELINE INFRASTRUCTURE ONLY: timed as the
- * CPU baseline by bench.py (and cross-checked against the GPU by tests); the
- * product library never uses it.
+ * CPU baseline by bench.py, which also checks the GPU results of its
+ * benchmark steps against these routines' outputs; the routines themselves
+ * are pinned to the oracle (xt_oracle.c) bit for bit on small seeded inputs
+ * by tests/test_baseline_port.py.  The product library never uses it.
  *
  * Each routine restates what xtensor 0.27.1 executes for the call, in the
  * same loop order and arithmetic types, compiled -O2 with OpenMP over the
