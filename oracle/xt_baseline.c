@@ -29,6 +29,17 @@
  *                       (xsort.hpp:1158-1235).
  *   bl_c0_*             E = A * b + exp(-A * A); r = sum(E, {1}).
  *   bl_sum_*            full sums (sequential, as the lazy reducer).
+ *   bl_stat_*_f32 / _bf16
+ *                       the precision workload's full reductions, one
+ *                       sequential pass each as the lazy reducer runs them,
+ *                       single-threaded (the reference's reducers are):
+ *                       sum in the value type (bfloat16 values widen to
+ *                       float, their sum type); mean = sum / (double)n
+ *                       (xmath.hpp:1860-1872); variance = mean over
+ *                       square(x - mean) with the double mean, summed in
+ *                       double (xmath.hpp:2033-2037); norm_l2 = sqrt of the
+ *                       double sum of x * x computed in the value type
+ *                       (xnorm.hpp:397-437, norm_sq(t) = t * t).
  *   bl_cumsum_*         xt::cumsum(x, axis) on a contiguous (d0, d1, d2) array:
  *                       `res = x`, then res[.., i, ..] += res[.., i-1, ..]
  *                       walking the storage with the axis stride
@@ -160,6 +171,43 @@ int64_t bl_sum_i32_i64(const int32_t* x, int64_t n) {
     for (int64_t i = 0; i < n; ++i) s += x[i];
     return s;
 }
+
+static inline float bl_bf16(uint16_t b) {
+    uint32_t u = (uint32_t)b << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+#define DEF_STATS(NAME, T, LOAD)                                                     \
+    float bl_stat_sum_##NAME(const T* x, int64_t n) {                                \
+        float s = 0.f;                                                               \
+        for (int64_t i = 0; i < n; ++i) s = s + LOAD(x[i]);                          \
+        return s;                                                                    \
+    }                                                                                \
+    double bl_stat_mean_##NAME(const T* x, int64_t n) {                              \
+        return n ? (double)bl_stat_sum_##NAME(x, n) / (double)n : 0.0;               \
+    }                                                                                \
+    double bl_stat_variance_##NAME(const T* x, int64_t n) {                          \
+        const double m = bl_stat_mean_##NAME(x, n);                                  \
+        double q = 0.0;                                                              \
+        for (int64_t i = 0; i < n; ++i) {                                            \
+            const double d = (double)LOAD(x[i]) - m;                                 \
+            q = q + d * d;                                                           \
+        }                                                                            \
+        return n ? q / (double)n : 0.0;                                              \
+    }                                                                                \
+    double bl_stat_norm_l2_##NAME(const T* x, int64_t n) {                           \
+        double q = 0.0;                                                              \
+        for (int64_t i = 0; i < n; ++i) {                                            \
+            const float v = LOAD(x[i]);                                              \
+            q = q + (double)(v * v);                                                 \
+        }                                                                            \
+        return sqrt(q);                                                              \
+    }
+#define BL_ID(v) (v)
+DEF_STATS(f32, float, BL_ID)
+DEF_STATS(bf16, uint16_t, bl_bf16)
 
 
 #define DEF_CUMSUM(T, NAME)                                                                           \

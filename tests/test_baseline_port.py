@@ -14,6 +14,8 @@ compared with the oracle's restatement of the reference
   * C0's E = A * b + exp(-A * A) and its row sums: bit-exact (the same
     libm expf, the same sequential float fold);
   * full float32 / int32 -> int64 sums: bit-exact (sequential folds);
+  * the precision workload's sum / mean / variance / norm_l2 of float32
+    and bfloat16 arrays: bit-exact;
   * cumsum along each axis and flattened: bit-exact.
 """
 from __future__ import annotations
@@ -47,6 +49,11 @@ def port():
     L.bl_sum_i32_i64.restype = C.c_int64
     for t in ("f32", "f64", "i32"):
         getattr(L, f"bl_cumsum_{t}").argtypes = [P, P, I64, I64, I64, C.c_int]
+    for t in ("f32", "bf16"):
+        for op in ("sum", "mean", "variance", "norm_l2"):
+            f = getattr(L, f"bl_stat_{op}_{t}")
+            f.argtypes = [P, I64]
+            f.restype = C.c_float if op == "sum" else C.c_double
     return L
 
 
@@ -127,3 +134,20 @@ def test_port_cumsum_equals_oracle(dt, axis):
     getattr(L, f"bl_cumsum_{t}")(ptr(x), ptr(r), *shape, axis)
     ref = O.accumulate("cumsum", HostArray(x), None if axis < 0 else axis)
     np.testing.assert_array_equal(r.reshape(ref.shape), ref)
+
+
+@pytest.mark.parametrize("dt", ["float32", "bfloat16"])
+@pytest.mark.parametrize("n", [1, 7, 10007])
+def test_port_precision_stats_equal_oracle(dt, n):
+    from util import f32_to_bf16_bits
+    L = port()
+    g = np.random.default_rng(2)
+    x = (g.lognormal(0, 2, n) * g.choice([-1, 1], n)).astype(np.float32)
+    arr, t = (x, "f32") if dt == "float32" else (f32_to_bf16_bits(x), "bf16")
+    h = HostArray(arr, dt)
+    for op in ("sum", "mean", "variance", "norm_l2"):
+        got = getattr(L, f"bl_stat_{op}_{t}")(ptr(arr), n)
+        ref = O.reduce(op, h)
+        want = ref.astype(np.float32 if op == "sum" else np.float64)
+        got = np.asarray(got, dtype=want.dtype)
+        assert got.tobytes() == want.tobytes(), (op, dt, n, got, want)
