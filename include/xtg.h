@@ -490,19 +490,22 @@ xtg_status xtg_fill_random(const xtg_array* a, int32_t dist, double p0, double p
 
 /* ---- reduction without allocation ------------------------------------------------
  * No counterpart in the reference.  For callers that must not allocate device
- * memory while they reduce — code running during CUDA stream capture (where
- * cudaMalloc is not permitted), code whose device memory is owned by its own
- * allocator or budget, loops that must never enter an allocator.
+ * memory while they reduce: code whose device memory is owned by its own
+ * allocator or budget (a framework that reserved the device's memory up
+ * front, where an allocation by this library would fail or fragment it), and
+ * loops with latency limits that must never enter an allocator.
  * Sum of the n contiguous float32 values at device pointer x, written to the
  * float at device pointer out — the same kernels and plan as xtg_reduce(sum,
- * all axes) on that array, with the split-reduction partials in a static
- * device buffer of XTG_NOALLOC_SCRATCH_BYTES (every GPU the library is used
- * on keeps it until exit).  Inputs whose plan would need more partials than
- * the buffer holds, or more than 2^32 vectors, are rejected with
- * XTG_ERR_UNSUPPORTED.  The first call on a device resolves the buffer's
- * address (cudaGetSymbolAddress, which also loads the library's device code):
- * make that first call before any stream capture.  All calls share the
- * buffer: calls whose kernels may overlap on the GPU (unordered streams) race
+ * all axes) on that array, so the result is bit-identical to it, with the
+ * split-reduction partials in a static device array of
+ * XTG_NOALLOC_SCRATCH_BYTES (every GPU the library is used on keeps it until
+ * exit).  Inputs whose plan would need more partials than the array holds,
+ * or more than 2^32 vectors, are rejected with XTG_ERR_UNSUPPORTED before any
+ * launch.  The first call in a CUDA context resolves the array's address
+ * there (cudaGetSymbolAddress, which also loads the library's device code):
+ * make that first call before any stream capture.  A device reset or another
+ * context on the same device gets its own address.  All calls share the
+ * array: calls whose kernels may overlap on the GPU (unordered streams) race
  * and must be serialised by the caller. */
 #define XTG_NOALLOC_SCRATCH_BYTES (256u * 1024u)
 xtg_status xtg_sum_f32_noalloc(const float* x, int64_t n, float* out, xtg_stream stream);

@@ -1,12 +1,16 @@
 """The allocation-free float32 sum (xtg_sum_f32_noalloc), called through the
 C ABI, against the regular entry point xtg_reduce(sum, all axes).
 
-It is for callers that cannot allocate device memory while they reduce
-(stream capture, a caller-owned memory budget): its partials live in a static
-device buffer shared by every call.  Two calls in a row with different inputs
-check that whatever the previous call left in that buffer does not leak into
-the next result.  Tolerance: the one the sum tests use, 1e-6 * sum|x| against
-the regular entry point and against an FP64 evaluation.
+It serves callers that cannot allocate device memory while they reduce (their
+device memory is owned by their own allocator or budget, or they run loops
+that must never enter an allocator): its partials live in a static device
+array shared by every call.  It runs the same kernels and plan as the regular
+entry point, so its result must be bit-identical to xtg_reduce's on the same
+input, and within 1e-6 * sum|x| of the FP64 value (the tolerance the sum tests
+use).  Calls in a row with different inputs check that whatever the previous
+call left in the shared array does not leak into the next result.  The sizes
+cover every path of the plan: the empty sum, a single split written directly,
+a few splits merged by one thread, and thousands of splits merged by a block.
 
 This file is collected last so that a run stopping at its first failure has
 already run every other test; it also passes alone in a fresh process.
@@ -37,24 +41,38 @@ def _one_call(f, x: np.ndarray) -> None:
     dx = DeviceArray.from_numpy(x)
     out = DeviceArray.empty((), "float32")
     xg.check(f(dx.ptr, x.size, out.ptr, None))
-    got = float(out.to_numpy())
-    regular = float(ops.reduce("sum", dx).to_numpy())
+    got = out.to_numpy()
+    regular = ops.reduce("sum", dx).to_numpy()
+    assert got.tobytes() == regular.tobytes(), (x.size, float(got), float(regular))
     xd = x.astype(np.float64)
     bound = 1e-6 * float(np.abs(xd).sum())
-    assert abs(got - regular) <= bound, (got, regular)
-    assert abs(got - float(xd.sum())) <= bound, (got, float(xd.sum()))
+    assert abs(float(got) - float(xd.sum())) <= bound, (x.size, float(got), float(xd.sum()))
 
 
-def test_noalloc_sum_two_calls():
+def test_noalloc_sum_calls_in_a_row():
     xg.init(0)
     f = _noalloc()
     g = np.random.default_rng(21)
-    # sign-random lognormal data (heavy cancellation); an odd size (scalar
-    # loads, many chunks) then a size with 16-byte vectors.
-    a = (g.lognormal(0.0, 2.0, 1_000_003) * g.choice([-1.0, 1.0], 1_000_003)).astype(np.float32)
-    b = g.standard_normal(4 << 20).astype(np.float32)
-    _one_call(f, a)
-    _one_call(f, b)
+
+    def lognormal(n):
+        return (g.lognormal(0.0, 2.0, n) * g.choice([-1.0, 1.0], n)).astype(np.float32)
+
+    # sign-random lognormal data (heavy cancellation): thousands of splits
+    # merged by a block (an odd size: scalar loads), then a size with 16-byte
+    # vectors, then a few splits merged by one thread, then one split written
+    # directly, then the empty sum, then the first input again
+    a = lognormal(1_000_003)
+    for x in (a, g.standard_normal(4 << 20).astype(np.float32), lognormal(20_000), lognormal(1_000),
+              np.zeros(0, np.float32), a):
+        _one_call(f, x)
+
+
+def test_noalloc_empty_sum_is_zero():
+    xg.init(0)
+    f = _noalloc()
+    out = DeviceArray.from_numpy(np.full((), 7.0, np.float32))
+    xg.check(f(None, 0, out.ptr, None))
+    assert out.to_numpy().tobytes() == np.float32(0.0).tobytes()
 
 
 def test_noalloc_rejects_oversized_plan():

@@ -376,41 +376,64 @@ xtg_status xtg_batch_build(xtg_batch* b, int32_t autotune, xtg_stream stream) {
             cpsm = tc;
             b->tuned = 2;
         } else {
-            // measured search: group width x tile size x CTAs per SM
+            // measured search: group width x tile size x CTAs per SM.  Stage
+            // 1 times every candidate (median of 5); stage 2 re-times the
+            // candidates within 3% of the best (median of 9) and keeps the
+            // fastest, where a candidate must beat the one before it in the
+            // fixed order by more than 1% to replace it, so that near-ties
+            // resolve the same way on every run.
             const int gls[3] = {8, 16, 32};
             const int64_t tes[3] = {8192, 32768, 131072};
             const int cps[3] = {2, 4, 8};
+            struct Cand {
+                int g;
+                int64_t t;
+                int c;
+                double ms;
+            };
+            std::vector<Cand> cands;
             double best = 1e30;
             cudaEvent_t e0, e1;
             XTG_CUDA(cudaEventCreate(&e0));
             XTG_CUDA(cudaEventCreate(&e1));
-            for (int64_t tcand : tes) {
-                XTG_TRY(upload_tiles(b, tcand, s));
+            auto time_cand = [&](const Cand& cd, int reps, double* med) -> xtg_status {
+                XTG_TRY(upload_tiles(b, cd.t, s));
                 b->params.tiles = b->d_tiles;
                 b->params.ntiles = b->ntiles;
-                for (int gcand : gls) {
-                    XTG_TRY(get_kernel(kernel_name(b, t, gcand, b->reduce ? &ch : nullptr), 256, &b->k));
-                    for (int ccand : cps) {
-                        b->cpsm = ccand;
-                        XTG_TRY(launch_once(b, s));  // warm-up
-                        float ms[3];
-                        for (int r = 0; r < 3; ++r) {
-                            XTG_CUDA(cudaEventRecord(e0, s));
-                            XTG_TRY(launch_once(b, s));
-                            XTG_CUDA(cudaEventRecord(e1, s));
-                            XTG_CUDA(cudaEventSynchronize(e1));
-                            XTG_CUDA(cudaEventElapsedTime(&ms[r], e0, e1));
-                        }
-                        std::sort(ms, ms + 3);
-                        if (ms[1] < best) {
-                            best = ms[1];
-                            gl = gcand;
-                            te = tcand;
-                            cpsm = ccand;
-                        }
-                    }
+                XTG_TRY(get_kernel(kernel_name(b, t, cd.g, b->reduce ? &ch : nullptr), 256, &b->k));
+                b->cpsm = cd.c;
+                XTG_TRY(launch_once(b, s));  // warm-up
+                std::vector<float> ms((size_t)reps);
+                for (int r = 0; r < reps; ++r) {
+                    XTG_CUDA(cudaEventRecord(e0, s));
+                    XTG_TRY(launch_once(b, s));
+                    XTG_CUDA(cudaEventRecord(e1, s));
+                    XTG_CUDA(cudaEventSynchronize(e1));
+                    XTG_CUDA(cudaEventElapsedTime(&ms[(size_t)r], e0, e1));
                 }
+                std::sort(ms.begin(), ms.end());
+                *med = ms[(size_t)reps / 2];
+                return XTG_OK;
+            };
+            for (int64_t tcand : tes)
+                for (int gcand : gls)
+                    for (int ccand : cps) {
+                        Cand cd{gcand, tcand, ccand, 0.0};
+                        XTG_TRY(time_cand(cd, 5, &cd.ms));
+                        cands.push_back(cd);
+                        best = std::min(best, cd.ms);
+                    }
+            const double cut = best * 1.03;
+            int pick = -1;
+            for (size_t i = 0; i < cands.size(); ++i) {
+                if (cands[i].ms > cut) continue;
+                XTG_TRY(time_cand(cands[i], 9, &cands[i].ms));
+                if (pick < 0 || cands[i].ms < cands[(size_t)pick].ms * 0.99) pick = (int)i;
             }
+            gl = cands[(size_t)pick].g;
+            te = cands[(size_t)pick].t;
+            cpsm = cands[(size_t)pick].c;
+            best = cands[(size_t)pick].ms;
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             tune_store(key, gl, te, cpsm, best * 1e3);

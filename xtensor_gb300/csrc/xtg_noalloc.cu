@@ -1,13 +1,15 @@
 // xtg_noalloc.cu — float32 full sum that allocates nothing.
 //
 // Some callers cannot allocate device memory at the moment they reduce: code
-// running while a CUDA stream is being captured (cudaMalloc is not allowed
-// there), code that owns the whole device memory budget through its own
-// allocator, or real-time loops that must not enter the allocator at all.
-// xtg_reduce gets the scratch for its split reduction from the stream-ordered
-// pool; xtg_sum_f32_noalloc runs the same two kernels (the split row
-// reduction and its in-order combine, compiled here ahead of time for
-// sm_103a) with the partials in a fixed static device array instead.
+// whose device memory is owned by its own allocator or budget (a framework
+// that reserved the device's memory up front, where a cudaMalloc of the
+// library would fail or fragment it), or loops with latency limits that must
+// never enter an allocator (a stream-ordered allocation can map new memory
+// with an unbounded delay).  xtg_reduce gets the scratch for its split
+// reduction from the stream-ordered pool; xtg_sum_f32_noalloc runs the same
+// two kernels (the split row reduction and its in-order combine, compiled
+// here ahead of time for sm_103a) with the partials in a fixed static device
+// array instead.
 //
 // The array below is a module-scope `__device__` buffer: every GPU on which
 // this library is used holds XTG_NOALLOC_SCRATCH_BYTES of it until the
@@ -39,16 +41,36 @@ typedef L<0, float> Tree;
 #define XTG_NOALLOC_COMBINE xtg::k_reduce_combine<AccSumC, float, 0, 1>
 #define XTG_NOALLOC_COMBINE_THREAD xtg::k_reduce_combine_thread<AccSumC, float, 0, 1>
 
-struct DeviceState {
-    bool ready = false;
-    void* scratch = nullptr;  // device address of g_xtg_noalloc_scratch
+// Launch geometry and the array's device address, per CUDA context: the
+// address belongs to the context that loaded this module, so a device reset
+// (which ends the context) or a second context on the same device gets its
+// own entry, keyed by the driver's unique context id.
+struct CtxState {
+    unsigned long long ctx_id = 0;
+    void* scratch = nullptr;  // device address of g_xtg_noalloc_scratch in this context
     int sms = 0;
     int occ[3][2] = {{0, 0}, {0, 0}, {0, 0}};  // [vec 1/2/4][group 32/256]
     int occ_combine = 0;
 };
-constexpr int kMaxDevices = 64;
-DeviceState g_state[kMaxDevices];
+constexpr size_t kMaxContexts = 64;
+CtxState g_state[kMaxContexts];
+size_t g_nstate = 0;
 std::mutex g_mu;
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
+
+template <class F> xtg_status driver_fn(const char* sym, F& fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion(sym, &p, 13000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+        return xtgh::fail(XTG_ERR_CUDA, std::string("driver entry point not found: ") + sym);
+    fn = reinterpret_cast<F>(p);
+    return XTG_OK;
+}
 
 template <class K> int occupancy(K k) {
     int n = 0;
@@ -59,27 +81,51 @@ template <class K> int occupancy(K k) {
     return n > 0 ? n : 1;
 }
 
-// Once per device, with that device current: resolve the scratch array's
-// device address and the launch geometry.
-xtg_status setup(int dev, DeviceState** out) {
+// The entry of the calling thread's current context; the first call in a
+// context resolves the scratch array's device address there
+// (cudaGetSymbolAddress, which also loads this library's device code and, on
+// a thread with no context yet, creates the device's primary context) and
+// the launch geometry.
+xtg_status setup(int dev, CtxState** out) {
     std::lock_guard<std::mutex> lk(g_mu);
-    DeviceState& s = g_state[dev];
-    if (!s.ready) {
-        void* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_xtg_noalloc_scratch);
-        if (e != cudaSuccess) return xtgh::cuda_fail(e, "cudaGetSymbolAddress(g_xtg_noalloc_scratch)");
-        XTG_CUDA(cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, dev));
-        s.occ[0][0] = occupancy(XTG_NOALLOC_ROW(1, 32));
-        s.occ[0][1] = occupancy(XTG_NOALLOC_ROW(1, 256));
-        s.occ[1][0] = occupancy(XTG_NOALLOC_ROW(2, 32));
-        s.occ[1][1] = occupancy(XTG_NOALLOC_ROW(2, 256));
-        s.occ[2][0] = occupancy(XTG_NOALLOC_ROW(4, 32));
-        s.occ[2][1] = occupancy(XTG_NOALLOC_ROW(4, 256));
-        s.occ_combine = occupancy(XTG_NOALLOC_COMBINE);
-        s.scratch = ptr;
-        s.ready = true;
+    if (!g_ctx_get_current) {
+        XTG_TRY(driver_fn("cuCtxGetCurrent", g_ctx_get_current));
+        XTG_TRY(driver_fn("cuCtxGetId", g_ctx_get_id));
     }
-    *out = &s;
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return xtgh::fail(XTG_ERR_CUDA, "cuCtxGetCurrent failed");
+    void* ptr = nullptr;
+    if (!ctx) {
+        const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_xtg_noalloc_scratch);
+        if (e != cudaSuccess) return xtgh::cuda_fail(e, "cudaGetSymbolAddress(g_xtg_noalloc_scratch)");
+        if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx)
+            return xtgh::fail(XTG_ERR_CUDA, "no CUDA context after loading the device code");
+    }
+    unsigned long long id = 0;
+    if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return xtgh::fail(XTG_ERR_CUDA, "cuCtxGetId failed");
+    for (size_t i = 0; i < g_nstate; ++i)
+        if (g_state[i].ctx_id == id) {
+            *out = &g_state[i];
+            return XTG_OK;
+        }
+    if (g_nstate == kMaxContexts) return xtgh::fail(XTG_ERR_UNSUPPORTED, "xtg_sum_f32_noalloc: too many CUDA contexts");
+    if (!ptr) {
+        const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_xtg_noalloc_scratch);
+        if (e != cudaSuccess) return xtgh::cuda_fail(e, "cudaGetSymbolAddress(g_xtg_noalloc_scratch)");
+    }
+    CtxState s;
+    s.ctx_id = id;
+    s.scratch = ptr;
+    XTG_CUDA(cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, dev));
+    s.occ[0][0] = occupancy(XTG_NOALLOC_ROW(1, 32));
+    s.occ[0][1] = occupancy(XTG_NOALLOC_ROW(1, 256));
+    s.occ[1][0] = occupancy(XTG_NOALLOC_ROW(2, 32));
+    s.occ[1][1] = occupancy(XTG_NOALLOC_ROW(2, 256));
+    s.occ[2][0] = occupancy(XTG_NOALLOC_ROW(4, 32));
+    s.occ[2][1] = occupancy(XTG_NOALLOC_ROW(4, 256));
+    s.occ_combine = occupancy(XTG_NOALLOC_COMBINE);
+    g_state[g_nstate] = s;
+    *out = &g_state[g_nstate++];
     return XTG_OK;
 }
 
@@ -96,8 +142,7 @@ extern "C" xtg_status xtg_sum_f32_noalloc(const float* x, int64_t n, float* out,
     if (n < 0) return fail(XTG_ERR_INVALID, "negative element count");
     int dev = 0;
     XTG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return fail(XTG_ERR_INVALID, "device index out of range");
-    DeviceState* S;
+    CtxState* S;
     XTG_TRY(setup(dev, &S));
 
     // The same plan as xtg_reduce(XTG_RED_SUM, all axes) on a contiguous
