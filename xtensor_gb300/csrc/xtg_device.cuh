@@ -2941,9 +2941,15 @@ __global__ void __launch_bounds__(128, MINB) k_rowfused_tma(const RowParams p) {
                 break;
             }
         }
+        // one decision for the whole warp: a lane that gave up must not
+        // leave while the others go on into full-mask shuffles
+        done = __all_sync(0xffffffffu, done);
         if (!done) {
             // give up: flag it, wait (bounded) for the copy into the other
-            // buffer if one was issued, and leave
+            // buffer if one was issued, and leave.  The copy that timed out
+            // may still be in flight into this block's shared memory when
+            // the block exits; the error word tells the host that the
+            // launch's results (and the device state) are not to be trusted.
             if (lane == 0) atomicExch(p.err, 1);
             if (NB == 2 && row + ng < p.n_rows) {
                 const unsigned par2 = (unsigned)((it + 1) >> 1) & 1u;
