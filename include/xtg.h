@@ -261,6 +261,17 @@ xtg_status xtg_reduce(const xtg_expr* e, const xtg_reduce_desc* rd,
 /* has_axis = 0: index into the flattened (row-major) expression. */
 xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_t axis,
                          const xtg_array* out, xtg_stream stream);
+/* Assignment followed by a reduction of its result, in one pass where the
+ * plan allows:  out_e = e  (as xtg_assign), then  out_r = reduce(rd, out_e)
+ * (as xtg_reduce on out_e).  Replaces the pair of reference calls
+ * `xt::xarray<T> E = e;` (assign_xexpression, core/xassign.hpp:214-226) and
+ * `auto r = xt::sum(E, axes);` (reduce, reducers/xreducer.hpp:987-1079) at
+ * one read of e's leaves and one write of E and r: when the reduction is a
+ * row plan (reduced run contiguous), the tree has no row statistics and out_e
+ * shares no memory with the leaves, one kernel stores every evaluated element
+ * and folds it; otherwise the two evaluations run in order. */
+xtg_status xtg_assign_reduce(const xtg_expr* e, const xtg_array* out_e, const xtg_reduce_desc* rd,
+                             const xtg_array* out_r, xtg_stream stream);
 
 /* ---- accumulators ----------------------------------------------------------------------
  * Cumulative sum / product of an expression along `axis` (has_axis = 1; the

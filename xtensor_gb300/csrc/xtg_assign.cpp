@@ -502,6 +502,18 @@ static void byte_range(const xtg_array& a, int64_t& lo, int64_t& hi) {
     hi = (int64_t)(uintptr_t)a.data + hi * sz + sz;
 }
 
+bool shares_memory(const Tree& t, const xtg_array& out) {
+    int64_t olo, ohi;
+    byte_range(out, olo, ohi);
+    if (olo >= ohi) return false;
+    for (const xtg_array& l : t.leaves) {
+        int64_t llo, lhi;
+        byte_range(l, llo, lhi);
+        if (llo < lhi && lhi > olo && llo < ohi) return true;
+    }
+    return false;
+}
+
 bool assign_hazard(const Tree& t, const xtg_array& out) {
     int64_t olo, ohi;
     byte_range(out, olo, ohi);

@@ -526,6 +526,21 @@ XTG_DI void two_sum(float a, float b, float& s, float& e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
+// Packed float32 pairs: one instruction advances two independent FP32
+// operations (sm_100+ FADD2 / FMUL2 / FFMA2).  a - b is fma(b, -1, a): the
+// exact difference rounded once, the same result as the subtraction (round
+// to nearest is symmetric, so fl(b - a) = -fl(a - b) as well).
+XTG_DI float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+XTG_DI float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+XTG_DI float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+XTG_DI float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// TwoSum on both lanes: s + e == a + b exactly, lane by lane.
+XTG_DI void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+    s = p_add(a, b);
+    const float2 bb = p_sub(s, a);
+    e = p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb));
+}
+
 // ---------------------------------------------------------------------------
 // Reduction accumulators.  Each is POD: init(p), add(x, pos), merge(other),
 // and result<Out>(p).  `pos` is the element's row-major position inside the
@@ -818,6 +833,137 @@ template <int NK> struct AccNormC {
     }
     XTG_DI void merge(const AccNormC& o) { a.merge(o.a); }
     XTG_DI double dval() const { return a.dval(); }
+};
+
+// Working accumulators of the row pass for the double-float states above:
+// two (hi, lo) lanes, even elements of a vector into lane 0 and odd ones into
+// lane 1, each lane updated by TwoSum exactly as the scalar state is, with
+// packed instructions (half the issue slots: these loops are issue-bound for
+// 2-byte inputs and for the two-sum moments).  from() starts lane 0 at the
+// stored state and lane 1 at zero; to() merges lane 1 into lane 0 with the
+// TwoSum merge when the work item ends, so partial slots and combines keep
+// the stored form.  add() (scalar, lane 0) serves odd vector widths.
+struct AccSumC2 {
+    float2 hi, lo;
+    XTG_DI void from(const AccSumC& a) {
+        hi = make_float2(a.hi, 0.f);
+        lo = make_float2(a.lo, 0.f);
+    }
+    XTG_DI void to(AccSumC& a) const {
+        a.hi = hi.x;
+        a.lo = lo.x;
+        AccSumC b;
+        b.hi = hi.y;
+        b.lo = lo.y;
+        a.merge(b);
+    }
+    XTG_DI void addp(float2 v) {
+        float2 s, e;
+        two_sum2(hi, v, s, e);
+        hi = s;
+        lo = p_add(lo, e);
+    }
+    XTG_DI void adds(float v) {
+        float s, e;
+        two_sum(hi.x, v, s, e);
+        hi.x = s;
+        lo.x += e;
+    }
+    template <class X> XTG_DI void add(X x, i64) { adds(cvt<float>(x)); }
+    template <class X> XTG_DI void add2(X x0, X x1, i64) { addp(make_float2(cvt<float>(x0), cvt<float>(x1))); }
+};
+template <int MODE> struct AccMom2 {
+    float k;
+    AccSumC2 s1, s2;
+    XTG_DI void from(const AccMom<float, MODE>& a) {
+        k = a.k;
+        s1.from(a.s1);
+        s2.from(a.s2);
+    }
+    XTG_DI void to(AccMom<float, MODE>& a) const {
+        a.k = k;
+        s1.to(a.s1);
+        s2.to(a.s2);
+    }
+    template <class X> XTG_DI void add(X x, i64) {
+        const float d = cvt<float>(x) - k;
+        s1.adds(d);
+        if (MODE != 0) {
+            const float q = d * d;
+            const float qe = fmaf(d, d, -q);
+            s2.adds(q);
+            s2.lo.x += qe;
+        }
+    }
+    template <class X> XTG_DI void add2(X x0, X x1, i64) {
+        const float2 kk = make_float2(k, k), x = make_float2(cvt<float>(x0), cvt<float>(x1));
+        const float2 d = p_sub(x, kk);
+        s1.addp(d);
+        if (MODE != 0) {
+            const float2 nd = p_sub(kk, x);    // -d, bit for bit
+            const float2 q = p_mul(d, d);
+            const float2 nqe = p_fma(nd, d, q);  // q - d * d: minus the square's rounding error (exact)
+            s2.addp(q);
+            s2.lo = p_sub(s2.lo, nqe);
+        }
+    }
+};
+template <int NK> struct AccNormC2 {
+    AccSumC2 a;
+    XTG_DI void from(const AccNormC<NK>& o) { a.from(o.a); }
+    XTG_DI void to(AccNormC<NK>& o) const { a.to(o.a); }
+    template <class X> XTG_DI void add(X x, i64) {
+        const float f = cvt<float>(x);
+        if (NK == 1) {
+            a.adds(fabsf(f));
+        } else {
+            const float q = f * f;
+            const float qe = fmaf(f, f, -q);
+            a.adds(q);
+            a.lo.x += qe;
+        }
+    }
+    template <class X> XTG_DI void add2(X x0, X x1, i64) {
+        const float2 f = make_float2(cvt<float>(x0), cvt<float>(x1));
+        if (NK == 1) {
+            a.addp(make_float2(fabsf(f.x), fabsf(f.y)));
+        } else {
+            const float2 q = p_mul(f, f);
+            const float2 nqe = p_fma(p_sub(make_float2(0.f, 0.f), f), f, q);
+            a.addp(q);
+            a.lo = p_sub(a.lo, nqe);
+        }
+    }
+};
+// The working form of a stored accumulator in the row pass.
+template <class A> struct Work { enum { packed = 0 }; typedef A T; };
+template <> struct Work<AccSumC> { enum { packed = 1 }; typedef AccSumC2 T; };
+template <int M> struct Work<AccMom<float, M>> { enum { packed = 1 }; typedef AccMom2<M> T; };
+template <int NK> struct Work<AccNormC<NK>> { enum { packed = 1 }; typedef AccNormC2<NK> T; };
+template <class A> struct HasAdd2 { enum { value = 0 }; };
+template <> struct HasAdd2<AccSumC2> { enum { value = 1 }; };
+template <int M> struct HasAdd2<AccMom2<M>> { enum { value = 1 }; };
+template <int NK> struct HasAdd2<AccNormC2<NK>> { enum { value = 1 }; };
+// One vector of tree values into an accumulator: in pairs where it takes
+// them, else element by element; p0 = the first element's position.
+template <bool PAIRS> struct AddVec {
+    template <int VEC, class Tree, class A, class RG, class C>
+    static XTG_DI void run(A& a, const RG& rg, i64 p0, const C& c) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) a.add(Tree::ev(rg, j, c), p0 + j);
+    }
+};
+template <> struct AddVec<true> {
+    template <int VEC, class Tree, class A, class RG, class C>
+    static XTG_DI void run(A& a, const RG& rg, i64 p0, const C& c) {
+        if (VEC % 2 == 0) {
+#pragma unroll
+            for (int j = 0; j < VEC; j += 2) a.add2(Tree::ev(rg, j, c), Tree::ev(rg, j + 1, c), p0 + j);
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) a.add(Tree::ev(rg, j, c), p0 + j);
+        }
+    }
 };
 
 // Arg-reductions (include/xtensor/misc/xsort.hpp:1158-1296): strict compare,
@@ -1183,7 +1329,15 @@ template <class... S, int VEC> struct Ring<LeafSet<S...>, VEC> {
 // K3/K5: ROW strategy — the reduced run is contiguous (or broadcast) for the
 // leaves; a group (warp or CTA) owns one (output, split) work item and strides
 // over its vectors.  Work items: w = o * nsplit + s.
-template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int GROUP, bool BIG, int UR = 4>
+// The values of an evaluated vector as a tree (fused assign + reduce: the
+// accumulator takes the values exactly as they were stored).
+struct ArrVal {
+    template <class RG, class C> static XTG_DI auto ev(const RG& r, int j, const C&) { return r[j]; }
+};
+// ES: 0 reduce only; 1 also store each evaluated vector, contiguous and
+// aligned, into p.eout (type ET); 2 the same with element-wise strided stores.
+template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int GROUP, bool BIG, int UR = 4,
+          int ES = 0, class ET = float>
 __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
     typedef typename LS::template R<VEC>::type RG;
     __shared__ Acc smem[32];
@@ -1245,8 +1399,24 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
             _Pragma("unroll") for (int u = 0; u < U; ++u) {                            \
                 const i64 r = r0 + (i64)u * gsz;                                       \
                 if (r < re) {                                                          \
-                    _Pragma("unroll") for (int j = 0; j < VEC; ++j)                    \
-                        A.add(Tree::ev(rg[u], j, c), r * VEC + j);                     \
+                    if constexpr (ES != 0) {                                           \
+                        ET ev[VEC];                                                    \
+                        _Pragma("unroll") for (int j = 0; j < VEC; ++j)                \
+                            ev[j] = cvt<ET>(Tree::ev(rg[u], j, c));                    \
+                        i64 ri[RR];                                                    \
+                        decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);                  \
+                        ri[RR - 1] *= VEC;                                             \
+                        i64 eo = 0;                                                    \
+                        _Pragma("unroll") for (int d = 0; d < RO; ++d) eo += ko[d] * p.eks[d]; \
+                        _Pragma("unroll") for (int d = 0; d < RR; ++d) eo += ri[d] * p.ers[d]; \
+                        st_out<ET, ES == 1 ? K_CONTIG : 2, VEC>(reinterpret_cast<ET*>(p.eout), eo, \
+                                                                 p.ers[RR - 1], ev);   \
+                        AddVec<HasAdd2<decltype(A)>::value != 0>::template run<VEC, ArrVal>( \
+                            A, ev, r * VEC, c);                                        \
+                    } else {                                                           \
+                        AddVec<HasAdd2<decltype(A)>::value != 0>::template run<VEC, Tree>( \
+                            A, rg[u], r * VEC, c);                                     \
+                    }                                                                  \
                 }                                                                      \
             }                                                                          \
         };                                                                             \
@@ -1260,7 +1430,7 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
             consume(rgb, r0 + step);                                                   \
         }                                                                              \
     }
-        if constexpr (FastSel<Acc>::value) {
+        if constexpr (FastSel<Acc>::value && ES == 0) {
             // amax / amin: a position-free pass; the exact pass with
             // positions only when some thread of the group met a NaN, a zero
             // or (float64) another special value
@@ -1272,6 +1442,12 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
             else ex = __syncthreads_or(ex) != 0;
             if (ex) XTG_ROW_PASS(acc)
             else fa.to(acc);
+        } else if constexpr (Work<Acc>::packed != 0) {
+            // double-float states: two lanes advanced by packed instructions
+            typename Work<Acc>::T wa;
+            wa.from(acc);
+            XTG_ROW_PASS(wa)
+            wa.to(acc);
         } else {
             XTG_ROW_PASS(acc)
         }

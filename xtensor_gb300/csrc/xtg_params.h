@@ -79,6 +79,12 @@ struct RedParams {
     double initial_f;
     i64 initial_i;
     double divisor;  // mean / variance divisor (already integer-divided like the reference)
+    // fused assign + reduce (row kernel with ES != 0): every evaluated
+    // element, converted to the destination type, is also stored at
+    // eout + sum(kept index * eks) + sum(reduced index * ers)
+    void* eout;
+    i64 eks[XTG_KMAX_RANK];
+    i64 ers[XTG_KMAX_RANK];
 };
 
 struct RowParams {

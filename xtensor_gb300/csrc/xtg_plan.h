@@ -81,6 +81,11 @@ xtg_status accumulate_call(const xtg_expr* e, int32_t op, int32_t has_axis, int6
 // assign_tree, through a temporary when a leaf shares memory with `out` but
 // is read at other positions than the ones written.
 xtg_status assign_guarded(const Tree& t, const xtg_array* out, cudaStream_t stream);
+// True when a leaf shares memory with `out` but is read at other positions
+// than the ones written.
+bool assign_hazard(const Tree& t, const xtg_array& out);
+// True when any leaf's byte range overlaps `out`'s.
+bool shares_memory(const Tree& t, const xtg_array& out);
 
 // Accumulator type string, post-operation and initial values of a reduction.
 struct AccChoice {
@@ -98,16 +103,16 @@ xtg_status choose_acc(const Tree& t, const xtg_reduce_desc* rd, AccChoice& ch);
 // ---- plan cache (xtg_plancache.cpp) -----------------------------------------------
 bool plan_cache_enabled();
 std::vector<unsigned char> plan_key(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out,
-                                    int32_t a0, int32_t a1, int64_t a2);
+                                    int32_t a0, int32_t a1, int64_t a2, const xtg_array* out2 = nullptr);
 bool plan_replay(const std::vector<unsigned char>& key, cudaStream_t s, xtg_status* st);
 void plan_store(std::vector<unsigned char>&& key, Recorder& rec);
 
 // Runs `fn` (a planning + launching call) through the plan cache.
 template <class F>
 xtg_status with_plan_cache(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, int32_t a0,
-                           int32_t a1, int64_t a2, cudaStream_t s, F&& fn) {
+                           int32_t a1, int64_t a2, cudaStream_t s, F&& fn, const xtg_array* out2 = nullptr) {
     if (!e || !out || !plan_cache_enabled() || recorder()) return fn();
-    std::vector<unsigned char> key = plan_key(kind, e, rd, out, a0, a1, a2);
+    std::vector<unsigned char> key = plan_key(kind, e, rd, out, a0, a1, a2, out2);
     xtg_status st;
     if (plan_replay(key, s, &st)) return st;
     Recorder rec;

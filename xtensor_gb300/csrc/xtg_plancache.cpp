@@ -67,7 +67,7 @@ void put_array(std::vector<unsigned char>& k, const xtg_array& a) {
 bool plan_cache_enabled() { return !dry_run() && opt("plan.cache", 1) != 0; }
 
 std::vector<unsigned char> plan_key(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out,
-                                    int32_t a0, int32_t a1, int64_t a2) {
+                                    int32_t a0, int32_t a1, int64_t a2, const xtg_array* out2) {
     std::vector<unsigned char> k;
     k.reserve(512);
     put(k, kind);
@@ -91,6 +91,7 @@ std::vector<unsigned char> plan_key(int kind, const xtg_expr* e, const xtg_reduc
     put(k, a1);
     put(k, a2);
     put_array(k, *out);
+    if (out2) put_array(k, *out2);
     return k;
 }
 

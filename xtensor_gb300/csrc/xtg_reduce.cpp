@@ -170,29 +170,38 @@ static int kind_of(int64_t s) { return s == 1 ? 0 : (s == 0 ? 1 : 2); }
 // Core launcher shared by xtg_reduce and xtg_argreduce.
 //   accname  — accumulator type string; post — POST code; out_dt — output type
 //   kept/red — dims of the expression shape; out strides per kept dim.
+// `eout` (fused assign + reduce): the evaluated elements are also stored
+// there, converted to its type (shape = the tree's shape); only the row
+// strategy does that — any other plan returns XTG_ERR_UNSUPPORTED before a
+// launch, and the caller evaluates in two calls instead.
+static const char* kNotFusable = "fused assign + reduce: not a row reduction plan";
 static xtg_status run_reduction(const Tree& t, const std::string& accname, int post, int out_dt, const int* kept,
                                 int nk, const int* red, int nr, const xtg_array& out, const int64_t* ostr_kept,
-                                xtg::RedParams& p, cudaStream_t stream, const ScratchSpec* scratch) {
+                                xtg::RedParams& p, cudaStream_t stream, const ScratchSpec* scratch,
+                                const xtg_array* eout = nullptr, bool* not_fusable = nullptr) {
     const int NL = (int)t.leaves.size();
     std::vector<std::array<int64_t, XTG_MAX_RANK>> full(NL);
     for (int l = 0; l < NL; ++l) leaf_bstrides(t, l, full[l].data());
-    // kept group (out strides first)
+    // kept group (out strides first; the fused destination's last)
     Dims K;
     K.R = nk;
-    K.st.resize(1 + NL);
+    K.st.resize(1 + NL + (eout ? 1 : 0));
     for (int i = 0; i < nk; ++i) {
         K.shape[i] = t.shape[kept[i]];
         K.st[0][i] = ostr_kept[i];
         for (int l = 0; l < NL; ++l) K.st[1 + l][i] = full[l][kept[i]];
+        if (eout) K.st[1 + NL][i] = eout->strides[kept[i]];
     }
     collapse(K);
     Dims Rd;
     Rd.R = nr;
-    Rd.st.resize(NL > 0 ? NL : 1);
+    Rd.st.resize((NL > 0 ? NL : 1) + (eout ? 1 : 0));
+    const int erow = NL > 0 ? NL : 1;  // the fused destination's row in Rd.st
     for (int i = 0; i < nr; ++i) {
         Rd.shape[i] = t.shape[red[i]];
         for (int l = 0; l < NL; ++l) Rd.st[l][i] = full[l][red[i]];
         if (NL == 0) Rd.st[0][i] = 0;
+        if (eout) Rd.st[erow][i] = eout->strides[red[i]];
     }
     collapse(Rd);
     const int RO = K.R, RR = Rd.R;
@@ -217,6 +226,10 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
     if (n_out > 1 && kept_in_stride == 1 && red_in_stride != 1) row = false;
     if (n_out >= 1024 && red_in_stride == 1 && Rd.shape[RR - 1] < 32 && kept_in_stride != 1 && RR == 1) row = false;
     if (opt("reduce.force_row", 0)) row = true;
+    if (eout && !row) {
+        if (not_fusable) *not_fusable = true;
+        return fail(XTG_ERR_UNSUPPORTED, kNotFusable);
+    }
 
     int maxsz = 1;
     std::vector<int> kinds(NL);
@@ -240,6 +253,26 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
     };
     while (vec > 1 && !vec_ok(vec)) vec >>= 1;
     if (n_red == 0) vec = 1;
+    // fused destination: one vector store per evaluated vector when it is
+    // contiguous along the reduced run and aligned like the loads, else
+    // element stores
+    int es = 0;
+    if (eout) {
+        es = 1;
+        const int64_t esz = dt(eout->dtype).size;
+        if (vec > 1) {
+            if (Rd.st[erow][RR - 1] != 1 || !aligned(eout->data, (int64_t)vec * esz)) es = 2;
+            for (int d = 0; d < RO; ++d)
+                if (K.st[1 + NL][d] % vec) es = 2;
+            for (int d = 0; d + 1 < RR; ++d)
+                if (Rd.st[erow][d] % vec) es = 2;
+        } else if (Rd.st[erow][RR - 1] != 1) {
+            es = 2;
+        }
+        p.eout = eout->data;
+        for (int d = 0; d < RO; ++d) p.eks[d] = K.st[1 + NL][d];
+        for (int d = 0; d < RR; ++d) p.ers[d] = Rd.st[erow][d];
+    }
 
     p.n_out = n_out;
     p.n_red = n_red;
@@ -314,7 +347,8 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         std::string name = "xtg::k_reduce_row<" + tree + ", " + ls + ", " + accname + ", " + outc + ", " +
                            std::to_string(post) + ", " + std::to_string(vec) + ", " + std::to_string(RO) + ", " +
                            std::to_string(RR) + ", " + std::to_string(group) + ", " + (big ? "true" : "false") + ", " +
-                           std::to_string(opt("reduce.row_unroll", 4)) + ">";
+                           std::to_string(opt("reduce.row_unroll", 4)) +
+                           (es ? ", " + std::to_string(es) + ", " + dt(eout->dtype).cname : std::string()) + ">";
         st = get_kernel(name, 256, &k);
         if (st == XTG_OK) {
             int64_t items = n_out * nsplit;
@@ -523,11 +557,97 @@ xtg_status argreduce_impl(const xtg_expr* e, int32_t op, int32_t has_axis, int64
     return run_reduction(t, acc, 0, out->dtype, kept, nk, red, nr, *out, ostr, p, stream, nullptr);
 }
 
+// Fused assign + reduce: out_e = e (xtg_assign semantics), then
+// out_r = reduce(out_e) (xtg_reduce on out_e) — one pass of the row kernel
+// that stores every evaluated element and folds it, when the reduction plan
+// is a row plan, the tree has no row statistics and out_e shares no memory
+// with the leaves; otherwise the two calls, in order.
+static xtg_status assign_reduce_impl(const xtg_expr* e, const xtg_array* oute, const xtg_reduce_desc* rd,
+                                     const xtg_array* outr, cudaStream_t stream) {
+    if (rd->op < XTG_RED_SUM || rd->op > XTG_RED_NORM_LINF) return fail(XTG_ERR_INVALID, "unknown reduction op");
+    if (!valid_dtype(oute->dtype) || oute->rank < 0 || oute->rank > XTG_MAX_RANK)
+        return fail(XTG_ERR_INVALID, "bad destination descriptor");
+    Tree t;
+    const bool demote = opt("fp32_compute", 1) != 0 && oute->dtype != XTG_FLOAT64;
+    XTG_TRY(build_tree(e, demote, t));
+    // the reduction's operand is the assigned destination itself
+    xtg_expr le;
+    memset(&le, 0, sizeof le);
+    le.n_nodes = 1;
+    le.nodes[0].op = XTG_OP_LEAF;
+    le.nodes[0].dtype = oute->dtype;
+    le.n_leaves = 1;
+    le.leaves[0] = *oute;
+    // (any overlap with a leaf is excluded, in-place updates too: every split
+    // of an output may read the output's first element, which another split
+    // could already have overwritten)
+    bool fusable = !t.n_rstats && oute->data && oute->rank == t.rank && !shares_memory(t, *oute);
+    for (int d = 0; fusable && d < t.rank; ++d)
+        if (oute->shape[d] != t.shape[d] || (oute->shape[d] > 1 && oute->strides[d] == 0)) fusable = false;
+    if (fusable) {
+        Tree te;
+        XTG_TRY(build_tree(&le, false, te));
+        RedShape S;
+        XTG_TRY(red_shape(te, rd, rd->keep_dims != 0, S));
+        const int rt = result_type(rd, te.nodes[te.root].cxx_dtype);
+        if (outr->dtype != rt)
+            return fail(XTG_ERR_INVALID, "destination dtype " + std::to_string(outr->dtype) +
+                                             " differs from the result type " + std::to_string(rt));
+        if (!out_matches(*outr, S.out_rank, S.out_shape)) return fail(XTG_ERR_SHAPE, "destination shape mismatch");
+        if (!outr->data) return fail(XTG_ERR_INVALID, "null destination data");
+        XTG_TRY(ensure_device(nullptr));
+        xtg::RedParams p;
+        memset(&p, 0, sizeof p);
+        AccChoice ch;
+        XTG_TRY(choose_acc(te, rd, ch));
+        p.init_f = ch.init_f;
+        p.init_i = ch.init_i;
+        p.has_initial = ch.has_initial;
+        p.initial_f = ch.initial_f;
+        p.initial_i = ch.initial_i;
+        int64_t size = 1, n_out = 1;
+        for (int d = 0; d < te.rank; ++d) size *= te.shape[d];
+        for (int d = 0; d < te.rank; ++d)
+            if (!S.is_red[d]) n_out *= te.shape[d];
+        const int64_t ddof = (rd->op == XTG_RED_VARIANCE || rd->op == XTG_RED_STDDEV) ? rd->ddof : 0;
+        p.divisor = n_out ? (double)((size - ddof) / n_out) : 0.0;
+        int kept[XTG_MAX_RANK], red[XTG_MAX_RANK], nk = 0, nr = 0;
+        int64_t ostr[XTG_MAX_RANK];
+        int oi = 0;
+        for (int d = 0; d < te.rank; ++d) {
+            if (S.is_red[d]) {
+                red[nr++] = d;
+                if (rd->keep_dims) ++oi;
+            } else {
+                kept[nk] = d;
+                ostr[nk] = outr->strides[oi++];
+                ++nk;
+            }
+        }
+        bool not_fusable = false;
+        const xtg_status st =
+            run_reduction(t, ch.acc, ch.post, rt, kept, nk, red, nr, *outr, ostr, p, stream, nullptr, oute, &not_fusable);
+        if (!not_fusable) return st;
+        clear_error();
+    }
+    XTG_TRY(assign_guarded(t, oute, stream));
+    return reduce_impl(&le, rd, outr, stream, nullptr);
+}
+
 }  // namespace xtgh
 
 using namespace xtgh;
 
 extern "C" {
+
+xtg_status xtg_assign_reduce(const xtg_expr* e, const xtg_array* out_e, const xtg_reduce_desc* rd,
+                             const xtg_array* out_r, xtg_stream stream) {
+    begin_call();
+    if (!e || !rd || !out_e || !out_r) return fail(XTG_ERR_INVALID, "null argument");
+    return with_plan_cache(
+        4, e, rd, out_r, 0, 0, 0, (cudaStream_t)stream,
+        [&]() { return assign_reduce_impl(e, out_e, rd, out_r, (cudaStream_t)stream); }, out_e);
+}
 
 xtg_status xtg_reduce_shape(const xtg_expr* e, const xtg_reduce_desc* rd, int32_t* rank, int64_t* shape,
                             int32_t* out_dtype) {

@@ -91,6 +91,25 @@ def reduce(op: str, e, axes=None, keep_dims=False, initial=None, acc_dtype=None,
     return out
 
 
+def assign_reduce(out_e: DeviceArray, e, op: str, axes=None, keep_dims=False, initial=None, acc_dtype=None, ddof=0,
+                  precision=0, out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
+    """out_e = e, then the reduction `op` of out_e (xtg_assign_reduce: one
+    pass when the plan allows); returns the reduction's result."""
+    kw = dict(axes=axes, keep_dims=keep_dims, initial=None, acc_dtype=acc_dtype, ddof=ddof, precision=precision)
+    shape, dt = reduce_shape(op, out_e, **kw)
+    if initial is not None:
+        from ._ffi import DTYPES
+        initial = float(initial) if dt in (DTYPES["float32"], DTYPES["float64"], DTYPES["bfloat16"]) else int(initial)
+    kw["initial"] = initial
+    if out is None:
+        out = DeviceArray.empty(shape, dt, stream)
+    ex, keep = lower(as_expr(e))
+    rd = make_desc(op, **kw)
+    oe, o = out_e.xtg_array(), out.xtg_array()
+    check(lib().xtg_assign_reduce(C.byref(ex), C.byref(oe), C.byref(rd), C.byref(o), _sh(stream)))
+    return out
+
+
 def argreduce(op: str, e, axis=None, out_dtype="int64", out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
     from .ops import broadcast_shape as _bs
     e = as_expr(e)
