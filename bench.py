@@ -75,6 +75,16 @@ def op_bytes(s: int) -> dict:
     }
 
 
+# The step's order: the four writers, then the readers, float64 amax first.
+# A kernel that follows a writer pays the write-back of the writer's last
+# dirty L2 lines (~100 MB, ~17 us on this part: a 512 MiB read takes 96 us
+# after a 512 MiB copy and 79 us after a read); the order puts that cost on
+# the largest read (amax float64, 1 GiB) instead of a 512 MiB one.  The
+# operations are independent, so the order changes no result.
+STEP_ORDER = (("transpose", 0), ("normalize", 0), ("transpose", 1), ("normalize", 1),
+              ("amax", 1), ("argmax", 1), ("amax", 0), ("argmax", 0))
+
+
 def step_bytes() -> int:
     return sum(op_bytes(4).values()) + sum(op_bytes(8).values())
 
@@ -199,10 +209,10 @@ class GpuStep:
 
         self.xg, self.lib = xg, xg.lib()
         self.stream = stream
-        self.calls = []  # (op name, dtype size, fn)
+        by_op = {}
         self.keep = []
         self.dev_in, self.dev_out = [], []
-        for x in (x32, x64):
+        for a, x in enumerate((x32, x64)):
             s = x.dtype.itemsize
             dx = DeviceArray.from_numpy(x)
             t = DeviceArray.empty((SHAPE[2], SHAPE[0], SHAPE[1]), x.dtype)
@@ -221,21 +231,42 @@ class GpuStep:
             o_ai = ai.xtg_array()
             self.keep += [e_t, k1, o_t, e_y, k2, o_y, e_x, k3, rd, o_am, o_ai]
             L, st = self.lib, stream
-            self.calls += [
-                ("transpose", s, lambda e=e_t, o=o_t: L.xtg_assign(C.byref(e), C.byref(o), st)),
-                ("normalize", s, lambda e=e_y, o=o_y: L.xtg_assign(C.byref(e), C.byref(o), st)),
-                ("amax", s, lambda e=e_x, r=rd, o=o_am: L.xtg_reduce(C.byref(e), C.byref(r), C.byref(o), st)),
-                ("argmax", s, lambda e=e_x, o=o_ai: L.xtg_argreduce(C.byref(e), 0, 1, 1, C.byref(o), st)),
-            ]
+            by_op[("transpose", a)] = (s, lambda e=e_t, o=o_t: L.xtg_assign(C.byref(e), C.byref(o), st), 0)
+            by_op[("normalize", a)] = (s, lambda e=e_y, o=o_y: L.xtg_assign(C.byref(e), C.byref(o), st), 1)
+            by_op[("amax", a)] = (s, lambda e=e_x, r=rd, o=o_am: L.xtg_reduce(C.byref(e), C.byref(r), C.byref(o), st), 2)
+            by_op[("argmax", a)] = (s, lambda e=e_x, o=o_ai: L.xtg_argreduce(C.byref(e), 0, 1, 1, C.byref(o), st), 3)
+        # (op name, element size, fn, input index, output index) in step order
+        self.calls = [(nm, *by_op[(nm, a)][:2], a, by_op[(nm, a)][2]) for nm, a in STEP_ORDER]
 
     def run(self, events=None):
         from xtensor_gb300._ffi import check
-        for i, (_, _, fn) in enumerate(self.calls):
+        for i, (_, _, fn, _, _) in enumerate(self.calls):
             if events is not None:
                 check(self.lib.xtg_event_record(events[i], self.stream))
             check(fn())
         if events is not None:
             check(self.lib.xtg_event_record(events[len(self.calls)], self.stream))
+
+
+def writeback_probe(step, lib, stream, reps) -> dict:
+    """amax float32 timed (CUDA events) right after the float32 normalisation
+    and right after the float32 argmax: the difference is the write-back of
+    the writer's dirty L2 lines, which lands on whichever kernel follows it."""
+    from xtensor_gb300._ffi import check
+    fn = {(nm, a): f for nm, _, f, a, _ in step.calls}
+    res = {}
+    for label, prev in (("after_normalize_f32", fn[("normalize", 0)]), ("after_argmax_f32", fn[("argmax", 0)])):
+        evs = [ev_create(lib, 2) for _ in range(reps)]
+        for k in range(reps):
+            check(prev())
+            check(lib.xtg_event_record(evs[k][0], stream))
+            check(fn[("amax", 0)]())
+            check(lib.xtg_event_record(evs[k][1], stream))
+        check(lib.xtg_stream_sync(stream))
+        res[f"amax_f32_ms_{label}"] = round(sum(ev_ms(lib, a, b) for a, b in evs) / reps, 4)
+    res["note"] = ("a kernel that follows a writer pays the write-back of the writer's last dirty L2 lines; "
+                   "the step orders writers first and the float64 amax right after them")
+    return res
 
 
 def ev_create(lib, n):
@@ -372,10 +403,10 @@ def run_gpu(args):
     value = total / (ms / 1e3) / 1e9
 
     # dominant kernel
-    names = [f"{nm}_{'f32' if s == 4 else 'f64'}" for nm, s, _ in step.calls]
+    names = [f"{nm}_{'f32' if s == 4 else 'f64'}" for nm, s, *_ in step.calls]
     avg = [t / args.steps for t in per_op]
     dom = int(np.argmax(avg))
-    nm, s, _ = step.calls[dom]
+    nm, s, *_ = step.calls[dom]
     dom_bytes = op_bytes(s)[nm]
     achieved = dom_bytes / (avg[dom] / 1e3) / 1e9
     peak, peak_kind = peaks()
@@ -391,6 +422,10 @@ def run_gpu(args):
                              "frac_nominal": round(op_bytes(step.calls[i][1])[step.calls[i][0]] / (avg[i] / 1e3) / 1e9
                                                    / NOMINAL_HBM_GBS, 3)}
                   for i in range(nops)}
+
+    # ---- write-back attribution: amax float32 right after the float32
+    # normalisation (a writer) and right after the float32 argmax (a reader)
+    wb = writeback_probe(step, lib, stream, max(5, min(args.steps, 20)))
 
     # ---- end to end through the C ABI with pinned host buffers
     e2e = None
@@ -438,6 +473,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "parity": parity,
+            "l2_writeback": wb,
             "gpu_launches": int(l1 - l0),
             "clocks": clk,
             **subs,
@@ -475,9 +511,12 @@ def run_e2e(lib, step, x32, x64, stream, steps, D):
     h2d = sum(n for _, n in hin)
     d2h = sum(n for _, n in hout)
     nops = len(step.calls)
-    per = len(step.calls) // 2  # calls per input array
     ev = [{"in": ev_create(lib, 2), "out": ev_create(lib, nops), "comp": ev_create(lib, 1)[0],
            "d2h": ev_create(lib, 1)[0]} for _ in sets]
+    # here the calls run grouped by input (float32 first), so the kernels of
+    # the first input overlap the copy of the second
+    order = sorted(range(nops), key=lambda i: (step.calls[i][3], i))
+    per = len(step.dev_out[0])
 
     def one(k):
         b = k % 2
@@ -488,16 +527,20 @@ def run_e2e(lib, step, x32, x64, stream, steps, D):
         for a, (h, n) in enumerate(hin):
             check(lib.xtg_memcpy(S.dev_in[a].ptr, h, n, H2D, s_in))
             check(lib.xtg_event_record(E["in"][a], s_in))
-        for i, (_, _, fn) in enumerate(S.calls):
-            if i % per == 0:
-                check(lib.xtg_stream_wait_event(stream, E["in"][i // per]))
+        waited = set()
+        for i in order:
+            _, _, fn, a, oi = S.calls[i]
+            if a not in waited:
+                check(lib.xtg_stream_wait_event(stream, E["in"][a]))
+                waited.add(a)
             check(fn())
             check(lib.xtg_event_record(E["out"][i], stream))
         check(lib.xtg_event_record(E["comp"], stream))
-        for i in range(nops):
+        for i in order:
+            _, _, _, a, oi = S.calls[i]
             check(lib.xtg_stream_wait_event(s_out, E["out"][i]))
-            o = S.dev_out[i // per][i % per]
-            check(lib.xtg_memcpy(hout[i][0], o.ptr, o.nbytes, D2H, s_out))
+            o = S.dev_out[a][oi]
+            check(lib.xtg_memcpy(hout[a * per + oi][0], o.ptr, o.nbytes, D2H, s_out))
         check(lib.xtg_event_record(E["d2h"], s_out))
 
     for k in range(2):
@@ -1418,6 +1461,8 @@ def c4_section(args):
         kind, op, e, axes, shape, keep, elems = pool[i]
         return sum(a.nbytes for a in keep) + outs[i].nbytes
 
+    dispatch_threads = args.dispatch_threads
+    xg.set_option("server.dispatch_threads", dispatch_threads)
     srv = Server(streams=8, max_inflight=128, batch_min_group=3)
     reqs = [srv.request(kind, e, outs[i], op=op, axes=axes, arg_axis=axes)[0] for i, (kind, op, e, axes, *_r) in
             enumerate(pool)]
@@ -1487,7 +1532,9 @@ def c4_section(args):
                 "served": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
                            "req_s": round(n / served_wall, 1), "GB/s": round(total_bytes / served_wall / 1e9, 1),
                            "batched_requests": st["batched_requests"], "batch_launches": st["batch_launches"],
-                           "waves": st["waves"]},
+                           "waves": st["waves"],
+                           # host time the dispatch threads spent launching, per second of the run and thread
+                           "dispatch_busy": round(st["dispatch_ms"] / (served_wall * 1e3 * dispatch_threads), 3)},
             })
         med = lambda arm, k: float(np.median([r[arm][k] for r in runs]))  # noqa: E731
         results.append({
@@ -1503,6 +1550,7 @@ def c4_section(args):
         "workload": C4_WORKLOAD, "templates": len(pool), "pool_bytes": int(sum(req_bytes(i) for i in range(len(pool)))),
         "value": best["median"]["served"]["req_s"], "unit": "req/s", "setup_s": round(t_setup, 1),
         "served_ge_plain_every_run": all(r["served_over_plain_req_s_min"] >= 1.0 for r in results),
+        "dispatch_threads": dispatch_threads,
         "sweep": results, "gpu_launches": int(l1 - l0),
         "e2e": None, "e2e_note": "operands are device-resident by definition of the serving workload",
     }
@@ -1826,6 +1874,7 @@ def main():
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rates", default="2000,16000,48000,96000")
     ap.add_argument("--repeats", type=int, default=3, help="c4: runs per offered rate")
+    ap.add_argument("--dispatch-threads", type=int, default=4, help="c4: the server's dispatch threads")
     ap.add_argument("--sub", default="c0,c2,c3,c4",
                     help="sub-results added to the default line (comma list of c0,c2,c3,c4; 'none' for none)")
     args = ap.parse_args()

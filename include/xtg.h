@@ -26,6 +26,9 @@
  *                      include/xtensor/reducers/xnorm.hpp:397-526
  *   xtg_argreduce   <- xt::argmax / xt::argmin (arg_func_impl)
  *                      include/xtensor/misc/xsort.hpp:1158-1296
+ *   xtg_assign_reduce
+ *                   <- the pair `E = e; r = reduce(E, axes)` (assign_xexpression
+ *                      then reduce), one pass where the plan allows
  *   xtg_accumulate  <- xt::cumsum / cumprod / nancumsum / nancumprod
  *                      (xt::accumulate, accumulator_impl)
  *                      include/xtensor/reducers/xaccumulator.hpp:154-367
@@ -479,6 +482,7 @@ typedef struct {
     int64_t waves, batched_requests, batch_launches;
     int64_t hbm_budget, hbm_reserved;
     double p50_ms, p99_ms, mean_ms;   /* over completed requests since the last reset */
+    double dispatch_ms;               /* host time the dispatch threads spent launching work since the last reset */
 } xtg_server_stats;
 xtg_status xtg_server_create(const xtg_server_config* cfg, xtg_server** s);
 xtg_status xtg_server_submit(xtg_server* s, const xtg_request* r, uint64_t* id);

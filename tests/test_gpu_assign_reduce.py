@@ -52,7 +52,7 @@ def test_c0_one_launch_equals_two_calls():
     assert E1.tobytes() == E2.tobytes()
     assert r1.tobytes() == r2.tobytes()
     names = [k for k in kernels.split(";") if k]
-    assert len(names) == 1 and names[0].startswith("xtg::k_reduce_row<") and names[0].endswith(", 1, float>"), names
+    assert len(names) == 1 and names[0].startswith("k_reduce_row<") and names[0].endswith(", 1, float>"), names
 
 
 @pytest.mark.parametrize("op,kw", [("sum", {}), ("mean", {}), ("prod", {}), ("amax", {}), ("amin", {}),

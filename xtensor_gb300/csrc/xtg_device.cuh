@@ -1336,8 +1336,10 @@ struct ArrVal {
 };
 // ES: 0 reduce only; 1 also store each evaluated vector, contiguous and
 // aligned, into p.eout (type ET); 2 the same with element-wise strided stores.
+// PK: 1 = the packed working accumulator (Work<Acc>) for double-float
+// states, 0 = the stored state's own add.
 template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int GROUP, bool BIG, int UR = 4,
-          int ES = 0, class ET = float>
+          int ES = 0, class ET = float, int PK = 1>
 __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
     typedef typename LS::template R<VEC>::type RG;
     __shared__ Acc smem[32];
@@ -1442,7 +1444,7 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
             else ex = __syncthreads_or(ex) != 0;
             if (ex) XTG_ROW_PASS(acc)
             else fa.to(acc);
-        } else if constexpr (Work<Acc>::packed != 0) {
+        } else if constexpr (Work<Acc>::packed != 0 && PK != 0) {
             // double-float states: two lanes advanced by packed instructions
             typename Work<Acc>::T wa;
             wa.from(acc);

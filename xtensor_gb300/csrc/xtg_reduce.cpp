@@ -237,6 +237,9 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         kinds[l] = kind_of(row ? Rd.st[l][RR - 1] : K.st[1 + l][RO - 1]);
         if (kinds[l] == 0) maxsz = std::max(maxsz, dt(t.leaves[l].dtype).size);
     }
+    // the fused destination's vectors are as wide as its own reduction's would
+    // be, so that the fold matches a later reduction of it
+    if (eout) maxsz = std::max(maxsz, dt(eout->dtype).size);
     int vec = 16 / maxsz;
     auto vec_ok = [&](int v) {
         if (v == 1) return true;
@@ -348,7 +351,9 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
                            std::to_string(post) + ", " + std::to_string(vec) + ", " + std::to_string(RO) + ", " +
                            std::to_string(RR) + ", " + std::to_string(group) + ", " + (big ? "true" : "false") + ", " +
                            std::to_string(opt("reduce.row_unroll", 4)) +
-                           (es ? ", " + std::to_string(es) + ", " + dt(eout->dtype).cname : std::string()) + ">";
+                           (es ? ", " + std::to_string(es) + ", " + dt(eout->dtype).cname : std::string()) +
+                           (opt("reduce.packed", 1) ? std::string() :
+                            std::string(es ? "" : ", 0, float") + ", 0") + ">";
         st = get_kernel(name, 256, &k);
         if (st == XTG_OK) {
             int64_t items = n_out * nsplit;

@@ -13,8 +13,12 @@
 //   dispatch — admitted small requests (at most batch_max_elems elements,
 //     2-D, elementwise or last-axis reductions) with the same tree shape and
 //     immediates form a group launched as ONE batched kernel; everything else
-//     goes out individually.  Units are spread round-robin over the stream
-//     pool so their work overlaps on the device.
+//     goes out individually.  The scheduler hands each wave's groups and
+//     requests round-robin to dispatch threads (option
+//     "server.dispatch_threads", default 4), each owning a share of the
+//     stream pool, so the host cost of launching (planning or plan-cache
+//     replay, kernel launches) is paid on several cores and the work
+//     overlaps on the device.
 //   completion — cudaLaunchHostFunc after each unit marks its requests done
 //     with a host timestamp and releases their budget; the scheduler frees
 //     batch work lists once their units completed.
@@ -54,12 +58,28 @@ struct Req {
 
 struct Unit;
 
+// Work handed to one dispatch thread: whole batch groups and single requests.
+struct Work {
+    std::vector<std::vector<Req*>> groups;
+    std::vector<Req*> singles;
+};
+struct Disp {
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Work> q;
+    std::vector<cudaStream_t> streams;  // this thread's share of the pool
+    size_t next_stream = 0;
+    bool stop = false;
+};
+
 }  // namespace
 
 struct xtg_server {
     xtg_server_config cfg;
     std::vector<cudaStream_t> streams;
-    size_t next_stream = 0;
+    std::vector<std::unique_ptr<Disp>> disp;
+    size_t next_disp = 0;
     std::mutex mu;
     std::condition_variable cv_sched, cv_done;
     std::deque<Req*> pending;
@@ -171,28 +191,22 @@ int dispatch_one(Req* r, cudaStream_t st) {
     return XTG_ERR_INVALID;
 }
 
-void dispatch(xtg_server* s, std::vector<Req*>& admitted) {
-    // group batchable requests by signature
-    std::map<std::string, std::vector<Req*>> groups;
-    std::vector<Req*> singles;
-    for (Req* r : admitted) {
-        if (r->batchable) groups[r->sig].push_back(r);
-        else singles.push_back(r);
-    }
-    for (auto& kv : groups) {
-        if ((int)kv.second.size() < s->cfg.batch_min_group) {
-            singles.insert(singles.end(), kv.second.begin(), kv.second.end());
-            continue;
-        }
-        cudaStream_t st = s->streams[s->next_stream++ % s->streams.size()];
+// Launches one dispatcher's share of a wave on its streams: each group as one
+// batched kernel (or, while its batch kernel is not built yet, one request
+// at a time), singles round-robin over the streams, and one completion
+// callback per stream used.
+void dispatch(xtg_server* s, Disp* d, Work& w) {
+    std::vector<Req*> singles = std::move(w.singles);
+    for (auto& grp : w.groups) {
+        cudaStream_t st = d->streams[d->next_stream++ % d->streams.size()];
         const auto now = Clock::now();
-        Req* f = kv.second[0];
+        Req* f = grp[0];
         xtg_batch* b = nullptr;
         int rc = xtg_batch_create(&f->r.expr, f->r.kind == XTG_REQ_REDUCE ? &f->r.rd : nullptr, &b);
-        for (size_t i = 0; rc == XTG_OK && i < kv.second.size(); ++i)
-            rc = xtg_batch_add(b, kv.second[i]->r.expr.leaves, kv.second[i]->r.expr.n_leaves, &kv.second[i]->r.out);
+        for (size_t i = 0; rc == XTG_OK && i < grp.size(); ++i)
+            rc = xtg_batch_add(b, grp[i]->r.expr.leaves, grp[i]->r.expr.n_leaves, &grp[i]->r.out);
         if (rc == XTG_OK) {
-            // never compile on the scheduler: a batch kernel that is not
+            // never compile on a dispatch thread: a batch kernel that is not
             // loaded yet is built in the background while this group runs
             // one request at a time
             std::string kname;
@@ -207,28 +221,28 @@ void dispatch(xtg_server* s, std::vector<Req*>& admitted) {
         if (rc != XTG_OK) {
             if (b) xtg_batch_destroy(b);
             // fall back to individual dispatch for this group
-            singles.insert(singles.end(), kv.second.begin(), kv.second.end());
+            singles.insert(singles.end(), grp.begin(), grp.end());
             continue;
         }
-        Unit* u = new Unit{s, kv.second, b};
+        Unit* u = new Unit{s, grp, b};
         {
             std::lock_guard<std::mutex> lk(s->mu);
-            for (Req* r : kv.second) {
+            for (Req* r : grp) {
                 r->t_dispatch = now;
                 r->dispatched = true;
                 r->batched = true;
             }
             s->st.batch_launches++;
-            s->st.batched_requests += (int64_t)kv.second.size();
+            s->st.batched_requests += (int64_t)grp.size();
         }
         complete_after(st, u);
     }
     // individual requests: round-robin over the streams, one completion
-    // callback per stream for this wave
-    std::vector<Unit*> per_stream(s->streams.size(), nullptr);
+    // callback per stream for this share of the wave
+    std::vector<Unit*> per_stream(d->streams.size(), nullptr);
     for (Req* r : singles) {
-        const size_t si = s->next_stream++ % s->streams.size();
-        cudaStream_t st = s->streams[si];
+        const size_t si = d->next_stream++ % d->streams.size();
+        cudaStream_t st = d->streams[si];
         {
             std::lock_guard<std::mutex> lk(s->mu);
             r->t_dispatch = Clock::now();
@@ -243,7 +257,56 @@ void dispatch(xtg_server* s, std::vector<Req*>& admitted) {
         per_stream[si]->reqs.push_back(r);
     }
     for (size_t si = 0; si < per_stream.size(); ++si)
-        if (per_stream[si]) complete_after(s->streams[si], per_stream[si]);
+        if (per_stream[si]) complete_after(d->streams[si], per_stream[si]);
+}
+
+void dispatcher(xtg_server* s, Disp* d) {
+    ensure_device(nullptr);
+    for (;;) {
+        std::deque<Work> mine;
+        {
+            std::unique_lock<std::mutex> lk(d->mu);
+            d->cv.wait(lk, [&] { return d->stop || !d->q.empty(); });
+            if (d->q.empty() && d->stop) break;
+            mine.swap(d->q);
+        }
+        const auto t0 = Clock::now();
+        for (Work& w : mine) dispatch(s, d, w);
+        const double ms = std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->st.dispatch_ms += ms;
+    }
+}
+
+// Splits an admitted wave: batchable requests grouped by signature (groups
+// below batch_min_group go out singly), then whole groups and singles
+// round-robin over the dispatch threads.
+void hand_out(xtg_server* s, std::vector<Req*>& admitted) {
+    std::map<std::string, std::vector<Req*>> groups;
+    std::vector<Req*> singles;
+    for (Req* r : admitted) {
+        if (r->batchable) groups[r->sig].push_back(r);
+        else singles.push_back(r);
+    }
+    const size_t K = s->disp.size();
+    std::vector<Work> work(K);
+    for (auto& kv : groups) {
+        if ((int)kv.second.size() < s->cfg.batch_min_group) {
+            singles.insert(singles.end(), kv.second.begin(), kv.second.end());
+            continue;
+        }
+        work[s->next_disp++ % K].groups.push_back(std::move(kv.second));
+    }
+    for (Req* r : singles) work[s->next_disp++ % K].singles.push_back(r);
+    for (size_t i = 0; i < K; ++i) {
+        if (work[i].groups.empty() && work[i].singles.empty()) continue;
+        Disp* d = s->disp[i].get();
+        {
+            std::lock_guard<std::mutex> lk(d->mu);
+            d->q.push_back(std::move(work[i]));
+        }
+        d->cv.notify_one();
+    }
 }
 
 void scheduler(xtg_server* s) {
@@ -287,7 +350,7 @@ void scheduler(xtg_server* s) {
             if (u->batch) xtg_batch_destroy(u->batch);
             delete u;
         }
-        if (!admitted.empty()) dispatch(s, admitted);
+        if (!admitted.empty()) hand_out(s, admitted);
     }
 }
 
@@ -321,7 +384,15 @@ xtg_status xtg_server_create(const xtg_server_config* cfg, xtg_server** out) {
         s->streams.push_back(st);
     }
     s->st.hbm_budget = s->budget;
+    // dispatch threads, each with every K-th stream of the pool
+    const int K = (int)std::max<int64_t>(1, std::min<int64_t>(opt("server.dispatch_threads", 4), c.streams));
+    for (int i = 0; i < K; ++i) {
+        std::unique_ptr<Disp> d(new Disp());
+        for (int j = i; j < c.streams; j += K) d->streams.push_back(s->streams[(size_t)j]);
+        s->disp.push_back(std::move(d));
+    }
     xtg_server* raw = s.release();
+    for (auto& d : raw->disp) d->th = std::thread(dispatcher, raw, d.get());
     raw->sched = std::thread(scheduler, raw);
     *out = raw;
     return XTG_OK;
@@ -461,6 +532,17 @@ xtg_status xtg_server_destroy(xtg_server* s) {
         s->cv_sched.notify_all();
     }
     if (s->sched.joinable()) s->sched.join();
+    // every admitted request has completed once the scheduler is done, so
+    // the dispatch threads' queues are empty
+    for (auto& d : s->disp) {
+        {
+            std::lock_guard<std::mutex> lk(d->mu);
+            d->stop = true;
+        }
+        d->cv.notify_one();
+    }
+    for (auto& d : s->disp)
+        if (d->th.joinable()) d->th.join();
     wait_background_compiles(60000);  // batch kernels it started building
     for (cudaStream_t st : s->streams) {
         if (!st) continue;

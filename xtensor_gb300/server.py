@@ -28,7 +28,7 @@ class Result(C.Structure):
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "rejected", "cancelled", "inflight",
                                          "pending", "waves", "batched_requests", "batch_launches", "hbm_budget",
-                                         "hbm_reserved")] + [(n, C.c_double) for n in ("p50_ms", "p99_ms", "mean_ms")]
+                                         "hbm_reserved")] + [(n, C.c_double) for n in ("p50_ms", "p99_ms", "mean_ms", "dispatch_ms")]
 
 
 def _sigs(L):
