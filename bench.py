@@ -1463,7 +1463,7 @@ def c4_section(args):
 
     dispatch_threads = args.dispatch_threads
     xg.set_option("server.dispatch_threads", dispatch_threads)
-    srv = Server(streams=8, max_inflight=128, batch_min_group=3)
+    srv = Server(streams=8, max_inflight=128, batch_min_group=2)
     reqs = [srv.request(kind, e, outs[i], op=op, axes=axes, arg_axis=axes)[0] for i, (kind, op, e, axes, *_r) in
             enumerate(pool)]
     s = Stream()
@@ -1874,7 +1874,7 @@ def main():
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--rates", default="2000,16000,48000,96000")
     ap.add_argument("--repeats", type=int, default=3, help="c4: runs per offered rate")
-    ap.add_argument("--dispatch-threads", type=int, default=4, help="c4: the server's dispatch threads")
+    ap.add_argument("--dispatch-threads", type=int, default=1, help="c4: the server's dispatch threads")
     ap.add_argument("--sub", default="c0,c2,c3,c4",
                     help="sub-results added to the default line (comma list of c0,c2,c3,c4; 'none' for none)")
     args = ap.parse_args()

@@ -87,6 +87,7 @@ struct lowering {
     xtg_expr e;
     std::vector<const void*> ids;
     std::vector<std::shared_ptr<void>> temps;  // evaluated sub-reductions
+    std::vector<const xtg_chunked*> chunked;   // per leaf: its chunked array, or null
     lowering() { std::memset(&e, 0, sizeof e); }
     int leaf(const xtg_array& a, const void* id) {
         for (size_t i = 0; i < ids.size(); ++i)
@@ -94,8 +95,22 @@ struct lowering {
         if (e.n_leaves >= XTG_MAX_LEAVES) throw std::runtime_error("xt: more than 8 distinct leaves in one expression");
         e.leaves[e.n_leaves] = a;
         ids.push_back(id);
+        chunked.push_back(nullptr);
         return e.n_leaves++;
     }
+    // a chunked array as a leaf: `a` is its stand-in (dtype, shape)
+    int chunked_leaf(const xtg_array& a, const void* id, const xtg_chunked* c) {
+        const int i = leaf(a, id);
+        chunked[(size_t)i] = c;
+        return i;
+    }
+    bool has_chunked() const {
+        for (const xtg_chunked* c : chunked)
+            if (c) return true;
+        return false;
+    }
+    // the tree is one chunked leaf
+    const xtg_chunked* only_chunked() const { return e.n_nodes == 1 && e.n_leaves == 1 ? chunked[0] : nullptr; }
     void node(int op, int dtype, int arg = 0, int aux = 0, xtg_value imm = xtg_value{0.0}) {
         if (e.n_nodes >= XTG_MAX_NODES) throw std::runtime_error("xt: expression tree too large");
         xtg_node& n = e.nodes[e.n_nodes++];
@@ -106,6 +121,26 @@ struct lowering {
         n.imm = imm;
     }
 };
+// Consumers that take dense leaves only: each chunked leaf is read into a
+// dense device temporary (xtg_chunked_to_dense) that lives with the lowering.
+inline void resolve_chunked(lowering& L) {
+    for (int i = 0; i < L.e.n_leaves; ++i) {
+        const xtg_chunked* c = L.chunked[(size_t)i];
+        if (!c) continue;
+        static const int sz[XTG_NUM_DTYPES] = {1, 1, 1, 2, 2, 4, 4, 8, 8, 2, 4, 8};
+        int64_t n = 1;
+        for (int d = 0; d < c->rank; ++d) n *= c->shape[d];
+        void* p = nullptr;
+        check(xtg_malloc(&p, (size_t)std::max<int64_t>(n * sz[c->dtype], 16), current_stream()));
+        std::shared_ptr<void> hold(p, [](void* q) { xtg_free(q, current_stream()); });
+        xtg_array d = L.e.leaves[i];
+        d.data = p;
+        check(xtg_chunked_to_dense(c, &d, current_stream()));
+        L.e.leaves[i] = d;
+        L.chunked[(size_t)i] = nullptr;
+        L.temps.push_back(hold);
+    }
+}
 }  // namespace detail
 
 inline void set_stream(xtg_stream s) { detail::current_stream() = s; }
@@ -437,7 +472,9 @@ public:
             std::vector<std::size_t>(ns.begin(), ns.end()) != std::vector<std::size_t>(m_shape.begin(), m_shape.end()))
             set_shape(ns);
     }
-    template <class S> void reshape(const S& s) {
+    // in place; returns the container so that call sites can chain it
+    // (`arange(1000).reshape({10, 10, 10})`)
+    template <class S> xdevice_container& reshape(const S& s) {
         auto ns = to_shape(s);
         std::size_t n = 1;
         for (auto v : ns) n *= v;
@@ -445,6 +482,10 @@ public:
         auto keep = m_buf;
         set_shape(ns, false);
         m_buf = keep;
+        return *this;
+    }
+    template <class I> xdevice_container& reshape(std::initializer_list<I> s) {
+        return reshape(std::vector<std::size_t>(s.begin(), s.end()));
     }
     void fill(T v) {
         std::vector<T> h(m_size, v);
@@ -834,6 +875,13 @@ public:
         m_e.lower(L);
         xtg_reduce_desc d = desc();
         xtg_array o = out.xtg_desc();
+        if (const xtg_chunked* c = L.only_chunked()) {
+            if (!d.has_initial && d.ddof == 0 && d.acc_dtype < 0) {
+                detail::check(xtg_chunked_reduce(c, &d, &o, detail::current_stream()));
+                return;
+            }
+        }
+        detail::resolve_chunked(L);
         detail::check(xtg_reduce(&L.e, &d, &o, detail::current_stream()));
     }
     xarray<value_type> eval() const {
@@ -1000,6 +1048,11 @@ void xdevice_container<T, N>::noalias_assign(const E& e) {
         detail::lowering L;
         e.lower(L);
         xtg_array o = xtg_desc();
+        if (const xtg_chunked* c = L.only_chunked()) {  // reading a chunked array
+            detail::check(xtg_chunked_to_dense(c, &o, detail::current_stream()));
+            return;
+        }
+        detail::resolve_chunked(L);
         detail::check(xtg_assign(&L.e, &o, detail::current_stream()));
     }
 }
@@ -1008,6 +1061,7 @@ template <class T> template <class E> xstrided_view<T>& xstrided_view<T>::operat
     detail::lowering L;
     e.derived_cast().lower(L);
     xtg_array o = xtg_desc();
+    detail::resolve_chunked(L);
     detail::check(xtg_assign(&L.e, &o, detail::current_stream()));
     return *this;
 }
@@ -1050,6 +1104,7 @@ template <class E> inline xarray<std::size_t> argmax(const xexpression<E>& e) {
     e.derived_cast().lower(L);
     xarray<std::size_t> out(std::vector<std::size_t>{});
     xtg_array o = out.xtg_desc();
+    detail::resolve_chunked(L);
     detail::check(xtg_argreduce(&L.e, XTG_ARGMAX, 0, 0, &o, detail::current_stream()));
     return out;
 }
@@ -1058,6 +1113,7 @@ template <class E> inline xarray<std::size_t> argmin(const xexpression<E>& e) {
     e.derived_cast().lower(L);
     xarray<std::size_t> out(std::vector<std::size_t>{});
     xtg_array o = out.xtg_desc();
+    detail::resolve_chunked(L);
     detail::check(xtg_argreduce(&L.e, XTG_ARGMIN, 0, 0, &o, detail::current_stream()));
     return out;
 }
@@ -1077,6 +1133,7 @@ template <class E> xarray<std::size_t> arg_axis(const E& e, std::ptrdiff_t axis,
     }
     xarray<std::size_t> out(os);
     xtg_array o = out.xtg_desc();
+    resolve_chunked(L);
     check(xtg_argreduce(&L.e, op, 1, axis, &o, current_stream()));
     return out;
 }
@@ -1101,6 +1158,7 @@ template <class R, class E> xarray<R> accumulate_into(const E& e, int op, int ha
     check(xtg_accumulate_shape(&L.e, op, has_axis, axis, dtype_of<R>::value, &r, sh, &dt));
     xarray<R> out(std::vector<std::size_t>(sh, sh + r));
     xtg_array o = out.xtg_desc();
+    resolve_chunked(L);
     check(xtg_accumulate(&L.e, op, has_axis, axis, dtype_of<R>::value, &o, current_stream()));
     return out;
 }
@@ -1308,6 +1366,7 @@ public:
         m_e.lower(L);
         xarray<value_type> out(std::vector<std::size_t>{m_n});
         xtg_array o = out.xtg_desc();
+        detail::resolve_chunked(L);
         detail::check(xtg_gather(&L.e, (const int64_t*)m_idx->ptr, (int64_t)m_n, &o, detail::current_stream()));
         return out;
     }
@@ -1350,6 +1409,7 @@ public:
         detail::lowering C;
         m_c.lower(C);
         int64_t n = 0;
+        detail::resolve_chunked(C);
         detail::check(xtg_filter_count(&C.e, &n, detail::current_stream()));
         return (std::size_t)n;
     }
@@ -1359,6 +1419,8 @@ public:
         m_c.lower(C);
         xarray<value_type> out(std::vector<std::size_t>{size()});
         xtg_array o = out.xtg_desc();
+        detail::resolve_chunked(L);
+        detail::resolve_chunked(C);
         detail::check(xtg_filter(&L.e, &C.e, &o, detail::current_stream()));
         return out;
     }
@@ -1381,6 +1443,8 @@ private:
             detail::lowering C;
             m_c.lower(C);
             xtg_array d = m_e.xtg_desc();
+            detail::resolve_chunked(rl.L);
+            detail::resolve_chunked(C);
             detail::check(xtg_filter_assign(&rl.L.e, &C.e, op, &d, detail::current_stream()));
             return *this;
         }
@@ -1413,6 +1477,8 @@ private:
         detail::lowering M;
         m_m.lower(M);
         xtg_array d = m_e.xtg_desc();
+        detail::resolve_chunked(rl.L);
+        detail::resolve_chunked(M);
         detail::check(xtg_masked_assign(&rl.L.e, &M.e, op, &d, detail::current_stream()));
         return *this;
     }
@@ -1513,3 +1579,5 @@ template <class T, std::ptrdiff_t N> inline std::ostream& operator<<(std::ostrea
 }
 
 }  // namespace xt
+
+#include "xt_chunked.hpp"

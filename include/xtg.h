@@ -36,6 +36,10 @@
  *   xtg_npy_*       <- xt::load_npy / xt::dump_npy (include/xtensor/io/xnpy.hpp:
  *                      237-450, 674-800)
  *   xtg_blockwise_* <- xt::blockwise::* (include/xtensor/reducers/xblockwise_reducer.hpp:269-533)
+ *   xtg_chunked_*   <- xt::xchunked_array / xt::as_chunked assignment, reading and reductions
+ *                      include/xtensor/chunk/xchunked_array.hpp:56-686,
+ *                      include/xtensor/chunk/xchunked_assign.hpp:185-272,
+ *                      include/xtensor/chunk/xchunked_view.hpp:77-176
  *   xtg_gather / xtg_scatter, xtg_filter* , xtg_masked_assign
  *                   <- reading and assigning through xt::index_view / filter /
  *                      filtration / masked_view
@@ -368,6 +372,43 @@ xtg_status xtg_blockwise_reduce(const xtg_array* in, const int64_t* block_shape,
 /* Shape and type of that result. */
 xtg_status xtg_blockwise_shape(const xtg_array* in, const xtg_reduce_desc* rd, int32_t* rank, int64_t* shape,
                                int32_t* out_dtype);
+
+/* ---- chunked arrays ------------------------------------------------------------------------
+ * A chunked array (xt::xchunked_array<xarray<xarray<T>>>, chunk/xchunked_array.hpp:56-686) in
+ * device memory: `shape` cut into a grid of ceil(shape / chunk_shape) chunks, each a separate
+ * row-major buffer of chunk_shape elements (the last chunk along a dimension ends inside its
+ * buffer; the rest is padding, as the reference's resize makes it, :601-625).  `chunks` is a
+ * host array of one device pointer per chunk, in the grid's row-major order.  Element
+ * (i0, .., iR-1) is element (i % chunk_shape) of chunk (i / chunk_shape) (:640-646). */
+typedef struct {
+    void* const* chunks;
+    int32_t dtype;
+    int32_t rank;
+    int64_t shape[XTG_MAX_RANK];
+    int64_t chunk_shape[XTG_MAX_RANK];
+} xtg_chunked;
+/* dst = e, chunk by chunk (xchunked_semantic::assign_xexpression and computed_assign,
+ * chunk/xchunked_assign.hpp:200-234; `a = e`, `noalias(a) = e`, `a += e`, `a += 2.` lower to it
+ * with `a` itself a leaf).  Leaf i of e is chunked when chunked_leaves != NULL and
+ * chunked_leaves[i] != NULL: its entry in e then only gives dtype and shape, and it must have
+ * dst's shape and chunk shape.  Other leaves are dense device arrays broadcast to dst's shape.
+ * One kernel for the whole grid; the padding of edge chunks is left untouched. */
+xtg_status xtg_chunked_assign(const xtg_expr* e, const xtg_chunked* const* chunked_leaves, const xtg_chunked* dst,
+                              xtg_stream stream);
+/* dst (a dense device array of src's shape, any strides) = src: reading a chunked array
+ * (`xt::xarray<T> b = a`, `noalias(b) = a`, `as_chunked(b, chunk_shape) = a`,
+ * chunk/xchunked_view.hpp:77-176). */
+xtg_status xtg_chunked_to_dense(const xtg_chunked* src, const xtg_array* dst, xtg_stream stream);
+/* out = reduce(rd, src): the reducers of xtg_reduce (xt::sum / prod / amin / amax / mean /
+ * variance / stddev / norm_*, reducers/xreducer.hpp:987-1079) over a chunked array, as the
+ * blockwise reducers run them: each chunk's valid region reduced on the device, the results
+ * of the chunks that share an output block folded in the grid's row-major order with the
+ * blockwise merge (sum +=, prod *=, amin / amax, variance by the pairwise update), then
+ * finalized.  out is a dense device array of the reduction's shape and result type.  Integer
+ * results equal xtg_reduce's on the same values; floating-point sums associate by chunk.
+ * xt::initial and ddof are rejected (XTG_ERR_UNSUPPORTED). */
+xtg_status xtg_chunked_reduce(const xtg_chunked* src, const xtg_reduce_desc* rd, const xtg_array* out,
+                              xtg_stream stream);
 
 /* ---- index, filter and masked views ----------------------------------------------------
  * Assignment operators for writes through a view: dst = op(dst, value). */

@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include "xtensor/chunk/xchunked_array.hpp"
+#include "xtensor/chunk/xchunked_view.hpp"
 #include "xtensor/containers/xarray.hpp"
 #include "xtensor/containers/xtensor.hpp"
 #include "xtensor/core/xmath.hpp"
@@ -22,6 +24,7 @@
 #include "xtensor/reducers/xblockwise_reducer.hpp"
 #include "xtensor/reducers/xnorm.hpp"
 #include "xtensor/reducers/xreducer.hpp"
+#include "xtensor/views/xbroadcast.hpp"
 #include "xtensor/views/xview.hpp"
 
 static int g_fail = 0, g_run = 0;
@@ -473,6 +476,133 @@ TEST(xblockwise_reducer, test_values) {
         // the same input from host memory, streamed by slabs
         check_blockwise(blockwise::sum(adapt_host(h.data(), shape), chunk_shape, axes), xt::sum(input_exp, axes), false);
     }
+}
+
+// ---- chunked arrays (test_xchunked_array.cpp, test_xchunked_view.cpp)
+TEST(xchunked_array, indexed_access) {  // test_xchunked_array.cpp:20-44
+    auto a = chunked_array<double>({10, 10, 10}, {2, 3, 4});
+    std::vector<size_t> idx = {3, 9, 8};
+    double val = 1.;
+    a[idx] = val;
+    EXPECT_EQ((double)a[idx], val);
+    EXPECT_EQ((double)a(3, 9, 8), val);
+    val = 2.;
+    a(3, 9, 8) = val;
+    EXPECT_EQ((double)a(3, 9, 8), val);
+    EXPECT_EQ((double)a[idx], val);
+}
+
+TEST(xchunked_array, assign_expression) {  // test_xchunked_array.cpp:46-126
+    std::vector<size_t> shape1 = {2, 2, 2};
+    std::vector<size_t> chunk_shape1 = {2, 3, 4};
+    auto a1 = chunked_array<double>(shape1, chunk_shape1);
+    double val = 3.;
+    a1 = broadcast(val, a1.shape());
+    for (double v : a1.to_host()) EXPECT_EQ(v, val);
+    std::vector<size_t> shape2 = {32, 10, 10};
+    auto a2 = chunked_array<double>(shape2, chunk_shape1);
+    a2 = broadcast(val, a2.shape());
+    for (double v : a2.to_host()) EXPECT_EQ(v, val);
+    a2 += a2;
+    for (double v : a2.to_host()) EXPECT_EQ(v, 2. * val);
+    a2 += 2.;
+    for (double v : a2.to_host()) EXPECT_EQ(v, 2. * val + 2.);
+    xarray<double> a3{{1., 2., 3.}, {4., 5., 6.}, {7., 8., 9.}};
+    EXPECT_EQ(is_chunked(a3), false);
+    std::vector<size_t> chunk_shape4 = {2, 2};
+    auto a4 = chunked_array(a3, chunk_shape4);
+    EXPECT_EQ(is_chunked(a4), true);
+    double i = 1.;
+    for (double v : a4.to_host()) {
+        EXPECT_EQ(v, i);
+        i += 1.;
+    }
+    auto a5 = xchunked_array<double>(a4, a4.chunk_shape());
+    EXPECT_EQ(is_chunked(a5), true);
+    for (auto v : a5.chunk_shape()) EXPECT_EQ(v, 2u);
+    auto a6 = chunked_array(a3);
+    EXPECT_EQ(is_chunked(a6), true);
+    for (auto v : a6.chunk_shape()) EXPECT_EQ(v, 3u);
+    std::vector<size_t> shape3 = {3, 3};
+    std::vector<size_t> chunk_shape3 = {1, 2};
+    auto a7 = chunked_array<double>(shape3, chunk_shape3);
+    a7 = a3;
+    for (auto it = a7.chunks().begin(); it != a7.chunks().end(); ++it)
+        EXPECT_TRUE(std::vector<size_t>(it->shape().begin(), it->shape().end()) == chunk_shape3);
+    EXPECT_TRUE(a7 == a3);
+}
+
+TEST(xchunked_array, noalias) {  // test_xchunked_array.cpp:128-137
+    std::vector<std::size_t> shape = {10, 10, 10};
+    std::vector<std::size_t> chunk_shape = {2, 2, 2};
+    auto a = chunked_array<double>(shape, chunk_shape);
+    xt::xarray<double> b = arange(1000).reshape({10, 10, 10});
+    noalias(a) = b;
+    EXPECT_TRUE(a == b);
+}
+
+TEST(xchunked_array, chunk_iterator) {  // test_xchunked_array.cpp:139-168
+    std::vector<std::size_t> shape = {10, 10, 10};
+    std::vector<std::size_t> chunk_shape = {2, 2, 2};
+    auto a = chunked_array<double>(shape, chunk_shape);
+    xt::xarray<double> b = arange(1000).reshape({10, 10, 10});
+    noalias(a) = b;
+    auto it = a.chunk_begin();
+    auto cit = a.chunk_cbegin();
+    for (size_t i = 0; i < 5; ++i)
+        for (size_t j = 0; j < 5; ++j)
+            for (size_t k = 0; k < 5; ++k) {
+                EXPECT_EQ((*it).flat(0), (double)a(2 * i, 2 * j, 2 * k));
+                EXPECT_EQ((*cit).flat(0), (double)a(2 * i, 2 * j, 2 * k));
+                ++it;
+                ++cit;
+            }
+    it = a.chunk_begin();
+    std::advance(it, 2);
+    EXPECT_EQ((*it).flat(0), (double)a(0, 0, 4));
+}
+
+TEST(xchunked_array, reducers) {  // xt::sum / amax / mean of a chunked array
+    xt::xarray<double> b = arange(1000).reshape({10, 10, 10});
+    auto a = chunked_array(b, std::vector<std::size_t>{3, 4, 5});
+    EXPECT_TRUE(xarray<double>(xt::sum(a, {1})) == xarray<double>(xt::sum(b, {1})));
+    EXPECT_TRUE(xarray<double>(xt::amax(a, {0, 2})) == xarray<double>(xt::amax(b, {0, 2})));
+    EXPECT_EQ(xt::sum(a)(), 499500.);
+    EXPECT_NEAR(xt::mean(a)(), 499.5, 1e-12);
+}
+
+TEST(xchunked_view, iterate) {  // test_xchunked_view.cpp:16-31
+    std::vector<std::size_t> shape = {3, 4};
+    std::vector<std::size_t> chunk_shape = {1, 2};
+    xarray<double> a(shape);
+    std::size_t chunk_nb = 0;
+    auto chunked_view = xchunked_view<xarray<double>>(a, chunk_shape);
+    for (auto it = chunked_view.chunk_begin(); it != chunked_view.chunk_end(); it++) chunk_nb++;
+    std::size_t expected_chunk_nb = (shape[0] / chunk_shape[0]) * (shape[1] / chunk_shape[1]);
+    EXPECT_EQ(chunk_nb, expected_chunk_nb);
+}
+
+TEST(xchunked_view, assign) {  // test_xchunked_view.cpp:33-45
+    std::vector<std::size_t> shape = {3, 4};
+    std::vector<std::size_t> chunk_shape = {1, 2};
+    xarray<double> a(shape);
+    std::vector<double> data = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12};
+    a.upload(data);
+    xarray<double> b(shape);
+    as_chunked(b, chunk_shape) = a;
+    EXPECT_TRUE(a == b);
+}
+
+TEST(xchunked_view, assign_chunked_array) {  // test_xchunked_view.cpp:47-61
+    std::vector<std::size_t> shape = {10, 10, 10};
+    std::vector<std::size_t> chunk_shape = {2, 3, 4};
+    auto a = chunked_array<double>(shape, chunk_shape);
+    xarray<double> b(shape);
+    auto ref = arange(1000).reshape({10, 10, 10});
+    as_chunked(a, chunk_shape) = ref;
+    as_chunked(b, chunk_shape) = a;
+    EXPECT_TRUE(ref == a);
+    EXPECT_TRUE(ref == b);
 }
 
 int main() {

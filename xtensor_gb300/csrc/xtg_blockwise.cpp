@@ -245,6 +245,77 @@ struct Resources {
     }
 };
 
+// One block result folded into its output region: the first of a region is
+// stored (converted on store when the block result type differs), later
+// ones merged by the reference's merge (xblockwise_reducer_functors.hpp:
+// 38-221): +=, *=, minimum, maximum, or the pairwise variance update, which
+// keeps the running mean in mean_a (var_state) and the block's in mean_b.
+// n_acc: elements folded into each output so far; n_b: in this block.
+xtg_status fold_partial(const Plan& P, const xtg_reduce_desc& prd, const xtg_array& slab, double p, bool first,
+                        const xtg_array& region, const xtg_array& part, const xtg_array& mean_a,
+                        const xtg_array& mean_b, bool var_state, double n_acc, double n_b, Resources& R,
+                        cudaStream_t stream) {
+    Ex x = part_tree(P, slab, p);
+    if (first) {
+        if (P.part_dtype == P.out_dtype) {
+            XTG_TRY(xtg_reduce(&x.e, &prd, &region, stream));
+        } else {  // amin / amax with a wider result type: the block result converts on store
+            xtg_array tmp = dense_like(region, P.part_dtype, nullptr);
+            XTG_TRY(R.alloc(&tmp.data, (size_t)numel(region) * dt(P.part_dtype).size));
+            XTG_TRY(xtg_reduce(&x.e, &prd, &tmp, stream));
+            Ex c;
+            c.leaf(tmp);
+            XTG_TRY(assign_expr(c, region, stream));
+        }
+        if (var_state) {
+            xtg_reduce_desc mrd = prd;
+            mrd.op = XTG_RED_MEAN;
+            Ex y;
+            y.leaf(slab);
+            XTG_TRY(xtg_reduce(&y.e, &mrd, &mean_a, stream));
+        }
+        return XTG_OK;
+    }
+    XTG_TRY(xtg_reduce(&x.e, &prd, &part, stream));
+    Ex m;
+    switch (P.merge) {
+        case M_ADD: m.leaf(region).leaf(part).op(XTG_OP_ADD); break;
+        case M_MUL: m.leaf(region).leaf(part).op(XTG_OP_MUL); break;
+        case M_MIN: m.leaf(part).leaf(region).op(XTG_OP_MINIMUM); break;
+        case M_MAX: m.leaf(part).leaf(region).op(XTG_OP_MAXIMUM); break;
+        case M_VAR: {
+            xtg_reduce_desc mrd = prd;
+            mrd.op = XTG_RED_MEAN;
+            Ex y;
+            y.leaf(slab);
+            XTG_TRY(xtg_reduce(&y.e, &mrd, &mean_b, stream));
+            // new_mean = (n_a mean_a + n_b mean_b) / (n_a + n_b)
+            // var = (n_a var_a + n_b var_b + n_a (mean_a - new_mean)^2
+            //        + n_b (mean_b - new_mean)^2) / (n_a + n_b)
+            // (variance_functor::merge, xblockwise_reducer_functors.hpp:195-221)
+            auto new_mean = [&](Ex& e) {
+                e.f64(n_acc).leaf(mean_a).op(XTG_OP_MUL).f64(n_b).leaf(mean_b).op(XTG_OP_MUL).op(XTG_OP_ADD);
+                e.f64(n_acc).f64(n_b).op(XTG_OP_ADD).op(XTG_OP_DIV);
+            };
+            m.f64(n_acc).leaf(region).op(XTG_OP_MUL);
+            m.f64(n_b).leaf(part).op(XTG_OP_MUL).op(XTG_OP_ADD);
+            m.f64(n_acc).leaf(mean_a);
+            new_mean(m);
+            m.op(XTG_OP_SUB).op(XTG_OP_SQUARE).op(XTG_OP_MUL).op(XTG_OP_ADD);
+            m.f64(n_b).leaf(mean_b);
+            new_mean(m);
+            m.op(XTG_OP_SUB).op(XTG_OP_SQUARE).op(XTG_OP_MUL).op(XTG_OP_ADD);
+            m.f64(n_acc).f64(n_b).op(XTG_OP_ADD).op(XTG_OP_DIV);
+            XTG_TRY(assign_expr(m, region, stream));
+            Ex nm;
+            new_mean(nm);
+            XTG_TRY(assign_expr(nm, mean_a, stream));
+            return XTG_OK;
+        }
+    }
+    return assign_expr(m, region, stream);
+}
+
 xtg_status blockwise_impl(const xtg_array* in, const int64_t* block, const xtg_reduce_desc* rd, double p,
                           const xtg_array* out, cudaStream_t stream) {
     if (!in || !block || !rd || !out) return fail(XTG_ERR_INVALID, "null argument");
@@ -401,67 +472,9 @@ xtg_status blockwise_impl(const xtg_array* in, const int64_t* block, const xtg_r
         double n_b = 1.0;
         for (int d = 0; d < rank; ++d)
             if (red[d]) n_b *= (double)slab.shape[d];
-        Ex x = part_tree(P, slab, p);
-        if (first) {
-            if (P.part_dtype == P.out_dtype) {
-                XTG_TRY(xtg_reduce(&x.e, &prd, &region, stream));
-            } else {  // amin / amax with a wider result type: the block result converts on store
-                xtg_array tmp = dense_like(region, P.part_dtype, nullptr);
-                XTG_TRY(R.alloc(&tmp.data, (size_t)numel(region) * dt(P.part_dtype).size));
-                XTG_TRY(xtg_reduce(&x.e, &prd, &tmp, stream));
-                Ex c;
-                c.leaf(tmp);
-                XTG_TRY(assign_expr(c, region, stream));
-            }
-            if (P.merge == M_VAR && slab_reduced && nslabs > 1) {
-                xtg_reduce_desc mrd = prd;
-                mrd.op = XTG_RED_MEAN;
-                Ex y;
-                y.leaf(slab);
-                XTG_TRY(xtg_reduce(&y.e, &mrd, &mean_a, stream));
-            }
-            n_acc = n_b;
-        } else {
-            XTG_TRY(xtg_reduce(&x.e, &prd, &part, stream));
-            Ex m;
-            switch (P.merge) {
-                case M_ADD: m.leaf(region).leaf(part).op(XTG_OP_ADD); break;
-                case M_MUL: m.leaf(region).leaf(part).op(XTG_OP_MUL); break;
-                case M_MIN: m.leaf(part).leaf(region).op(XTG_OP_MINIMUM); break;
-                case M_MAX: m.leaf(part).leaf(region).op(XTG_OP_MAXIMUM); break;
-                case M_VAR: {
-                    xtg_reduce_desc mrd = prd;
-                    mrd.op = XTG_RED_MEAN;
-                    Ex y;
-                    y.leaf(slab);
-                    XTG_TRY(xtg_reduce(&y.e, &mrd, &mean_b, stream));
-                    // new_mean = (n_a mean_a + n_b mean_b) / (n_a + n_b)
-                    // var = (n_a var_a + n_b var_b + n_a (mean_a - new_mean)^2
-                    //        + n_b (mean_b - new_mean)^2) / (n_a + n_b)
-                    // (variance_functor::merge, xblockwise_reducer_functors.hpp:195-221)
-                    auto new_mean = [&](Ex& e) {
-                        e.f64(n_acc).leaf(mean_a).op(XTG_OP_MUL).f64(n_b).leaf(mean_b).op(XTG_OP_MUL).op(XTG_OP_ADD);
-                        e.f64(n_acc).f64(n_b).op(XTG_OP_ADD).op(XTG_OP_DIV);
-                    };
-                    m.f64(n_acc).leaf(region).op(XTG_OP_MUL);
-                    m.f64(n_b).leaf(part).op(XTG_OP_MUL).op(XTG_OP_ADD);
-                    m.f64(n_acc).leaf(mean_a);
-                    new_mean(m);
-                    m.op(XTG_OP_SUB).op(XTG_OP_SQUARE).op(XTG_OP_MUL).op(XTG_OP_ADD);
-                    m.f64(n_b).leaf(mean_b);
-                    new_mean(m);
-                    m.op(XTG_OP_SUB).op(XTG_OP_SQUARE).op(XTG_OP_MUL).op(XTG_OP_ADD);
-                    m.f64(n_acc).f64(n_b).op(XTG_OP_ADD).op(XTG_OP_DIV);
-                    XTG_TRY(assign_expr(m, region, stream));
-                    Ex nm;
-                    new_mean(nm);
-                    XTG_TRY(assign_expr(nm, mean_a, stream));
-                    break;
-                }
-            }
-            if (P.merge != M_VAR) XTG_TRY(assign_expr(m, region, stream));
-            n_acc += n_b;
-        }
+        XTG_TRY(fold_partial(P, prd, slab, p, first, region, part, mean_a, mean_b,
+                             P.merge == M_VAR && slab_reduced && nslabs > 1, n_acc, n_b, R, stream));
+        n_acc = first ? n_b : n_acc + n_b;
         if (src != W_DEVICE) {
             XTG_CUDA(cudaEventRecord(R.ev[3 + b], stream));
             used[b] = true;
@@ -488,11 +501,155 @@ xtg_status blockwise_impl(const xtg_array* in, const int64_t* block, const xtg_r
     return XTG_OK;
 }
 
+// Reductions of a chunked array: each chunk's valid region (a view of its
+// buffer) is one block.  The grid is walked with its reduced dims outside and
+// its kept dims inside, so that every output block receives its chunks in the
+// grid's row-major order and all blocks share one running element count.
+xtg_status chunked_reduce_impl(const xtg_chunked* src, const xtg_reduce_desc* rd, const xtg_array* out,
+                               cudaStream_t stream) {
+    if (!src || !rd || !out) return fail(XTG_ERR_INVALID, "null argument");
+    if (rd->has_initial) return fail(XTG_ERR_UNSUPPORTED, "chunked reductions take no initial value");
+    if (rd->ddof != 0) return fail(XTG_ERR_UNSUPPORTED, "chunked variance takes no ddof");
+    if (rd->op > XTG_RED_NORM_LINF) return fail(XTG_ERR_INVALID, "unknown reduction op");
+    ChunkGrid G;
+    XTG_TRY(chunk_grid(*src, G));
+    const int rank = src->rank;
+    // the whole array as a dense descriptor: types and shapes only
+    xtg_array whole;
+    memset(&whole, 0, sizeof whole);
+    whole.dtype = src->dtype;
+    whole.rank = rank;
+    whole.data = G.n ? src->chunks[0] : nullptr;
+    for (int d = 0; d < rank; ++d) whole.shape[d] = src->shape[d];
+    whole = dense_like(whole, src->dtype, whole.data);
+    Plan P;
+    XTG_TRY(make_plan(whole, rd, P));
+    const std::vector<bool> red = reduced_axes(rd, rank);
+    xtg_reduce_desc prd = *rd;
+    prd.op = P.part_op;
+    prd.acc_dtype = P.part_acc;
+    {
+        Ex x = part_tree(P, whole, 0.0);
+        int32_t orank, odt;
+        int64_t oshape[XTG_MAX_RANK];
+        XTG_TRY(xtg_reduce_shape(&x.e, &prd, &orank, oshape, &odt));
+        if (out->dtype != P.out_dtype)
+            return fail(XTG_ERR_INVALID, "destination dtype " + std::to_string(out->dtype) +
+                                             " differs from the result type " + std::to_string(P.out_dtype));
+        bool same = out->rank == orank;
+        for (int d = 0; same && d < orank; ++d) same = out->shape[d] == oshape[d];
+        if (!same) return fail(XTG_ERR_SHAPE, "destination shape mismatch");
+    }
+    XTG_TRY(ensure_device(nullptr));
+    const int64_t on = numel(*out);
+    if (G.n == 0 || on == 0) {
+        // an empty reduced extent: the plain reducer's result of an empty range
+        if (on == 0) return XTG_OK;
+        xtg_array empty = whole;
+        empty.data = out->data;  // never read: some reduced extent is 0
+        Ex x;
+        x.leaf(empty);
+        return xtg_reduce(&x.e, rd, out, stream);
+    }
+    // output axis of each input dim (-1: reduced and dropped)
+    int oax[XTG_MAX_RANK];
+    for (int d = 0, j = 0; d < rank; ++d) oax[d] = (!red[d] || rd->keep_dims) ? j++ : -1;
+    int64_t cst[XTG_MAX_RANK];
+    chunk_strides(G, cst);
+    std::vector<int> rdims, kdims;
+    for (int d = 0; d < rank; ++d) (red[d] ? rdims : kdims).push_back(d);
+    int64_t n_rcomb = 1, n_kcomb = 1;
+    for (int d : rdims) n_rcomb *= G.grid[d];
+    for (int d : kdims) n_kcomb *= G.grid[d];
+
+    Resources R;
+    R.stream = stream;
+    const bool var_state = P.merge == M_VAR && n_rcomb > 1;
+    xtg_array part = dense_like(*out, P.part_dtype, nullptr), mean_a = dense_like(*out, P.out_dtype, nullptr);
+    xtg_array mean_b = dense_like(*out, P.out_dtype, nullptr);
+    if (n_rcomb > 1) {
+        XTG_TRY(R.alloc(&part.data, (size_t)on * dt(P.part_dtype).size));
+        if (var_state) {
+            XTG_TRY(R.alloc(&mean_a.data, (size_t)on * dt(P.out_dtype).size));
+            XTG_TRY(R.alloc(&mean_b.data, (size_t)on * dt(P.out_dtype).size));
+        }
+    }
+    // the view of a dense output-shaped array over one chunk's output block
+    auto block_view = [&](const xtg_array& a, const int64_t* gc, const int64_t* ext) {
+        xtg_array v = a;
+        int64_t off = 0;
+        for (int d = 0; d < rank; ++d) {
+            if (oax[d] < 0) continue;
+            if (red[d]) {
+                v.shape[oax[d]] = 1;
+            } else {
+                v.shape[oax[d]] = ext[d];
+                off += gc[d] * G.cs[d] * a.strides[oax[d]];
+            }
+        }
+        if (a.data) v.data = (char*)a.data + off * dt(a.dtype).size;
+        return v;
+    };
+    double n_acc = 0.0;
+    for (int64_t rc = 0; rc < n_rcomb; ++rc) {
+        int64_t gc[XTG_MAX_RANK] = {0};
+        int64_t q = rc;
+        for (int i = (int)rdims.size() - 1; i >= 0; --i) {
+            gc[rdims[(size_t)i]] = q % G.grid[rdims[(size_t)i]];
+            q /= G.grid[rdims[(size_t)i]];
+        }
+        double n_b = 1.0;
+        for (int d : rdims) n_b *= (double)std::min(G.cs[d], G.shape[d] - gc[d] * G.cs[d]);
+        for (int64_t kc = 0; kc < n_kcomb; ++kc) {
+            int64_t k = kc;
+            for (int i = (int)kdims.size() - 1; i >= 0; --i) {
+                gc[kdims[(size_t)i]] = k % G.grid[kdims[(size_t)i]];
+                k /= G.grid[kdims[(size_t)i]];
+            }
+            int64_t ci = 0, ext[XTG_MAX_RANK];
+            for (int d = 0; d < rank; ++d) {
+                ci = ci * G.grid[d] + gc[d];
+                ext[d] = std::min(G.cs[d], G.shape[d] - gc[d] * G.cs[d]);
+            }
+            xtg_array slab = whole;
+            slab.data = src->chunks[ci];
+            for (int d = 0; d < rank; ++d) {
+                slab.shape[d] = ext[d];
+                slab.strides[d] = cst[d];
+            }
+            XTG_TRY(fold_partial(P, prd, slab, 0.0, rc == 0, block_view(*out, gc, ext), block_view(part, gc, ext),
+                                 block_view(mean_a, gc, ext), block_view(mean_b, gc, ext), var_state, n_acc, n_b, R,
+                                 stream));
+        }
+        n_acc = rc == 0 ? n_b : n_acc + n_b;
+    }
+    if (P.fin != F_NONE) {
+        Ex f;
+        f.leaf(*out);
+        if (P.fin == F_DIV) {
+            int64_t factor = 1;
+            for (int d = 0; d < rank; ++d)
+                if (red[d]) factor *= src->shape[d];
+            f.scalar(P.out_dtype, (double)factor).op(XTG_OP_DIV);
+        } else if (P.fin == F_SQRT) {
+            f.op(XTG_OP_SQRT);
+        }
+        XTG_TRY(assign_expr(f, *out, stream));
+    }
+    return XTG_OK;
+}
+
 }  // namespace
 
 }  // namespace xtgh
 
 using namespace xtgh;
+
+extern "C" xtg_status xtg_chunked_reduce(const xtg_chunked* src, const xtg_reduce_desc* rd, const xtg_array* out,
+                                         xtg_stream stream) {
+    begin_call();
+    return chunked_reduce_impl(src, rd, out, (cudaStream_t)stream);
+}
 
 extern "C" xtg_status xtg_blockwise_reduce(const xtg_array* in, const int64_t* block_shape, const xtg_reduce_desc* rd,
                                            double p, const xtg_array* out, xtg_stream stream) {

@@ -477,6 +477,59 @@ __global__ void __launch_bounds__(256) k_assign(const AssignParams p) {
 
 
 // ---------------------------------------------------------------------------
+// K12: assignment over a chunk grid (xchunked_semantic::assign_xexpression,
+// include/xtensor/chunk/xchunked_assign.hpp:200-219): every chunk's region of
+// the expression into the chunk, for all chunks in one launch.  Work item q
+// = (chunk, vector inside the chunk); elements outside the chunk's valid
+// extents (the padding of edge chunks) are neither read nor written.  With
+// VEC > 1 every chunk is whole along the innermost dim (the host checks), so
+// only the outer dims need the extent test.
+template <class Tree, class LS, class OutT, int OUTKIND, int VEC, int R, int U, bool BIG>
+__global__ void __launch_bounds__(256) k_assign_chunks(const ChunkParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    Ctx<0> c;
+    c.scal = p.scal;
+    const i64 nv = p.sp.nvec;
+    const i64 total = p.n_chunks * nv;
+    const i64 step = (i64)gridDim.x * blockDim.x * U;
+    for (i64 base = (i64)blockIdx.x * blockDim.x * U + threadIdx.x; base < total; base += step) {
+        RG rg[U];
+        i64 ooff[U];
+        void* optr[U];
+        bool ok[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const i64 q = base + (i64)u * blockDim.x;
+            ok[u] = false;
+            if (q < total) {
+                const i64 ch = q / nv;
+                i64 idx[R];
+                decode<R, VEC, BIG>(p.sp, q - ch * nv, idx);
+                const ChunkEntry& ent = p.tab[ch];
+                bool in = true;
+#pragma unroll
+                for (int d = 0; d < R; ++d) in = in && idx[d] < ent.ext[d];
+                if (in) {
+                    ok[u] = true;
+                    LoadLeaves<LS>::template run<VEC, R>(rg[u], ent.leaf, p.leaf_strides, idx);
+                    ooff[u] = dot_idx<R>(idx, p.out_strides);
+                    optr[u] = ent.out;
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (ok[u]) {
+                OutT v[VEC];
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) v[j] = cvt<OutT>(Tree::ev(rg[u], j, c));
+                st_out<OutT, OUTKIND, VEC>(reinterpret_cast<OutT*>(optr[u]), ooff[u], p.out_strides[R - 1], v);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Generic warp shuffle of a POD accumulator (word by word).
 template <class A> XTG_DI A shfl_xor_pod(const A& a, int m) {
     union U { A a; u32 w[(sizeof(A) + 3) / 4]; };

@@ -40,6 +40,24 @@ struct AssignParams {
     Scalars scal;
 };
 
+// Chunked evaluation (K12): the iteration space is one chunk (all chunks
+// share its shape), repeated for every chunk of the grid; per chunk a table
+// entry gives the leaves' and the destination's base pointers and the
+// chunk's valid extents (edge chunks end inside their buffer).
+struct ChunkEntry {
+    const void* leaf[XTG_KMAX_LEAVES];
+    void* out;
+    i64 ext[XTG_KMAX_RANK];
+};
+struct ChunkParams {
+    Space sp;                 // one chunk, innermost dim in vectors
+    i64 n_chunks;
+    const ChunkEntry* tab;    // n_chunks entries, chunk-grid row-major
+    i64 leaf_strides[XTG_KMAX_LEAVES][XTG_KMAX_RANK];  // within a chunk
+    i64 out_strides[XTG_KMAX_RANK];
+    Scalars scal;
+};
+
 struct TransposeParams {
     i64 sa, sb;            // extents of A and B
     i64 ntile_a, ntile_b;

@@ -87,6 +87,21 @@ bool assign_hazard(const Tree& t, const xtg_array& out);
 // True when any leaf's byte range overlaps `out`'s.
 bool shares_memory(const Tree& t, const xtg_array& out);
 
+// Chunk grid of a chunked array: chunks per dimension (the edge chunk
+// included) and their count.
+struct ChunkGrid {
+    int rank = 0;
+    int64_t shape[XTG_MAX_RANK] = {0};
+    int64_t cs[XTG_MAX_RANK] = {0};
+    int64_t grid[XTG_MAX_RANK] = {0};
+    int64_t n = 0;
+};
+xtg_status chunk_grid(const xtg_chunked& c, ChunkGrid& g);
+// Grid coordinates of chunk i (row-major).
+void chunk_coords(const ChunkGrid& g, int64_t i, int64_t* gc);
+// Row-major element strides inside a chunk.
+void chunk_strides(const ChunkGrid& g, int64_t* st);
+
 // Accumulator type string, post-operation and initial values of a reduction.
 struct AccChoice {
     std::string acc;

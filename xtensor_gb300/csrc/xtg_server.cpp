@@ -15,10 +15,10 @@
 //     immediates form a group launched as ONE batched kernel; everything else
 //     goes out individually.  The scheduler hands each wave's groups and
 //     requests round-robin to dispatch threads (option
-//     "server.dispatch_threads", default 4), each owning a share of the
-//     stream pool, so the host cost of launching (planning or plan-cache
-//     replay, kernel launches) is paid on several cores and the work
-//     overlaps on the device.
+//     "server.dispatch_threads", default 1), each owning a share of the
+//     stream pool, so that several cores can pay the host cost of launching
+//     (planning or plan-cache replay, kernel launches); the work overlaps on
+//     the device across the streams.
 //   completion — cudaLaunchHostFunc after each unit marks its requests done
 //     with a host timestamp and releases their budget; the scheduler frees
 //     batch work lists once their units completed.
@@ -30,6 +30,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -80,6 +81,7 @@ struct xtg_server {
     std::vector<cudaStream_t> streams;
     std::vector<std::unique_ptr<Disp>> disp;
     size_t next_disp = 0;
+    std::set<std::string> warmed;  // batchable shapes whose batch kernel build has started
     std::mutex mu;
     std::condition_variable cv_sched, cv_done;
     std::deque<Req*> pending;
@@ -288,6 +290,21 @@ void hand_out(xtg_server* s, std::vector<Req*>& admitted) {
         if (r->batchable) groups[r->sig].push_back(r);
         else singles.push_back(r);
     }
+    // the first request of a batchable shape starts building its batch
+    // kernel in the background, so that groups of that shape arriving later
+    // find it loaded instead of running one request at a time meanwhile
+    for (auto& kv : groups) {
+        if (!s->warmed.insert(kv.first).second) continue;
+        Req* f = kv.second[0];
+        xtg_batch* b = nullptr;
+        if (xtg_batch_create(&f->r.expr, f->r.kind == XTG_REQ_REDUCE ? &f->r.rd : nullptr, &b) == XTG_OK &&
+            xtg_batch_add(b, f->r.expr.leaves, f->r.expr.n_leaves, &f->r.out) == XTG_OK) {
+            std::string kname;
+            if (batch_planned_kernel(b, &kname) == XTG_OK && !kernel_ready(kname)) compile_async(kname, 256);
+        }
+        if (b) xtg_batch_destroy(b);
+        clear_error();
+    }
     const size_t K = s->disp.size();
     std::vector<Work> work(K);
     for (auto& kv : groups) {
@@ -385,7 +402,7 @@ xtg_status xtg_server_create(const xtg_server_config* cfg, xtg_server** out) {
     }
     s->st.hbm_budget = s->budget;
     // dispatch threads, each with every K-th stream of the pool
-    const int K = (int)std::max<int64_t>(1, std::min<int64_t>(opt("server.dispatch_threads", 4), c.streams));
+    const int K = (int)std::max<int64_t>(1, std::min<int64_t>(opt("server.dispatch_threads", 1), c.streams));
     for (int i = 0; i < K; ++i) {
         std::unique_ptr<Disp> d(new Disp());
         for (int j = i; j < c.streams; j += K) d->streams.push_back(s->streams[(size_t)j]);
