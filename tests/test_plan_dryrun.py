@@ -86,7 +86,8 @@ def test_c2_precision_full_reductions():
         out = fake((), "float32")
         ops.reduce("sum", x, out=out)
         ks = last_kernels()
-        assert fam(ks) == ["k_reduce_row", "k_reduce_combine"] and acc in ks[0]
+        # 2^28 contiguous elements in 16-byte vectors: the streaming full reduction
+        assert fam(ks) == ["k_reduce_stream", "k_reduce_combine"] and acc in ks[0]
         for op, a in [("mean", "AccSumC"), ("variance", "AccMom<float, 1>"), ("norm_l2", "AccNormC<2>")]:
             o = fake((), "float64")
             ops.reduce(op, x, out=o)

@@ -3088,6 +3088,132 @@ XTG_DI void bulk_g2s(void* dst, const void* src, unsigned bytes, u64* bar) {
 XTG_DI void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 XTG_DI void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
+// K13: a full reduction of one contiguous leaf streamed through shared
+// memory.  Each block walks its work items (the same fixed partition as K3),
+// each item in stages of 1024 16-byte vectors that one thread copies with
+// cp.async.bulk into a ring of NS buffers (mbarrier completion), so NS stages
+// are in flight per block whatever the registers of the accumulator.  Thread
+// t folds vectors t, t + 256, t + 512, t + 768 of every stage of its item —
+// the vectors and the order of K3 with a 256-thread group — and the block
+// combines its threads with K3's tree, so results equal K3's bit for bit.
+// Every wait is bounded; a block that gives up (decided for the whole block)
+// sets the error word, waits (bounded) for its copies in flight and returns.
+template <class T> struct SmemVec16 {
+    template <int VEC> static XTG_DI void get(T (&dst)[VEC], const unsigned char* p) {
+        union {
+            uint4 q;
+            T e[VEC];
+        } u;
+        u.q = *reinterpret_cast<const uint4*>(p);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) dst[j] = u.e[j];
+    }
+};
+template <class Tree, class LS, class TL, class Acc, class Out, int POST, int VEC, int NS>
+__global__ void __launch_bounds__(256) k_reduce_stream(const RedParams p) {
+    typedef typename LS::template R<VEC>::type RG;
+    constexpr unsigned SB = 16384;  // stage bytes: 1024 vectors
+    extern __shared__ __align__(128) unsigned char sbuf[];
+    __shared__ u64 bars[NS];
+    __shared__ Acc smem[32];
+    Ctx<0> c;
+    c.scal = p.scal;
+    const int tid = (int)threadIdx.x;
+    const i64 nitems = p.nsplit;
+    const char* base = reinterpret_cast<const char*>(p.leaf[0]);
+    auto item_len = [&](i64 w) -> i64 {
+        const i64 rb = w * p.chunk;
+        const i64 re = rb + p.chunk < p.n_redv ? rb + p.chunk : p.n_redv;
+        return re - rb;
+    };
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    // the copy cursor (thread 0): next item and stage to fetch
+    i64 iw = blockIdx.x, is = 0;
+    i64 issued = 0;
+    auto issue_next = [&](int slot) {
+        if (iw >= nitems) return;
+        const i64 len = item_len(iw);
+        const i64 v0 = is * 1024;
+        const i64 nv = len - v0 < 1024 ? len - v0 : 1024;
+        const unsigned bytes = (unsigned)(nv * 16);
+        mbar_expect_tx(&bars[slot], bytes);
+        bulk_g2s(sbuf + (size_t)slot * SB, base + (iw * p.chunk + v0) * 16, bytes, &bars[slot]);
+        ++issued;
+        if (++is * 1024 >= len) {
+            iw += gridDim.x;
+            is = 0;
+        }
+    };
+    if (tid == 0)
+        for (int s = 0; s < NS; ++s) issue_next(s);
+    i64 consumed = 0;
+    for (i64 w = blockIdx.x; w < nitems; w += gridDim.x) {
+        Acc acc;
+        acc.init(p);
+        if (NeedsShift<Acc>::value && p.n_red > 0) {
+            typename LS::template R<1>::type rg1;
+            i64 off[XTG_KMAX_LEAVES] = {0};
+            i64 inner[XTG_KMAX_LEAVES] = {1};
+            LoadLeavesAt<LS>::template run<1>(rg1, p.leaf, off, inner);
+            Shift<Acc>::set(acc, Tree::ev(rg1, 0, c));
+        }
+        typename Work<Acc>::T wa;
+        wa.from(acc);
+        const i64 len = item_len(w);
+        const i64 ns = (len + 1023) / 1024;
+        for (i64 s = 0; s < ns; ++s, ++consumed) {
+            const int slot = (int)(consumed % NS);
+            const unsigned parity = (unsigned)((consumed / NS) & 1);
+            bool ok = false;
+            for (int k = 0; k < (1 << 22); ++k)
+                if (mbar_try_wait(&bars[slot], parity)) {
+                    ok = true;
+                    break;
+                }
+            if (__syncthreads_or(!ok)) {
+                // give up: flag it, wait (bounded) for the copies still in flight
+                if (tid == 0) {
+                    atomicExch(p.err, 1);
+                    for (i64 q = consumed + 1; q < issued; ++q)
+                        for (int k = 0; k < (1 << 22); ++k)
+                            if (mbar_try_wait(&bars[q % NS], (unsigned)((q / NS) & 1))) break;
+                }
+                return;
+            }
+            const unsigned char* buf = sbuf + (size_t)slot * SB;
+            const i64 nvs = len - s * 1024 < 1024 ? len - s * 1024 : 1024;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int v = tid + 256 * j;
+                if (v < nvs) {
+                    RG rg;
+                    SmemVec16<TL>::template get<VEC>(RegAt<0>::get(rg), buf + (size_t)v * 16);
+                    AddVec<HasAdd2<typename Work<Acc>::T>::value != 0>::template run<VEC, Tree>(
+                        wa, rg, (w * p.chunk + s * 1024 + v) * VEC, c);
+                }
+            }
+            __syncthreads();  // every thread is done with the slot
+            if (tid == 0) {
+                fence_proxy_async_smem();
+                issue_next(slot);
+            }
+        }
+        wa.to(acc);
+        acc = group_reduce<256>(acc, smem);
+        if (tid == 0) {
+            if (p.nsplit > 1) reinterpret_cast<Acc*>(p.partial)[w] = acc;
+            else reinterpret_cast<Out*>(p.out)[0] = finish<Out, Acc, POST>(acc, p);
+        }
+        __syncthreads();
+    }
+}
+
+
 template <class T, int VEC>
 XTG_DI void ld_smem(T (&dst)[VEC], const T* p) {
     const int B = (int)sizeof(T) * VEC;

@@ -103,6 +103,7 @@ struct RedParams {
     void* eout;
     i64 eks[XTG_KMAX_RANK];
     i64 ers[XTG_KMAX_RANK];
+    int* err;  // streaming row kernel: set to 1 when a bounded wait gives up
 };
 
 struct RowParams {

@@ -343,7 +343,26 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
 
     Kernel* k;
     xtg_status st;
-    if (row) {
+    // K13: a full reduction of one contiguous leaf in 16-byte vectors with a
+    // double-float accumulator streams through shared memory (the same
+    // vectors, order and tree as K3 with a 256-thread group, so the same bits)
+    const bool dfloat = accname == "xtg::AccSumC" || accname.rfind("xtg::AccMom<float", 0) == 0 ||
+                        accname.rfind("xtg::AccNormC<", 0) == 0;
+    if (row && !eout && n_out == 1 && RR == 1 && NL == 1 && kinds[0] == 0 && dfloat && opt("reduce.packed", 1) &&
+        opt("reduce.stream", 1) && vec * dt(t.leaves[0].dtype).size == 16 && aligned(t.leaves[0].data, 16) &&
+        chunk >= opt("reduce.cta_chunk", 2048)) {
+        const int NS = (int)std::max<int64_t>(2, std::min<int64_t>(opt("reduce.stream_stages", 4), 6));
+        const size_t smem = (size_t)NS * 16384;
+        int* err = nullptr;
+        XTG_TRY(device_error_word(&err));
+        p.err = err;
+        const std::string name = "xtg::k_reduce_stream<" + tree + ", " + ls + ", " + dt(t.leaves[0].dtype).cname + ", " +
+                                 accname + ", " + outc + ", " + std::to_string(post) + ", " + std::to_string(vec) + ", " +
+                                 std::to_string(NS) + ">";
+        Kernel* k;
+        st = get_kernel(name, 256, &k, smem);
+        if (st == XTG_OK) st = launch(k, grid_cap(k, nsplit), 256, &p, stream, smem, part_off);
+    } else if (row) {
         const int group = (chunk >= opt("reduce.cta_chunk", 2048)) ? 256 : 32;
         // (a copy ring as in the column kernel measured slower here: these
         // loops are instruction-bound once two register batches are in flight)

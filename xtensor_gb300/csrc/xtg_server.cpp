@@ -13,7 +13,10 @@
 //   dispatch — admitted small requests (at most batch_max_elems elements,
 //     2-D, elementwise or last-axis reductions) with the same tree shape and
 //     immediates form a group launched as ONE batched kernel; everything else
-//     goes out individually.  The scheduler hands each wave's groups and
+//     goes out individually.  A batchable request waits up to
+//     "server.batch_window_us" (default 200) for others of its shape while
+//     other work is on the device; a group leaves at once when it reaches
+//     "server.batch_max_group" (default 64) or the device has nothing else.  The scheduler hands each wave's groups and
 //     requests round-robin to dispatch threads (option
 //     "server.dispatch_threads", default 1), each owning a share of the
 //     stream pool, so that several cores can pay the host cost of launching
@@ -329,18 +332,34 @@ void hand_out(xtg_server* s, std::vector<Req*>& admitted) {
 void scheduler(xtg_server* s) {
     ensure_device(nullptr);
     const double aging_ms = (double)opt("server.aging_ms", 50);
+    // batchable requests of one shape wait up to this long for others of the
+    // same shape (continuous batching's collect window); a group leaves as
+    // soon as it is full or nothing else is on the device
+    const auto window = std::chrono::microseconds(opt("server.batch_window_us", 200));
+    const size_t max_group = (size_t)std::max<int64_t>(2, opt("server.batch_max_group", 64));
+    std::map<std::string, std::vector<Req*>> forming;
+    size_t n_forming = 0;
     uint64_t seen = ~0ull;
     for (;;) {
         std::vector<Req*> admitted;
         std::vector<Unit*> done;
+        bool idle = false;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             // wake for work to clean up, for a change that may let a pending
-            // request in, or to finish once stopping has drained the device
-            s->cv_sched.wait(lk, [&] {
+            // request in, to finish once stopping has drained the device, or
+            // when the oldest forming group's window closes
+            auto ready = [&] {
                 return !s->finished_units.empty() || (!s->pending.empty() && s->events != seen) ||
-                       (s->stop && s->inflight == 0);
-            });
+                       (s->stop && s->inflight == (int64_t)n_forming);
+            };
+            if (n_forming == 0) {
+                s->cv_sched.wait(lk, ready);
+            } else {
+                auto oldest = Clock::time_point::max();
+                for (auto& kv : forming) oldest = std::min(oldest, kv.second[0]->t_submit);
+                s->cv_sched.wait_until(lk, oldest + window, ready);
+            }
             seen = s->events;
             done.swap(s->finished_units);
             if (s->stop && s->pending.empty() && s->inflight == 0 && done.empty()) break;
@@ -362,12 +381,34 @@ void scheduler(xtg_server* s) {
                 it = s->pending.erase(it);
             }
             if (!admitted.empty()) s->st.waves++;
+            // nothing dispatched is still running: forming groups need not wait
+            idle = s->inflight - (int64_t)(n_forming + admitted.size()) <= 0 || s->stop;
         }
         for (Unit* u : done) {
             if (u->batch) xtg_batch_destroy(u->batch);
             delete u;
         }
-        if (!admitted.empty()) hand_out(s, admitted);
+        // batchable requests join their shape's forming group; the rest go out now
+        std::vector<Req*> now_out;
+        for (Req* r : admitted) {
+            if (r->batchable && window.count() > 0) {
+                forming[r->sig].push_back(r);
+                ++n_forming;
+            } else {
+                now_out.push_back(r);
+            }
+        }
+        const auto now = Clock::now();
+        for (auto it = forming.begin(); it != forming.end();) {
+            if (idle || it->second.size() >= max_group || now - it->second[0]->t_submit >= window) {
+                n_forming -= it->second.size();
+                now_out.insert(now_out.end(), it->second.begin(), it->second.end());
+                it = forming.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        if (!now_out.empty()) hand_out(s, now_out);
     }
 }
 
