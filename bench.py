@@ -1569,6 +1569,133 @@ def run_c4(args):
     return 0
 
 
+CHUNK_WORKLOAD = ("chunked arrays: x float32 (256,512,1024) N(0,1) seed 1 as xt::chunked_array in chunks "
+                  "(64,256,1024) and, with edge chunks, (100,200,1000); a = x*2+1 into the chunks, "
+                  "b = a read back dense, sum(a, {2}), sum(a)")
+
+
+def run_chunked(args):
+    """Chunked arrays (xt::xchunked_array) over device chunks: assignment of
+    an expression into every chunk (one K12 launch), reading the chunked
+    array into a dense one (K12), sum over the last axis and the full sum
+    (per-chunk reductions merged in grid order).  Chunk shapes: whole chunks
+    (64, 256, 1024) = 8 chunks of 64 MiB, and (100, 200, 1000) = 3 x 3 x 2
+    chunks of 80 MB with edge chunks on every axis.  Algorithmic bytes: the
+    array's 512 MiB read and 512 MiB written for the assignment and the
+    read-back; 512 MiB read (+ the result) for the sums.  CPU baseline: the
+    compiled port of the reference's chunk-by-chunk assignment, element-wise
+    read-back and lazy sum over the last axis (oracle/xt_baseline.c
+    bl_chunked_*, pinned to the oracle)."""
+    import xtensor_gb300 as xg
+    from xtensor_gb300._ffi import check
+    from xtensor_gb300.chunked import ChunkedArray, chunked_reduce
+    from xtensor_gb300.device import DeviceArray
+    xg.init(0)
+    lib = xg.lib()
+    g = np.random.default_rng(1)
+    x = g.standard_normal(SHAPE, dtype=np.float32)
+    dx = DeviceArray.from_numpy(x)
+    nb = x.nbytes
+    peak, peak_kind = peaks()
+    res = {}
+    calls = []
+    for tag, cs in (("whole", (64, 256, 1024)), ("edges", (100, 200, 1000))):
+        a = ChunkedArray(SHAPE, cs, "float32")
+        dense = DeviceArray.empty(SHAPE, "float32")
+        s2 = DeviceArray.empty(SHAPE[:2], "float32")
+        s0 = DeviceArray.empty((), "float32")
+        calls += [
+            (f"assign_{tag}", 2 * nb, lambda a=a: a.assign(dx * 2.0 + 1.0)),
+            (f"read_{tag}", 2 * nb, lambda a=a, d=dense: a.to_device(d)),
+            (f"sum2_{tag}", nb + s2.nbytes, lambda a=a, o=s2: chunked_reduce("sum", a, axes=[2], out=o)),
+            (f"sum_{tag}", nb + 4, lambda a=a, o=s0: chunked_reduce("sum", a, out=o)),
+        ]
+        res[tag] = (a, dense, s2, s0, cs)
+    for _ in range(max(3, args.warmup)):
+        for _, _, fn in calls:
+            fn()
+    check(lib.xtg_device_sync())
+    K = args.steps
+    evs = [ev_create(lib, len(calls) + 1) for _ in range(K)]
+    l0 = xg.jit_stats()["launches"]
+    for k in range(K):
+        for i, (_, _, fn) in enumerate(calls):
+            check(lib.xtg_event_record(evs[k][i], None))
+            fn()
+        check(lib.xtg_event_record(evs[k][len(calls)], None))
+    check(lib.xtg_device_sync())
+    l1 = xg.jit_stats()["launches"]
+    per = [sum(ev_ms(lib, evs[k][i], evs[k][i + 1]) for k in range(K)) / K for i in range(len(calls))]
+    per_kernel = {nm: {"ms": round(t, 4), "GB/s": round(b / (t / 1e3) / 1e9, 1), "frac": round(b / (t / 1e3) / 1e9 / peak, 3)}
+                  for (nm, b, _), t in zip(calls, per)}
+    total = sum(b for _, b, _ in calls)
+    ms = sum(per)
+    dom = max(per_kernel, key=lambda k: per_kernel[k]["ms"])
+    # parity against an FP64 evaluation of the same values (the port is
+    # checked against the oracle by the tests)
+    parity = {}
+    want = x * np.float32(2.0) + np.float32(1.0)
+    wd = want.astype(np.float64)
+    sa2 = np.abs(wd).sum(2)
+    for tag, (a, dense, s2, s0, cs) in res.items():
+        parity[tag] = {"read_back_bit_exact": bool(np.array_equal(dense.to_numpy(), want)),
+                       "sum2_max_err_over_sum_abs": float(np.max(np.abs(s2.to_numpy() - wd.sum(2)) / sa2)),
+                       "sum_err_over_sum_abs": float(abs(float(s0.to_numpy()) - float(wd.sum())) / float(np.abs(wd).sum()))}
+    parity["ok"] = all(v["read_back_bit_exact"] and v["sum2_max_err_over_sum_abs"] <= 1e-6 and
+                       v["sum_err_over_sum_abs"] <= 1e-6 for v in parity.values())
+    cpu = None
+    if not args.no_cpu:
+        from oracle.oracle import SO, lib as olib
+        olib()
+        L = C.CDLL(str(SO))
+        PP = C.POINTER(C.c_void_p)
+        L.bl_chunked_axpb_f32.argtypes = [C.c_void_p, PP, C.c_void_p, C.c_void_p, C.c_float, C.c_float]
+        L.bl_chunked_read_f32.argtypes = [PP, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.bl_chunked_sum2_f32.argtypes = [PP, C.c_void_p, C.c_void_p, C.c_void_p]
+        cs = (64, 256, 1024)
+        n = int(np.prod([(d + c - 1) // c for d, c in zip(SHAPE, cs)]))
+        chunks = [np.empty(cs, np.float32) for _ in range(n)]
+        tab = (C.c_void_p * n)(*[c.ctypes.data for c in chunks])
+        d = np.array(SHAPE, np.int64)
+        c = np.array(cs, np.int64)
+        dense_h = np.empty(SHAPE, np.float32)
+        s2_h = np.empty(SHAPE[:2], np.float32)
+        t0 = time.perf_counter()
+        L.bl_chunked_axpb_f32(x.ctypes.data, tab, d.ctypes.data, c.ctypes.data, 2.0, 1.0)
+        L.bl_chunked_read_f32(tab, dense_h.ctypes.data, d.ctypes.data, c.ctypes.data)
+        L.bl_chunked_sum2_f32(tab, s2_h.ctypes.data, d.ctypes.data, c.ctypes.data)
+        t1 = time.perf_counter()
+        cb = 2 * nb + 2 * nb + nb
+        cpu = {"value": round(cb / (t1 - t0) / 1e9, 3), "unit": "GB/s", "cores": cores(), "kind": "port",
+               "sample": f"assignment, read-back and sum over axis 2 in chunks {cs}, once (compiled port of the "
+                         f"reference's chunk-by-chunk assignment and element-wise access, OpenMP {cores()} threads)"}
+    line = {
+        "metric": "HBM GB/s (frac of roofline) of chunked-array assignment, read-back and reductions", "unit": "GB/s",
+        "value": round(total / (ms / 1e3) / 1e9, 3), "higher_is_better": True, "n_gpus": 1, "steps": K,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": CHUNK_WORKLOAD, "algorithmic_bytes_per_step": total,
+                                        "l2": "512 MiB arrays, larger than L2: no flush"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": per_kernel[dom]["GB/s"], "peak": peak, "unit": "GB/s",
+                     "frac": per_kernel[dom]["frac"], "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "per_kernel": per_kernel, "parity": parity, "cpu_baseline": cpu, "e2e": None,
+        "gpu_launches": int(l1 - l0),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_section(args, name):
+    """One sub-result of the default line as its own line (profiling runs)."""
+    import xtensor_gb300 as xg
+    from xtensor_gb300._ffi import check
+    xg.init(0)
+    st = C.c_void_p()
+    check(xg.lib().xtg_stream_create(C.byref(st)))
+    r = (c0_section if name == "c0" else c2_section)(args, st.value)
+    print(json.dumps({"metric": METRIC, "workload": name, **r}))
+    return 0
+
+
 def _npy_dir(need: int) -> str:
     import shutil
     import tempfile
@@ -1865,7 +1992,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--shape", default=None, help="profiling only: d0,d1,d2 instead of 256,512,1024")
-    ap.add_argument("--workload", default="c1", choices=["c1", "c3", "c4", "scan", "views", "npy", "blockwise"],
+    ap.add_argument("--workload", default="c1",
+                    choices=["c1", "c0", "c2", "c3", "c4", "scan", "views", "npy", "blockwise", "chunked"],
                     help="c1: strided/axis work (default, the headline); c3: batching of uneven instances; "
                          "c4: served Poisson request mix; scan: cumsum along rows, columns and flattened")
     ap.add_argument("--instances", type=int, default=4096)
@@ -1900,6 +2028,10 @@ def main():
         return run_npy(args)
     if args.workload == "blockwise":
         return run_blockwise(args)
+    if args.workload == "chunked":
+        return run_chunked(args)
+    if args.workload in ("c0", "c2"):
+        return run_section(args, args.workload)
     return run_gpu(args)
 
 

@@ -53,6 +53,8 @@
  *                       order, the mean divided at the end
  *                       (xblockwise_reducer.hpp:129-194, functors :38-160);
  *                       OpenMP over independent outputs.
+ *   bl_chunked_*        chunked arrays of rank 3: assignment chunk by chunk,
+ *                       reading, and sum over the last axis (below).
  *   bl_npy_load         xt::load_npy<T>(filename): read the magic and version,
  *                       the header length and the header, take the word
  *                       size from 'descr' and the shape from 'shape', then
@@ -326,5 +328,61 @@ void bl_blockwise_mean_12_f32(const float* x, double* out, int64_t d0, int64_t d
                 first = 0;
             }
         out[i] = acc / (double)(d1 * d2);
+    }
+}
+
+/* Chunked arrays of rank 3 (shape d, chunk shape c, grid g = ceil(d / c)),
+ * chunks row-major of c elements, given as an array of chunk pointers in the
+ * grid's row-major order:
+ *   bl_chunked_axpb_f32   a = x * s + t into the chunks, chunk by chunk in
+ *                         grid order (xchunked_semantic::assign_xexpression,
+ *                         chunk/xchunked_assign.hpp:200-219), each chunk's
+ *                         valid region only; OpenMP over chunks;
+ *   bl_chunked_read_f32   the dense array of a chunked one (reading it
+ *                         element by element through the chunk index,
+ *                         xchunked_array.hpp:440-460, 640-646);
+ *   bl_chunked_sum2_f32   xt::sum(a, {2}): per output a sequential float fold
+ *                         over the last axis through the chunk index (the
+ *                         lazy reducer, xreducer.hpp:1801-1828); OpenMP over
+ *                         outputs. */
+static inline const float* bl_chunk_at(float* const* chunks, const int64_t* d, const int64_t* c, int64_t i, int64_t j,
+                                       int64_t k) {
+    const int64_t g1 = (d[1] + c[1] - 1) / c[1], g2 = (d[2] + c[2] - 1) / c[2];
+    const int64_t ci = ((i / c[0]) * g1 + j / c[1]) * g2 + k / c[2];
+    return chunks[ci] + ((i % c[0]) * c[1] + j % c[1]) * c[2] + k % c[2];
+}
+
+void bl_chunked_axpb_f32(const float* x, float* const* chunks, const int64_t* d, const int64_t* c, float s, float t) {
+    const int64_t g0 = (d[0] + c[0] - 1) / c[0], g1 = (d[1] + c[1] - 1) / c[1], g2 = (d[2] + c[2] - 1) / c[2];
+    _Pragma("omp parallel for schedule(dynamic)")
+    for (int64_t ci = 0; ci < g0 * g1 * g2; ++ci) {
+        const int64_t a = ci / (g1 * g2), b = (ci / g2) % g1, e = ci % g2;
+        const int64_t e0 = d[0] - a * c[0] < c[0] ? d[0] - a * c[0] : c[0];
+        const int64_t e1 = d[1] - b * c[1] < c[1] ? d[1] - b * c[1] : c[1];
+        const int64_t e2 = d[2] - e * c[2] < c[2] ? d[2] - e * c[2] : c[2];
+        float* ch = chunks[ci];
+        for (int64_t i = 0; i < e0; ++i)
+            for (int64_t j = 0; j < e1; ++j) {
+                const float* xr = x + ((a * c[0] + i) * d[1] + b * c[1] + j) * d[2] + e * c[2];
+                float* cr = ch + (i * c[1] + j) * c[2];
+                for (int64_t k = 0; k < e2; ++k) cr[k] = xr[k] * s + t;
+            }
+    }
+}
+
+void bl_chunked_read_f32(float* const* chunks, float* out, const int64_t* d, const int64_t* c) {
+    _Pragma("omp parallel for schedule(static)")
+    for (int64_t i = 0; i < d[0]; ++i)
+        for (int64_t j = 0; j < d[1]; ++j)
+            for (int64_t k = 0; k < d[2]; ++k) out[(i * d[1] + j) * d[2] + k] = *bl_chunk_at(chunks, d, c, i, j, k);
+}
+
+void bl_chunked_sum2_f32(float* const* chunks, float* out, const int64_t* d, const int64_t* c) {
+    _Pragma("omp parallel for schedule(static)")
+    for (int64_t r = 0; r < d[0] * d[1]; ++r) {
+        const int64_t i = r / d[1], j = r % d[1];
+        float s = 0.f;
+        for (int64_t k = 0; k < d[2]; ++k) s = s + *bl_chunk_at(chunks, d, c, i, j, k);
+        out[r] = s;
     }
 }

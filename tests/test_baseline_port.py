@@ -16,7 +16,9 @@ compared with the oracle's restatement of the reference
   * full float32 / int32 -> int64 sums: bit-exact (sequential folds);
   * the precision workload's sum / mean / variance / norm_l2 of float32
     and bfloat16 arrays: bit-exact;
-  * cumsum along each axis and flattened: bit-exact.
+  * cumsum along each axis and flattened: bit-exact;
+  * chunked arrays (assignment chunk by chunk, reading, sum over the last
+    axis): bit-exact, the padding of edge chunks untouched.
 """
 from __future__ import annotations
 
@@ -151,3 +153,32 @@ def test_port_precision_stats_equal_oracle(dt, n):
         want = ref.astype(np.float32 if op == "sum" else np.float64)
         got = np.asarray(got, dtype=want.dtype)
         assert got.tobytes() == want.tobytes(), (op, dt, n, got, want)
+
+
+@pytest.mark.parametrize("shape,cs", [((9, 10, 11), (4, 3, 5)), ((8, 6, 16), (4, 3, 8)), ((5, 7, 3), (8, 8, 8))])
+def test_port_chunked_equals_oracle(shape, cs):
+    from oracle import chunked as OC
+    O.lib()
+    L = C.CDLL(str(O.SO))
+    PP = C.POINTER(C.c_void_p)
+    L.bl_chunked_axpb_f32.argtypes = [P, PP, P, P, C.c_float, C.c_float]
+    L.bl_chunked_read_f32.argtypes = [PP, P, P, P]
+    L.bl_chunked_sum2_f32.argtypes = [PP, P, P, P]
+    g = np.random.default_rng(71)
+    x = g.standard_normal(shape).astype(np.float32)
+    n = int(np.prod(OC.grid_shape(shape, cs)))
+    chunks = [np.full(cs, -5.0, np.float32) for _ in range(n)]
+    tab = (C.c_void_p * n)(*[c.ctypes.data for c in chunks])
+    d = np.array(shape, np.int64)
+    c = np.array(cs, np.int64)
+    L.bl_chunked_axpb_f32(ptr(x), tab, ptr(d), ptr(c), 2.0, 1.0)
+    vals = O.assign(HostArray(x) * np.float32(2.0) + np.float32(1.0))
+    want = OC.assign_chunks([np.full(cs, -5.0, np.float32) for _ in range(n)], vals, cs)
+    for u, v in zip(chunks, want):
+        assert u.tobytes() == v.tobytes()  # the padding of edge chunks untouched
+    dense = np.empty(shape, np.float32)
+    L.bl_chunked_read_f32(tab, ptr(dense), ptr(d), ptr(c))
+    np.testing.assert_array_equal(dense, vals)
+    s2 = np.empty(shape[:2], np.float32)
+    L.bl_chunked_sum2_f32(tab, ptr(s2), ptr(d), ptr(c))
+    np.testing.assert_array_equal(s2, O.reduce("sum", HostArray(vals), [2]))
