@@ -105,8 +105,12 @@ def test_chunked_view_assign():
 
 
 # ---------------------------------------------------------------- parity with the oracle
+# chunk classes per case: 8 (edges along three dims, scalar), 8, 1 (whole
+# chunks, vectors), 2 (an edge of 40 along the vectorised dim), 8, 1 (one chunk
+# larger than the array), 4 (vectorised, with edges), 16 (more classes than one
+# launch holds: padded chunks with extent tests)
 CASES = [((37, 70, 45), (8, 16, 16)), ((37, 70, 45), (5, 9, 7)), ((64, 128), (16, 64)), ((1000,), (96,)),
-         ((3, 5, 7, 9), (2, 2, 4, 3)), ((8, 8), (16, 16))]
+         ((3, 5, 7, 9), (2, 2, 4, 3)), ((8, 8), (16, 16)), ((50, 1000), (16, 96)), ((3, 5, 7, 9, 11), (2, 2, 4, 3, 5))]
 
 
 @pytest.mark.parametrize("shape,cs", CASES)
@@ -158,10 +162,23 @@ def test_reading_into_a_strided_destination():
     np.testing.assert_array_equal(big.to_numpy()[1::2], 0)
 
 
+def separate_chunks(x, cs):
+    """A chunked array whose chunks are separate allocations (not at equal
+    distances: the reductions take the chunk-by-chunk path)."""
+    from xtensor_gb300.chunked import grid_shape
+    import math
+    n = math.prod(grid_shape(x.shape, cs))
+    chunks = [DeviceArray.empty(cs, x.dtype) for _ in range(n)]
+    a = ChunkedArray(x.shape, cs, x.dtype, chunks=chunks)
+    a.assign(DeviceArray.from_numpy(x))
+    return a
+
+
+@pytest.mark.parametrize("alloc", ["slab", "separate"])
 @pytest.mark.parametrize("op", ["sum", "prod", "amax", "amin", "mean", "variance", "stddev", "norm_l1", "norm_l2",
                                 "norm_linf", "norm_sq"])
 @pytest.mark.parametrize("axes,kd", [(None, False), ([0], False), ([1, 2], False), ([0, 2], True), ([2], True)])
-def test_reductions_match_oracle(op, axes, kd):
+def test_reductions_match_oracle(op, axes, kd, alloc):
     xg.init(0)
     g = np.random.default_rng(63)
     shape, cs = (13, 22, 17), (4, 8, 5)
@@ -170,7 +187,7 @@ def test_reductions_match_oracle(op, axes, kd):
     if op == "prod":
         xf = 1 + 0.01 * xf
     for x in (xi, xf):
-        a = ChunkedArray.from_numpy(x, cs)
+        a = ChunkedArray.from_numpy(x, cs) if alloc == "slab" else separate_chunks(x, cs)
         got = chunked_reduce(op, a, axes=axes, keep_dims=kd).to_numpy()
         ref = O.reduce(op, HostArray(x), axes=axes, keep_dims=kd)
         assert got.shape == ref.shape and got.dtype == ref.dtype

@@ -3,8 +3,9 @@
 (chunk/xchunked_view.hpp), over the C ABI's xtg_chunked_* entry points.
 
 A ChunkedArray cuts its shape into a grid of ceil(shape / chunk_shape)
-chunks, each its own device buffer of chunk_shape elements; the last chunk
-along a dimension ends inside its buffer (padding), as in the reference.  It
+chunks, each a device buffer of chunk_shape elements (one allocation holds
+them all, at equal distances); the last chunk along a dimension ends inside
+its buffer (padding), as in the reference.  It
 is an expression leaf like DeviceArray, so `a.assign(a + a)`, `a += 2.0`,
 `a.assign(b * 3)` and reductions work on it; chunked operands of one
 assignment must share the destination's grid.
@@ -65,8 +66,15 @@ class ChunkedArray(ExprOps):
         self.dtype = dtype_code(dtype)
         self.grid_shape = grid_shape(self.shape, self.chunk_shape)
         n = math.prod(self.grid_shape)
-        self.chunks = list(chunks) if chunks is not None else \
-            [DeviceArray.empty(self.chunk_shape, self.dtype, stream) for _ in range(n)]
+        if chunks is None:
+            # one slab, chunks at a fixed 256-byte aligned distance: the
+            # library then reduces a class of equal chunks as one strided array
+            es = ITEMSIZE[self.dtype]
+            dist = -(-max(math.prod(self.chunk_shape) * es, 1) // 256) * 256
+            self._slab = DeviceArray.empty((n * dist // es,), self.dtype, stream)
+            chunks = [DeviceArray(self.chunk_shape, self.dtype, self._slab.ptr + i * dist, base=self._slab)
+                      for i in range(n)]
+        self.chunks = list(chunks)
         if len(self.chunks) != n:
             raise ValueError("one chunk per grid cell")
         self._ptrs = (C.c_void_p * max(n, 1))(*[c.ptr for c in self.chunks])

@@ -501,6 +501,24 @@ xtg_status blockwise_impl(const xtg_array* in, const int64_t* block, const xtg_r
     return XTG_OK;
 }
 
+// The reducer's last step over the merged block results (mean: / count,
+// stddev: sqrt).
+static xtg_status chunked_finish(const Plan& P, const xtg_chunked* src, const std::vector<bool>& red,
+                                 const xtg_array& out, cudaStream_t stream) {
+    if (P.fin == F_NONE) return XTG_OK;
+    Ex f;
+    f.leaf(out);
+    if (P.fin == F_DIV) {
+        int64_t factor = 1;
+        for (int d = 0; d < src->rank; ++d)
+            if (red[(size_t)d]) factor *= src->shape[d];
+        f.scalar(P.out_dtype, (double)factor).op(XTG_OP_DIV);
+    } else if (P.fin == F_SQRT) {
+        f.op(XTG_OP_SQRT);
+    }
+    return assign_expr(f, out, stream);
+}
+
 // Reductions of a chunked array: each chunk's valid region (a view of its
 // buffer) is one block.  The grid is walked with its reduced dims outside and
 // its kept dims inside, so that every output block receives its chunks in the
@@ -564,6 +582,114 @@ xtg_status chunked_reduce_impl(const xtg_chunked* src, const xtg_reduce_desc* rd
 
     Resources R;
     R.stream = stream;
+
+    // Chunks at equal distances in memory (a chunked array allocated as one
+    // slab): the array is a strided array of rank 2 * rank, dims (chunk
+    // index, position in the chunk) per dim, and a class of chunks with equal
+    // valid extents (per dim: the full chunks, the edge chunk) is a box of
+    // it.  Each class is then ONE reduction (its dims pair up: both reduced or
+    // both kept), merged over the classes of the reduced dims in order.
+    const int es = dt(src->dtype).size;
+    const int64_t celems = [&] {
+        int64_t n = 1;
+        for (int d = 0; d < rank; ++d) n *= G.cs[d];
+        return n;
+    }();
+    int64_t S = celems * es;
+    bool spaced = rank >= 1 && 2 * rank <= XTG_MAX_RANK;
+    if (spaced && G.n > 1) {
+        S = (int64_t)((const char*)src->chunks[1] - (const char*)src->chunks[0]);
+        spaced = S >= celems * es && S % es == 0;
+        for (int64_t i = 2; spaced && i < G.n; ++i)
+            spaced = (const char*)src->chunks[i] == (const char*)src->chunks[0] + i * S;
+    }
+    if (spaced) {
+        struct Kind { int64_t lo, cnt, ext; };
+        std::vector<Kind> kinds[XTG_MAX_RANK];
+        for (int d = 0; d < rank; ++d) {
+            if (G.grid[d] == 1) kinds[d] = {{0, 1, G.shape[d]}};
+            else if (G.shape[d] % G.cs[d] == 0) kinds[d] = {{0, G.grid[d], G.cs[d]}};
+            else kinds[d] = {{0, G.grid[d] - 1, G.cs[d]}, {G.grid[d] - 1, 1, G.shape[d] - (G.grid[d] - 1) * G.cs[d]}};
+        }
+        int64_t gst[XTG_MAX_RANK];
+        for (int d = rank - 1, g = 1; d >= 0; --d) {
+            gst[d] = g;
+            g *= (int)G.grid[d];
+        }
+        int64_t n_rp = 1, n_kp = 1;
+        for (int d : rdims) n_rp *= (int64_t)kinds[d].size();
+        for (int d : kdims) n_kp *= (int64_t)kinds[d].size();
+        const bool var_s = P.merge == M_VAR && n_rp > 1;
+        xtg_array part = dense_like(*out, P.part_dtype, nullptr), mean_a = dense_like(*out, P.out_dtype, nullptr);
+        xtg_array mean_b = dense_like(*out, P.out_dtype, nullptr);
+        if (n_rp > 1) {
+            XTG_TRY(R.alloc(&part.data, (size_t)on * dt(P.part_dtype).size));
+            if (var_s) {
+                XTG_TRY(R.alloc(&mean_a.data, (size_t)on * dt(P.out_dtype).size));
+                XTG_TRY(R.alloc(&mean_b.data, (size_t)on * dt(P.out_dtype).size));
+            }
+        }
+        xtg_reduce_desc prd2 = prd;
+        prd2.keep_dims = 0;
+        prd2.n_axes = 0;
+        for (int d : rdims) {
+            prd2.axes[prd2.n_axes++] = 2 * d;
+            prd2.axes[prd2.n_axes++] = 2 * d + 1;
+        }
+        const Kind* sel[XTG_MAX_RANK];
+        // the output-shaped array `a` over the kept dims' kinds: dims
+        // (chunks, extent) per kept dim
+        auto out_view = [&](const xtg_array& a) {
+            xtg_array v = a;
+            v.rank = 0;
+            int64_t off = 0;
+            for (int d : kdims) {
+                const int64_t st = a.strides[oax[d]];
+                v.shape[v.rank] = sel[d]->cnt;
+                v.strides[v.rank++] = G.cs[d] * st;
+                v.shape[v.rank] = sel[d]->ext;
+                v.strides[v.rank++] = st;
+                off += sel[d]->lo * G.cs[d] * st;
+            }
+            if (a.data) v.data = (char*)a.data + off * dt(a.dtype).size;
+            return v;
+        };
+        double n_acc2 = 0.0;
+        for (int64_t rp = 0; rp < n_rp; ++rp) {
+            int64_t q = rp;
+            for (int i = (int)rdims.size() - 1; i >= 0; --i) {
+                const int d = rdims[(size_t)i];
+                sel[d] = &kinds[d][(size_t)(q % (int64_t)kinds[d].size())];
+                q /= (int64_t)kinds[d].size();
+            }
+            double n_b = 1.0;
+            for (int d : rdims) n_b *= (double)(sel[d]->cnt * sel[d]->ext);
+            for (int64_t kp = 0; kp < n_kp; ++kp) {
+                int64_t k = kp;
+                for (int i = (int)kdims.size() - 1; i >= 0; --i) {
+                    const int d = kdims[(size_t)i];
+                    sel[d] = &kinds[d][(size_t)(k % (int64_t)kinds[d].size())];
+                    k /= (int64_t)kinds[d].size();
+                }
+                xtg_array slab = whole;
+                slab.rank = 2 * rank;
+                int64_t first = 0;
+                for (int d = 0; d < rank; ++d) {
+                    slab.shape[2 * d] = sel[d]->cnt;
+                    slab.strides[2 * d] = gst[d] * (S / es);
+                    slab.shape[2 * d + 1] = sel[d]->ext;
+                    slab.strides[2 * d + 1] = cst[d];
+                    first += sel[d]->lo * gst[d];
+                }
+                slab.data = (void*)((const char*)src->chunks[0] + first * S);
+                XTG_TRY(fold_partial(P, prd2, slab, 0.0, rp == 0, out_view(*out), out_view(part), out_view(mean_a),
+                                     out_view(mean_b), var_s, n_acc2, n_b, R, stream));
+            }
+            n_acc2 = rp == 0 ? n_b : n_acc2 + n_b;
+        }
+        return chunked_finish(P, src, red, *out, stream);
+    }
+
     const bool var_state = P.merge == M_VAR && n_rcomb > 1;
     xtg_array part = dense_like(*out, P.part_dtype, nullptr), mean_a = dense_like(*out, P.out_dtype, nullptr);
     xtg_array mean_b = dense_like(*out, P.out_dtype, nullptr);
@@ -623,20 +749,7 @@ xtg_status chunked_reduce_impl(const xtg_chunked* src, const xtg_reduce_desc* rd
         }
         n_acc = rc == 0 ? n_b : n_acc + n_b;
     }
-    if (P.fin != F_NONE) {
-        Ex f;
-        f.leaf(*out);
-        if (P.fin == F_DIV) {
-            int64_t factor = 1;
-            for (int d = 0; d < rank; ++d)
-                if (red[d]) factor *= src->shape[d];
-            f.scalar(P.out_dtype, (double)factor).op(XTG_OP_DIV);
-        } else if (P.fin == F_SQRT) {
-            f.op(XTG_OP_SQRT);
-        }
-        XTG_TRY(assign_expr(f, *out, stream));
-    }
-    return XTG_OK;
+    return chunked_finish(P, src, red, *out, stream);
 }
 
 }  // namespace

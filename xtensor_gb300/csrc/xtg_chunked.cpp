@@ -13,10 +13,13 @@
 // Assignment walks the chunks in the grid's row-major order and assigns the
 // matching region of the expression into each (assign_xexpression,
 // xchunked_assign.hpp:200-219).  Here that is ONE launch of K12 over
-// (chunk, vector inside the chunk) for the whole grid: per chunk a table
-// entry holds the destination chunk's address, each leaf's address at the
-// chunk's origin (a dense leaf) or its own chunk (a chunked leaf with the same
-// grid), and the chunk's valid extents, so edge chunks skip their padding.
+// (chunk, vector inside the chunk's valid region) for the whole grid: per
+// chunk a table entry holds the destination chunk's address, each leaf's
+// address at the chunk's origin (a dense leaf) or its own chunk (a chunked
+// leaf with the same grid), and the chunk's valid extents.  Chunks of equal
+// valid extents form a class (at most 2 per dim: full and edge), and the
+// table is ordered by class, so the kernel decodes positions inside valid
+// regions only and edge chunks cost no idle threads.
 // The same kernel copies a chunked array into a dense destination (reading it:
 // `noalias(b) = a`, `as_chunked(b, cs) = a`).  Reductions run per chunk
 // through the blockwise machinery (xtg_blockwise.cpp).
@@ -106,9 +109,11 @@ static xtg_status run_chunks(const Tree& t, const std::vector<const xtg_chunked*
         if (kinds[l] == 0) maxsz = std::max(maxsz, dt(t.leaves[l].dtype).size);
     }
     const int okind = os[R - 1] == 1 ? 0 : 2;
+    // valid extent of the edge chunk along the innermost dim
+    const int64_t edge_inner = G.shape[R - 1] - (G.grid[R - 1] - 1) * G.cs[R - 1];
     auto vec_ok = [&](int v) {
         if (v == 1) return true;
-        if (G.cs[R - 1] % v || G.shape[R - 1] % G.cs[R - 1]) return false;
+        if (G.cs[R - 1] % v || edge_inner % v) return false;
         auto strides_ok = [&](const std::array<int64_t, XTG_MAX_RANK>& st) {
             for (int d = 0; d + 1 < R; ++d)
                 if (st[d] % v) return false;
@@ -140,10 +145,40 @@ static xtg_status run_chunks(const Tree& t, const std::vector<const xtg_chunked*
     if (vec < 1) vec = 1;
     while (vec > 1 && !vec_ok(vec)) vec >>= 1;
 
-    // the chunk table
-    std::vector<xtg::ChunkEntry> tab((size_t)G.n);
+    // classes of equal valid extents: per dim, full chunks and (when the
+    // shape does not divide) the edge chunk; class id = mixed-radix digits
+    int nkind[XTG_MAX_RANK];
+    int n_cls = 1;
+    for (int d = 0; d < R; ++d) {
+        nkind[d] = (G.grid[d] > 1 && G.shape[d] % G.cs[d]) ? 2 : 1;
+        n_cls *= nkind[d];
+    }
+    const bool pad = n_cls > XTG_KCHUNK_CLS;
+    auto class_of = [&](const int64_t* gc) {
+        int c = 0;
+        for (int d = 0; d < R; ++d) c = c * nkind[d] + (nkind[d] == 2 && gc[d] == G.grid[d] - 1 ? 1 : 0);
+        return pad ? 0 : c;
+    };
+    if (pad) n_cls = 1;
+    std::vector<int64_t> cls_count((size_t)n_cls, 0), cls_first((size_t)n_cls, 0);
+    std::vector<std::array<int64_t, XTG_MAX_RANK>> cls_ext((size_t)n_cls);
+    std::vector<int> cls_of((size_t)G.n);
     for (int64_t i = 0; i < G.n; ++i) {
-        xtg::ChunkEntry& e = tab[(size_t)i];
+        int64_t gc[XTG_MAX_RANK];
+        chunk_coords(G, i, gc);
+        const int c = class_of(gc);
+        cls_of[(size_t)i] = c;
+        if (cls_count[(size_t)c]++ == 0)
+            for (int d = 0; d < R; ++d)
+                cls_ext[(size_t)c][d] = pad ? G.cs[d] : std::min(G.cs[d], G.shape[d] - gc[d] * G.cs[d]);
+    }
+    for (int c = 1; c < n_cls; ++c) cls_first[(size_t)c] = cls_first[(size_t)c - 1] + cls_count[(size_t)c - 1];
+
+    // the chunk table, class by class (grid row-major inside a class)
+    std::vector<xtg::ChunkEntry> tab((size_t)G.n);
+    std::vector<int64_t> fill(cls_first);
+    for (int64_t i = 0; i < G.n; ++i) {
+        xtg::ChunkEntry& e = tab[(size_t)fill[(size_t)cls_of[(size_t)i]]++];
         memset(&e, 0, sizeof e);
         int64_t gc[XTG_MAX_RANK];
         chunk_coords(G, i, gc);
@@ -179,16 +214,28 @@ static xtg_status run_chunks(const Tree& t, const std::vector<const xtg_chunked*
 
     xtg::ChunkParams p;
     memset(&p, 0, sizeof p);
-    int64_t nvec = 1;
-    for (int d = 0; d < R; ++d) {
-        p.sp.shape[d] = d == R - 1 ? G.cs[d] / vec : G.cs[d];
-        nvec *= p.sp.shape[d];
+    p.n_cls = n_cls;
+    int64_t total = 0, largest = 0;
+    for (int c = 0; c < n_cls; ++c) {
+        xtg::ChunkClass& K = p.cls[c];
+        int64_t nvec = 1;
+        for (int d = 0; d < R; ++d) {
+            K.sp.shape[d] = d == R - 1 ? cls_ext[(size_t)c][d] / vec : cls_ext[(size_t)c][d];
+            nvec *= K.sp.shape[d];
+        }
+        K.sp.nvec = nvec;
+        K.first = cls_first[(size_t)c];
+        K.count = cls_count[(size_t)c];
+        total += nvec * K.count;
+        largest = std::max<int64_t>(largest, nvec * K.count);
     }
-    p.sp.nvec = nvec;
-    const bool big = nvec > 0xFFFFFFF0ll;
+    const bool big = largest > (int64_t)0xFFFFFFF0ll;
     if (!big)
-        for (int d = 0; d < R; ++d) p.sp.fd[d] = make_fd((uint64_t)p.sp.shape[d]);
-    p.n_chunks = G.n;
+        for (int c = 0; c < n_cls; ++c) {
+            xtg::ChunkClass& K = p.cls[c];
+            for (int d = 0; d < R; ++d) K.sp.fd[d] = make_fd((uint64_t)K.sp.shape[d]);
+            K.fdn = make_fd((uint64_t)K.sp.nvec);
+        }
     p.tab = (const xtg::ChunkEntry*)dtab;
     for (int l = 0; l < NL; ++l)
         for (int d = 0; d < R; ++d) p.leaf_strides[l][d] = ls[l][d];
@@ -206,13 +253,14 @@ static xtg_status run_chunks(const Tree& t, const std::vector<const xtg_chunked*
     const int U = vec * maxsz >= 16 ? 4 : 8;
     const std::string name = "xtg::k_assign_chunks<" + tree_type(t, t.root, map) + ", " + ls_s + ", " +
                              dt(out_dtype).cname + ", " + std::to_string(okind) + ", " + std::to_string(vec) + ", " +
-                             std::to_string(R) + ", " + std::to_string(U) + ", " + (big ? "true" : "false") + ">";
+                             std::to_string(R) + ", " + std::to_string(U) + ", " + (big ? "true" : "false") + ", " +
+                             (pad ? "true" : "false") + ">";
     Kernel* k;
     xtg_status st = get_kernel(name, 256, &k);
     if (st == XTG_OK) {
         DeviceInfo* dev;
         ensure_device(&dev);
-        const int64_t need = (G.n * nvec + 256 * U - 1) / (256 * U);
+        const int64_t need = (total + 256 * U - 1) / (256 * U);
         const int64_t cap = (int64_t)k->max_blocks_per_sm * dev->sm_count;
         st = launch(k, (unsigned)std::max<int64_t>(1, std::min(need, cap)), 256, &p, stream);
     }

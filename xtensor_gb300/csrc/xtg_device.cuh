@@ -479,51 +479,66 @@ __global__ void __launch_bounds__(256) k_assign(const AssignParams p) {
 // ---------------------------------------------------------------------------
 // K12: assignment over a chunk grid (xchunked_semantic::assign_xexpression,
 // include/xtensor/chunk/xchunked_assign.hpp:200-219): every chunk's region of
-// the expression into the chunk, for all chunks in one launch.  Work item q
-// = (chunk, vector inside the chunk); elements outside the chunk's valid
-// extents (the padding of edge chunks) are neither read nor written.  With
-// VEC > 1 every chunk is whole along the innermost dim (the host checks), so
-// only the outer dims need the extent test.
-template <class Tree, class LS, class OutT, int OUTKIND, int VEC, int R, int U, bool BIG>
+// the expression into the chunk, for all chunks in one launch.  The chunks
+// come in classes of equal valid extents; the launch walks the classes in
+// turn, and inside a class work item q = (chunk, vector of the chunk's valid
+// region), so no thread lands in the padding of an edge chunk.  The host
+// picks VEC so that it divides every class's innermost extent.  PAD (more
+// classes than the parameter block holds): one class of padded chunks, the
+// entries' extents bound the elements.
+template <class Tree, class LS, class OutT, int OUTKIND, int VEC, int R, int U, bool BIG, bool PAD = false>
 __global__ void __launch_bounds__(256) k_assign_chunks(const ChunkParams p) {
     typedef typename LS::template R<VEC>::type RG;
     Ctx<0> c;
     c.scal = p.scal;
-    const i64 nv = p.sp.nvec;
-    const i64 total = p.n_chunks * nv;
     const i64 step = (i64)gridDim.x * blockDim.x * U;
-    for (i64 base = (i64)blockIdx.x * blockDim.x * U + threadIdx.x; base < total; base += step) {
-        RG rg[U];
-        i64 ooff[U];
-        void* optr[U];
-        bool ok[U];
+    for (int k = 0; k < p.n_cls; ++k) {
+        const ChunkClass& K = p.cls[k];
+        const i64 nv = K.sp.nvec;
+        const i64 total = K.count * nv;
+        for (i64 base = (i64)blockIdx.x * blockDim.x * U + threadIdx.x; base < total; base += step) {
+            RG rg[U];
+            i64 ooff[U];
+            void* optr[U];
+            bool ok[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const i64 q = base + (i64)u * blockDim.x;
-            ok[u] = false;
-            if (q < total) {
-                const i64 ch = q / nv;
-                i64 idx[R];
-                decode<R, VEC, BIG>(p.sp, q - ch * nv, idx);
-                const ChunkEntry& ent = p.tab[ch];
-                bool in = true;
+            for (int u = 0; u < U; ++u) {
+                const i64 q = base + (i64)u * blockDim.x;
+                ok[u] = false;
+                if (q < total) {
+                    i64 ch, loc;
+                    if (BIG) {
+                        ch = q / nv;
+                        loc = q - ch * nv;
+                    } else {
+                        const u32 qq = fdiv((u32)q, K.fdn);
+                        ch = qq;
+                        loc = (u32)q - qq * K.fdn.d;
+                    }
+                    i64 idx[R];
+                    decode<R, VEC, BIG>(K.sp, loc, idx);
+                    const ChunkEntry& ent = p.tab[K.first + ch];
+                    bool in = true;
+                    if (PAD) {
 #pragma unroll
-                for (int d = 0; d < R; ++d) in = in && idx[d] < ent.ext[d];
-                if (in) {
-                    ok[u] = true;
-                    LoadLeaves<LS>::template run<VEC, R>(rg[u], ent.leaf, p.leaf_strides, idx);
-                    ooff[u] = dot_idx<R>(idx, p.out_strides);
-                    optr[u] = ent.out;
+                        for (int d = 0; d < R; ++d) in = in && idx[d] < ent.ext[d];
+                    }
+                    if (in) {
+                        ok[u] = true;
+                        LoadLeaves<LS>::template run<VEC, R>(rg[u], ent.leaf, p.leaf_strides, idx);
+                        ooff[u] = dot_idx<R>(idx, p.out_strides);
+                        optr[u] = ent.out;
+                    }
                 }
             }
-        }
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            if (ok[u]) {
-                OutT v[VEC];
+            for (int u = 0; u < U; ++u) {
+                if (ok[u]) {
+                    OutT v[VEC];
 #pragma unroll
-                for (int j = 0; j < VEC; ++j) v[j] = cvt<OutT>(Tree::ev(rg[u], j, c));
-                st_out<OutT, OUTKIND, VEC>(reinterpret_cast<OutT*>(optr[u]), ooff[u], p.out_strides[R - 1], v);
+                    for (int j = 0; j < VEC; ++j) v[j] = cvt<OutT>(Tree::ev(rg[u], j, c));
+                    st_out<OutT, OUTKIND, VEC>(reinterpret_cast<OutT*>(optr[u]), ooff[u], p.out_strides[R - 1], v);
+                }
             }
         }
     }
@@ -593,6 +608,22 @@ XTG_DI void two_sum2(float2 a, float2 b, float2& s, float2& e) {
     const float2 bb = p_sub(s, a);
     e = p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb));
 }
+
+// Pairwise sums of N float32 values (a vector's elements): depth log2(N), the
+// rounding error of the whole sum at most ceil(log2 N) u sum |f| (u = 2^-24).
+template <int N> struct Pw {
+    static XTG_DI float sum(const float* f) { return Pw<N / 2>::sum(f) + Pw<N - N / 2>::sum(f + N / 2); }
+    // sum of squares: pairs as fma(a, a, b * b), then pairwise
+    static XTG_DI float sq(const float* f) { return Pw<N / 2>::sq(f) + Pw<N - N / 2>::sq(f + N / 2); }
+};
+template <> struct Pw<1> {
+    static XTG_DI float sum(const float* f) { return f[0]; }
+    static XTG_DI float sq(const float* f) { return f[0] * f[0]; }
+};
+template <> struct Pw<2> {
+    static XTG_DI float sum(const float* f) { return f[0] + f[1]; }
+    static XTG_DI float sq(const float* f) { return fmaf(f[0], f[0], f[1] * f[1]); }
+};
 
 // ---------------------------------------------------------------------------
 // Reduction accumulators.  Each is POD: init(p), add(x, pos), merge(other),
@@ -924,6 +955,8 @@ struct AccSumC2 {
     }
     template <class X> XTG_DI void add(X x, i64) { adds(cvt<float>(x)); }
     template <class X> XTG_DI void add2(X x0, X x1, i64) { addp(make_float2(cvt<float>(x0), cvt<float>(x1))); }
+    // a vector of N values: their pairwise sum, then one TwoSum
+    template <int N> XTG_DI void addblk(const float (&f)[N]) { adds(Pw<N>::sum(f)); }
 };
 template <int MODE> struct AccMom2 {
     float k;
@@ -960,6 +993,16 @@ template <int MODE> struct AccMom2 {
             s2.lo = p_sub(s2.lo, nqe);
         }
     }
+    // a vector of N values: pairwise sums of the deviations and of their
+    // squares (terms >= 0: relative error <= (ceil(log2 N) + 1) u), one
+    // TwoSum each into the states
+    template <int N> XTG_DI void addblk(const float (&f)[N]) {
+        float d[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) d[j] = f[j] - k;
+        s1.adds(Pw<N>::sum(d));
+        if (MODE != 0) s2.adds(Pw<N>::sq(d));
+    }
 };
 template <int NK> struct AccNormC2 {
     AccSumC2 a;
@@ -987,6 +1030,16 @@ template <int NK> struct AccNormC2 {
             a.lo = p_sub(a.lo, nqe);
         }
     }
+    template <int N> XTG_DI void addblk(const float (&f)[N]) {
+        if (NK == 1) {
+            float g[N];
+#pragma unroll
+            for (int j = 0; j < N; ++j) g[j] = fabsf(f[j]);
+            a.adds(Pw<N>::sum(g));
+        } else {
+            a.adds(Pw<N>::sq(f));
+        }
+    }
 };
 // The working form of a stored accumulator in the row pass.
 template <class A> struct Work { enum { packed = 0 }; typedef A T; };
@@ -997,6 +1050,19 @@ template <class A> struct HasAdd2 { enum { value = 0 }; };
 template <> struct HasAdd2<AccSumC2> { enum { value = 1 }; };
 template <int M> struct HasAdd2<AccMom2<M>> { enum { value = 1 }; };
 template <int NK> struct HasAdd2<AccNormC2<NK>> { enum { value = 1 }; };
+// Vector-blocked working forms: a vector's values are summed pairwise in
+// float32 and the block enters the double-float state by one TwoSum (about 5
+// FP32 operations per element for the moments instead of 19, 2 for sums of
+// 2-byte values instead of 7: those loops are FP32-pipe bound at HBM speed).
+// Used for the moments of variance / stddev (the squares' terms are >= 0) and
+// for sums, means and norms of 2-byte inputs (bfloat16 / float16: 8 or 11
+// significant bits, so a vector's pairwise sum is mostly exact); float32 sums,
+// means and norms keep a TwoSum per element.
+template <class W, class X> struct BlockAdd { enum { value = 0 }; };
+template <class X> struct BlockAdd<AccSumC2, X> { enum { value = sizeof(X) == 2 }; };
+template <int NK, class X> struct BlockAdd<AccNormC2<NK>, X> { enum { value = sizeof(X) == 2 }; };
+template <int M, class X> struct BlockAdd<AccMom2<M>, X> { enum { value = M != 0 || sizeof(X) == 2 }; };
+
 // One vector of tree values into an accumulator: in pairs where it takes
 // them, else element by element; p0 = the first element's position.
 template <bool PAIRS> struct AddVec {
@@ -1009,7 +1075,13 @@ template <bool PAIRS> struct AddVec {
 template <> struct AddVec<true> {
     template <int VEC, class Tree, class A, class RG, class C>
     static XTG_DI void run(A& a, const RG& rg, i64 p0, const C& c) {
-        if (VEC % 2 == 0) {
+        typedef decltype(Tree::ev(rg, 0, c)) X;
+        if constexpr (BlockAdd<A, X>::value != 0 && VEC > 1) {
+            float f[VEC];
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) f[j] = cvt<float>(Tree::ev(rg, j, c));
+            a.template addblk<VEC>(f);
+        } else if (VEC % 2 == 0) {
 #pragma unroll
             for (int j = 0; j < VEC; j += 2) a.add2(Tree::ev(rg, j, c), Tree::ev(rg, j + 1, c), p0 + j);
         } else {

@@ -49,10 +49,20 @@ struct ChunkEntry {
     void* out;
     i64 ext[XTG_KMAX_RANK];
 };
+// Chunks whose valid extents agree form a class (full chunks, the edge chunk
+// along some dims, ...); a class's chunks occupy entries [first, first +
+// count) of the table.  With PAD the launch has one class of padded chunks
+// and the entries' extents bound the elements.
+#define XTG_KCHUNK_CLS 8
+struct ChunkClass {
+    Space sp;          // one chunk of the class, innermost dim in vectors
+    FastDiv fdn;       // divisor sp.nvec (32-bit launches)
+    i64 first, count;
+};
 struct ChunkParams {
-    Space sp;                 // one chunk, innermost dim in vectors
-    i64 n_chunks;
-    const ChunkEntry* tab;    // n_chunks entries, chunk-grid row-major
+    ChunkClass cls[XTG_KCHUNK_CLS];
+    int n_cls;
+    const ChunkEntry* tab;
     i64 leaf_strides[XTG_KMAX_LEAVES][XTG_KMAX_RANK];  // within a chunk
     i64 out_strides[XTG_KMAX_RANK];
     Scalars scal;
