@@ -1577,15 +1577,16 @@ CHUNK_WORKLOAD = ("chunked arrays: x float32 (256,512,1024) N(0,1) seed 1 as xt:
 def run_chunked(args):
     """Chunked arrays (xt::xchunked_array) over device chunks: assignment of
     an expression into every chunk (one K12 launch), reading the chunked
-    array into a dense one (K12), sum over the last axis and the full sum
-    (per-chunk reductions merged in grid order).  Chunk shapes: whole chunks
+    array into a dense one (K12), sum over the last axis and the full sum.  Chunk shapes: whole chunks
     (64, 256, 1024) = 8 chunks of 64 MiB, and (100, 200, 1000) = 3 x 3 x 2
     chunks of 80 MB with edge chunks on every axis.  Algorithmic bytes: the
     array's 512 MiB read and 512 MiB written for the assignment and the
     read-back; 512 MiB read (+ the result) for the sums.  CPU baseline: the
     compiled port of the reference's chunk-by-chunk assignment, element-wise
     read-back and lazy sum over the last axis (oracle/xt_baseline.c
-    bl_chunked_*, pinned to the oracle)."""
+    bl_chunked_*, pinned to the oracle).  The chunked arrays sit in one slab,
+    so each sum is one strided reduction per class of equal chunks; the same
+    sums over the dense array are timed beside them (`dense`)."""
     import xtensor_gb300 as xg
     from xtensor_gb300._ffi import check
     from xtensor_gb300.chunked import ChunkedArray, chunked_reduce
@@ -1631,6 +1632,25 @@ def run_chunked(args):
     total = sum(b for _, b, _ in calls)
     ms = sum(per)
     dom = max(per_kernel, key=lambda k: per_kernel[k]["ms"])
+    # the same sums over the dense array, for comparison (not in the totals)
+    from xtensor_gb300 import ops
+    s2d, s0d = DeviceArray.empty(SHAPE[:2], "float32"), DeviceArray.empty((), "float32")
+    dcalls = [("sum2", nb + s2d.nbytes, lambda: ops.reduce("sum", dx, [2], out=s2d)),
+              ("sum", nb + 4, lambda: ops.reduce("sum", dx, None, out=s0d))]
+    for _ in range(3):
+        for _, _, fn in dcalls:
+            fn()
+    check(lib.xtg_device_sync())
+    devs = [ev_create(lib, len(dcalls) + 1) for _ in range(K)]
+    for k in range(K):
+        for i, (_, _, fn) in enumerate(dcalls):
+            check(lib.xtg_event_record(devs[k][i], None))
+            fn()
+        check(lib.xtg_event_record(devs[k][len(dcalls)], None))
+    check(lib.xtg_device_sync())
+    dms = [sum(ev_ms(lib, devs[k][i], devs[k][i + 1]) for k in range(K)) / K for i in range(len(dcalls))]
+    dense_ref = {nm: {"ms": round(t, 4), "GB/s": round(b / (t / 1e3) / 1e9, 1), "frac": round(b / (t / 1e3) / 1e9 / peak, 3)}
+                 for (nm, b, _), t in zip(dcalls, dms)}
     # parity against an FP64 evaluation of the same values (the port is
     # checked against the oracle by the tests)
     parity = {}
@@ -1677,7 +1697,7 @@ def run_chunked(args):
                                         "l2": "512 MiB arrays, larger than L2: no flush"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": per_kernel[dom]["GB/s"], "peak": peak, "unit": "GB/s",
                      "frac": per_kernel[dom]["frac"], "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
-        "per_kernel": per_kernel, "parity": parity, "cpu_baseline": cpu, "e2e": None,
+        "per_kernel": per_kernel, "dense": dense_ref, "parity": parity, "cpu_baseline": cpu, "e2e": None,
         "gpu_launches": int(l1 - l0),
     }
     print(json.dumps(line))
@@ -1688,11 +1708,13 @@ def run_section(args, name):
     """One sub-result of the default line as its own line (profiling runs)."""
     import xtensor_gb300 as xg
     from xtensor_gb300._ffi import check
+    global C2_N
+    C2_N = 1 << args.c2_log2n
     xg.init(0)
     st = C.c_void_p()
     check(xg.lib().xtg_stream_create(C.byref(st)))
     r = (c0_section if name == "c0" else c2_section)(args, st.value)
-    print(json.dumps({"metric": METRIC, "workload": name, **r}))
+    print(json.dumps({"metric": METRIC, "workload": name, **r, **({"elements": C2_N} if name == "c2" else {})}))
     return 0
 
 
@@ -1992,6 +2014,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--shape", default=None, help="profiling only: d0,d1,d2 instead of 256,512,1024")
+    ap.add_argument("--c2-log2n", type=int, default=28, help="profiling only: C2 inputs of 2^n elements")
     ap.add_argument("--workload", default="c1",
                     choices=["c1", "c0", "c2", "c3", "c4", "scan", "views", "npy", "blockwise", "chunked"],
                     help="c1: strided/axis work (default, the headline); c3: batching of uneven instances; "

@@ -629,13 +629,14 @@ xtg_status chunked_reduce_impl(const xtg_chunked* src, const xtg_reduce_desc* rd
                 XTG_TRY(R.alloc(&mean_b.data, (size_t)on * dt(P.out_dtype).size));
             }
         }
+        // dims of the strided array: the reduced dims' chunk indexes, their
+        // positions in the chunk, then (chunk index, position) per kept dim.
+        // Reduced dims come first, grouped so that whole chunks merge into
+        // long runs (a full reduction of a slab without gaps is one run).
         xtg_reduce_desc prd2 = prd;
         prd2.keep_dims = 0;
-        prd2.n_axes = 0;
-        for (int d : rdims) {
-            prd2.axes[prd2.n_axes++] = 2 * d;
-            prd2.axes[prd2.n_axes++] = 2 * d + 1;
-        }
+        prd2.n_axes = 2 * (int)rdims.size();
+        for (int i = 0; i < prd2.n_axes; ++i) prd2.axes[i] = i;
         const Kind* sel[XTG_MAX_RANK];
         // the output-shaped array `a` over the kept dims' kinds: dims
         // (chunks, extent) per kept dim
@@ -672,14 +673,22 @@ xtg_status chunked_reduce_impl(const xtg_chunked* src, const xtg_reduce_desc* rd
                     k /= (int64_t)kinds[d].size();
                 }
                 xtg_array slab = whole;
-                slab.rank = 2 * rank;
+                slab.rank = 0;
                 int64_t first = 0;
-                for (int d = 0; d < rank; ++d) {
-                    slab.shape[2 * d] = sel[d]->cnt;
-                    slab.strides[2 * d] = gst[d] * (S / es);
-                    slab.shape[2 * d + 1] = sel[d]->ext;
-                    slab.strides[2 * d + 1] = cst[d];
-                    first += sel[d]->lo * gst[d];
+                for (int d = 0; d < rank; ++d) first += sel[d]->lo * gst[d];
+                for (int d : rdims) {
+                    slab.shape[slab.rank] = sel[d]->cnt;
+                    slab.strides[slab.rank++] = gst[d] * (S / es);
+                }
+                for (int d : rdims) {
+                    slab.shape[slab.rank] = sel[d]->ext;
+                    slab.strides[slab.rank++] = cst[d];
+                }
+                for (int d : kdims) {
+                    slab.shape[slab.rank] = sel[d]->cnt;
+                    slab.strides[slab.rank++] = gst[d] * (S / es);
+                    slab.shape[slab.rank] = sel[d]->ext;
+                    slab.strides[slab.rank++] = cst[d];
                 }
                 slab.data = (void*)((const char*)src->chunks[0] + first * S);
                 XTG_TRY(fold_partial(P, prd2, slab, 0.0, rp == 0, out_view(*out), out_view(part), out_view(mean_a),

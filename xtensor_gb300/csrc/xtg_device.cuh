@@ -3159,17 +3159,38 @@ XTG_DI void bulk_g2s(void* dst, const void* src, unsigned bytes, u64* bar) {
 }
 XTG_DI void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 XTG_DI void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+XTG_DI void mbar_arrive(u64* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Named barrier 1 over the first NT threads of the block (the consumer warps
+// of a kernel whose last warp is a producer that never joins it).
+template <int NT> XTG_DI void bar_sync_n() { asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory"); }
+template <int NT> XTG_DI bool bar_or_n(bool v) {
+    unsigned r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, %2, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((unsigned)v), "n"(NT)
+        : "memory");
+    return r != 0;
+}
 
 // K13: a full reduction of one contiguous leaf streamed through shared
 // memory.  Each block walks its work items (the same fixed partition as K3),
-// each item in stages of 1024 16-byte vectors that one thread copies with
-// cp.async.bulk into a ring of NS buffers (mbarrier completion), so NS stages
-// are in flight per block whatever the registers of the accumulator.  Thread
-// t folds vectors t, t + 256, t + 512, t + 768 of every stage of its item —
-// the vectors and the order of K3 with a 256-thread group — and the block
-// combines its threads with K3's tree, so results equal K3's bit for bit.
-// Every wait is bounded; a block that gives up (decided for the whole block)
-// sets the error word, waits (bounded) for its copies in flight and returns.
+// each item in stages of 1024 16-byte vectors.  The block's last warp is the
+// producer: its lane 0 copies every stage with cp.async.bulk into a ring of
+// NS buffers, completion on the slot's "full" mbarrier, and reuses a slot
+// once the 8 consumer warps have arrived on its "empty" mbarrier — consumer
+// warps never wait for one another between stages.  Consumer thread t folds
+// vectors t, t + 256, t + 512, t + 768 of every stage of its item (the
+// vectors and the order of K3 with a 256-thread group) and the consumers
+// combine with K3's tree, so results equal K3's bit for bit.
+// Every wait is bounded.  A consumer warp that gives up stops arriving (so
+// the slot is never refilled under it); at the end of the item the
+// consumers decide together, set the error word and return.  The producer
+// gives up when a slot is not released in time, and before it returns it
+// waits (bounded) for its copies still in flight, so the block's shared
+// memory outlives every copy.
 template <class T> struct SmemVec16 {
     template <int VEC> static XTG_DI void get(T (&dst)[VEC], const unsigned char* p) {
         union {
@@ -3181,15 +3202,32 @@ template <class T> struct SmemVec16 {
         for (int j = 0; j < VEC; ++j) dst[j] = u.e[j];
     }
 };
+// K3's block tree (group_reduce<256>) over the 256 consumer threads.
+template <class A> XTG_DI A consumer_reduce(A a, A* smem) {
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) {
+        A o = shfl_xor_pod(a, m);
+        a.merge(o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    bar_sync_n<256>();
+    if (lane == 0) smem[warp] = a;
+    bar_sync_n<256>();
+    if (threadIdx.x == 0) {
+        A r = smem[0];
+        for (int w = 1; w < 8; ++w) r.merge(smem[w]);
+        a = r;
+    }
+    return a;
+}
 template <class Tree, class LS, class TL, class Acc, class Out, int POST, int VEC, int NS>
-__global__ void __launch_bounds__(256) k_reduce_stream(const RedParams p) {
+__global__ void __launch_bounds__(288) k_reduce_stream(const RedParams p) {
     typedef typename LS::template R<VEC>::type RG;
     constexpr unsigned SB = 16384;  // stage bytes: 1024 vectors
+    constexpr int kPolls = 1 << 22;
     extern __shared__ __align__(128) unsigned char sbuf[];
-    __shared__ u64 bars[NS];
-    __shared__ Acc smem[32];
-    Ctx<0> c;
-    c.scal = p.scal;
+    __shared__ u64 full[NS], empty[NS];
+    __shared__ Acc smem[8];
     const int tid = (int)threadIdx.x;
     const i64 nitems = p.nsplit;
     const char* base = reinterpret_cast<const char*>(p.leaf[0]);
@@ -3200,30 +3238,62 @@ __global__ void __launch_bounds__(256) k_reduce_stream(const RedParams p) {
     };
     if (tid == 0) {
 #pragma unroll
-        for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 8);
+        }
         fence_mbar_init();
     }
     __syncthreads();
-    // the copy cursor (thread 0): next item and stage to fetch
-    i64 iw = blockIdx.x, is = 0;
-    i64 issued = 0;
-    auto issue_next = [&](int slot) {
-        if (iw >= nitems) return;
-        const i64 len = item_len(iw);
-        const i64 v0 = is * 1024;
-        const i64 nv = len - v0 < 1024 ? len - v0 : 1024;
-        const unsigned bytes = (unsigned)(nv * 16);
-        mbar_expect_tx(&bars[slot], bytes);
-        bulk_g2s(sbuf + (size_t)slot * SB, base + (iw * p.chunk + v0) * 16, bytes, &bars[slot]);
-        ++issued;
-        if (++is * 1024 >= len) {
-            iw += gridDim.x;
-            is = 0;
+    if (tid >= 256) {
+        // the producer (lane 0 of the last warp)
+        if (tid != 256) return;
+        i64 q = 0;
+        bool stop = false;
+        for (i64 w = blockIdx.x; w < nitems && !stop; w += gridDim.x) {
+            const i64 len = item_len(w);
+            for (i64 v0 = 0; v0 < len; v0 += 1024) {
+                const int slot = (int)(q % NS);
+                if (q >= NS) {
+                    const unsigned par = (unsigned)(((q / NS) - 1) & 1);
+                    bool ok = false;
+                    for (int k = 0; k < kPolls; ++k)
+                        if (mbar_try_wait(&empty[slot], par)) {
+                            ok = true;
+                            break;
+                        }
+                    if (!ok) {
+                        stop = true;
+                        break;
+                    }
+                }
+                const i64 nv = len - v0 < 1024 ? len - v0 : 1024;
+                const unsigned bytes = (unsigned)(nv * 16);
+                if (q >= NS) fence_proxy_async_smem();  // the consumers' reads before the copy's writes
+                mbar_expect_tx(&full[slot], bytes);
+                bulk_g2s(sbuf + (size_t)slot * SB, base + (w * p.chunk + v0) * 16, bytes, &full[slot]);
+                ++q;
+            }
         }
-    };
-    if (tid == 0)
-        for (int s = 0; s < NS; ++s) issue_next(s);
-    i64 consumed = 0;
+        // the copies that may still be in flight: the last issued stage of each slot
+        bool drained = true;
+        for (i64 r = q > NS ? q - NS : 0; r < q; ++r) {
+            bool ok = false;
+            for (int k = 0; k < kPolls; ++k)
+                if (mbar_try_wait(&full[r % NS], (unsigned)((r / NS) & 1))) {
+                    ok = true;
+                    break;
+                }
+            drained = drained && ok;
+        }
+        if (stop || !drained) atomicExch(p.err, 1);
+        return;
+    }
+    // the 256 consumers
+    Ctx<0> c;
+    c.scal = p.scal;
+    i64 q = 0;
+    bool bad = false;
     for (i64 w = blockIdx.x; w < nitems; w += gridDim.x) {
         Acc acc;
         acc.init(p);
@@ -3238,50 +3308,48 @@ __global__ void __launch_bounds__(256) k_reduce_stream(const RedParams p) {
         wa.from(acc);
         const i64 len = item_len(w);
         const i64 ns = (len + 1023) / 1024;
-        for (i64 s = 0; s < ns; ++s, ++consumed) {
-            const int slot = (int)(consumed % NS);
-            const unsigned parity = (unsigned)((consumed / NS) & 1);
-            bool ok = false;
-            for (int k = 0; k < (1 << 22); ++k)
-                if (mbar_try_wait(&bars[slot], parity)) {
-                    ok = true;
-                    break;
-                }
-            if (__syncthreads_or(!ok)) {
-                // give up: flag it, wait (bounded) for the copies still in flight
-                if (tid == 0) {
-                    atomicExch(p.err, 1);
-                    for (i64 q = consumed + 1; q < issued; ++q)
-                        for (int k = 0; k < (1 << 22); ++k)
-                            if (mbar_try_wait(&bars[q % NS], (unsigned)((q / NS) & 1))) break;
-                }
-                return;
+        for (i64 s = 0; s < ns; ++s, ++q) {
+            const int slot = (int)(q % NS);
+            if (!bad) {
+                const unsigned par = (unsigned)((q / NS) & 1);
+                bool ok = false;
+                for (int k = 0; k < kPolls; ++k)
+                    if (mbar_try_wait(&full[slot], par)) {
+                        ok = true;
+                        break;
+                    }
+                bad = !ok;
             }
-            const unsigned char* buf = sbuf + (size_t)slot * SB;
-            const i64 nvs = len - s * 1024 < 1024 ? len - s * 1024 : 1024;
+            if (!bad) {
+                const unsigned char* buf = sbuf + (size_t)slot * SB;
+                const i64 nvs = len - s * 1024 < 1024 ? len - s * 1024 : 1024;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int v = tid + 256 * j;
-                if (v < nvs) {
-                    RG rg;
-                    SmemVec16<TL>::template get<VEC>(RegAt<0>::get(rg), buf + (size_t)v * 16);
-                    AddVec<HasAdd2<typename Work<Acc>::T>::value != 0>::template run<VEC, Tree>(
-                        wa, rg, (w * p.chunk + s * 1024 + v) * VEC, c);
+                for (int j = 0; j < 4; ++j) {
+                    const int v = tid + 256 * j;
+                    if (v < nvs) {
+                        RG rg;
+                        SmemVec16<TL>::template get<VEC>(RegAt<0>::get(rg), buf + (size_t)v * 16);
+                        AddVec<HasAdd2<typename Work<Acc>::T>::value != 0>::template run<VEC, Tree>(
+                            wa, rg, (w * p.chunk + s * 1024 + v) * VEC, c);
+                    }
                 }
             }
-            __syncthreads();  // every thread is done with the slot
-            if (tid == 0) {
-                fence_proxy_async_smem();
-                issue_next(slot);
-            }
+            // every lane has read the slot: the warp releases it
+            if (__any_sync(0xffffffffu, bad)) bad = true;
+            __syncwarp();
+            if (!bad && (tid & 31) == 0) mbar_arrive(&empty[slot]);
         }
         wa.to(acc);
-        acc = group_reduce<256>(acc, smem);
+        if (bar_or_n<256>(bad)) {
+            if (tid == 0) atomicExch(p.err, 1);
+            return;
+        }
+        acc = consumer_reduce(acc, smem);
         if (tid == 0) {
             if (p.nsplit > 1) reinterpret_cast<Acc*>(p.partial)[w] = acc;
             else reinterpret_cast<Out*>(p.out)[0] = finish<Out, Acc, POST>(acc, p);
         }
-        __syncthreads();
+        bar_sync_n<256>();  // smem is reused by the next item's combine
     }
 }
 

@@ -360,8 +360,8 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
                                  accname + ", " + outc + ", " + std::to_string(post) + ", " + std::to_string(vec) + ", " +
                                  std::to_string(NS) + ">";
         Kernel* k;
-        st = get_kernel(name, 256, &k, smem);
-        if (st == XTG_OK) st = launch(k, grid_cap(k, nsplit), 256, &p, stream, smem, part_off);
+        st = get_kernel(name, 288, &k, smem);  // 8 consumer warps + the producer warp
+        if (st == XTG_OK) st = launch(k, grid_cap(k, nsplit), 288, &p, stream, smem, part_off);
     } else if (row) {
         const int group = (chunk >= opt("reduce.cta_chunk", 2048)) ? 256 : 32;
         // (a copy ring as in the column kernel measured slower here: these
