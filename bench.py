@@ -907,6 +907,36 @@ class C2Step:
         return {nm: o.to_numpy() for (nm, _, _), o in zip(self.calls, self.dev_out)}
 
 
+class C2Moments(C2Step):
+    """C2's float32 and bfloat16 statistics as one xtg_reduce_moments call
+    each (sum, mean, variance, norm_l2 from one read of the input)."""
+
+    def __init__(self, step: C2Step):
+        from xtensor_gb300 import ops
+        from xtensor_gb300._ffi import Array
+        from xtensor_gb300.device import DeviceArray
+        from xtensor_gb300.expr import lower
+        self.lib = L = step.lib
+        self.dev_out, self.calls, self.keep, self.names = [], [], [], []
+        for tag, d in (("f32", step.dev_in[0]), ("bf16", step.dev_in[1])):
+            e, k = lower(d)
+            outs = []
+            for op in C2_OPS:
+                shape, dt = ops.reduce_shape(op, d)
+                outs.append(DeviceArray.empty(shape, dt))
+            rd = ops.make_desc("variance")
+            arrs = [o.xtg_array() for o in outs]
+            self.keep += [e, k, rd, arrs]
+            self.dev_out += outs
+            self.names += [f"{op}_{tag}" for op in C2_OPS]
+            self.calls.append((f"moments_{tag}", d.nbytes + sum(o.nbytes for o in outs),
+                               lambda st, e=e, rd=rd, a=arrs: L.xtg_reduce_moments(
+                                   C.byref(e), C.byref(rd), *[C.byref(x) for x in a], st)))
+
+    def results(self) -> dict:
+        return {nm: o.to_numpy() for nm, o in zip(self.names, self.dev_out)}
+
+
 def c2_exact(x, bf):
     """FP64 values of the C2 reductions over the (rounded) data."""
     res = {}
@@ -955,6 +985,26 @@ def c2_section(args, stream):
     ms = sum(per)
     dom = max(per_kernel, key=lambda k: per_kernel[k]["ms"])
     got = step.results()
+    # the same statistics from one pass per input (xtg_reduce_moments)
+    mstep = C2Moments(step)
+    for _ in range(max(3, args.warmup)):
+        mstep.launch(stream)
+    check(lib.xtg_stream_sync(stream))
+    mevs = [ev_create(lib, len(mstep.calls) + 1) for _ in range(K)]
+    for k in range(K):
+        mstep.launch(stream, mevs[k])
+    check(lib.xtg_stream_sync(stream))
+    mper = [sum(ev_ms(lib, mevs[k][i], mevs[k][i + 1]) for k in range(K)) / K for i in range(len(mstep.calls))]
+    mgot = mstep.results()
+    one_pass = {
+        "form": "one xtg_reduce_moments call per input: sum, mean, variance and norm_l2 from one read",
+        "algorithmic_bytes_per_step": sum(nb for _, nb, _ in mstep.calls),
+        "ms_per_step": round(sum(mper), 4),
+        "per_kernel": {nm: {"ms": round(t, 4), "GB/s": round(nb / (t / 1e3) / 1e9, 1),
+                            "frac": round(nb / (t / 1e3) / 1e9 / peak, 3)} for (nm, nb, _), t in zip(mstep.calls, mper)},
+        "separate_calls_ms": round(sum(per[:2 * len(C2_OPS)]), 4),
+        "results_equal_separate_calls_bitwise": all(mgot[k].tobytes() == got[k].tobytes() for k in mgot),
+    }
     ex = c2_exact(x, bf)
     acc = {}
     for tag in ("f32", "bf16"):
@@ -972,6 +1022,7 @@ def c2_section(args, stream):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": per_kernel[dom]["GB/s"], "peak": peak,
                      "unit": "GB/s", "frac": per_kernel[dom]["frac"],
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "one_pass": one_pass,
         "accuracy": {"rel_err_vs_fp64": {k: float(f"{v:.3e}") for k, v in acc.items()}, "bound": 1e-6,
                      "int32_to_int64_sum_bit_exact": int(got["sum_i32"]) == exact_i,
                      "ok": bool(max(acc.values()) <= 1e-6 and int(got["sum_i32"]) == exact_i)},

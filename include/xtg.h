@@ -279,6 +279,17 @@ xtg_status xtg_argreduce(const xtg_expr* e, int32_t op, int32_t has_axis, int64_
  * and folds it; otherwise the two evaluations run in order. */
 xtg_status xtg_assign_reduce(const xtg_expr* e, const xtg_array* out_e, const xtg_reduce_desc* rd,
                              const xtg_array* out_r, xtg_stream stream);
+/* The four reducers xt::sum, xt::mean, xt::variance (rd->ddof) and
+ * xt::norm_l2 of one expression over rd's axes (rd->op is ignored; any
+ * destination may be null) — core/xmath.hpp:367-423, 1828-1911, 2082-2103 and
+ * reducers/xnorm.hpp:494-526 called one after the other on the same operand.
+ * When the plan streams (a full reduction of one contiguous float32 / bf16
+ * array in 16-byte vectors) the leaves are read once and each result equals
+ * the corresponding xtg_reduce call bit for bit (its accumulator sees the
+ * same values in the same order); otherwise the four reductions run in turn. */
+xtg_status xtg_reduce_moments(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* sum,
+                              const xtg_array* mean, const xtg_array* variance, const xtg_array* norm_l2,
+                              xtg_stream stream);
 
 /* ---- accumulators ----------------------------------------------------------------------
  * Cumulative sum / product of an expression along `axis` (has_axis = 1; the

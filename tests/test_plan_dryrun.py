@@ -98,6 +98,18 @@ def test_c2_precision_full_reductions():
     assert "AccPlain<long long, 0>" in last_kernels()[0]
 
 
+@pytest.mark.parametrize("dt", ["float32", "bfloat16"])
+def test_c2_one_pass_moments(dt):
+    # sum, mean, variance and norm_l2 of 2^28 elements: one streaming launch
+    # with the four accumulators, one combine writing the four results
+    x = fake((1 << 28,), dt)
+    outs = {nm: fake(*ops.reduce_shape(nm, x)) for nm in ops.MOMENTS}
+    ops.reduce_moments(x, outs=outs)
+    ks = last_kernels()
+    assert fam(ks) == ["k_reduce_stream", "k_reduce_combine"] and "AccStats" in ks[0]
+    assert "StatsOut<float, double, double, double>" in ks[1]
+
+
 def test_views_and_broadcast_plans():
     x = fake((64, 48), "float32")
     o = fake((32, 40), "float32")

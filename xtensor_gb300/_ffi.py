@@ -146,6 +146,8 @@ def lib() -> C.CDLL:
             "xtg_reduce": (st, [C.POINTER(Expr), C.POINTER(ReduceDesc), C.POINTER(Array), vp]),
             "xtg_argreduce": (st, [C.POINTER(Expr), i32, i32, i64, C.POINTER(Array), vp]),
             "xtg_assign_reduce": (st, [C.POINTER(Expr), C.POINTER(Array), C.POINTER(ReduceDesc), C.POINTER(Array), vp]),
+            "xtg_reduce_moments": (st, [C.POINTER(Expr), C.POINTER(ReduceDesc), C.POINTER(Array), C.POINTER(Array),
+                                        C.POINTER(Array), C.POINTER(Array), vp]),
             "xtg_accumulate_shape": (st, [C.POINTER(Expr), i32, i32, i64, i32, C.POINTER(i32), C.POINTER(i64),
                                           C.POINTER(i32)]),
             "xtg_accumulate": (st, [C.POINTER(Expr), i32, i32, i64, i32, C.POINTER(Array), vp]),

@@ -609,20 +609,22 @@ XTG_DI void two_sum2(float2 a, float2 b, float2& s, float2& e) {
     e = p_add(p_sub(a, p_sub(s, bb)), p_sub(b, bb));
 }
 
-// Pairwise sums of N float32 values (a vector's elements): depth log2(N), the
-// rounding error of the whole sum at most ceil(log2 N) u sum |f| (u = 2^-24).
-template <int N> struct Pw {
-    static XTG_DI float sum(const float* f) { return Pw<N / 2>::sum(f) + Pw<N - N / 2>::sum(f + N / 2); }
-    // sum of squares: pairs as fma(a, a, b * b), then pairwise
-    static XTG_DI float sq(const float* f) { return Pw<N / 2>::sq(f) + Pw<N - N / 2>::sq(f + N / 2); }
+// Pairwise sums of 2N float32 values held as N pairs, with packed
+// instructions: lane x sums the even values, lane y the odd ones, and x + y
+// closes the tree — depth log2(2N), so the rounding error of the whole sum
+// is at most ceil(log2 2N) u sum |f| (u = 2^-24).  Squares: pairs as
+// fma(a, a, b * b), then pairwise.
+template <int N> struct Pw2 {
+    static XTG_DI float2 sum(const float2* f) { return p_add(Pw2<N / 2>::sum(f), Pw2<N - N / 2>::sum(f + N / 2)); }
+    static XTG_DI float2 sq(const float2* f) { return p_add(Pw2<N / 2>::sq(f), Pw2<N - N / 2>::sq(f + N / 2)); }
 };
-template <> struct Pw<1> {
-    static XTG_DI float sum(const float* f) { return f[0]; }
-    static XTG_DI float sq(const float* f) { return f[0] * f[0]; }
+template <> struct Pw2<1> {
+    static XTG_DI float2 sum(const float2* f) { return f[0]; }
+    static XTG_DI float2 sq(const float2* f) { return p_mul(f[0], f[0]); }
 };
-template <> struct Pw<2> {
-    static XTG_DI float sum(const float* f) { return f[0] + f[1]; }
-    static XTG_DI float sq(const float* f) { return fmaf(f[0], f[0], f[1] * f[1]); }
+template <> struct Pw2<2> {
+    static XTG_DI float2 sum(const float2* f) { return p_add(f[0], f[1]); }
+    static XTG_DI float2 sq(const float2* f) { return p_fma(f[0], f[0], p_mul(f[1], f[1])); }
 };
 
 // ---------------------------------------------------------------------------
@@ -955,53 +957,57 @@ struct AccSumC2 {
     }
     template <class X> XTG_DI void add(X x, i64) { adds(cvt<float>(x)); }
     template <class X> XTG_DI void add2(X x0, X x1, i64) { addp(make_float2(cvt<float>(x0), cvt<float>(x1))); }
-    // a vector of N values: their pairwise sum, then one TwoSum
-    template <int N> XTG_DI void addblk(const float (&f)[N]) { adds(Pw<N>::sum(f)); }
+    // a vector of 2M values (M pairs): their pairwise sum, then one TwoSum
+    template <int M> XTG_DI void addblk(const float2 (&f)[M]) {
+        const float2 h = Pw2<M>::sum(f);
+        adds(h.x + h.y);
+    }
 };
+// Working form of the float32 moments: one packed double-float pair, lane x
+// the sum of deviations from the shift k, lane y the sum of their squares,
+// so a single packed TwoSum advances both.
 template <int MODE> struct AccMom2 {
     float k;
-    AccSumC2 s1, s2;
+    float2 hi, lo;
     XTG_DI void from(const AccMom<float, MODE>& a) {
         k = a.k;
-        s1.from(a.s1);
-        s2.from(a.s2);
+        hi = make_float2(a.s1.hi, a.s2.hi);
+        lo = make_float2(a.s1.lo, a.s2.lo);
     }
     XTG_DI void to(AccMom<float, MODE>& a) const {
         a.k = k;
-        s1.to(a.s1);
-        s2.to(a.s2);
+        a.s1.hi = hi.x;
+        a.s1.lo = lo.x;
+        a.s2.hi = hi.y;
+        a.s2.lo = lo.y;
+    }
+    XTG_DI void addp2(float2 v) {
+        float2 s, e;
+        two_sum2(hi, v, s, e);
+        hi = s;
+        lo = p_add(lo, e);
     }
     template <class X> XTG_DI void add(X x, i64) {
         const float d = cvt<float>(x) - k;
-        s1.adds(d);
-        if (MODE != 0) {
-            const float q = d * d;
-            const float qe = fmaf(d, d, -q);
-            s2.adds(q);
-            s2.lo.x += qe;
-        }
+        const float q = d * d;
+        addp2(make_float2(d, q));
+        lo.y += fmaf(d, d, -q);  // the square's rounding error (exact)
     }
-    template <class X> XTG_DI void add2(X x0, X x1, i64) {
-        const float2 kk = make_float2(k, k), x = make_float2(cvt<float>(x0), cvt<float>(x1));
-        const float2 d = p_sub(x, kk);
-        s1.addp(d);
-        if (MODE != 0) {
-            const float2 nd = p_sub(kk, x);    // -d, bit for bit
-            const float2 q = p_mul(d, d);
-            const float2 nqe = p_fma(nd, d, q);  // q - d * d: minus the square's rounding error (exact)
-            s2.addp(q);
-            s2.lo = p_sub(s2.lo, nqe);
-        }
+    template <class X> XTG_DI void add2(X x0, X x1, i64 p0) {
+        add(x0, p0);
+        add(x1, p0 + 1);
     }
-    // a vector of N values: pairwise sums of the deviations and of their
-    // squares (terms >= 0: relative error <= (ceil(log2 N) + 1) u), one
-    // TwoSum each into the states
-    template <int N> XTG_DI void addblk(const float (&f)[N]) {
-        float d[N];
+    // a vector of 2M values: pairwise sums of the deviations and of their
+    // squares (terms >= 0: relative error <= (ceil(log2 2M) + 1) u), one
+    // packed TwoSum for both
+    template <int M> XTG_DI void addblk(const float2 (&f)[M]) {
+        const float2 kk = make_float2(k, k);
+        float2 d[M];
 #pragma unroll
-        for (int j = 0; j < N; ++j) d[j] = f[j] - k;
-        s1.adds(Pw<N>::sum(d));
-        if (MODE != 0) s2.adds(Pw<N>::sq(d));
+        for (int i = 0; i < M; ++i) d[i] = p_sub(f[i], kk);
+        const float2 hs = Pw2<M>::sum(d);
+        const float2 hq = Pw2<M>::sq(d);
+        addp2(make_float2(hs.x + hs.y, hq.x + hq.y));
     }
 };
 template <int NK> struct AccNormC2 {
@@ -1030,15 +1036,17 @@ template <int NK> struct AccNormC2 {
             a.lo = p_sub(a.lo, nqe);
         }
     }
-    template <int N> XTG_DI void addblk(const float (&f)[N]) {
+    template <int M> XTG_DI void addblk(const float2 (&f)[M]) {
+        float2 h;
         if (NK == 1) {
-            float g[N];
+            float2 g[M];
 #pragma unroll
-            for (int j = 0; j < N; ++j) g[j] = fabsf(f[j]);
-            a.adds(Pw<N>::sum(g));
+            for (int j = 0; j < M; ++j) g[j] = make_float2(fabsf(f[j].x), fabsf(f[j].y));
+            h = Pw2<M>::sum(g);
         } else {
-            a.adds(Pw<N>::sq(f));
+            h = Pw2<M>::sq(f);
         }
+        a.adds(h.x + h.y);
     }
 };
 // The working form of a stored accumulator in the row pass.
@@ -1050,10 +1058,44 @@ template <class A> struct HasAdd2 { enum { value = 0 }; };
 template <> struct HasAdd2<AccSumC2> { enum { value = 1 }; };
 template <int M> struct HasAdd2<AccMom2<M>> { enum { value = 1 }; };
 template <int NK> struct HasAdd2<AccNormC2<NK>> { enum { value = 1 }; };
+// One pass for sum, mean, variance and norm_l2 (xtg_reduce_moments): the
+// four reducers' accumulators side by side (sum and mean share one), each
+// fed exactly what its own reduction feeds it, so each result equals that
+// reduction's bit for bit.
+struct AccStats {
+    AccSumC s;
+    AccMom<float, 1> m;
+    AccNormC<2> q;
+    template <class P> XTG_DI void init(const P& p);
+    XTG_DI void merge(const AccStats& o) {
+        s.merge(o.s);
+        m.merge(o.m);
+        q.merge(o.q);
+    }
+};
+struct AccStats2 {
+    AccSumC2 s;
+    AccMom2<1> m;
+    AccNormC2<2> q;
+    XTG_DI void from(const AccStats& a) {
+        s.from(a.s);
+        m.from(a.m);
+        q.from(a.q);
+    }
+    XTG_DI void to(AccStats& a) const {
+        s.to(a.s);
+        m.to(a.m);
+        q.to(a.q);
+    }
+};
+template <> struct Work<AccStats> { enum { packed = 1 }; typedef AccStats2 T; };
+template <> struct HasAdd2<AccStats2> { enum { value = 1 }; };
+
 // Vector-blocked working forms: a vector's values are summed pairwise in
-// float32 and the block enters the double-float state by one TwoSum (about 5
-// FP32 operations per element for the moments instead of 19, 2 for sums of
-// 2-byte values instead of 7: those loops are FP32-pipe bound at HBM speed).
+// float32 and the block enters the double-float state by one TwoSum (for the
+// moments about 21 FP32 instructions per 8 values, packed, instead of 76; for
+// sums of 2-byte values about 11 instead of 28: at HBM speed those loops are
+// bound by instruction issue and the FP32 pipe).
 // Used for the moments of variance / stddev (the squares' terms are >= 0) and
 // for sums, means and norms of 2-byte inputs (bfloat16 / float16: 8 or 11
 // significant bits, so a vector's pairwise sum is mostly exact); float32 sums,
@@ -1062,6 +1104,9 @@ template <class W, class X> struct BlockAdd { enum { value = 0 }; };
 template <class X> struct BlockAdd<AccSumC2, X> { enum { value = sizeof(X) == 2 }; };
 template <int NK, class X> struct BlockAdd<AccNormC2<NK>, X> { enum { value = sizeof(X) == 2 }; };
 template <int M, class X> struct BlockAdd<AccMom2<M>, X> { enum { value = M != 0 || sizeof(X) == 2 }; };
+
+template <class A> struct IsStats2 { enum { value = 0 }; };
+template <> struct IsStats2<AccStats2> { enum { value = 1 }; };
 
 // One vector of tree values into an accumulator: in pairs where it takes
 // them, else element by element; p0 = the first element's position.
@@ -1076,11 +1121,16 @@ template <> struct AddVec<true> {
     template <int VEC, class Tree, class A, class RG, class C>
     static XTG_DI void run(A& a, const RG& rg, i64 p0, const C& c) {
         typedef decltype(Tree::ev(rg, 0, c)) X;
-        if constexpr (BlockAdd<A, X>::value != 0 && VEC > 1) {
-            float f[VEC];
+        if constexpr (IsStats2<A>::value) {
+            run<VEC, Tree>(a.s, rg, p0, c);
+            run<VEC, Tree>(a.m, rg, p0, c);
+            run<VEC, Tree>(a.q, rg, p0, c);
+        } else if constexpr (BlockAdd<A, X>::value != 0 && VEC > 1) {
+            float2 f[VEC / 2];
 #pragma unroll
-            for (int j = 0; j < VEC; ++j) f[j] = cvt<float>(Tree::ev(rg, j, c));
-            a.template addblk<VEC>(f);
+            for (int j = 0; j < VEC / 2; ++j)
+                f[j] = make_float2(cvt<float>(Tree::ev(rg, 2 * j, c)), cvt<float>(Tree::ev(rg, 2 * j + 1, c)));
+            a.template addblk<VEC / 2>(f);
         } else if (VEC % 2 == 0) {
 #pragma unroll
             for (int j = 0; j < VEC; j += 2) a.add2(Tree::ev(rg, j, c), Tree::ev(rg, j + 1, c), p0 + j);
@@ -1113,6 +1163,15 @@ template <class A, int MAXOP> struct AccArg {
         if (MAXOP ? Cmp<A>::gt(a, v) : Cmp<A>::lt(a, v)) {
             v = a;
             idx = ps;
+        }
+    }
+    // add_held() when every position of the work item has idx's high 32
+    // bits: only the low word is selected
+    template <class X> XTG_DI void add_held_lo(X x, u32 lo) {
+        A a = cvt<A>(x);
+        if (MAXOP ? Cmp<A>::gt(a, v) : Cmp<A>::lt(a, v)) {
+            v = a;
+            idx = (i64)(((u64)idx & 0xFFFFFFFF00000000ull) | (u64)lo);
         }
     }
     XTG_DI bool held() const { return idx >= 0; }
@@ -1218,6 +1277,11 @@ template <int MODE> template <class P> XTG_DI void AccMom<float, MODE>::init(con
     s1.hi = s1.lo = s2.hi = s2.lo = 0.f;
 }
 template <int MODE> template <class P> XTG_DI void AccMom<double, MODE>::init(const P&) { k = 0.0; s1 = s2 = 0.0; }
+template <class P> XTG_DI void AccStats::init(const P& p) {
+    s.init(p);
+    m.init(p);
+    q.init(p);
+}
 
 // Shift for the moment accumulators (the output's first element).
 template <class A> struct Shift {
@@ -1229,7 +1293,11 @@ template <int MODE> struct Shift<AccMom<float, MODE>> {
 template <int MODE> struct Shift<AccMom<double, MODE>> {
     template <class X> static XTG_DI void set(AccMom<double, MODE>& a, X x) { a.k = MODE == 0 ? 0.0 : cvt<double>(x); }
 };
+template <> struct Shift<AccStats> {
+    template <class X> static XTG_DI void set(AccStats& a, X x) { Shift<AccMom<float, 1>>::set(a.m, x); }
+};
 template <class A> struct NeedsShift { enum { value = 0 }; };
+template <> struct NeedsShift<AccStats> { enum { value = 1 }; };
 template <int MODE> struct NeedsShift<AccMom<float, MODE>> { enum { value = MODE != 0 }; };
 template <int MODE> struct NeedsShift<AccMom<double, MODE>> { enum { value = MODE != 0 }; };
 // arg-reductions whose update has a cheaper form once a value is held
@@ -1242,11 +1310,16 @@ template <int M> struct HeldFast<AccArg<double, M>> { enum { value = 0 }; };
 // (held == true) the compare-and-select form.
 template <class Tree, class Acc, int VEC> struct ColStep {
     template <class RG, class C>
-    static XTG_DI void run(Acc (&acc)[VEC], const RG& rg, i64 r, const C& c, bool& held) {
+    static XTG_DI void run(Acc (&acc)[VEC], const RG& rg, i64 r, const C& c, bool& held, bool lo32) {
         if constexpr (HeldFast<Acc>::value) {
             if (held) {
+                if (lo32) {
 #pragma unroll
-                for (int j = 0; j < VEC; ++j) acc[j].add_held(Tree::ev(rg, j, c), r);
+                    for (int j = 0; j < VEC; ++j) acc[j].add_held_lo(Tree::ev(rg, j, c), (u32)r);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) acc[j].add_held(Tree::ev(rg, j, c), r);
+                }
                 return;
             }
             bool h = true;
@@ -1339,6 +1412,31 @@ template <class Out, class Acc, int POST, class P> XTG_DI Out finish(const Acc& 
     typedef typename FinT<POST, Out>::type M;
     return post<POST, Out>(Fin<M, Acc>::go(a, p), p);
 }
+// A reduction's result(s) at output offset oo.
+template <class TS, class TM, class TV, class TN> struct StatsOut {};
+template <class Out, class Acc, int POST> struct Store {
+    static XTG_DI void put(const Acc& a, const RedParams& p, i64 oo) {
+        reinterpret_cast<Out*>(p.out)[oo] = finish<Out, Acc, POST>(a, p);
+    }
+};
+template <class TS, class TM, class TV, class TN, int POST> struct Store<StatsOut<TS, TM, TV, TN>, AccStats, POST> {
+    static XTG_DI void put(const AccStats& a, const RedParams& p, i64 oo) {
+        FinP pm;  // what the finishers read: no initial value, the mean's divisor
+        pm.init_f = 0.0;
+        pm.init_i = 0;
+        pm.has_initial = 0;
+        pm.initial_f = 0.0;
+        pm.initial_i = 0;
+        pm.divisor = p.divisor;
+        pm.n_red = p.n_red;
+        FinP pv = pm;  // the variance's divisor
+        pv.divisor = p.divisor2;
+        if (p.out) reinterpret_cast<TS*>(p.out)[oo] = finish<TS, AccSumC, 0>(a.s, pm);
+        if (p.out_more[0]) reinterpret_cast<TM*>(p.out_more[0])[oo] = finish<TM, AccSumC, 2>(a.s, pm);
+        if (p.out_more[1]) reinterpret_cast<TV*>(p.out_more[1])[oo] = finish<TV, AccMom<float, 1>, 0>(a.m, pv);
+        if (p.out_more[2]) reinterpret_cast<TN*>(p.out_more[2])[oo] = finish<TN, AccNormC<2>, 1>(a.q, pm);
+    }
+};
 
 // Offsets of every leaf at a (kept, reduced) multi-index pair.
 template <int NL, int RO, int RR>
@@ -1480,10 +1578,13 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
 #pragma unroll
     for (int l = 0; l < LS::N; ++l) inner[l] = p.lrs[l][RR - 1];
     for (i64 w = gid; w < nwork; w += ngroups) {
-        const i64 o = w / p.nsplit;
+        const i64 o = p.nsplit == 1 ? w : w / p.nsplit;
         const i64 s = w - o * p.nsplit;
         i64 ko[RO];
-        decode_dims<RO, true>(p.oshape, p.ofd, o, ko);
+        // 32-bit multiply-shift division when the outputs fit (the host sets
+        // every ofd), 64-bit division otherwise
+        if (p.n_out <= 0xFFFFFFF0ll) decode_dims<RO, false>(p.oshape, p.ofd, o, ko);
+        else decode_dims<RO, true>(p.oshape, p.ofd, o, ko);
         Acc acc;
         acc.init(p);
         if (NeedsShift<Acc>::value && p.n_red > 0) {
@@ -1499,6 +1600,21 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
         const i64 rb = s * p.chunk;
         i64 re = rb + p.chunk;
         if (re > p.n_redv) re = p.n_redv;
+        // each leaf's (and the fused destination's) offset of the output
+        // position, once per work item: the vectors add the reduced part only
+        i64 kbase[XTG_KMAX_LEAVES];
+#pragma unroll
+        for (int l = 0; l < LS::N; ++l) {
+            i64 o = 0;
+#pragma unroll
+            for (int d = 0; d < RO; ++d) o += ko[d] * p.lks[l][d];
+            kbase[l] = o;
+        }
+        i64 ebase = 0;
+        if constexpr (ES != 0) {
+#pragma unroll
+            for (int d = 0; d < RO; ++d) ebase += ko[d] * p.eks[d];
+        }
         // two register batches of U vectors: the next batch's loads are in
         // flight while the current one is reduced; each thread still visits
         // its positions in increasing order
@@ -1514,7 +1630,13 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
                     decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);
                     ri[RR - 1] *= VEC;
                     i64 off[XTG_KMAX_LEAVES];
-                    red_offsets<LS::N, RO, RR>(p, ko, ri, off);
+#pragma unroll
+                    for (int l = 0; l < LS::N; ++l) {
+                        i64 o = kbase[l];
+#pragma unroll
+                        for (int d = 0; d < RR; ++d) o += ri[d] * p.lrs[l][d];
+                        off[l] = o;
+                    }
                     LoadLeavesAt<LS>::template run<VEC>(rg[u], p.leaf, off, inner);
                 }
             }
@@ -1533,8 +1655,7 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
                         i64 ri[RR];                                                    \
                         decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);                  \
                         ri[RR - 1] *= VEC;                                             \
-                        i64 eo = 0;                                                    \
-                        _Pragma("unroll") for (int d = 0; d < RO; ++d) eo += ko[d] * p.eks[d]; \
+                        i64 eo = ebase;                                                \
                         _Pragma("unroll") for (int d = 0; d < RR; ++d) eo += ri[d] * p.ers[d]; \
                         st_out<ET, ES == 1 ? K_CONTIG : 2, VEC>(reinterpret_cast<ET*>(p.eout), eo, \
                                                                  p.ers[RR - 1], ev);   \
@@ -1635,15 +1756,36 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
         i64 re = rb + p.chunk;
         if (re > p.n_redv) re = p.n_redv;
         bool held = false;
+        // each leaf's offset of the output position, once per work item
+        i64 kbase[XTG_KMAX_LEAVES];
+#pragma unroll
+        for (int l = 0; l < LS::N; ++l) {
+            i64 o = 0;
+#pragma unroll
+            for (int d = 0; d < RO; ++d) o += ko[d] * p.lks[l][d];
+            kbase[l] = o;
+        }
+        auto offsets = [&](i64 r, i64(&off)[XTG_KMAX_LEAVES]) {
+            i64 ri[RR];
+            decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);
+#pragma unroll
+            for (int l = 0; l < LS::N; ++l) {
+                i64 o = kbase[l];
+#pragma unroll
+                for (int d = 0; d < RR; ++d) o += ri[d] * p.lrs[l][d];
+                off[l] = o;
+            }
+        };
+        // positions of the item share their high 32 bits: the held
+        // arg-update selects the low word only
+        const bool lo32 = (rb >> 32) == ((re - 1) >> 32);
         if constexpr (RS > 0) {
             const int lstride = (int)blockDim.x * 16;
             const int sstride = LS::N * lstride;
             unsigned char* mine = col_ring + (size_t)threadIdx.x * 16;
             auto issue = [&](i64 r, int st) {
-                i64 ri[RR];
-                decode_dims<RR, BIG>(p.rshape, p.rfd, r, ri);
                 i64 off[XTG_KMAX_LEAVES];
-                red_offsets<LS::N, RO, RR>(p, ko, ri, off);
+                offsets(r, off);
                 Ring<LS, VEC>::issue(mine + (size_t)st * sstride, lstride, p.leaf, off);
             };
 #pragma unroll
@@ -1660,7 +1802,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
                 const int sf = st == 0 ? RS - 1 : st - 1;
                 if (r + RS - 1 < re) issue(r + RS - 1, sf);
                 cp_async_commit();
-                ColStep<Tree, Acc, VEC>::run(acc, rg, r, c, held);
+                ColStep<Tree, Acc, VEC>::run(acc, rg, r, c, held, lo32);
                 st = st == RS - 1 ? 0 : st + 1;
             }
             cp_async_wait<0>();
@@ -1670,16 +1812,14 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 if (r + u < re) {
-                    i64 ri[RR];
-                    decode_dims<RR, BIG>(p.rshape, p.rfd, r + u, ri);
                     i64 off[XTG_KMAX_LEAVES];
-                    red_offsets<LS::N, RO, RR>(p, ko, ri, off);
+                    offsets(r + u, off);
                     LoadLeavesAt<LS>::template run<VEC>(rg[u], p.leaf, off, inner);
                 }
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                if (r + u < re) ColStep<Tree, Acc, VEC>::run(acc, rg[u], r + u, c, held);
+                if (r + u < re) ColStep<Tree, Acc, VEC>::run(acc, rg[u], r + u, c, held, lo32);
             }
         }
         }
@@ -1715,7 +1855,7 @@ __global__ void __launch_bounds__(256) k_reduce_combine_thread(const RedParams p
         i64 oo = 0;
 #pragma unroll
         for (int d = 0; d < RO; ++d) oo += ko[d] * p.ostr[d];
-        reinterpret_cast<Out*>(p.out)[oo] = finish<Out, Acc, POST>(a, p);
+        Store<Out, Acc, POST>::put(a, p, oo);
     }
 }
 
@@ -1739,7 +1879,7 @@ __global__ void __launch_bounds__(256) k_reduce_combine(const RedParams p) {
             i64 oo = 0;
 #pragma unroll
             for (int d = 0; d < RO; ++d) oo += ko[d] * p.ostr[d];
-            reinterpret_cast<Out*>(p.out)[oo] = finish<Out, Acc, POST>(a, p);
+            Store<Out, Acc, POST>::put(a, p, oo);
         }
         __syncthreads();
     }
@@ -3347,7 +3487,7 @@ __global__ void __launch_bounds__(288) k_reduce_stream(const RedParams p) {
         acc = consumer_reduce(acc, smem);
         if (tid == 0) {
             if (p.nsplit > 1) reinterpret_cast<Acc*>(p.partial)[w] = acc;
-            else reinterpret_cast<Out*>(p.out)[0] = finish<Out, Acc, POST>(acc, p);
+            else Store<Out, Acc, POST>::put(acc, p, 0);
         }
         bar_sync_n<256>();  // smem is reused by the next item's combine
     }

@@ -114,6 +114,11 @@ struct RedParams {
     i64 eks[XTG_KMAX_RANK];
     i64 ers[XTG_KMAX_RANK];
     int* err;  // streaming row kernel: set to 1 when a bounded wait gives up
+    // one-pass moments (xtg_reduce_moments): mean, variance and norm_l2
+    // destinations beside the sum's `out` (null: not wanted), and the
+    // variance divisor (the mean's is `divisor`)
+    void* out_more[3];
+    double divisor2;
 };
 
 struct RowParams {

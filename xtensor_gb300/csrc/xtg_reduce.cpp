@@ -175,10 +175,19 @@ static int kind_of(int64_t s) { return s == 1 ? 0 : (s == 0 ? 1 : 2); }
 // strategy does that — any other plan returns XTG_ERR_UNSUPPORTED before a
 // launch, and the caller evaluates in two calls instead.
 static const char* kNotFusable = "fused assign + reduce: not a row reduction plan";
+// One-pass moments (xtg_reduce_moments): the accumulator is xtg::AccStats and
+// `outc` names the xtg::StatsOut of the four result types; only the streaming
+// kernel (K13) takes it — any other plan returns XTG_ERR_UNSUPPORTED before a
+// launch (with *not_fusable set) and the caller runs the four reductions.
+struct StatsSpec {
+    std::string outc;
+    bool has_sum;  // the sum's destination is `out` (else `out` only shapes the plan)
+};
 static xtg_status run_reduction(const Tree& t, const std::string& accname, int post, int out_dt, const int* kept,
                                 int nk, const int* red, int nr, const xtg_array& out, const int64_t* ostr_kept,
                                 xtg::RedParams& p, cudaStream_t stream, const ScratchSpec* scratch,
-                                const xtg_array* eout = nullptr, bool* not_fusable = nullptr) {
+                                const xtg_array* eout = nullptr, bool* not_fusable = nullptr,
+                                const StatsSpec* stats = nullptr) {
     const int NL = (int)t.leaves.size();
     std::vector<std::array<int64_t, XTG_MAX_RANK>> full(NL);
     for (int l = 0; l < NL; ++l) leaf_bstrides(t, l, full[l].data());
@@ -292,7 +301,7 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
         for (int d = 0; d < RO; ++d) p.lks[l][d] = K.st[1 + l][d];
         for (int d = 0; d < RR; ++d) p.lrs[l][d] = Rd.st[l][d];
     }
-    p.out = out.data;
+    p.out = (stats && !stats->has_sum) ? nullptr : out.data;
     for (int d = 0; d < RO; ++d) p.ostr[d] = K.st[0][d];
     memset(&p.scal, 0, sizeof p.scal);
     for (size_t i = 0; i < t.scalars.size(); ++i) p.scal.v[i] = t.scalars[i];
@@ -323,10 +332,24 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
     }
     ls += ">";
     const std::string tree = tree_type(t, t.root, map);
-    const std::string outc = dt(out_dt).cname;
+    const std::string outc = stats ? stats->outc : std::string(dt(out_dt).cname);
+
+    // K13: a full reduction of one contiguous leaf in 16-byte vectors with a
+    // double-float accumulator streams through shared memory (the same
+    // vectors, order and tree as K3 with a 256-thread group, so the same bits)
+    const bool dfloat = stats || accname == "xtg::AccSumC" || accname.rfind("xtg::AccMom<float", 0) == 0 ||
+                        accname.rfind("xtg::AccNormC<", 0) == 0;
+    const bool k13 = row && !eout && n_out == 1 && RR == 1 && NL == 1 && kinds[0] == 0 && dfloat &&
+                     opt("reduce.packed", 1) && opt("reduce.stream", 1) && vec * dt(t.leaves[0].dtype).size == 16 &&
+                     aligned(t.leaves[0].data, 16) && chunk >= opt("reduce.cta_chunk", 2048);
+    if (stats && !k13) {
+        if (not_fusable) *not_fusable = true;
+        return fail(XTG_ERR_UNSUPPORTED, "one-pass moments: not a streaming plan");
+    }
 
     void* part = nullptr;
-    const size_t part_bytes = (size_t)n_out * (size_t)nsplit * 32;
+    // split partial slots: 32 bytes, 64 for the one-pass moments' state
+    const size_t part_bytes = (size_t)n_out * (size_t)nsplit * (stats ? 64 : 32);
     if (nsplit > 1) {
         if (scratch && scratch->fixed) {
             if (part_bytes > scratch->fixed_bytes)
@@ -343,14 +366,7 @@ static xtg_status run_reduction(const Tree& t, const std::string& accname, int p
 
     Kernel* k;
     xtg_status st;
-    // K13: a full reduction of one contiguous leaf in 16-byte vectors with a
-    // double-float accumulator streams through shared memory (the same
-    // vectors, order and tree as K3 with a 256-thread group, so the same bits)
-    const bool dfloat = accname == "xtg::AccSumC" || accname.rfind("xtg::AccMom<float", 0) == 0 ||
-                        accname.rfind("xtg::AccNormC<", 0) == 0;
-    if (row && !eout && n_out == 1 && RR == 1 && NL == 1 && kinds[0] == 0 && dfloat && opt("reduce.packed", 1) &&
-        opt("reduce.stream", 1) && vec * dt(t.leaves[0].dtype).size == 16 && aligned(t.leaves[0].data, 16) &&
-        chunk >= opt("reduce.cta_chunk", 2048)) {
+    if (k13) {
         const int NS = (int)std::max<int64_t>(2, std::min<int64_t>(opt("reduce.stream_stages", 4), 6));
         const size_t smem = (size_t)NS * 16384;
         int* err = nullptr;
@@ -658,11 +674,98 @@ static xtg_status assign_reduce_impl(const xtg_expr* e, const xtg_array* oute, c
     return reduce_impl(&le, rd, outr, stream, nullptr);
 }
 
+// sum, mean, variance (ddof from rd) and norm_l2 of e over rd's axes from
+// one pass when the plan streams (K13), else the four reductions in turn.
+xtg_status moments_impl(const xtg_expr* e, const xtg_reduce_desc* rd0, const xtg_array* const outs[4],
+                        cudaStream_t stream) {
+    static const int kOps[4] = {XTG_RED_SUM, XTG_RED_MEAN, XTG_RED_VARIANCE, XTG_RED_NORM_L2};
+    if (!rd0) return fail(XTG_ERR_INVALID, "null reduce descriptor");
+    int first = -1;
+    for (int i = 0; i < 4; ++i)
+        if (outs[i] && first < 0) first = i;
+    if (first < 0) return fail(XTG_ERR_INVALID, "no destination");
+    xtg_reduce_desc rds[4];
+    for (int i = 0; i < 4; ++i) {
+        rds[i] = *rd0;
+        rds[i].op = kOps[i];
+        if (i != 2) rds[i].ddof = 0;
+    }
+    Tree t;
+    XTG_TRY(build_tree(e, opt("fp32_compute", 1) != 0, t));
+    bool one_pass = !t.n_rstats && !rd0->has_initial;
+    RedShape S;
+    if (one_pass) XTG_TRY(red_shape(t, rd0, rd0->keep_dims != 0, S));
+    const int vt = t.nodes[t.root].cxx_dtype;
+    int rts[4];
+    for (int i = 0; one_pass && i < 4; ++i) {
+        rts[i] = result_type(&rds[i], vt);
+        if (!outs[i]) continue;
+        if (outs[i]->dtype != rts[i])
+            return fail(XTG_ERR_INVALID, "destination dtype " + std::to_string(outs[i]->dtype) +
+                                             " differs from the result type " + std::to_string(rts[i]));
+        if (!out_matches(*outs[i], S.out_rank, S.out_shape)) return fail(XTG_ERR_SHAPE, "destination shape mismatch");
+        if (!outs[i]->data) return fail(XTG_ERR_INVALID, "null destination data");
+    }
+    if (one_pass) {
+        AccChoice ch[4];
+        for (int i = 0; i < 4; ++i) XTG_TRY(choose_acc(t, &rds[i], ch[i]));
+        one_pass = ch[0].acc == "xtg::AccSumC" && ch[1].acc == "xtg::AccSumC" && ch[2].acc == "xtg::AccMom<float, 1>" &&
+                   ch[3].acc == "xtg::AccNormC<2>";
+    }
+    if (one_pass) {
+        XTG_TRY(ensure_device(nullptr));
+        xtg::RedParams p;
+        memset(&p, 0, sizeof p);
+        int64_t size = 1, n_out = 1;
+        for (int d = 0; d < t.rank; ++d) size *= t.shape[d];
+        for (int d = 0; d < t.rank; ++d)
+            if (!S.is_red[d]) n_out *= t.shape[d];
+        p.divisor = n_out ? (double)(size / n_out) : 0.0;
+        p.divisor2 = n_out ? (double)((size - rd0->ddof) / n_out) : 0.0;
+        for (int i = 1; i < 4; ++i) p.out_more[i - 1] = outs[i] ? outs[i]->data : nullptr;
+        const xtg_array& ref = *outs[first];
+        int kept[XTG_MAX_RANK], red[XTG_MAX_RANK], nk = 0, nr = 0;
+        int64_t ostr[XTG_MAX_RANK];
+        int oi = 0;
+        for (int d = 0; d < t.rank; ++d) {
+            if (S.is_red[d]) {
+                red[nr++] = d;
+                if (rd0->keep_dims) ++oi;
+            } else {
+                kept[nk] = d;
+                ostr[nk] = ref.strides[oi++];
+                ++nk;
+            }
+        }
+        StatsSpec ss;
+        ss.outc = std::string("xtg::StatsOut<") + dt(rts[0]).cname + ", " + dt(rts[1]).cname + ", " + dt(rts[2]).cname +
+                  ", " + dt(rts[3]).cname + ">";
+        ss.has_sum = outs[0] != nullptr;
+        bool not_streaming = false;
+        const xtg_status st = run_reduction(t, "xtg::AccStats", 0, rts[first], kept, nk, red, nr, ref, ostr, p, stream,
+                                            nullptr, nullptr, &not_streaming, &ss);
+        if (!not_streaming) return st;
+        clear_error();
+    }
+    for (int i = 0; i < 4; ++i)
+        if (outs[i]) XTG_TRY(reduce_impl(e, &rds[i], outs[i], stream, nullptr));
+    return XTG_OK;
+}
+
 }  // namespace xtgh
 
 using namespace xtgh;
 
 extern "C" {
+
+xtg_status xtg_reduce_moments(const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* sum,
+                              const xtg_array* mean, const xtg_array* variance, const xtg_array* norm_l2,
+                              xtg_stream stream) {
+    begin_call();
+    if (!e) return fail(XTG_ERR_INVALID, "null expression");
+    const xtg_array* outs[4] = {sum, mean, variance, norm_l2};
+    return moments_impl(e, rd, outs, (cudaStream_t)stream);
+}
 
 xtg_status xtg_assign_reduce(const xtg_expr* e, const xtg_array* out_e, const xtg_reduce_desc* rd,
                              const xtg_array* out_r, xtg_stream stream) {

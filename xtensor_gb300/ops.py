@@ -91,6 +91,30 @@ def reduce(op: str, e, axes=None, keep_dims=False, initial=None, acc_dtype=None,
     return out
 
 
+MOMENTS = ("sum", "mean", "variance", "norm_l2")
+
+
+def reduce_moments(e, axes=None, keep_dims=False, ddof=0, which=MOMENTS, outs: Optional[dict] = None,
+                   stream=None) -> dict:
+    """sum, mean, variance (ddof) and norm_l2 of e over the same axes
+    (xtg_reduce_moments: one pass over e when the plan streams, each result
+    equal to its own reduce() call); returns {name: DeviceArray} for `which`."""
+    e = as_expr(e)
+    outs = dict(outs or {})
+    for nm in which:
+        if nm not in MOMENTS:
+            raise ValueError(f"unknown moment {nm!r}")
+        if nm not in outs:
+            shape, dt = reduce_shape(nm, e, axes=axes, keep_dims=keep_dims, ddof=ddof if nm == "variance" else 0)
+            outs[nm] = DeviceArray.empty(shape, dt, stream)
+    ex, keep = lower(e)
+    rd = make_desc("variance", axes=axes, keep_dims=keep_dims, ddof=ddof)
+    arrs = [outs[nm].xtg_array() if nm in which else None for nm in MOMENTS]
+    ptrs = [C.byref(a) if a is not None else None for a in arrs]
+    check(lib().xtg_reduce_moments(C.byref(ex), C.byref(rd), *ptrs, _sh(stream)))
+    return {nm: outs[nm] for nm in which}
+
+
 def assign_reduce(out_e: DeviceArray, e, op: str, axes=None, keep_dims=False, initial=None, acc_dtype=None, ddof=0,
                   precision=0, out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
     """out_e = e, then the reduction `op` of out_e (xtg_assign_reduce: one
