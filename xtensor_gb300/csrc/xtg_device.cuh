@@ -1165,15 +1165,6 @@ template <class A, int MAXOP> struct AccArg {
             idx = ps;
         }
     }
-    // add_held() when every position of the work item has idx's high 32
-    // bits: only the low word is selected
-    template <class X> XTG_DI void add_held_lo(X x, u32 lo) {
-        A a = cvt<A>(x);
-        if (MAXOP ? Cmp<A>::gt(a, v) : Cmp<A>::lt(a, v)) {
-            v = a;
-            idx = (i64)(((u64)idx & 0xFFFFFFFF00000000ull) | (u64)lo);
-        }
-    }
     XTG_DI bool held() const { return idx >= 0; }
     XTG_DI void merge(const AccArg& o) {
         if (o.idx < 0) return;
@@ -1310,16 +1301,11 @@ template <int M> struct HeldFast<AccArg<double, M>> { enum { value = 0 }; };
 // (held == true) the compare-and-select form.
 template <class Tree, class Acc, int VEC> struct ColStep {
     template <class RG, class C>
-    static XTG_DI void run(Acc (&acc)[VEC], const RG& rg, i64 r, const C& c, bool& held, bool lo32) {
+    static XTG_DI void run(Acc (&acc)[VEC], const RG& rg, i64 r, const C& c, bool& held) {
         if constexpr (HeldFast<Acc>::value) {
             if (held) {
-                if (lo32) {
 #pragma unroll
-                    for (int j = 0; j < VEC; ++j) acc[j].add_held_lo(Tree::ev(rg, j, c), (u32)r);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < VEC; ++j) acc[j].add_held(Tree::ev(rg, j, c), r);
-                }
+                for (int j = 0; j < VEC; ++j) acc[j].add_held(Tree::ev(rg, j, c), r);
                 return;
             }
             bool h = true;
@@ -1776,9 +1762,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
                 off[l] = o;
             }
         };
-        // positions of the item share their high 32 bits: the held
-        // arg-update selects the low word only
-        const bool lo32 = (rb >> 32) == ((re - 1) >> 32);
+
         if constexpr (RS > 0) {
             const int lstride = (int)blockDim.x * 16;
             const int sstride = LS::N * lstride;
@@ -1802,7 +1786,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
                 const int sf = st == 0 ? RS - 1 : st - 1;
                 if (r + RS - 1 < re) issue(r + RS - 1, sf);
                 cp_async_commit();
-                ColStep<Tree, Acc, VEC>::run(acc, rg, r, c, held, lo32);
+                ColStep<Tree, Acc, VEC>::run(acc, rg, r, c, held);
                 st = st == RS - 1 ? 0 : st + 1;
             }
             cp_async_wait<0>();
@@ -1819,7 +1803,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                if (r + u < re) ColStep<Tree, Acc, VEC>::run(acc, rg[u], r + u, c, held, lo32);
+                if (r + u < re) ColStep<Tree, Acc, VEC>::run(acc, rg[u], r + u, c, held);
             }
         }
         }

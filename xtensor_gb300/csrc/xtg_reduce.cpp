@@ -147,14 +147,15 @@ static void lim_max(int t, double& f, int64_t& i) {
 
 // Stages of the column kernel's asynchronous-copy ring (0: register loads): used
 // when every leaf is contiguous along the vectorised dimension with 4-, 8-
-// or 16-byte vectors; 8 / leaves stages (at least 2), at most 4 leaves.
+// or 16-byte vectors; 8 / leaves stages by default (the option takes up to
+// 16 / leaves; at least 2), at most 4 leaves.
 static int async_stages(const Tree& t, const std::vector<int>& kinds, int NL, int vec, const char* on_key, const char* stages_key) {
     if (!opt(on_key, 1) || NL < 1 || NL > 4) return 0;
     for (int l = 0; l < NL; ++l) {
         const int b = vec * dt(t.leaves[l].dtype).size;
         if (kinds[l] != 0 || !(b == 4 || b == 8 || b == 16)) return 0;
     }
-    return (int)std::max<int64_t>(2, std::min<int64_t>(opt(stages_key, 8), 8 / NL));
+    return (int)std::max<int64_t>(2, std::min<int64_t>(opt(stages_key, 8 / NL), 16 / NL));
 }
 
 static unsigned grid_cap(Kernel* k, int64_t need) {
