@@ -586,6 +586,7 @@ def port_lib():
         getattr(L, f"bl_argmax_1_{t}").argtypes = [P, P, i64, i64, i64, P]
     L.bl_c0_assign.argtypes = [P, P, P, i64, i64]
     L.bl_c0_sum.argtypes = [P, P, i64, i64]
+    L.bl_c3_rowsum_f32.argtypes = [P, P, P, P, i64, i64]
     L.bl_sum_i32_i64.argtypes = [P, i64]
     L.bl_sum_i32_i64.restype = i64
     for t in ("f32", "bf16"):
@@ -1220,6 +1221,34 @@ def c3_section(args):
     info = b.info()
     b.close()
     gbs = total / (graph_ms / 1e3) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        # the port of the reference's lazy row sum over a bounded sample: the
+        # first 192 instances (about 3 GB), copied to the host, best of 2
+        Lp = port_lib()
+        k_s = min(192, n_inst)
+        host = [(A.to_numpy(), v.to_numpy(), Cm.to_numpy(), np.empty(out.shape, np.float32))
+                for A, v, Cm, out in inst[:k_s]]
+        sb = int(sum(4 * (2 * a.size + vv.size + o.size) for a, vv, _, o in host))
+
+        def port_run():
+            for a, vv, cm, o in host:
+                Lp.bl_c3_rowsum_f32(a.ctypes.data, vv.ctypes.data, cm.ctypes.data, o.ctypes.data, a.shape[0],
+                                    a.shape[1])
+        port_run()
+        ts = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            port_run()
+            ts.append(time.perf_counter() - t0)
+        dev_err = max(float(np.max(np.abs(out.to_numpy().astype(np.float64) - o.astype(np.float64)) /
+                                   (np.abs(a.astype(np.float64) * vv.astype(np.float64)) +
+                                    np.abs(cm.astype(np.float64))).sum(1)))
+                      for (a, vv, cm, o), (_, _, _, out) in zip(host, inst))
+        cpu = {"value": round(sb / min(ts) / 1e9, 3), "unit": "GB/s", "cores": cores(), "kind": "port",
+               "sample": f"the first {k_s} of the {n_inst} instances ({sb / 1e9:.2f} GB), best of 2 after a warm-up "
+                         f"(compiled port of the reference's lazy row sum, OpenMP {cores()} threads over rows)",
+               "gpu_vs_port_max_err_over_sum_abs": dev_err}
     return {
         "workload": C3_WORKLOAD, "instances": n_inst, "algorithmic_bytes": total, "elements": int(info["elements"]),
         "value": round(gbs, 1), "unit": "GB/s", "l2": "68.9 GB of operands, far larger than L2: no flush",
@@ -1235,6 +1264,7 @@ def c3_section(args):
         "build_s": round(t_build, 2), "gpu_launches": int(l1 - l0),
         "accuracy": {"max_rel_err_vs_fp64_sum_abs": worst, "plain_max_rel_err_vs_fp64_sum_abs": worst_plain,
                      "bound": 1e-6, "sample": "first 16 instances"},
+        "cpu_baseline": cpu,
         "e2e": None,
         "e2e_note": "operands are generated and kept on the device by definition of the batching workload",
     }

@@ -350,13 +350,19 @@ namespace detail {
 struct device_buffer {
     void* ptr = nullptr;
     std::size_t bytes = 0;
+    std::shared_ptr<device_buffer> base;  // set: a view of `bytes` at `ptr` inside base (freed with it)
     explicit device_buffer(std::size_t b) : bytes(b) { check(xtg_malloc(&ptr, b ? b : 1, current_stream())); }
+    device_buffer(std::shared_ptr<device_buffer> b, std::size_t offset, std::size_t n)
+        : ptr((char*)b->ptr + offset), bytes(n), base(std::move(b)) {}
     ~device_buffer() {
-        if (ptr) xtg_free(ptr, current_stream());
+        if (ptr && !base) xtg_free(ptr, current_stream());
     }
     device_buffer(const device_buffer&) = delete;
     device_buffer& operator=(const device_buffer&) = delete;
 };
+// tag of the constructor that adopts existing device storage
+struct adopt_t {};
+constexpr adopt_t adopt{};
 
 template <class S> std::vector<std::ptrdiff_t> row_major_strides(const S& shape) {
     std::vector<std::ptrdiff_t> st(shape.size());
@@ -426,6 +432,11 @@ public:
         from_nested(l);
     }
     template <class E> xdevice_container(const xexpression<E>& e) { assign_expr(e.derived_cast(), true); }
+    // a row-major container of `shape` over existing device storage
+    template <class S> xdevice_container(detail::adopt_t, const S& shape, std::shared_ptr<detail::device_buffer> buf) {
+        set_shape(to_shape(shape), false);
+        m_buf = std::move(buf);
+    }
     xdevice_container(const xdevice_container& o) {
         set_shape(o.m_shape);
         copy_from(o);

@@ -5,12 +5,15 @@
 // scalar (views/xbroadcast.hpp).  Included by xt.hpp.
 //
 // Every chunk is a device xarray of chunk_shape (edge chunks keep their
-// padding, as in the reference).  Assigning an expression to a chunked array
+// padding, as in the reference); the chunks of one array share one
+// allocation, at a 256-byte aligned distance, so that the library reduces a
+// class of equal chunks as one strided array.  Assigning an expression to a chunked array
 // evaluates all chunks in one kernel (xtg_chunked_assign); a chunked operand
 // of the same grid is read chunk by chunk in place, one of another grid is
 // first read into a dense temporary.  Reading a chunked array into a dense
 // container is xtg_chunked_to_dense; xt::sum / mean / ... of a chunked array
-// reduce chunk by chunk (xtg_chunked_reduce).
+// reduce through xtg_chunked_reduce (one strided reduction per class of
+// equal chunks of the slab).
 #pragma once
 
 #include <numeric>
@@ -75,16 +78,12 @@ public:
         reshape_grid(shape_of(e.derived_cast()));
         noalias_assign(e.derived_cast());
     }
-    xchunked_array(const xchunked_array& o) : m_shape(o.m_shape), m_chunk_shape(o.m_chunk_shape), m_grid(o.m_grid) {
-        for (const auto& c : o.m_chunks) m_chunks.push_back(c);
-    }
+    xchunked_array(const xchunked_array& o) : m_chunk_shape(o.m_chunk_shape) { copy_from(o); }
     xchunked_array(xchunked_array&&) noexcept = default;
     xchunked_array& operator=(const xchunked_array& o) {
         if (this != &o) {
-            m_shape = o.m_shape;
             m_chunk_shape = o.m_chunk_shape;
-            m_grid = o.m_grid;
-            m_chunks = o.m_chunks;
+            copy_from(o);
         }
         return *this;
     }
@@ -216,9 +215,23 @@ private:
             m_grid[d] = shape[d] / m_chunk_shape[d] + (shape[d] % m_chunk_shape[d] > 0 ? 1 : 0);
             n *= m_grid[d];
         }
+        // one slab, chunks at a 256-byte aligned distance
+        std::size_t celems = 1;
+        for (auto c : m_chunk_shape) celems *= c;
+        const std::size_t dist = (std::max<std::size_t>(celems * sizeof(T), 1) + 255) / 256 * 256;
+        auto slab = std::make_shared<detail::device_buffer>(n * dist);
         m_chunks.clear();
         m_chunks.reserve(n);
-        for (std::size_t i = 0; i < n; ++i) m_chunks.emplace_back(m_chunk_shape);
+        for (std::size_t i = 0; i < n; ++i)
+            m_chunks.emplace_back(detail::adopt, m_chunk_shape,
+                                  std::make_shared<detail::device_buffer>(slab, i * dist, celems * sizeof(T)));
+    }
+    // a copy with its own slab: every chunk's buffer, padding included
+    void copy_from(const xchunked_array& o) {
+        reshape_grid(o.m_shape);
+        for (std::size_t i = 0; i < m_chunks.size(); ++i)
+            detail::check(xtg_memcpy(m_chunks[i].data(), o.m_chunks[i].data(), o.m_chunks[i].size() * sizeof(T),
+                                     XTG_MEMCPY_D2D, detail::current_stream()));
     }
     bool same_grid(const xtg_chunked& c) const {
         if (c.rank != (int32_t)m_shape.size()) return false;

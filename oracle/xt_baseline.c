@@ -28,6 +28,7 @@
  *                       last, then a strict-greater scan per row
  *                       (xsort.hpp:1158-1235).
  *   bl_c0_*             E = A * b + exp(-A * A); r = sum(E, {1}).
+ *   bl_c3_rowsum_f32    one batching instance: r = sum(A * v + C, {1}).
  *   bl_sum_*            full sums (sequential, as the lazy reducer).
  *   bl_stat_*_f32 / _bf16
  *                       the precision workload's full reductions, one
@@ -158,6 +159,19 @@ void bl_c0_sum(const float* E, float* r, int64_t n, int64_t m) {
     for (int64_t i = 0; i < n; ++i) {
         float s = 0.f;
         for (int64_t j = 0; j < m; ++j) s = s + E[i * m + j];
+        r[i] = s;
+    }
+}
+
+/* C3, one instance: r = sum(A * v + C, {1}) with A, C (n, m) and v (m,)
+ * float32: the lazy reducer evaluates the xfunction element by element in
+ * float and folds each row sequentially in float (xreducer.hpp:1819-1825);
+ * rows in parallel. */
+void bl_c3_rowsum_f32(const float* A, const float* v, const float* Cm, float* r, int64_t n, int64_t m) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        float s = 0.f;
+        for (int64_t j = 0; j < m; ++j) s = s + (A[i * m + j] * v[j] + Cm[i * m + j]);
         r[i] = s;
     }
 }

@@ -13,6 +13,7 @@ compared with the oracle's restatement of the reference
     variance in double, the tree in double, one cast);
   * C0's E = A * b + exp(-A * A) and its row sums: bit-exact (the same
     libm expf, the same sequential float fold);
+  * one C3 instance, sum(A * v + C, {1}): bit-exact;
   * full float32 / int32 -> int64 sums: bit-exact (sequential folds);
   * the precision workload's sum / mean / variance / norm_l2 of float32
     and bfloat16 arrays: bit-exact;
@@ -45,6 +46,7 @@ def port():
         getattr(L, f"bl_argmax_1_{t}").argtypes = [P, P, I64, I64, I64, P]
     L.bl_c0_assign.argtypes = [P, P, P, I64, I64]
     L.bl_c0_sum.argtypes = [P, P, I64, I64]
+    L.bl_c3_rowsum_f32.argtypes = [P, P, P, P, I64, I64]
     L.bl_sum_f32.argtypes = [P, I64]
     L.bl_sum_f32.restype = C.c_float
     L.bl_sum_i32_i64.argtypes = [P, I64]
@@ -112,6 +114,19 @@ def test_port_c0_equals_oracle(n, m):
     r = np.empty((n,), np.float32)
     L.bl_c0_sum(ptr(E), ptr(r), n, m)
     np.testing.assert_array_equal(r, O.reduce("sum", HostArray(E), [1]))
+
+
+@pytest.mark.parametrize("n,m", [(1, 16), (37, 45), (5, 2048)])
+def test_port_c3_instance_equals_oracle(n, m):
+    L = port()
+    g = np.random.default_rng(3)
+    A = g.uniform(-1, 1, (n, m)).astype(np.float32)
+    v = g.standard_normal(m).astype(np.float32)
+    Cm = g.uniform(-1, 1, (n, m)).astype(np.float32)
+    r = np.empty((n,), np.float32)
+    L.bl_c3_rowsum_f32(ptr(A), ptr(v), ptr(Cm), ptr(r), n, m)
+    want = O.reduce("sum", HostArray(A) * HostArray(v) + HostArray(Cm), [1])
+    np.testing.assert_array_equal(r, want)
 
 
 def test_port_full_sums_equal_oracle():

@@ -225,7 +225,9 @@ def as_chunked_assign(dst: DeviceArray, chunk_shape, e, stream=None) -> DeviceAr
 
 def chunked_reduce(op: str, src: ChunkedArray, axes=None, keep_dims=False, acc_dtype=None,
                    out: Optional[DeviceArray] = None, stream=None) -> DeviceArray:
-    """A reducer over a chunked array (xt::sum(a, axes), ...), chunk by chunk."""
+    """A reducer over a chunked array (xt::sum(a, axes), ...): one strided
+    reduction per class of equal chunks when the chunks sit at equal
+    distances (as this module allocates them), chunk by chunk otherwise."""
     from .ops import make_desc, reduce_shape
     shape, dt = reduce_shape(op, _DenseLike(src), axes=axes, keep_dims=keep_dims, acc_dtype=acc_dtype)
     if out is None:

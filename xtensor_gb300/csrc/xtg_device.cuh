@@ -1165,6 +1165,15 @@ template <class A, int MAXOP> struct AccArg {
             idx = ps;
         }
     }
+    // add_held() with the candidate's position kept as a 32-bit offset `ro`
+    // from the work item's start, in `bo` (the caller adds the start back)
+    template <class X> XTG_DI void add_held_off(X x, u32 ro, u32& bo) {
+        A a = cvt<A>(x);
+        if (MAXOP ? Cmp<A>::gt(a, v) : Cmp<A>::lt(a, v)) {
+            v = a;
+            bo = ro;
+        }
+    }
     XTG_DI bool held() const { return idx >= 0; }
     XTG_DI void merge(const AccArg& o) {
         if (o.idx < 0) return;
@@ -1778,6 +1787,11 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
                 cp_async_commit();
             }
             int st = 0;
+            // held arg-updates keep the best position as a 32-bit offset from
+            // rb (one select instead of two per element) when the item allows
+            u32 bo[VEC];
+            bool h32 = false;
+            const bool can32 = re - rb <= (i64)0xFFFFFFFF;
             for (i64 r = rb; r < re; ++r) {
                 cp_async_wait<RS - 2>();  // row r's copies have landed
                 RG rg;
@@ -1786,8 +1800,29 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
                 const int sf = st == 0 ? RS - 1 : st - 1;
                 if (r + RS - 1 < re) issue(r + RS - 1, sf);
                 cp_async_commit();
-                ColStep<Tree, Acc, VEC>::run(acc, rg, r, c, held);
+                if constexpr (HeldFast<Acc>::value) {
+                    if (h32) {
+                        const u32 ro = (u32)(r - rb);
+#pragma unroll
+                        for (int j = 0; j < VEC; ++j) acc[j].add_held_off(Tree::ev(rg, j, c), ro, bo[j]);
+                    } else {
+                        ColStep<Tree, Acc, VEC>::run(acc, rg, r, c, held);
+                        if (held && can32) {
+                            h32 = true;
+#pragma unroll
+                            for (int j = 0; j < VEC; ++j) bo[j] = (u32)(acc[j].idx - rb);
+                        }
+                    }
+                } else {
+                    ColStep<Tree, Acc, VEC>::run(acc, rg, r, c, held);
+                }
                 st = st == RS - 1 ? 0 : st + 1;
+            }
+            if constexpr (HeldFast<Acc>::value) {
+                if (h32) {
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) acc[j].idx = rb + (i64)bo[j];
+                }
             }
             cp_async_wait<0>();
         } else {
