@@ -1096,13 +1096,15 @@ template <> struct HasAdd2<AccStats2> { enum { value = 1 }; };
 // moments about 21 FP32 instructions per 8 values, packed, instead of 76; for
 // sums of 2-byte values about 11 instead of 28: at HBM speed those loops are
 // bound by instruction issue and the FP32 pipe).
-// Used for the moments of variance / stddev (the squares' terms are >= 0) and
-// for sums, means and norms of 2-byte inputs (bfloat16 / float16: 8 or 11
-// significant bits, so a vector's pairwise sum is mostly exact); float32 sums,
-// means and norms keep a TwoSum per element.
+// Used where the blocks' rounding stays small against the result: the
+// moments of variance / stddev and the norms (squares and absolute values:
+// every term >= 0, so a block's error is relative to the block's own sum),
+// and sums and means of 2-byte inputs (bfloat16: 8 significant bits, so a
+// vector's pairwise sum is mostly exact); float32 sums and means keep a
+// TwoSum per element (their terms cancel).
 template <class W, class X> struct BlockAdd { enum { value = 0 }; };
 template <class X> struct BlockAdd<AccSumC2, X> { enum { value = sizeof(X) == 2 }; };
-template <int NK, class X> struct BlockAdd<AccNormC2<NK>, X> { enum { value = sizeof(X) == 2 }; };
+template <int NK, class X> struct BlockAdd<AccNormC2<NK>, X> { enum { value = 1 }; };
 template <int M, class X> struct BlockAdd<AccMom2<M>, X> { enum { value = M != 0 || sizeof(X) == 2 }; };
 
 template <class A> struct IsStats2 { enum { value = 0 }; };
