@@ -67,9 +67,6 @@ int64_t opt(const char* key, int64_t dflt);
 // Default work items a ROW reduction is split into (reduce.target_items):
 // shared by every planner of a reduction so equal calls partition alike.
 constexpr int64_t kReduceTargetItems = 2048;
-// Row plans whose items are a warp each fill up to this many items (about
-// 54 warps on each of 152 SMs) by splitting rows further.
-constexpr int64_t kReduceFillItems = 8192;
 // Option "jit.dry_run": plan and compile kernels without a GPU (no launches).
 bool dry_run();
 

@@ -468,8 +468,7 @@ xtg_status xtg_server_submit(xtg_server* s, const xtg_request* r, uint64_t* id) 
     if (r->kind == XTG_REQ_REDUCE || r->kind == XTG_REQ_ARGREDUCE) {
         int64_t n_out = 1;
         for (int d = 0; d < r->out.rank; ++d) n_out *= r->out.shape[d];
-        scratch = (std::max(opt("reduce.target_items", kReduceTargetItems), opt("reduce.fill_items", kReduceFillItems)) +
-                   n_out) * 32;
+        scratch = (opt("reduce.target_items", kReduceTargetItems) + n_out) * 32;
     }
     q->cost = std::max<int64_t>(0, r->workspace_bytes) + scratch;
     const bool last_axis = r->kind == XTG_REQ_REDUCE && r->rd.n_axes == 1 &&
