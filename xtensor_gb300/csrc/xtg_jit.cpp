@@ -128,7 +128,10 @@ xtg_status compile(const std::string& expr, const std::string& arch, std::string
 
 }  // namespace
 
-static thread_local std::string t_last_kernels;
+// The kernels launched by the calling thread's last evaluation call, as a
+// list of kernels (the names are joined only when asked for: they are long).
+static thread_local std::vector<const Kernel*> t_last_kernels;
+static thread_local std::string t_last_kernels_str;
 
 void begin_call() { t_last_kernels.clear(); }
 
@@ -310,8 +313,7 @@ xtg_status launch_raw(Kernel* k, unsigned grid, unsigned block, const void* para
         l.scratch_off = scratch_off;
         rec->launches.push_back(std::move(l));
     }
-    if (!t_last_kernels.empty()) t_last_kernels += ";";
-    t_last_kernels += k->name.compare(0, 5, "xtg::") == 0 ? k->name.substr(5) : k->name;
+    t_last_kernels.push_back(k);
     if (dry_run()) {
         g_launches.fetch_add(1, std::memory_order_relaxed);
         return XTG_OK;
@@ -326,7 +328,15 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 }  // namespace xtgh
 
-extern "C" const char* xtg_last_kernels(void) { return xtgh::t_last_kernels.c_str(); }
+extern "C" const char* xtg_last_kernels(void) {
+    std::string& r = xtgh::t_last_kernels_str;
+    r.clear();
+    for (const xtgh::Kernel* k : xtgh::t_last_kernels) {
+        if (!r.empty()) r += ";";
+        r += k->name.compare(0, 5, "xtg::") == 0 ? k->name.substr(5) : k->name;
+    }
+    return r.c_str();
+}
 
 extern "C" xtg_status xtg_get_jit_stats(xtg_jit_stats* st) {
     if (!st) return xtgh::fail(XTG_ERR_INVALID, "null stats");

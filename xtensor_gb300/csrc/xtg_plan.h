@@ -117,24 +117,24 @@ xtg_status choose_acc(const Tree& t, const xtg_reduce_desc* rd, AccChoice& ch);
 
 // ---- plan cache (xtg_plancache.cpp) -----------------------------------------------
 bool plan_cache_enabled();
-std::vector<unsigned char> plan_key(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out,
+std::vector<unsigned char>& plan_key(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out,
                                     int32_t a0, int32_t a1, int64_t a2, const xtg_array* out2 = nullptr);
 bool plan_replay(const std::vector<unsigned char>& key, cudaStream_t s, xtg_status* st);
-void plan_store(std::vector<unsigned char>&& key, Recorder& rec);
+void plan_store(const std::vector<unsigned char>& key, Recorder& rec);
 
 // Runs `fn` (a planning + launching call) through the plan cache.
 template <class F>
 xtg_status with_plan_cache(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out, int32_t a0,
                            int32_t a1, int64_t a2, cudaStream_t s, F&& fn, const xtg_array* out2 = nullptr) {
     if (!e || !out || !plan_cache_enabled() || recorder()) return fn();
-    std::vector<unsigned char> key = plan_key(kind, e, rd, out, a0, a1, a2, out2);
     xtg_status st;
-    if (plan_replay(key, s, &st)) return st;
+    if (plan_replay(plan_key(kind, e, rd, out, a0, a1, a2, out2), s, &st)) return st;
     Recorder rec;
     recorder() = &rec;
     st = fn();
     recorder() = nullptr;
-    if (st == XTG_OK) plan_store(std::move(key), rec);
+    // (the planning call may itself have used the thread's key buffer)
+    if (st == XTG_OK) plan_store(plan_key(kind, e, rd, out, a0, a1, a2, out2), rec);
     return st;
 }
 

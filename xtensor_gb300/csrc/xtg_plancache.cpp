@@ -38,10 +38,20 @@ Cache& cache() {
     return c;
 }
 
+// FNV-1a over 8-byte words (the tail byte by byte): keys are a few hundred
+// bytes and are hashed on every call.
 uint64_t fnv(const std::vector<unsigned char>& v) {
     uint64_t h = 1469598103934665603ull;
-    for (unsigned char c : v) {
-        h ^= c;
+    const size_t n = v.size(), nw = n / 8;
+    for (size_t i = 0; i < nw; ++i) {
+        uint64_t w;
+        memcpy(&w, v.data() + 8 * i, 8);
+        h ^= w;
+        h *= 1099511628211ull;
+        h ^= h >> 29;
+    }
+    for (size_t i = nw * 8; i < n; ++i) {
+        h ^= v[i];
         h *= 1099511628211ull;
     }
     return h;
@@ -66,10 +76,12 @@ void put_array(std::vector<unsigned char>& k, const xtg_array& a) {
 
 bool plan_cache_enabled() { return !dry_run() && opt("plan.cache", 1) != 0; }
 
-std::vector<unsigned char> plan_key(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out,
-                                    int32_t a0, int32_t a1, int64_t a2, const xtg_array* out2) {
-    std::vector<unsigned char> k;
-    k.reserve(512);
+std::vector<unsigned char>& plan_key(int kind, const xtg_expr* e, const xtg_reduce_desc* rd, const xtg_array* out,
+                                     int32_t a0, int32_t a1, int64_t a2, const xtg_array* out2) {
+    // one buffer per thread, reused: no allocation on the replay path
+    static thread_local std::vector<unsigned char> k;
+    k.clear();
+    k.reserve(1024);
     put(k, kind);
     put(k, opt_generation());
     put(k, e->n_nodes);
@@ -131,10 +143,10 @@ bool plan_replay(const std::vector<unsigned char>& key, cudaStream_t s, xtg_stat
     return true;
 }
 
-void plan_store(std::vector<unsigned char>&& key, Recorder& rec) {
+void plan_store(const std::vector<unsigned char>& key, Recorder& rec) {
     if (rec.scratch_allocs > 1 || rec.nocache) return;  // keep such calls uncached
     auto p = std::make_shared<Plan>();
-    p->key = std::move(key);
+    p->key = key;
     p->launches = std::move(rec.launches);
     p->scratch_bytes = rec.scratch_allocs ? rec.scratch_bytes : 0;
     for (auto& l : p->launches)
