@@ -53,6 +53,12 @@ struct bf16 {
     XTG_DI operator float() const { return __uint_as_float(((u32)bits) << 16); }
 };
 
+// Programmatic dependent launch: the host may launch a kernel while the one
+// before it in the stream still drains; every kernel waits here for its
+// predecessors (their writes visible) before it touches global memory.
+// Without the launch attribute this is a no-op.
+XTG_DI void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // Conversions: C++ static_cast semantics for arithmetic types, bf16 via float.
 template <class To> struct Cvt {
@@ -445,6 +451,7 @@ template <class T, class Cd, class A, class B> struct Where {
 // loads outstanding) so that HBM latency is hidden with few CTAs per SM.
 template <class Tree, class LS, class OutT, int OUTKIND, int VEC, int R, int U, bool BIG>
 __global__ void __launch_bounds__(256) k_assign(const AssignParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     Ctx<0> c;
     c.scal = p.scal;
@@ -488,6 +495,7 @@ __global__ void __launch_bounds__(256) k_assign(const AssignParams p) {
 // entries' extents bound the elements.
 template <class Tree, class LS, class OutT, int OUTKIND, int VEC, int R, int U, bool BIG, bool PAD = false>
 __global__ void __launch_bounds__(256) k_assign_chunks(const ChunkParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     Ctx<0> c;
     c.scal = p.scal;
@@ -1561,6 +1569,7 @@ struct ArrVal {
 template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int GROUP, bool BIG, int UR = 4,
           int ES = 0, class ET = float, int PK = 1>
 __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     __shared__ Acc smem[32];
     Ctx<0> c;
@@ -1721,6 +1730,7 @@ __global__ void __launch_bounds__(256) k_reduce_row(const RedParams p) {
 // Work items: w = s * n_outv + ov (consecutive threads -> consecutive outputs).
 template <class Tree, class LS, class Acc, class Out, int POST, int VEC, int RO, int RR, int U, bool BIG, int RS = 0>
 __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     extern __shared__ __align__(16) unsigned char col_ring[];
     Ctx<0> c;
@@ -1867,6 +1877,7 @@ __global__ void __launch_bounds__(256) k_reduce_col(const RedParams p) {
 // partials in split order.
 template <class Acc, class Out, int POST, int RO>
 __global__ void __launch_bounds__(256) k_reduce_combine_thread(const RedParams p) {
+    pdl_wait();
     const Acc* part = reinterpret_cast<const Acc*>(p.partial);
     for (i64 o = (i64)blockIdx.x * blockDim.x + threadIdx.x; o < p.n_out; o += (i64)gridDim.x * blockDim.x) {
         Acc a = part[o * p.nsplit];
@@ -1884,6 +1895,7 @@ __global__ void __launch_bounds__(256) k_reduce_combine_thread(const RedParams p
 // splits t, t+blockDim, … in order, then a fixed block tree.
 template <class Acc, class Out, int POST, int RO>
 __global__ void __launch_bounds__(256) k_reduce_combine(const RedParams p) {
+    pdl_wait();
     __shared__ Acc smem[32];
     const Acc* part = reinterpret_cast<const Acc*>(p.partial);
     for (i64 o = blockIdx.x; o < p.n_out; o += gridDim.x) {
@@ -1932,6 +1944,7 @@ template <class RT, int OP> struct ScanOp {
 // sequential order.
 template <class Tree, class LS, class RT, int OP, int VEC, int OKIND, int U>
 __global__ void __launch_bounds__(256) k_scan_col(const ScanParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     Ctx<0> c;
     c.scal = p.scal;
@@ -1987,6 +2000,7 @@ __global__ void __launch_bounds__(256) k_scan_col(const ScanParams p) {
 // multiples of VEC (the host checks).
 template <class Tree, class LS, class RT, int OP, int VEC, bool RAW = false>
 __global__ void __launch_bounds__(64) k_scan_rows(const ScanParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     constexpr int CW = 32 * VEC;        // columns per chunk
     constexpr int RS = CW + VEC;        // padded row stride (keeps 16-byte rows)
@@ -2247,6 +2261,7 @@ XTG_DI void scan_load16(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kt, i
 
 template <class Tree, class LS, class RT, int OP, int VEC>
 __global__ void __launch_bounds__(256) k_scan_seg_reduce(const ScanParams p) {
+    pdl_wait();
     typedef ScanState<RT, OP> ST;
     __shared__ ST wsum[9];
     Ctx<0> c;
@@ -2304,6 +2319,7 @@ __global__ void __launch_bounds__(256) k_scan_seg_reduce(const ScanParams p) {
 // (B) one CTA per row: exclusive prefixes of the row's segment totals, in place
 template <class RT, int OP>
 __global__ void __launch_bounds__(256) k_scan_seg_offsets(const ScanParams p) {
+    pdl_wait();
     typedef ScanState<RT, OP> ST;
     __shared__ ST wsum[9];
     const i64 nseg = nseg_of(p);
@@ -2329,6 +2345,7 @@ __global__ void __launch_bounds__(256) k_scan_seg_offsets(const ScanParams p) {
 // coalesced stores; the tile total joins the carry
 template <class Tree, class LS, class RT, int OP, int VEC>
 __global__ void __launch_bounds__(256) k_scan_seg_apply(const ScanParams p) {
+    pdl_wait();
     typedef ScanState<RT, OP> ST;
     __shared__ RT buf[VEC > 1 ? 1 : XTG_SCAN_TILE + XTG_SCAN_TILE / 32];
     __shared__ ST wsum[9];
@@ -2454,6 +2471,7 @@ __global__ void __launch_bounds__(256) k_scan_seg_apply(const ScanParams p) {
 // raise it.
 template <class Tree, class LS, class VT, class DT, class CT, int MODE, int R, int OP>
 __global__ void __launch_bounds__(256) k_indexed(const IndexParams p) {
+    pdl_wait();
     typedef typename LS::template R<1>::type RG;
     Ctx<0> c;
     c.scal = p.scal;
@@ -2585,6 +2603,7 @@ XTG_DI unsigned filter_flags16(const FilterParams& p, const Ctx<0>& c, i64 k0) {
 
 template <class CTree, class CLS, int R, bool BIG, bool V16 = false>
 __global__ void __launch_bounds__(256) k_filter_count(const FilterParams p) {
+    pdl_wait();
     __shared__ int ws[8];
     Ctx<0> c;
     c.scal = p.cscal;
@@ -2608,6 +2627,7 @@ __global__ void __launch_bounds__(256) k_filter_count(const FilterParams p) {
 template <class CTree, class CLS, class VTree, class VLS, class VT, class DT, class CT, int MODE, int R, int OP, bool BIG,
           bool V16 = false>
 __global__ void __launch_bounds__(256) k_filter_tile(const FilterParams p) {
+    pdl_wait();
     typedef typename VLS::template R<1>::type VRG;
     __shared__ int ws[9];
     Ctx<0> cc, vc;
@@ -2692,6 +2712,7 @@ __global__ void __launch_bounds__(256) k_filter_tile(const FilterParams p) {
 // the destination).  Other leaves are read directly at (a, b).
 template <class Tree, class LS, class OutT, int NB, int TILE, int ROWS>
 __global__ void __launch_bounds__(TILE * ROWS) k_transpose(const TransposeParams p) {
+    pdl_wait();
     typedef typename LS::template R<1>::type RG;
     typedef typename RG::elem0 T0;
     __shared__ T0 tile[TILE][TILE + 1];
@@ -3235,6 +3256,7 @@ template <int K, int MODE, class C, class Sub, class... Rest> struct Stats<StatL
 // FULL: row_len == NV * group size * VEC, so no element needs a bounds mask.
 template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int GROUP, int RO, int NSTAT, int FULL>
 __global__ void __launch_bounds__(256) k_rowfused(const RowParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     __shared__ __align__(16) unsigned char smem_raw[32 * 48];
     Ctx<NSTAT> c;
@@ -3383,6 +3405,7 @@ template <class A> XTG_DI A consumer_reduce(A a, A* smem) {
 }
 template <class Tree, class LS, class TL, class Acc, class Out, int POST, int VEC, int NS>
 __global__ void __launch_bounds__(288) k_reduce_stream(const RedParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     constexpr unsigned SB = 16384;  // stage bytes: 1024 vectors
     constexpr int kPolls = 1 << 22;
@@ -3553,6 +3576,7 @@ template <class... S> struct LoadRowSmem<LeafSet<S...>> {
 // per SM).  MINB: the launch-bounds minimum of resident blocks per SM.
 template <class Tree, class SL, class LS, class OutT, int VEC, int NV, int RO, int NSTAT, int FULL, int NB = 2, int MINB = 1>
 __global__ void __launch_bounds__(128, MINB) k_rowfused_tma(const RowParams p) {
+    pdl_wait();
     typedef typename LS::template R<VEC>::type RG;
     extern __shared__ __align__(128) unsigned char dsmem[];
     __shared__ __align__(16) unsigned char red_smem[32 * 48];
@@ -3787,6 +3811,7 @@ XTG_DI void batch_row_vec(const BatchInst* I, i64 row, int gl, Acc& acc, Ctx<0>&
 
 template <class Tree, class LS, class Acc, class Out, int POST, int GL, int U, int VEC = 1, int MINB = 1>
 __global__ void __launch_bounds__(256, MINB) k_batch_rowreduce(const BatchParams p) {
+    pdl_wait();
     typedef typename LS::template R<1>::type RG;
     __shared__ i64 s_tile;
     Ctx<0> c;
@@ -3875,6 +3900,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_rowreduce(const BatchParams
 
 template <class Tree, class LS, class OutT, int GL, int U>
 __global__ void __launch_bounds__(256) k_batch_assign(const BatchParams p) {
+    pdl_wait();
     typedef typename LS::template R<1>::type RG;
     __shared__ i64 s_tile;
     Ctx<0> c;

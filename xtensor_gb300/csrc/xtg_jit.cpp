@@ -319,7 +319,28 @@ xtg_status launch_raw(Kernel* k, unsigned grid, unsigned block, const void* para
         return XTG_OK;
     }
     void* args[1] = {const_cast<void*>(params)};
-    XTG_CU(drv().LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, (unsigned)dyn_smem, (CUstream)stream, args, nullptr));
+    if (opt("launch.pdl", 1)) {
+        // programmatic dependent launch: the kernel may be set up while the
+        // one before it drains (every kernel waits for its predecessors on
+        // entry, griddepcontrol.wait)
+        CUlaunchAttribute at[1];
+        memset(at, 0, sizeof at);
+        at[0].id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
+        at[0].value.programmaticStreamSerializationAllowed = 1;
+        CUlaunchConfig cfg;
+        memset(&cfg, 0, sizeof cfg);
+        cfg.gridDimX = grid;
+        cfg.gridDimY = cfg.gridDimZ = 1;
+        cfg.blockDimX = block;
+        cfg.blockDimY = cfg.blockDimZ = 1;
+        cfg.sharedMemBytes = (unsigned)dyn_smem;
+        cfg.hStream = (CUstream)stream;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        XTG_CU(drv().LaunchKernelEx(&cfg, k->fn, args, nullptr));
+    } else {
+        XTG_CU(drv().LaunchKernel(k->fn, grid, 1, 1, block, 1, 1, (unsigned)dyn_smem, (CUstream)stream, args, nullptr));
+    }
     g_launches.fetch_add(1, std::memory_order_relaxed);
     return XTG_OK;
 }

@@ -46,6 +46,7 @@ static xtg_status resolve_driver() {
     XTG_TRY(resolve("cuModuleLoadData", g_drv.ModuleLoadData));
     XTG_TRY(resolve("cuModuleGetFunction", g_drv.ModuleGetFunction));
     XTG_TRY(resolve("cuLaunchKernel", g_drv.LaunchKernel));
+    XTG_TRY(resolve("cuLaunchKernelEx", g_drv.LaunchKernelEx));
     XTG_TRY(resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", g_drv.OccupancyMaxActiveBlocksPerMultiprocessor));
     XTG_TRY(resolve("cuGetErrorString", g_drv.GetErrorString));
     XTG_TRY(resolve("cuFuncSetAttribute", g_drv.FuncSetAttribute));
