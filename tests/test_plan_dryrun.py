@@ -191,3 +191,52 @@ def test_view_plans():
     sq = fake((64, 64), "float32")
     xg.assign(sq, sq.transpose((1, 0)))
     assert fam(last_kernels()) == ["k_transpose", "k_assign"]
+
+
+def fake_chunked(shape, cs, dt, spaced=True):
+    """A chunked array over fake device addresses: chunks at a 256-byte
+    aligned distance (one slab) or scattered."""
+    import math
+    from xtensor_gb300._ffi import ITEMSIZE, dtype_code
+    from xtensor_gb300.chunked import ChunkedArray, grid_shape
+    n = math.prod(grid_shape(shape, cs))
+    es = ITEMSIZE[dtype_code(dt)]
+    dist = -(-math.prod(cs) * es // 256) * 256
+    base = _next[0]
+    _next[0] += 1 << 40
+    chunks = [DeviceArray(cs, dt, base + (i * dist if spaced else i * (dist + 4096) + (i % 3) * 256)) for i in range(n)]
+    return ChunkedArray(shape, cs, dt, chunks=chunks)
+
+
+@pytest.mark.parametrize("shape,cs,vec,pad", [
+    ((256, 512, 1024), (64, 256, 1024), 4, "false"),   # whole chunks: one class
+    ((256, 512, 1024), (100, 200, 1000), 4, "false"),  # edges on every axis: 8 classes, edge of 24 divides by 4
+    ((37, 70, 45), (5, 9, 7), 1, "false"),             # an odd inner extent: scalar elements
+    ((3, 5, 7, 9, 11), (2, 2, 4, 3, 5), 1, "true"),    # 16 classes: padded chunks with extent tests
+])
+def test_chunked_assign_plan(shape, cs, vec, pad):
+    # xtg_chunked_assign: one k_assign_chunks launch over the chunk classes
+    x = fake(shape, "float32")
+    a = fake_chunked(shape, cs, "float32")
+    a.assign(x * 2.0 + 1.0)
+    ks = last_kernels()
+    assert fam(ks) == ["k_assign_chunks"], ks
+    tail = ks[0].rsplit(">", 1)[0].split(", ")[-6:]  # OUTKIND, VEC, R, U, BIG, PAD
+    assert tail[1] == str(vec) and tail[2] == str(len(shape)) and tail[5] == pad, tail
+
+
+def test_chunked_full_sum_of_a_slab_is_one_streaming_reduction():
+    # whole chunks in one slab: the full sum is one run of the slab (K13)
+    from xtensor_gb300.chunked import chunked_reduce
+    a = fake_chunked((256, 512, 1024), (64, 256, 1024), "float32")
+    out = fake((), "float32")
+    n0 = xg.jit_stats()["launches"]
+    chunked_reduce("sum", a, out=out)
+    assert xg.jit_stats()["launches"] - n0 == 2
+    assert fam(last_kernels()) == ["k_reduce_stream", "k_reduce_combine"]
+    # the same 8 chunks scattered in memory: chunk by chunk, each chunk's
+    # reduction then a merge into the result
+    b = fake_chunked((256, 512, 1024), (64, 256, 1024), "float32", spaced=False)
+    n0 = xg.jit_stats()["launches"]
+    chunked_reduce("sum", b, out=out)
+    assert xg.jit_stats()["launches"] - n0 >= 8 + 7
