@@ -569,9 +569,8 @@ xtg_status xtg_fill_random(const xtg_array* a, int32_t dist, double p0, double p
  * exit).  Inputs whose plan would need more partials than the array holds,
  * or more than 2^32 vectors, are rejected with XTG_ERR_UNSUPPORTED before any
  * launch.  The first call in a CUDA context resolves the array's address
- * there (cudaGetSymbolAddress, which also loads the library's device code):
- * make that first call before any stream capture.  A device reset or another
- * context on the same device gets its own address.  All calls share the
+ * there (cudaGetSymbolAddress, which also loads the library's device code).
+ * A device reset or another context on the same device gets its own address.  All calls share the
  * array: calls whose kernels may overlap on the GPU (unordered streams) race
  * and must be serialised by the caller. */
 #define XTG_NOALLOC_SCRATCH_BYTES (256u * 1024u)
