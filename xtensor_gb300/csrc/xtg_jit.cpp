@@ -135,8 +135,8 @@ static thread_local std::string t_last_kernels_str;
 
 void begin_call() { t_last_kernels.clear(); }
 
-// Occupancy for a (block, dynamic shared memory) configuration; raises the
-// kernel's dynamic shared memory limit above the 48 KiB default when needed.
+// Occupancy for a (block, dynamic shared memory) configuration; sets the
+// kernel's dynamic shared memory limit to the request.
 static xtg_status configure(Kernel* k, int block, size_t dyn_smem) {
     if (dry_run() || !k->fn) {
         k->block = block;
@@ -144,7 +144,9 @@ static xtg_status configure(Kernel* k, int block, size_t dyn_smem) {
         return XTG_OK;
     }
     if (k->block == block && k->dyn_smem == dyn_smem && k->max_blocks_per_sm > 0) return XTG_OK;
-    if (dyn_smem > 48 * 1024)
+    // the dynamic limit covers the request whatever the kernel's static
+    // shared memory (static + dynamic above 48 KiB needs the opt-in)
+    if (dyn_smem > 0)
         XTG_CU(drv().FuncSetAttribute(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn_smem));
     int nb = 0;
     if (drv().OccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, block, dyn_smem) != CUDA_SUCCESS) nb = 1;
