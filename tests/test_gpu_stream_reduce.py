@@ -63,3 +63,23 @@ def test_stream_equals_row_kernel(n, dt, cta_chunk):
     finally:
         xg.set_option("reduce.cta_chunk", -1)
     check(xg.lib().xtg_check_device_errors())
+
+
+@pytest.mark.parametrize("stages", [2, 3, 5, 6])
+def test_ring_depths(stages):
+    # 2-6 stages of 16 KiB (3 stages: exactly 48 KiB of dynamic shared
+    # memory beside the kernel's static barriers); results as K3's
+    xg.init(0)
+    g = np.random.default_rng(132)
+    x = g.standard_normal((1 << 25) + 4000).astype(np.float32)
+    dx = DeviceArray.from_numpy(x)
+    xg.set_option("reduce.stream_stages", stages)
+    try:
+        for op in ("sum", "variance", "norm_l2"):
+            a, ka = _run(op, dx, True)
+            b, kb = _run(op, dx, False)
+            assert ka[0].startswith("k_reduce_stream<") and ka[0].split(",")[-1].strip() == f"{stages}>", ka
+            assert a.tobytes() == b.tobytes(), (op, stages)
+    finally:
+        xg.set_option("reduce.stream_stages", -1)
+    check(xg.lib().xtg_check_device_errors())
