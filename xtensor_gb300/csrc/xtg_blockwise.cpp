@@ -21,6 +21,8 @@
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "xtg_plan.h"
@@ -205,6 +207,60 @@ bool dense(const xtg_array& a) {
     }
     return true;
 }
+
+// Work spread over side streams and joined back: open() makes the side
+// streams wait for everything queued on `main` so far; join() (or the
+// destructor, on an early return) makes `main` wait for the side streams.
+// The side streams are created once per device and kept.
+struct Fork {
+    cudaStream_t main = nullptr;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> ev;
+    bool joined = true;
+    static std::vector<cudaStream_t>& pool(int dev) {
+        static std::mutex mu;
+        static std::map<int, std::vector<cudaStream_t>> p;
+        std::lock_guard<std::mutex> lk(mu);
+        return p[dev];
+    }
+    xtg_status open(cudaStream_t s, int n) {
+        main = s;
+        int dev = 0;
+        XTG_CUDA(cudaGetDevice(&dev));
+        std::vector<cudaStream_t>& P = pool(dev);
+        {
+            static std::mutex mu;
+            std::lock_guard<std::mutex> lk(mu);
+            while ((int)P.size() < n) {
+                cudaStream_t t;
+                XTG_CUDA(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking));
+                P.push_back(t);
+            }
+        }
+        side.assign(P.begin(), P.begin() + n);
+        ev.assign((size_t)n + 1, nullptr);
+        for (auto& e : ev) XTG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        XTG_CUDA(cudaEventRecord(ev[0], main));
+        joined = false;
+        for (cudaStream_t t : side) XTG_CUDA(cudaStreamWaitEvent(t, ev[0], 0));
+        return XTG_OK;
+    }
+    cudaStream_t stream(int i) const { return side[(size_t)i % side.size()]; }
+    xtg_status join() {
+        if (joined) return XTG_OK;
+        joined = true;
+        for (size_t i = 0; i < side.size(); ++i) {
+            XTG_CUDA(cudaEventRecord(ev[i + 1], side[i]));
+            XTG_CUDA(cudaStreamWaitEvent(main, ev[i + 1], 0));
+        }
+        return XTG_OK;
+    }
+    ~Fork() {
+        join();
+        for (auto e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
 
 struct Resources {
     cudaStream_t stream;
@@ -655,6 +711,90 @@ xtg_status chunked_reduce_impl(const xtg_chunked* src, const xtg_reduce_desc* rd
             if (a.data) v.data = (char*)a.data + off * dt(a.dtype).size;
             return v;
         };
+        // the strided array of the class selected in sel[]
+        auto class_slab = [&]() {
+            xtg_array slab = whole;
+            slab.rank = 0;
+            int64_t first = 0;
+            for (int d = 0; d < rank; ++d) first += sel[d]->lo * gst[d];
+            for (int d : rdims) {
+                slab.shape[slab.rank] = sel[d]->cnt;
+                slab.strides[slab.rank++] = gst[d] * (S / es);
+            }
+            for (int d : rdims) {
+                slab.shape[slab.rank] = sel[d]->ext;
+                slab.strides[slab.rank++] = cst[d];
+            }
+            for (int d : kdims) {
+                slab.shape[slab.rank] = sel[d]->cnt;
+                slab.strides[slab.rank++] = gst[d] * (S / es);
+                slab.shape[slab.rank] = sel[d]->ext;
+                slab.strides[slab.rank++] = cst[d];
+            }
+            slab.data = (void*)((const char*)src->chunks[0] + first * S);
+            return slab;
+        };
+        // Merges other than the variance's with at most 8 reduced classes:
+        // every class reduces into its own slice at once, spread over side
+        // streams, then one elementwise launch per output region folds the
+        // slices into it in class order (the sequential merge, one launch).
+        const bool concurrent = P.merge != M_VAR && n_rp > 1 && n_rp <= 8 && P.part_dtype == P.out_dtype &&
+                                opt("chunked.streams", 4) > 0 && !dry_run();
+        if (concurrent) {
+            const size_t psz = (size_t)on * dt(P.part_dtype).size;
+            void* parts = nullptr;
+            XTG_TRY(R.alloc(&parts, psz * (size_t)(n_rp - 1)));
+            Fork F;
+            XTG_TRY(F.open(stream, (int)std::min<int64_t>(opt("chunked.streams", 4), n_rp * n_kp)));
+            int next = 0;
+            for (int64_t rp = 0; rp < n_rp; ++rp) {
+                int64_t q = rp;
+                for (int i = (int)rdims.size() - 1; i >= 0; --i) {
+                    const int d = rdims[(size_t)i];
+                    sel[d] = &kinds[d][(size_t)(q % (int64_t)kinds[d].size())];
+                    q /= (int64_t)kinds[d].size();
+                }
+                xtg_array dst = rp == 0 ? *out : dense_like(*out, P.part_dtype, (char*)parts + psz * (size_t)(rp - 1));
+                for (int64_t kp = 0; kp < n_kp; ++kp) {
+                    int64_t k = kp;
+                    for (int i = (int)kdims.size() - 1; i >= 0; --i) {
+                        const int d = kdims[(size_t)i];
+                        sel[d] = &kinds[d][(size_t)(k % (int64_t)kinds[d].size())];
+                        k /= (int64_t)kinds[d].size();
+                    }
+                    const xtg_array slab = class_slab();
+                    Ex x = part_tree(P, slab, 0.0);
+                    const xtg_array o = out_view(dst);
+                    XTG_TRY(xtg_reduce(&x.e, &prd2, &o, F.stream(next++)));
+                }
+            }
+            XTG_TRY(F.join());
+            for (int64_t kp = 0; kp < n_kp; ++kp) {
+                int64_t k = kp;
+                for (int i = (int)kdims.size() - 1; i >= 0; --i) {
+                    const int d = kdims[(size_t)i];
+                    sel[d] = &kinds[d][(size_t)(k % (int64_t)kinds[d].size())];
+                    k /= (int64_t)kinds[d].size();
+                }
+                const xtg_array region = out_view(*out);
+                Ex m;
+                if (P.merge == M_ADD || P.merge == M_MUL) {
+                    m.leaf(region);
+                    for (int64_t rp = 1; rp < n_rp; ++rp) {
+                        m.leaf(out_view(dense_like(*out, P.part_dtype, (char*)parts + psz * (size_t)(rp - 1))));
+                        m.op(P.merge == M_ADD ? XTG_OP_ADD : XTG_OP_MUL);
+                    }
+                } else {
+                    // minimum(part_k, ... minimum(part_1, region)): the sequential merge's order
+                    for (int64_t rp = n_rp - 1; rp >= 1; --rp)
+                        m.leaf(out_view(dense_like(*out, P.part_dtype, (char*)parts + psz * (size_t)(rp - 1))));
+                    m.leaf(region);
+                    for (int64_t rp = 1; rp < n_rp; ++rp) m.op(P.merge == M_MIN ? XTG_OP_MINIMUM : XTG_OP_MAXIMUM);
+                }
+                XTG_TRY(assign_expr(m, region, stream));
+            }
+            return chunked_finish(P, src, red, *out, stream);
+        }
         double n_acc2 = 0.0;
         for (int64_t rp = 0; rp < n_rp; ++rp) {
             int64_t q = rp;
@@ -672,25 +812,7 @@ xtg_status chunked_reduce_impl(const xtg_chunked* src, const xtg_reduce_desc* rd
                     sel[d] = &kinds[d][(size_t)(k % (int64_t)kinds[d].size())];
                     k /= (int64_t)kinds[d].size();
                 }
-                xtg_array slab = whole;
-                slab.rank = 0;
-                int64_t first = 0;
-                for (int d = 0; d < rank; ++d) first += sel[d]->lo * gst[d];
-                for (int d : rdims) {
-                    slab.shape[slab.rank] = sel[d]->cnt;
-                    slab.strides[slab.rank++] = gst[d] * (S / es);
-                }
-                for (int d : rdims) {
-                    slab.shape[slab.rank] = sel[d]->ext;
-                    slab.strides[slab.rank++] = cst[d];
-                }
-                for (int d : kdims) {
-                    slab.shape[slab.rank] = sel[d]->cnt;
-                    slab.strides[slab.rank++] = gst[d] * (S / es);
-                    slab.shape[slab.rank] = sel[d]->ext;
-                    slab.strides[slab.rank++] = cst[d];
-                }
-                slab.data = (void*)((const char*)src->chunks[0] + first * S);
+                xtg_array slab = class_slab();
                 XTG_TRY(fold_partial(P, prd2, slab, 0.0, rp == 0, out_view(*out), out_view(part), out_view(mean_a),
                                      out_view(mean_b), var_s, n_acc2, n_b, R, stream));
             }
