@@ -1602,6 +1602,7 @@ def c4_section(args):
                 rid = C.c_uint64()
                 check(srv.L.xtg_server_submit(srv.h, C.byref(reqs[int(p)]), C.byref(rid)))
                 ids.append(rid.value)
+            submit_s = time.perf_counter() - t0
             srv.drain(600000)
             served_wall = time.perf_counter() - t0
             for rid in ids:
@@ -1615,6 +1616,9 @@ def c4_section(args):
                            "req_s": round(n / served_wall, 1), "GB/s": round(total_bytes / served_wall / 1e9, 1),
                            "batched_requests": st["batched_requests"], "batch_launches": st["batch_launches"],
                            "waves": st["waves"],
+                           # the rate the client managed to submit at (the offered rate when the
+                           # arrival loop kept up with its schedule)
+                           "submitted_req_s": round(n / submit_s, 1),
                            # host time the dispatch threads spent launching, per second of the run and thread
                            "dispatch_busy": round(st["dispatch_ms"] / (served_wall * 1e3 * dispatch_threads), 3)},
             })
