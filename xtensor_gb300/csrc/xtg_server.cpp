@@ -3,7 +3,8 @@
 // expression at a time on the calling thread).
 //
 // Threads: callers submit (never blocking on the GPU); one scheduler thread
-// admits and dispatches; CUDA stream callbacks complete requests.
+// admits and dispatches; a completion thread polls CUDA events and completes
+// requests.
 //   admission — in arrival order, a pending request is admitted when the
 //     in-flight count is below the limit and its cost (declared workspace +
 //     the split-reduction scratch its plan may take) fits the remaining HBM
@@ -22,9 +23,10 @@
 //     stream pool, so that several cores can pay the host cost of launching
 //     (planning or plan-cache replay, kernel launches); the work overlaps on
 //     the device across the streams.
-//   completion — cudaLaunchHostFunc after each unit marks its requests done
-//     with a host timestamp and releases their budget; the scheduler frees
-//     batch work lists once their units completed.
+//   completion — an event recorded after each unit; the completion thread
+//     polls the events, marks the unit's requests done with a host
+//     timestamp and releases their budget; the scheduler frees batch work
+//     lists once their units completed.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -76,6 +78,18 @@ struct Disp {
     size_t next_stream = 0;
     bool stop = false;
 };
+// Completion by events: a unit's event is recorded on its stream after its
+// launches; the completion thread polls the recorded events and completes
+// the units whose events have passed.  (A host callback per unit would stop
+// its stream until CUDA's single callback thread ran it.)
+struct Completer {
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<std::pair<cudaEvent_t, Unit*>> q;
+    std::vector<cudaEvent_t> spare;
+    bool stop = false;
+};
 
 }  // namespace
 
@@ -90,6 +104,7 @@ struct xtg_server {
     std::deque<Req*> pending;
     std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
     std::vector<Unit*> finished_units;
+    Completer comp;
     uint64_t next_id = 1;
     uint64_t events = 0;  // submits + completions + cancels: admission retries only when it changes
     int64_t budget = 0, reserved = 0, inflight = 0;
@@ -127,16 +142,82 @@ void CUDART_CB on_unit_done(void* p) {
 }
 
 // Completion of a unit once the stream reaches this point (inline in dry-run
-// mode, where nothing runs on a device).
+// mode, where nothing runs on a device): an event the completion thread
+// polls, or with option "server.host_callbacks" a stream host callback.
 void complete_after(cudaStream_t st, Unit* u) {
     if (dry_run()) {
         on_unit_done(u);
         return;
     }
-    if (cudaLaunchHostFunc(st, on_unit_done, u) != cudaSuccess) {
+    xtg_server* s = u->srv;
+    if (opt("server.host_callbacks", 0)) {
+        if (cudaLaunchHostFunc(st, on_unit_done, u) != cudaSuccess) {
+            cudaGetLastError();
+            cudaStreamSynchronize(st);
+            on_unit_done(u);
+        }
+        return;
+    }
+    cudaEvent_t e = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(s->comp.mu);
+        if (!s->comp.spare.empty()) {
+            e = s->comp.spare.back();
+            s->comp.spare.pop_back();
+        }
+    }
+    if ((!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) ||
+        cudaEventRecord(e, st) != cudaSuccess) {
         cudaGetLastError();
         cudaStreamSynchronize(st);
+        if (e) cudaEventDestroy(e);
         on_unit_done(u);
+        return;
+    }
+    {
+        std::lock_guard<std::mutex> lk(s->comp.mu);
+        s->comp.q.emplace_back(e, u);
+    }
+    s->comp.cv.notify_one();
+}
+
+// The completion thread: polls the pending units' events (in any order: the
+// streams run independently), completes those that passed, and naps a few
+// microseconds when none did.
+void completer(xtg_server* s) {
+    ensure_device(nullptr);
+    Completer& C = s->comp;
+    std::vector<std::pair<cudaEvent_t, Unit*>> mine;
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(C.mu);
+            if (mine.empty()) C.cv.wait(lk, [&] { return C.stop || !C.q.empty(); });
+            while (!C.q.empty()) {
+                mine.push_back(C.q.front());
+                C.q.pop_front();
+            }
+            if (mine.empty() && C.stop) break;
+        }
+        bool progress = false;
+        std::vector<cudaEvent_t> passed;
+        for (size_t i = 0; i < mine.size();) {
+            const cudaError_t r = cudaEventQuery(mine[i].first);
+            if (r == cudaErrorNotReady) {
+                ++i;
+                continue;
+            }
+            if (r != cudaSuccess) cudaGetLastError();  // completed with an error: the unit still ends
+            on_unit_done(mine[i].second);
+            passed.push_back(mine[i].first);
+            mine[i] = mine.back();
+            mine.pop_back();
+            progress = true;
+        }
+        if (!passed.empty()) {
+            std::lock_guard<std::mutex> lk(C.mu);
+            C.spare.insert(C.spare.end(), passed.begin(), passed.end());
+        }
+        if (!progress && !mine.empty()) std::this_thread::sleep_for(std::chrono::microseconds(5));
     }
 }
 
@@ -451,6 +532,7 @@ xtg_status xtg_server_create(const xtg_server_config* cfg, xtg_server** out) {
     }
     xtg_server* raw = s.release();
     for (auto& d : raw->disp) d->th = std::thread(dispatcher, raw, d.get());
+    raw->comp.th = std::thread(completer, raw);
     raw->sched = std::thread(scheduler, raw);
     *out = raw;
     return XTG_OK;
@@ -601,6 +683,14 @@ xtg_status xtg_server_destroy(xtg_server* s) {
     }
     for (auto& d : s->disp)
         if (d->th.joinable()) d->th.join();
+    // every unit has completed: the completion thread has nothing left
+    {
+        std::lock_guard<std::mutex> lk(s->comp.mu);
+        s->comp.stop = true;
+    }
+    s->comp.cv.notify_one();
+    if (s->comp.th.joinable()) s->comp.th.join();
+    for (cudaEvent_t e : s->comp.spare) cudaEventDestroy(e);
     wait_background_compiles(60000);  // batch kernels it started building
     for (cudaStream_t st : s->streams) {
         if (!st) continue;
