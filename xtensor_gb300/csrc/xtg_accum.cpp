@@ -280,23 +280,14 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
         const int64_t groups = (n_outer + 31) / 32;
         return launch(k, grid_of(k, (groups + 1) / 2), 64, &p, stream);
     }
-    // K9c: segmented reduce-then-scan; about four segments per SM overall
+    // K9c: segmented reduce-then-scan, one warp per segment: warp tiles of
+    // 256 elements, about one segment per resident warp of the apply pass
+    // (so every warp of its single wave has one segment of equal length)
     DeviceInfo* dev;
     XTG_TRY(ensure_device(&dev));
-    const int64_t ntiles = (len + 4095) / 4096;
-    const int64_t target = std::max<int64_t>(1, (int64_t)4 * dev->sm_count / std::max<int64_t>(1, n_outer));
-    const int64_t seg_tiles = std::max<int64_t>(1, (ntiles + target - 1) / target);
-    const int64_t nseg = (ntiles + seg_tiles - 1) / seg_tiles;
-    if (seg_tiles >= (1ll << 32) || nseg >= (1ll << 30)) return fail(XTG_ERR_UNSUPPORTED, "scan too long");
-    p.ntiles = ntiles;
-    p.n_inner = (nseg << 32) | seg_tiles;
-    void* agg = nullptr;
-    XTG_TRY(scratch_alloc(&agg, (size_t)n_outer * (size_t)nseg * 16, stream));
-    p.agg = agg;
-    const int agg_off = (int)offsetof(xtg::ScanParams, agg);
     // 16-byte register loads / stores when every leaf is contiguous or
     // broadcast along the rows and the destination contiguous, all aligned
-    int sv = 16 / dt(rt).size;
+    int sv = std::min(8, 16 / dt(rt).size);  // at most the 8 elements a lane holds
     for (int l = 0; l < NL; ++l)
         if (p.lsa[l] == 1) sv = std::min(sv, 16 / dt(t.leaves[l].dtype).size);
     auto sv_ok = [&](int v) {
@@ -314,15 +305,28 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
     for (int l = 0; l < NL; ++l) sk[l] = sv > 1 ? kind_of_s(p.lsa[l]) : 2;
     const std::string sls = leafset_s(t, sk), svs = std::to_string(sv);
     Kernel *ka, *kb, *kc;
-    xtg_status st =
-        get_kernel("xtg::k_scan_seg_reduce<" + tree + ", " + sls + ", " + rts + ", " + ops + ", " + svs + ">", 256, &ka);
-    if (st == XTG_OK) st = get_kernel("xtg::k_scan_seg_offsets<" + rts + ", " + ops + ">", 256, &kb);
-    if (st == XTG_OK)
-        st = get_kernel("xtg::k_scan_seg_apply<" + tree + ", " + sls + ", " + rts + ", " + ops + ", " + svs + ">", 256,
-                        &kc);
-    if (st == XTG_OK) st = launch(ka, grid_of(ka, n_outer * nseg), 256, &p, stream, 0, agg_off);
+    XTG_TRY(get_kernel("xtg::k_scan_seg_reduce<" + tree + ", " + sls + ", " + rts + ", " + ops + ", " + svs + ">", 256,
+                       &ka));
+    XTG_TRY(get_kernel("xtg::k_scan_seg_offsets<" + rts + ", " + ops + ">", 256, &kb));
+    XTG_TRY(get_kernel("xtg::k_scan_seg_apply<" + tree + ", " + sls + ", " + rts + ", " + ops + ", " + svs + ">", 256,
+                       &kc));
+    const int64_t wtile = 256;  // 32 lanes x 8 elements
+    const int64_t ntiles = (len + wtile - 1) / wtile;
+    const int64_t warps = (int64_t)kc->max_blocks_per_sm * dev->sm_count * 8;
+    const int64_t target = std::max<int64_t>(1, warps / std::max<int64_t>(1, n_outer));
+    const int64_t seg_tiles = std::max<int64_t>(1, (ntiles + target - 1) / target);
+    const int64_t nseg = (ntiles + seg_tiles - 1) / seg_tiles;
+    if (seg_tiles >= (1ll << 32) || nseg >= (1ll << 30)) return fail(XTG_ERR_UNSUPPORTED, "scan too long");
+    p.ntiles = ntiles;
+    p.n_inner = (nseg << 32) | seg_tiles;
+    void* agg = nullptr;
+    XTG_TRY(scratch_alloc(&agg, (size_t)n_outer * (size_t)nseg * 16, stream));
+    p.agg = agg;
+    const int agg_off = (int)offsetof(xtg::ScanParams, agg);
+    const int64_t blocks = (n_outer * nseg + 7) / 8;  // eight warps per block
+    xtg_status st = launch(ka, grid_of(ka, blocks), 256, &p, stream, 0, agg_off);
     if (st == XTG_OK) st = launch(kb, grid_of(kb, n_outer), 256, &p, stream, 0, agg_off);
-    if (st == XTG_OK) st = launch(kc, grid_of(kc, n_outer * nseg), 256, &p, stream, 0, agg_off);
+    if (st == XTG_OK) st = launch(kc, grid_of(kc, blocks), 256, &p, stream, 0, agg_off);
     xtg_status fs = scratch_free(agg, stream);
     return st != XTG_OK ? st : fs;
 }

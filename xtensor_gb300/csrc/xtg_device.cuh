@@ -572,6 +572,15 @@ template <class A> XTG_DI A shfl_up_pod(const A& a, int d) {
     return out.a;
 }
 
+template <class A> XTG_DI A shfl_idx_pod(const A& a, int src) {
+    union U { A a; u32 w[(sizeof(A) + 3) / 4]; };
+    U in, out;
+    in.a = a;
+#pragma unroll
+    for (int i = 0; i < (int)((sizeof(A) + 3) / 4); ++i) out.w[i] = __shfl_sync(0xffffffffu, in.w[i], src);
+    return out.a;
+}
+
 // Deterministic group reduction: warp butterfly, then warp 0 folds the
 // per-warp results in warp order.  Result valid in thread 0 of the group
 // (GROUP == 32: lane 0 of the warp; GROUP == block: thread 0).
@@ -2164,8 +2173,7 @@ template <int OP> struct ScanState<float, OP> {
     XTG_DI float value() const { return lo == 0.f ? hi : hi + lo; }
 };
 
-constexpr int XTG_SCAN_TILE = 4096;  // 256 threads x 16 elements
-constexpr int XTG_SCAN_IPT = 16;
+constexpr int XTG_SCAN_IPT = 8;  // consecutive elements per lane of a warp tile
 
 template <class Tree, class LS, class RT>
 XTG_DI RT scan_elem(const ScanParams& p, const Ctx<0>& c, i64 row, i64 k) {
@@ -2225,22 +2233,26 @@ template <class ST> XTG_DI ST block_inorder_scan(ST v, ST* wsum, ST& excl_in_blo
     return wsum[nw];
 }
 
-// Segmented reduce-then-scan (no CTA ever waits on another): a row is cut
-// into segments of seg_tiles tiles (about four segments per SM over the
-// launch); (A) each segment's total, (B) per row, the exclusive prefix of
-// the segment totals in order, (C) each segment again, tile by tile, from
-// its prefix with the running total carried inside the CTA.
-// ScanParams.ntiles = tiles per row; segments per row and tiles per segment
-// ride in n_inner (unused for these rows) as nseg * 2^32 + seg_tiles.
+// Segmented reduce-then-scan, one warp per segment (no warp ever waits on
+// another, and no block barrier): a row is cut into segments of seg_tiles
+// warp tiles (32 lanes x 8 consecutive elements per lane), about one
+// segment per resident warp of the launch; (A) each segment's total, (B) per
+// row, the exclusive prefixes of the segment totals in order, (C) each
+// segment again, tile by tile, from its prefix: every lane folds its 8
+// elements, the warp scans the lane totals in lane order, every lane
+// rescans its elements from (carry, the lanes before it) and the tile total
+// joins the carry.  A fixed structure, so results do not depend on timing.
+// ScanParams.ntiles = warp tiles per row; segments per row and tiles per
+// segment ride in n_inner (unused for these rows) as nseg * 2^32 + seg_tiles.
+constexpr int XTG_SCAN_WTILE = 32 * XTG_SCAN_IPT;
 XTG_DI i64 seg_tiles_of(const ScanParams& p) { return p.n_inner & 0xffffffffll; }
 XTG_DI i64 nseg_of(const ScanParams& p) { return p.n_inner >> 32; }
 
-// A thread's 16 consecutive elements of a tile into registers: VEC-wide
-// loads when all 16 lie before `ke` (VEC > 1: every leaf contiguous or
-// broadcast along the row, rows VEC-aligned — the host checks), else one by
-// one.
+// A lane's 8 consecutive elements into registers: VEC-wide loads when all
+// 8 lie before `ke` (VEC > 1: every leaf contiguous or broadcast along the
+// row, rows VEC-aligned — the host checks), else one by one.
 template <class Tree, class LS, class RT, int VEC>
-XTG_DI void scan_load16(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kt, i64 ke, RT (&v)[XTG_SCAN_IPT]) {
+XTG_DI void scan_loadv(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kt, i64 ke, RT (&v)[XTG_SCAN_IPT]) {
     if (VEC > 1 && kt + XTG_SCAN_IPT <= ke) {
         typedef typename LS::template R<VEC>::type RG;
 #pragma unroll
@@ -2259,60 +2271,100 @@ XTG_DI void scan_load16(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kt, i
     }
 }
 
+// VEC == 1 (strided leaves): a warp tile through the warp's own buffer in
+// shared memory — coalesced loads (lane l takes l, l + 32, ...), then each
+// lane its 8 consecutive elements (rows padded by one element per 32).
+template <class Tree, class LS, class RT>
+XTG_DI void scan_loadw(const ScanParams& p, const Ctx<0>& c, i64 row, i64 k0, i64 ke, RT* wb,
+                             RT (&v)[XTG_SCAN_IPT]) {
+    const int lane = (int)threadIdx.x & 31;
+#pragma unroll
+    for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+        const int q = i * 32 + lane;
+        if (k0 + q < ke) wb[q + (q >> 5)] = scan_elem<Tree, LS, RT>(p, c, row, k0 + q);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+        const int q = lane * XTG_SCAN_IPT + i;
+        v[i] = k0 + q < ke ? wb[q + (q >> 5)] : RT(0);
+    }
+    __syncwarp();
+}
+
+// The warp tiles [kb, ke) of one row in order, each handed to f(v, k0) in
+// the lanes' registers; with VEC > 1 the next tile's loads are in flight
+// while f works on the current one.
+template <class Tree, class LS, class RT, int VEC, class F>
+XTG_DI void scan_walk(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kb, i64 ke, RT* wb, F&& f) {
+    const i64 lofs = (i64)((int)threadIdx.x & 31) * XTG_SCAN_IPT;
+    if constexpr (VEC > 1) {
+        RT va[XTG_SCAN_IPT], vb[XTG_SCAN_IPT];
+        if (kb < ke) scan_loadv<Tree, LS, RT, VEC>(p, c, row, kb + lofs, ke, va);
+        for (i64 k0 = kb; k0 < ke; k0 += 2 * XTG_SCAN_WTILE) {
+            if (k0 + XTG_SCAN_WTILE < ke)
+                scan_loadv<Tree, LS, RT, VEC>(p, c, row, k0 + XTG_SCAN_WTILE + lofs, ke, vb);
+            f(va, k0);
+            if (k0 + XTG_SCAN_WTILE >= ke) break;
+            if (k0 + 2 * XTG_SCAN_WTILE < ke)
+                scan_loadv<Tree, LS, RT, VEC>(p, c, row, k0 + 2 * XTG_SCAN_WTILE + lofs, ke, va);
+            f(vb, k0 + XTG_SCAN_WTILE);
+        }
+    } else {
+        RT v[XTG_SCAN_IPT];
+        for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_WTILE) {
+            scan_loadw<Tree, LS, RT>(p, c, row, k0, ke, wb, v);
+            f(v, k0);
+        }
+    }
+}
+
+// In-order inclusive scan of one state per lane (Kogge-Stone: the earlier
+// lanes' part always on the left).
+template <class ST> XTG_DI ST warp_inorder_scan(ST v) {
+    const int lane = (int)threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        ST y = shfl_up_pod(v, d);
+        if (lane >= d) {
+            y.merge(v);
+            v = y;
+        }
+    }
+    return v;
+}
+
+// Shared-memory words per warp for the VEC == 1 tile buffer.
+template <class RT, int VEC> struct ScanWarpBuf {
+    static constexpr int n = VEC > 1 ? 1 : XTG_SCAN_WTILE + XTG_SCAN_WTILE / 32;
+};
+
 template <class Tree, class LS, class RT, int OP, int VEC>
 __global__ void __launch_bounds__(256) k_scan_seg_reduce(const ScanParams p) {
     pdl_wait();
     typedef ScanState<RT, OP> ST;
-    __shared__ ST wsum[9];
+    constexpr int WB = ScanWarpBuf<RT, VEC>::n;
+    __shared__ RT wbuf[8 * WB];
     Ctx<0> c;
     c.scal = p.scal;
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    RT* wb = wbuf + warp * WB;
     const i64 nseg = nseg_of(p), st = seg_tiles_of(p);
     const i64 nitems = p.n_outer * nseg;
-    for (i64 it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const i64 lofs = (i64)lane * XTG_SCAN_IPT;
+    for (i64 it = (i64)blockIdx.x * 8 + warp; it < nitems; it += (i64)gridDim.x * 8) {
         const i64 row = it / nseg, sg = it - row * nseg;
-        i64 kb = sg * st * XTG_SCAN_TILE;
-        i64 ke = kb + st * XTG_SCAN_TILE;
-        if (ke > p.len) ke = p.len;
+        const i64 kb = sg * st * XTG_SCAN_WTILE;
+        const i64 ke = kb + st * XTG_SCAN_WTILE < p.len ? kb + st * XTG_SCAN_WTILE : p.len;
         ST s = ST::ident();
-        if constexpr (VEC > 1) {
-            // each thread its 16 consecutive elements (vector loads); the
-            // next tile's loads are in flight while this one is added (the
-            // additions keep their order)
-            RT va[XTG_SCAN_IPT], vb[XTG_SCAN_IPT];
-            const i64 tofs = (i64)threadIdx.x * XTG_SCAN_IPT;
-            auto add = [&](const RT(&v)[XTG_SCAN_IPT], i64 k0) {
-                const i64 kt = k0 + tofs;
+        scan_walk<Tree, LS, RT, VEC>(p, c, row, kb, ke, wb, [&](RT(&v)[XTG_SCAN_IPT], i64 k0) {
+            const i64 kt = k0 + lofs;
 #pragma unroll
-                for (int i = 0; i < XTG_SCAN_IPT; ++i)
-                    if (kt + i < ke) s.add(v[i]);
-            };
-            if (kb < ke) scan_load16<Tree, LS, RT, VEC>(p, c, row, kb + tofs, ke, va);
-            for (i64 k0 = kb; k0 < ke; k0 += 2 * XTG_SCAN_TILE) {
-                if (k0 + XTG_SCAN_TILE < ke) scan_load16<Tree, LS, RT, VEC>(p, c, row, k0 + XTG_SCAN_TILE + tofs, ke, vb);
-                add(va, k0);
-                if (k0 + XTG_SCAN_TILE >= ke) break;
-                if (k0 + 2 * XTG_SCAN_TILE < ke)
-                    scan_load16<Tree, LS, RT, VEC>(p, c, row, k0 + 2 * XTG_SCAN_TILE + tofs, ke, va);
-                add(vb, k0 + XTG_SCAN_TILE);
-            }
-        } else
-        for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_TILE) {
-            RT v[XTG_SCAN_IPT];
-            {
-                // coalesced scalar loads: thread th takes th, th + 256, ...
-#pragma unroll
-                for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-                    const i64 k = k0 + (i64)i * 256 + threadIdx.x;
-                    v[i] = k < ke ? scan_elem<Tree, LS, RT>(p, c, row, k) : RT(0);
-                }
-#pragma unroll
-                for (int i = 0; i < XTG_SCAN_IPT; ++i)
-                    if (k0 + (i64)i * 256 + threadIdx.x < ke) s.add(v[i]);
-            }
-        }
-        ST unused;
-        const ST tot = block_inorder_scan(s, wsum, unused);
-        if (threadIdx.x == 0) reinterpret_cast<ST*>(p.agg)[it] = tot;
+            for (int i = 0; i < XTG_SCAN_IPT; ++i)
+                if (kt + i < ke) s.add(v[i]);
+        });
+        const ST tot = warp_inorder_scan(s);
+        if (lane == 31) reinterpret_cast<ST*>(p.agg)[it] = tot;
     }
 }
 
@@ -2340,123 +2392,69 @@ __global__ void __launch_bounds__(256) k_scan_seg_offsets(const ScanParams p) {
     }
 }
 
-// (C) each segment, tile by tile: coalesced loads into shared memory, thread
-// th folds 16 consecutive elements from (carry, then the threads before it),
-// coalesced stores; the tile total joins the carry
+// (C) each segment again from its prefix.  Results leave the lanes'
+// registers: 16-byte stores when the lane's 8 elements are whole (VEC > 1:
+// the destination contiguous and aligned — the host checks).  Four blocks
+// per SM for 4-byte types with vector access (a register bound of 64, no
+// spill), two otherwise.
 template <class Tree, class LS, class RT, int OP, int VEC>
-__global__ void __launch_bounds__(256) k_scan_seg_apply(const ScanParams p) {
+__global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : 2) k_scan_seg_apply(const ScanParams p) {
     pdl_wait();
     typedef ScanState<RT, OP> ST;
-    __shared__ RT buf[VEC > 1 ? 1 : XTG_SCAN_TILE + XTG_SCAN_TILE / 32];
-    __shared__ ST wsum[9];
+    constexpr int WB = ScanWarpBuf<RT, VEC>::n;
+    __shared__ RT wbuf[8 * WB];
     Ctx<0> c;
     c.scal = p.scal;
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    RT* wb = wbuf + warp * WB;
     const i64 nseg = nseg_of(p), st = seg_tiles_of(p);
     const i64 nitems = p.n_outer * nseg;
-    const int q0 = (int)threadIdx.x * XTG_SCAN_IPT;
-    for (i64 it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const i64 lofs = (i64)lane * XTG_SCAN_IPT;
+    for (i64 it = (i64)blockIdx.x * 8 + warp; it < nitems; it += (i64)gridDim.x * 8) {
         const i64 row = it / nseg, sg = it - row * nseg;
-        const i64 kb = sg * st * XTG_SCAN_TILE;
-        i64 ke = kb + st * XTG_SCAN_TILE;
-        if (ke > p.len) ke = p.len;
+        const i64 kb = sg * st * XTG_SCAN_WTILE;
+        const i64 ke = kb + st * XTG_SCAN_WTILE < p.len ? kb + st * XTG_SCAN_WTILE : p.len;
         ST carry = reinterpret_cast<const ST*>(p.agg)[it];
-        if constexpr (VEC > 1) {
-            // registers only: each thread its 16 consecutive elements; the
-            // next tile's loads are issued before this tile's block scan
-            auto tile = [&](RT(&v)[XTG_SCAN_IPT], i64 k0) {
-                const i64 kt = k0 + q0;
-                ST s = ST::ident();
-#pragma unroll
-                for (int i = 0; i < XTG_SCAN_IPT; ++i)
-                    if (kt + i < ke) s.add(v[i]);
-                ST thr_excl;
-                const ST tile_tot = block_inorder_scan(s, wsum, thr_excl);
-                ST pre = carry;
-                pre.merge(thr_excl);
-#pragma unroll
-                for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-                    const i64 k = kt + i;
-                    if (k < ke) {
-                        if (k == 0) {
-                            pre.hi = ScanOp<RT, OP>::init(v[i]);
-                            pre.lo = RT(0);
-                        } else {
-                            pre.add(v[i]);
-                        }
-                        v[i] = pre.value();
-                    }
-                }
-                RT* o = reinterpret_cast<RT*>(p.out) + row * p.oso;
-                if (kt + XTG_SCAN_IPT <= ke) {
-#pragma unroll
-                    for (int m = 0; m < XTG_SCAN_IPT / VEC; ++m) {
-                        RT w[VEC];
-#pragma unroll
-                        for (int j = 0; j < VEC; ++j) w[j] = v[m * VEC + j];
-                        st_out<RT, K_CONTIG, VEC>(o, kt + m * VEC, 1, w);
-                    }
-                } else {
-#pragma unroll
-                    for (int i = 0; i < XTG_SCAN_IPT; ++i)
-                        if (kt + i < ke) o[kt + i] = v[i];
-                }
-                carry.merge(tile_tot);
-            };
-            RT va[XTG_SCAN_IPT], vb[XTG_SCAN_IPT];
-            if (kb < ke) scan_load16<Tree, LS, RT, VEC>(p, c, row, kb + q0, ke, va);
-            for (i64 k0 = kb; k0 < ke; k0 += 2 * XTG_SCAN_TILE) {
-                if (k0 + XTG_SCAN_TILE < ke) scan_load16<Tree, LS, RT, VEC>(p, c, row, k0 + XTG_SCAN_TILE + q0, ke, vb);
-                tile(va, k0);
-                if (k0 + XTG_SCAN_TILE >= ke) break;
-                if (k0 + 2 * XTG_SCAN_TILE < ke)
-                    scan_load16<Tree, LS, RT, VEC>(p, c, row, k0 + 2 * XTG_SCAN_TILE + q0, ke, va);
-                tile(vb, k0 + XTG_SCAN_TILE);
-            }
-            continue;
-        }
-        for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_TILE) {
-#pragma unroll
-            for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-                const int q = i * 256 + (int)threadIdx.x;
-                const i64 k = k0 + q;
-                if (k < ke) buf[q + (q >> 5)] = scan_elem<Tree, LS, RT>(p, c, row, k);
-            }
-            __syncthreads();
+        RT* o = reinterpret_cast<RT*>(p.out) + row * p.oso;
+        scan_walk<Tree, LS, RT, VEC>(p, c, row, kb, ke, wb, [&](RT(&v)[XTG_SCAN_IPT], i64 k0) {
+            const i64 kt = k0 + lofs;
             ST s = ST::ident();
 #pragma unroll
-            for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-                const int q = q0 + i;
-                if (k0 + q < ke) s.add(buf[q + (q >> 5)]);
-            }
-            ST thr_excl;
-            const ST tile_tot = block_inorder_scan(s, wsum, thr_excl);
+            for (int i = 0; i < XTG_SCAN_IPT; ++i)
+                if (kt + i < ke) s.add(v[i]);
+            const ST inc = warp_inorder_scan(s);
+            const ST lex = shfl_up_pod(inc, 1);
+            const ST tile_tot = shfl_idx_pod(inc, 31);
             ST pre = carry;
-            pre.merge(thr_excl);
+            if (lane > 0) pre.merge(lex);
 #pragma unroll
             for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-                const int q = q0 + i;
-                const i64 k = k0 + q;
+                const i64 k = kt + i;
                 if (k < ke) {
-                    const RT x = buf[q + (q >> 5)];
                     if (k == 0) {
-                        pre.hi = ScanOp<RT, OP>::init(x);
+                        pre.hi = ScanOp<RT, OP>::init(v[i]);
                         pre.lo = RT(0);
                     } else {
-                        pre.add(x);
+                        pre.add(v[i]);
                     }
-                    buf[q + (q >> 5)] = pre.value();
+                    v[i] = pre.value();
                 }
             }
-            __syncthreads();
+            if (VEC > 1 && kt + XTG_SCAN_IPT <= ke) {
 #pragma unroll
-            for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-                const int q = i * 256 + (int)threadIdx.x;
-                const i64 k = k0 + q;
-                if (k < ke) reinterpret_cast<RT*>(p.out)[row * p.oso + k * p.osa] = buf[q + (q >> 5)];
+                for (int m = 0; m < XTG_SCAN_IPT / VEC; ++m) {
+                    RT w[VEC > 1 ? VEC : 1];
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) w[j] = v[m * VEC + j];
+                    st_out<RT, K_CONTIG, VEC>(o, kt + m * VEC, 1, w);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < XTG_SCAN_IPT; ++i)
+                    if (kt + i < ke) o[(kt + i) * p.osa] = v[i];
             }
             carry.merge(tile_tot);
-            __syncthreads();
-        }
+        });
     }
 }
 
