@@ -246,3 +246,77 @@ def test_tile_scan_strided_and_broadcast_operands(strategy):
     f = g.standard_normal((2, 50000)).astype(np.float32)
     got = ops.accumulate("cumsum", dev(f)[:, ::3], 1).to_numpy()
     _tile_tol_check(got, np.ascontiguousarray(f[:, ::3]), "cumsum", "strided float32")
+
+
+@pytest.fixture
+def scan_opts():
+    names = []
+
+    def set_(name, v):
+        names.append(name)
+        xg.set_option(name, v)
+    yield set_
+    for n in names:
+        xg.set_option(n, -1)
+
+
+@pytest.mark.parametrize("op", ["cumsum", "cumprod", "nancumsum"])
+def test_float64_streamed_scan_lane_totals(op, scan_opts, strategy):
+    """float64 operands of the segmented scan stream through the apply pass's
+    cp.async ring, and pass A keeps the lanes' tile totals for it: the lane
+    totals are the same values pass C would fold, so results are identical
+    bit for bit with and without them; and close to the reference's
+    sequential fold (1e-12 of the prefix magnitude for sums, 1e-9 relative
+    for products of 3M factors: both folds carry rounding errors growing with
+    the length; a wrong segment prefix would be off by O(1)).  Lengths that
+    end inside a warp tile, several segments per row, a few long rows."""
+    g = rng(61)
+    # rows of an even length: 16-byte aligned rows (the streamed form);
+    # 700002 = 1367 x 512 + 98 ends inside a warp tile and a lane's elements
+    for shape, axis in (((3_000_001,), None), ((3, 700_002), 1)):
+        if op == "cumprod":
+            x = 1.0 + 1e-6 * g.standard_normal(shape)
+        else:
+            x = g.standard_normal(shape)
+            if op == "nancumsum":
+                x[..., ::997] = np.nan
+        strategy(2 if axis is not None else -1)
+        d = dev(x)
+        on = ops.accumulate(op, d, axis).to_numpy()
+        apply = last_kernels()[-1]
+        assert apply.startswith("k_scan_seg_apply") and apply.endswith(", 16, true>"), apply
+        scan_opts("scan.lane_totals", 0)
+        off = ops.accumulate(op, d, axis).to_numpy()
+        assert last_kernels()[-1].endswith(", 16, false>")
+        xg.set_option("scan.lane_totals", -1)
+        np.testing.assert_array_equal(on.view(np.uint64), off.view(np.uint64))
+        ref = O.accumulate(op, H(x), axis)
+        xs = np.where(np.isnan(x), 0.0, x) if op == "nancumsum" else x
+        if op == "cumprod":
+            assert (np.abs(on - ref) <= 1e-9 * np.abs(ref)).all()
+        else:
+            mag = np.cumsum(np.abs(xs), -1 if axis is not None else None).reshape(on.shape)
+            assert (np.abs(on - ref) <= 1e-12 * mag).all()
+
+
+def test_streamed_and_register_forms_agree(scan_opts):
+    """The streamed apply pass (plain contiguous float32 / int32 operands,
+    tiles of 32 x 16 through shared memory) and the register form (tiles of
+    32 x 8) fold in different associations: integers are equal, float32
+    both within the double-float bound of the exact prefix."""
+    g = rng(62)
+    n = (1 << 22) + 777
+    xi = g.integers(-1000, 1000, n).astype(np.int32)
+    x = g.standard_normal(n).astype(np.float32)
+    outs = {}
+    for mode in (1, 0):
+        scan_opts("scan.async", mode)
+        outs[mode] = (ops.accumulate("cumsum", dev(xi), None).to_numpy(),
+                      ops.accumulate("cumsum", dev(x), None).to_numpy())
+        assert last_kernels()[-1].endswith(", 3, 16, false>" if mode else ", 0, 8, false>"), last_kernels()[-1]
+    np.testing.assert_array_equal(outs[1][0], outs[0][0])
+    np.testing.assert_array_equal(outs[1][0], np.cumsum(xi.astype(np.int64)).astype(np.int32))
+    exact = np.cumsum(x.astype(np.float64))
+    tol = 2.0**-23 * np.abs(exact) + 2.0**-36 * np.cumsum(np.abs(x.astype(np.float64)))
+    for mode in (1, 0):
+        assert (np.abs(outs[mode][1] - exact) <= tol).all(), mode

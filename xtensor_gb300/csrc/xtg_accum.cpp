@@ -280,19 +280,21 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
         const int64_t groups = (n_outer + 31) / 32;
         return launch(k, grid_of(k, (groups + 1) / 2), 64, &p, stream);
     }
-    // K9c: segmented reduce-then-scan, one warp per segment: warp tiles of
-    // 256 elements, about one segment per resident warp of the apply pass
-    // (so every warp of its single wave has one segment of equal length)
+    // K9c: segmented reduce-then-scan, one warp per segment: segments of
+    // whole 512-element units, about one segment per resident warp of the
+    // apply pass (so every warp of its single wave has one segment of equal
+    // length)
     DeviceInfo* dev;
     XTG_TRY(ensure_device(&dev));
+    const int rsz = dt(rt).size;
     // 16-byte register loads / stores when every leaf is contiguous or
     // broadcast along the rows and the destination contiguous, all aligned
-    int sv = std::min(8, 16 / dt(rt).size);  // at most the 8 elements a lane holds
+    int sv = std::min(8, 16 / rsz);  // at most the 8 elements a lane holds in the register form
     for (int l = 0; l < NL; ++l)
         if (p.lsa[l] == 1) sv = std::min(sv, 16 / dt(t.leaves[l].dtype).size);
     auto sv_ok = [&](int v) {
         if (v == 1) return true;
-        if (p.osa != 1 || p.oso % v || !aligned_to(out.data, (int64_t)v * dt(rt).size)) return false;
+        if (p.osa != 1 || p.oso % v || !aligned_to(out.data, (int64_t)v * rsz)) return false;
         for (int l = 0; l < NL; ++l) {
             if (p.lsa[l] != 0 && p.lsa[l] != 1) return false;
             if (p.lsa[l] == 1 && (p.lso[l] % v || !aligned_to(p.leaf[l], (int64_t)v * dt(t.leaves[l].dtype).size)))
@@ -304,29 +306,51 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
     std::vector<int> sk(NL);
     for (int l = 0; l < NL; ++l) sk[l] = sv > 1 ? kind_of_s(p.lsa[l]) : 2;
     const std::string sls = leafset_s(t, sk), svs = std::to_string(sv);
+    // A plain contiguous operand of the accumulation type (4 or 8 bytes,
+    // 16-byte vectors): the apply pass streams warp tiles of 32 x 16 elements
+    // through a per-warp cp.async ring of NS stages; for float64 pass A keeps
+    // the lanes' tile totals for it (CS).  Otherwise warp tiles of 32 x 8
+    // in registers.
+    const bool raw = opt("scan.async", 1) && NL == 1 && t.nodes[t.root].op == XTG_OP_LEAF &&
+                     t.leaves[0].dtype == rt && p.lsa[0] == 1 && (rsz == 4 || rsz == 8) && sv * rsz == 16;
+    const int ns = raw ? (int)std::max<int64_t>(2, std::min<int64_t>(8, opt("scan.seg_stages", 3))) : 0;
+    const int ipt_c = raw ? 16 : 8;
+    const bool cs = raw && rt == XTG_FLOAT64 && opt("scan.lane_totals", 1);
+    const int ipt_a = raw || rsz <= 4 ? 16 : 8;  // streamed operands: pass A's tiles are pass C's
+    // stages x warps x (warp tile + the lanes' totals)
+    const size_t ring = (size_t)ns * 8 * ((size_t)32 * ipt_c * rsz + (cs ? 32 * rsz : 0));
+    const std::string tail_a = ", " + svs + ", " + std::to_string(ipt_a) + ", " + (cs ? "true" : "false") + ">";
+    const std::string tail_c = ", " + svs + ", " + std::to_string(ns) + ", " + std::to_string(ipt_c) + ", " +
+                               (cs ? "true" : "false") + ">";
     Kernel *ka, *kb, *kc;
-    XTG_TRY(get_kernel("xtg::k_scan_seg_reduce<" + tree + ", " + sls + ", " + rts + ", " + ops + ", " + svs + ">", 256,
-                       &ka));
-    XTG_TRY(get_kernel("xtg::k_scan_seg_offsets<" + rts + ", " + ops + ">", 256, &kb));
-    XTG_TRY(get_kernel("xtg::k_scan_seg_apply<" + tree + ", " + sls + ", " + rts + ", " + ops + ", " + svs + ">", 256,
-                       &kc));
-    const int64_t wtile = 256;  // 32 lanes x 8 elements
-    const int64_t ntiles = (len + wtile - 1) / wtile;
+    XTG_TRY(get_kernel("xtg::k_scan_seg_reduce<" + tree + ", " + sls + ", " + rts + ", " + ops + tail_a, 256, &ka));
+    XTG_TRY(get_kernel("xtg::k_scan_seg_apply<" + tree + ", " + sls + ", " + rts + ", " + ops + tail_c, 256, &kc, ring));
+    const int64_t unit = 512;
+    const int64_t nunits = (len + unit - 1) / unit;
     const int64_t warps = (int64_t)kc->max_blocks_per_sm * dev->sm_count * 8;
     const int64_t target = std::max<int64_t>(1, warps / std::max<int64_t>(1, n_outer));
-    const int64_t seg_tiles = std::max<int64_t>(1, (ntiles + target - 1) / target);
-    const int64_t nseg = (ntiles + seg_tiles - 1) / seg_tiles;
-    if (seg_tiles >= (1ll << 32) || nseg >= (1ll << 30)) return fail(XTG_ERR_UNSUPPORTED, "scan too long");
-    p.ntiles = ntiles;
-    p.n_inner = (nseg << 32) | seg_tiles;
+    const int64_t seg_units = std::max<int64_t>(1, (nunits + target - 1) / target);
+    const int64_t nseg = (nunits + seg_units - 1) / seg_units;
+    if (seg_units >= (1ll << 32) || nseg >= (1ll << 30)) return fail(XTG_ERR_UNSUPPORTED, "scan too long");
+    // pass B stages a row's segment totals in shared memory
+    const size_t seg_smem = ((size_t)nseg * 16 + 15) & ~(size_t)15;
+    if (seg_smem > 200 * 1024) return fail(XTG_ERR_UNSUPPORTED, "scan: too many segments per row");
+    XTG_TRY(get_kernel("xtg::k_scan_seg_offsets<" + rts + ", " + ops + ">", 256, &kb, seg_smem));
+    p.ntiles = nunits;
+    p.n_inner = (nseg << 32) | seg_units;
+    // one scratch block: the segment states, then (CS) one value per lane
+    // of every warp tile of every row
+    const size_t agg_bytes = ((size_t)n_outer * (size_t)nseg * 16 + 255) & ~(size_t)255;
+    const size_t cs_bytes = cs ? (size_t)n_outer * (size_t)nunits * 32 * rsz : 0;
+    p.csum_off = cs ? (int64_t)agg_bytes : 0;
     void* agg = nullptr;
-    XTG_TRY(scratch_alloc(&agg, (size_t)n_outer * (size_t)nseg * 16, stream));
+    XTG_TRY(scratch_alloc(&agg, agg_bytes + cs_bytes, stream));
     p.agg = agg;
     const int agg_off = (int)offsetof(xtg::ScanParams, agg);
     const int64_t blocks = (n_outer * nseg + 7) / 8;  // eight warps per block
     xtg_status st = launch(ka, grid_of(ka, blocks), 256, &p, stream, 0, agg_off);
-    if (st == XTG_OK) st = launch(kb, grid_of(kb, n_outer), 256, &p, stream, 0, agg_off);
-    if (st == XTG_OK) st = launch(kc, grid_of(kc, blocks), 256, &p, stream, 0, agg_off);
+    if (st == XTG_OK) st = launch(kb, grid_of(kb, n_outer), 256, &p, stream, seg_smem, agg_off);
+    if (st == XTG_OK) st = launch(kc, grid_of(kc, blocks), 256, &p, stream, ring, agg_off);
     xtg_status fs = scratch_free(agg, stream);
     return st != XTG_OK ? st : fs;
 }

@@ -2173,7 +2173,6 @@ template <int OP> struct ScanState<float, OP> {
     XTG_DI float value() const { return lo == 0.f ? hi : hi + lo; }
 };
 
-constexpr int XTG_SCAN_IPT = 8;  // consecutive elements per lane of a warp tile
 
 template <class Tree, class LS, class RT>
 XTG_DI RT scan_elem(const ScanParams& p, const Ctx<0>& c, i64 row, i64 k) {
@@ -2234,29 +2233,33 @@ template <class ST> XTG_DI ST block_inorder_scan(ST v, ST* wsum, ST& excl_in_blo
 }
 
 // Segmented reduce-then-scan, one warp per segment (no warp ever waits on
-// another, and no block barrier): a row is cut into segments of seg_tiles
-// warp tiles (32 lanes x 8 consecutive elements per lane), about one
-// segment per resident warp of the launch; (A) each segment's total, (B) per
-// row, the exclusive prefixes of the segment totals in order, (C) each
-// segment again, tile by tile, from its prefix: every lane folds its 8
-// elements, the warp scans the lane totals in lane order, every lane
-// rescans its elements from (carry, the lanes before it) and the tile total
-// joins the carry.  A fixed structure, so results do not depend on timing.
-// ScanParams.ntiles = warp tiles per row; segments per row and tiles per
-// segment ride in n_inner (unused for these rows) as nseg * 2^32 + seg_tiles.
-constexpr int XTG_SCAN_WTILE = 32 * XTG_SCAN_IPT;
-XTG_DI i64 seg_tiles_of(const ScanParams& p) { return p.n_inner & 0xffffffffll; }
+// another, and no block barrier): a row is cut into segments of whole units
+// of 512 elements, about one segment per resident warp of the apply pass;
+// (A) each segment's total, (B) per row, the exclusive prefixes of the
+// segment totals in order, (C) each segment again, warp tile by warp tile
+// (32 lanes x IPT consecutive elements per lane), from its prefix: every
+// lane folds its IPT elements, the warp scans the lane totals in lane order,
+// every lane rescans its elements from (carry, the lanes before it) and the
+// tile total joins the carry.  A fixed structure, so results do not depend
+// on timing.  With CS (float64 operands streamed by the apply pass) pass A
+// also stores every lane's fold of every tile, and pass C takes the lane
+// totals from there instead of folding again — the same values, one FP64
+// add per element less on a part whose FP64 rate bounds this scan.
+// ScanParams.ntiles = units per row; segments per row and units per segment
+// ride in n_inner (unused for these rows) as nseg * 2^32 + seg_units.
+constexpr int XTG_SCAN_UNIT = 512;
+XTG_DI i64 seg_units_of(const ScanParams& p) { return p.n_inner & 0xffffffffll; }
 XTG_DI i64 nseg_of(const ScanParams& p) { return p.n_inner >> 32; }
 
-// A lane's 8 consecutive elements into registers: VEC-wide loads when all
-// 8 lie before `ke` (VEC > 1: every leaf contiguous or broadcast along the
+// A lane's IPT consecutive elements into registers: VEC-wide loads when all
+// lie before `ke` (VEC > 1: every leaf contiguous or broadcast along the
 // row, rows VEC-aligned — the host checks), else one by one.
-template <class Tree, class LS, class RT, int VEC>
-XTG_DI void scan_loadv(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kt, i64 ke, RT (&v)[XTG_SCAN_IPT]) {
-    if (VEC > 1 && kt + XTG_SCAN_IPT <= ke) {
+template <class Tree, class LS, class RT, int VEC, int IPT>
+XTG_DI void scan_loadv(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kt, i64 ke, RT (&v)[IPT]) {
+    if (VEC > 1 && kt + IPT <= ke) {
         typedef typename LS::template R<VEC>::type RG;
 #pragma unroll
-        for (int m = 0; m < XTG_SCAN_IPT / VEC; ++m) {
+        for (int m = 0; m < IPT / VEC; ++m) {
             i64 off[XTG_KMAX_LEAVES];
 #pragma unroll
             for (int l = 0; l < LS::N; ++l) off[l] = row * p.lso[l] + (kt + m * VEC) * p.lsa[l];
@@ -2267,26 +2270,25 @@ XTG_DI void scan_loadv(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kt, i6
         }
     } else {
 #pragma unroll
-        for (int i = 0; i < XTG_SCAN_IPT; ++i) v[i] = kt + i < ke ? scan_elem<Tree, LS, RT>(p, c, row, kt + i) : RT(0);
+        for (int i = 0; i < IPT; ++i) v[i] = kt + i < ke ? scan_elem<Tree, LS, RT>(p, c, row, kt + i) : RT(0);
     }
 }
 
 // VEC == 1 (strided leaves): a warp tile through the warp's own buffer in
 // shared memory — coalesced loads (lane l takes l, l + 32, ...), then each
-// lane its 8 consecutive elements (rows padded by one element per 32).
-template <class Tree, class LS, class RT>
-XTG_DI void scan_loadw(const ScanParams& p, const Ctx<0>& c, i64 row, i64 k0, i64 ke, RT* wb,
-                             RT (&v)[XTG_SCAN_IPT]) {
+// lane its IPT consecutive elements (rows padded by one element per 32).
+template <class Tree, class LS, class RT, int IPT>
+XTG_DI void scan_loadw(const ScanParams& p, const Ctx<0>& c, i64 row, i64 k0, i64 ke, RT* wb, RT (&v)[IPT]) {
     const int lane = (int)threadIdx.x & 31;
 #pragma unroll
-    for (int i = 0; i < XTG_SCAN_IPT; ++i) {
+    for (int i = 0; i < IPT; ++i) {
         const int q = i * 32 + lane;
         if (k0 + q < ke) wb[q + (q >> 5)] = scan_elem<Tree, LS, RT>(p, c, row, k0 + q);
     }
     __syncwarp();
 #pragma unroll
-    for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-        const int q = lane * XTG_SCAN_IPT + i;
+    for (int i = 0; i < IPT; ++i) {
+        const int q = lane * IPT + i;
         v[i] = k0 + q < ke ? wb[q + (q >> 5)] : RT(0);
     }
     __syncwarp();
@@ -2295,25 +2297,24 @@ XTG_DI void scan_loadw(const ScanParams& p, const Ctx<0>& c, i64 row, i64 k0, i6
 // The warp tiles [kb, ke) of one row in order, each handed to f(v, k0) in
 // the lanes' registers; with VEC > 1 the next tile's loads are in flight
 // while f works on the current one.
-template <class Tree, class LS, class RT, int VEC, class F>
+template <class Tree, class LS, class RT, int VEC, int IPT, class F>
 XTG_DI void scan_walk(const ScanParams& p, const Ctx<0>& c, i64 row, i64 kb, i64 ke, RT* wb, F&& f) {
-    const i64 lofs = (i64)((int)threadIdx.x & 31) * XTG_SCAN_IPT;
+    constexpr int WT = 32 * IPT;
+    const i64 lofs = (i64)((int)threadIdx.x & 31) * IPT;
     if constexpr (VEC > 1) {
-        RT va[XTG_SCAN_IPT], vb[XTG_SCAN_IPT];
-        if (kb < ke) scan_loadv<Tree, LS, RT, VEC>(p, c, row, kb + lofs, ke, va);
-        for (i64 k0 = kb; k0 < ke; k0 += 2 * XTG_SCAN_WTILE) {
-            if (k0 + XTG_SCAN_WTILE < ke)
-                scan_loadv<Tree, LS, RT, VEC>(p, c, row, k0 + XTG_SCAN_WTILE + lofs, ke, vb);
+        RT va[IPT], vb[IPT];
+        if (kb < ke) scan_loadv<Tree, LS, RT, VEC, IPT>(p, c, row, kb + lofs, ke, va);
+        for (i64 k0 = kb; k0 < ke; k0 += 2 * WT) {
+            if (k0 + WT < ke) scan_loadv<Tree, LS, RT, VEC, IPT>(p, c, row, k0 + WT + lofs, ke, vb);
             f(va, k0);
-            if (k0 + XTG_SCAN_WTILE >= ke) break;
-            if (k0 + 2 * XTG_SCAN_WTILE < ke)
-                scan_loadv<Tree, LS, RT, VEC>(p, c, row, k0 + 2 * XTG_SCAN_WTILE + lofs, ke, va);
-            f(vb, k0 + XTG_SCAN_WTILE);
+            if (k0 + WT >= ke) break;
+            if (k0 + 2 * WT < ke) scan_loadv<Tree, LS, RT, VEC, IPT>(p, c, row, k0 + 2 * WT + lofs, ke, va);
+            f(vb, k0 + WT);
         }
     } else {
-        RT v[XTG_SCAN_IPT];
-        for (i64 k0 = kb; k0 < ke; k0 += XTG_SCAN_WTILE) {
-            scan_loadw<Tree, LS, RT>(p, c, row, k0, ke, wb, v);
+        RT v[IPT];
+        for (i64 k0 = kb; k0 < ke; k0 += WT) {
+            scan_loadw<Tree, LS, RT, IPT>(p, c, row, k0, ke, wb, v);
             f(v, k0);
         }
     }
@@ -2334,115 +2335,178 @@ template <class ST> XTG_DI ST warp_inorder_scan(ST v) {
     return v;
 }
 
-// Shared-memory words per warp for the VEC == 1 tile buffer.
-template <class RT, int VEC> struct ScanWarpBuf {
-    static constexpr int n = VEC > 1 ? 1 : XTG_SCAN_WTILE + XTG_SCAN_WTILE / 32;
+// Shared-memory elements per warp for the VEC == 1 tile buffer.
+template <int VEC, int IPT> struct ScanWarpBuf {
+    static constexpr int n = VEC > 1 ? 1 : 32 * IPT + IPT;
 };
 
-template <class Tree, class LS, class RT, int OP, int VEC>
+// Lane totals of pass A kept for pass C: one value per (row, warp tile, lane).
+template <class RT> XTG_DI RT* scan_csum(const ScanParams& p) {
+    return reinterpret_cast<RT*>(reinterpret_cast<char*>(p.agg) + p.csum_off);
+}
+
+template <class Tree, class LS, class RT, int OP, int VEC, int IPT, bool CS>
 __global__ void __launch_bounds__(256) k_scan_seg_reduce(const ScanParams p) {
     pdl_wait();
     typedef ScanState<RT, OP> ST;
-    constexpr int WB = ScanWarpBuf<RT, VEC>::n;
+    constexpr int WB = ScanWarpBuf<VEC, IPT>::n, WT = 32 * IPT;
     __shared__ RT wbuf[8 * WB];
     Ctx<0> c;
     c.scal = p.scal;
     const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
     RT* wb = wbuf + warp * WB;
-    const i64 nseg = nseg_of(p), st = seg_tiles_of(p);
+    const i64 nseg = nseg_of(p), su = seg_units_of(p);
     const i64 nitems = p.n_outer * nseg;
-    const i64 lofs = (i64)lane * XTG_SCAN_IPT;
+    const i64 lofs = (i64)lane * IPT;
+    const i64 tiles_per_row = p.ntiles * (XTG_SCAN_UNIT / WT);
     for (i64 it = (i64)blockIdx.x * 8 + warp; it < nitems; it += (i64)gridDim.x * 8) {
         const i64 row = it / nseg, sg = it - row * nseg;
-        const i64 kb = sg * st * XTG_SCAN_WTILE;
-        const i64 ke = kb + st * XTG_SCAN_WTILE < p.len ? kb + st * XTG_SCAN_WTILE : p.len;
+        const i64 kb = sg * su * XTG_SCAN_UNIT;
+        const i64 ke = kb + su * XTG_SCAN_UNIT < p.len ? kb + su * XTG_SCAN_UNIT : p.len;
         ST s = ST::ident();
-        scan_walk<Tree, LS, RT, VEC>(p, c, row, kb, ke, wb, [&](RT(&v)[XTG_SCAN_IPT], i64 k0) {
+        scan_walk<Tree, LS, RT, VEC, IPT>(p, c, row, kb, ke, wb, [&](RT(&v)[IPT], i64 k0) {
+            // the lane's fold of each tile (what pass C folds), then merged
             const i64 kt = k0 + lofs;
+            ST t = ST::ident();
+            if (kt + IPT <= ke) {
 #pragma unroll
-            for (int i = 0; i < XTG_SCAN_IPT; ++i)
-                if (kt + i < ke) s.add(v[i]);
+                for (int i = 0; i < IPT; ++i) t.add(v[i]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < IPT; ++i)
+                    if (kt + i < ke) t.add(v[i]);
+            }
+            if constexpr (CS) scan_csum<RT>(p)[(row * tiles_per_row + k0 / WT) * 32 + lane] = t.hi;
+            s.merge(t);
         });
         const ST tot = warp_inorder_scan(s);
         if (lane == 31) reinterpret_cast<ST*>(p.agg)[it] = tot;
     }
 }
 
-// (B) one CTA per row: exclusive prefixes of the row's segment totals, in place
+// (B) one CTA per row: exclusive prefixes of the row's segment totals, in
+// place.  The row's totals (at most one per resident warp: under 160 KB)
+// are staged in shared memory by coalesced asynchronous copies, all in
+// flight at once; thread t owns the run of
+// `per` consecutive totals from t * per: it folds them in order, one block
+// scan of the runs' totals gives each run its prefix, and the thread
+// rewrites its run from that prefix.
 template <class RT, int OP>
 __global__ void __launch_bounds__(256) k_scan_seg_offsets(const ScanParams p) {
     pdl_wait();
     typedef ScanState<RT, OP> ST;
     __shared__ ST wsum[9];
+    extern __shared__ __align__(16) unsigned char seg_smem[];
+    ST* sa = reinterpret_cast<ST*>(seg_smem);
     const i64 nseg = nseg_of(p);
+    const i64 per = (nseg + 255) / 256;
+    const i64 b0 = (i64)threadIdx.x * per;
+    const i64 b1 = b0 + per < nseg ? b0 + per : nseg;
     for (i64 row = blockIdx.x; row < p.n_outer; row += gridDim.x) {
         ST* a = reinterpret_cast<ST*>(p.agg) + row * nseg;
-        ST carry = ST::ident();
-        for (i64 b = 0; b < nseg; b += 256) {
-            const i64 i = b + threadIdx.x;
-            const ST v = i < nseg ? a[i] : ST::ident();
-            ST ex;
-            const ST tot = block_inorder_scan(v, wsum, ex);
-            ST pre = carry;
-            pre.merge(ex);
-            if (i < nseg) a[i] = pre;
-            carry.merge(tot);
-            __syncthreads();
+        if constexpr (sizeof(ST) == 16 || sizeof(ST) == 8 || sizeof(ST) == 4) {
+            // every copy in flight at once
+            for (i64 i = threadIdx.x; i < nseg; i += 256) cp_async<(int)sizeof(ST)>(&sa[i], &a[i]);
+            cp_async_commit();
+            cp_async_wait<0>();
+        } else {
+            for (i64 i = threadIdx.x; i < nseg; i += 256) sa[i] = a[i];
         }
+        __syncthreads();
+        ST run = ST::ident();
+        for (i64 i = b0; i < b1; ++i) run.merge(sa[i]);
+        ST pre;
+        block_inorder_scan(run, wsum, pre);
+        for (i64 i = b0; i < b1; ++i) {
+            const ST v = sa[i];
+            sa[i] = pre;
+            pre.merge(v);
+        }
+        __syncthreads();
+        for (i64 i = threadIdx.x; i < nseg; i += 256) a[i] = sa[i];
+        __syncthreads();
     }
 }
 
 // (C) each segment again from its prefix.  Results leave the lanes'
-// registers: 16-byte stores when the lane's 8 elements are whole (VEC > 1:
-// the destination contiguous and aligned — the host checks).  Four blocks
-// per SM for 4-byte types with vector access (a register bound of 64, no
-// spill), two otherwise.
-template <class Tree, class LS, class RT, int OP, int VEC>
-__global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : 2) k_scan_seg_apply(const ScanParams p) {
+// registers: 16-byte stores when the lane's elements are whole (VEC > 1:
+// the destination contiguous and aligned — the host checks).  NS > 0 (the
+// operand a plain contiguous array of the accumulation type, 4 or 8 bytes,
+// rows 16-byte aligned): every lane streams its own 16-byte chunks of the
+// next NS - 1 tiles into a per-warp ring in shared memory with cp.async, so
+// tiles are in flight without holding registers; a lane reads back only
+// what it copied itself (visible to it after cp.async.wait_group), so no
+// barrier is involved.  Chunk m of a lane lands in slot (m + rot) mod CPL of
+// the lane's 16-byte slots, rot = the lane's position within its 128 bytes
+// of the stage: the lanes of one 8-lane phase of a 16-byte read hit
+// distinct banks.  Four blocks per SM for 4-byte types with vector access
+// (a register bound of 64, no spill), fewer otherwise.
+template <class Tree, class LS, class RT, int OP, int VEC, int NS, int IPT, bool CS>
+__global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : NS > 0 && IPT <= 8 ? 3 : 2)
+    k_scan_seg_apply(const ScanParams p) {
     pdl_wait();
     typedef ScanState<RT, OP> ST;
-    constexpr int WB = ScanWarpBuf<RT, VEC>::n;
+    constexpr int WB = NS > 0 ? 1 : ScanWarpBuf<VEC, IPT>::n, WT = 32 * IPT;
     __shared__ RT wbuf[8 * WB];
+    extern __shared__ __align__(16) unsigned char ring[];
     Ctx<0> c;
     c.scal = p.scal;
     const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
     RT* wb = wbuf + warp * WB;
-    const i64 nseg = nseg_of(p), st = seg_tiles_of(p);
+    const i64 nseg = nseg_of(p), su = seg_units_of(p);
     const i64 nitems = p.n_outer * nseg;
-    const i64 lofs = (i64)lane * XTG_SCAN_IPT;
+    const i64 lofs = (i64)lane * IPT;
+    const i64 tiles_per_row = p.ntiles * (XTG_SCAN_UNIT / WT);
     for (i64 it = (i64)blockIdx.x * 8 + warp; it < nitems; it += (i64)gridDim.x * 8) {
         const i64 row = it / nseg, sg = it - row * nseg;
-        const i64 kb = sg * st * XTG_SCAN_WTILE;
-        const i64 ke = kb + st * XTG_SCAN_WTILE < p.len ? kb + st * XTG_SCAN_WTILE : p.len;
+        const i64 kb = sg * su * XTG_SCAN_UNIT;
+        const i64 ke = kb + su * XTG_SCAN_UNIT < p.len ? kb + su * XTG_SCAN_UNIT : p.len;
         ST carry = reinterpret_cast<const ST*>(p.agg)[it];
         RT* o = reinterpret_cast<RT*>(p.out) + row * p.oso;
-        scan_walk<Tree, LS, RT, VEC>(p, c, row, kb, ke, wb, [&](RT(&v)[XTG_SCAN_IPT], i64 k0) {
+        auto tile = [&](RT(&v)[IPT], i64 k0, RT csv) {
             const i64 kt = k0 + lofs;
+            // every tile but a row's last is whole: no per-element checks
+            const bool full = kt + IPT <= ke;
             ST s = ST::ident();
+            if constexpr (CS) {
+                s.hi = csv;
+            } else if (full) {
 #pragma unroll
-            for (int i = 0; i < XTG_SCAN_IPT; ++i)
-                if (kt + i < ke) s.add(v[i]);
+                for (int i = 0; i < IPT; ++i) s.add(v[i]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < IPT; ++i)
+                    if (kt + i < ke) s.add(v[i]);
+            }
             const ST inc = warp_inorder_scan(s);
             const ST lex = shfl_up_pod(inc, 1);
             const ST tile_tot = shfl_idx_pod(inc, 31);
             ST pre = carry;
             if (lane > 0) pre.merge(lex);
+            if (full && kt != 0) {
 #pragma unroll
-            for (int i = 0; i < XTG_SCAN_IPT; ++i) {
-                const i64 k = kt + i;
-                if (k < ke) {
-                    if (k == 0) {
-                        pre.hi = ScanOp<RT, OP>::init(v[i]);
-                        pre.lo = RT(0);
-                    } else {
-                        pre.add(v[i]);
-                    }
+                for (int i = 0; i < IPT; ++i) {
+                    pre.add(v[i]);
                     v[i] = pre.value();
                 }
-            }
-            if (VEC > 1 && kt + XTG_SCAN_IPT <= ke) {
+            } else {
 #pragma unroll
-                for (int m = 0; m < XTG_SCAN_IPT / VEC; ++m) {
+                for (int i = 0; i < IPT; ++i) {
+                    const i64 k = kt + i;
+                    if (k < ke) {
+                        if (k == 0) {
+                            pre.hi = ScanOp<RT, OP>::init(v[i]);
+                            pre.lo = RT(0);
+                        } else {
+                            pre.add(v[i]);
+                        }
+                        v[i] = pre.value();
+                    }
+                }
+            }
+            if (VEC > 1 && full) {
+#pragma unroll
+                for (int m = 0; m < IPT / VEC; ++m) {
                     RT w[VEC > 1 ? VEC : 1];
 #pragma unroll
                     for (int j = 0; j < VEC; ++j) w[j] = v[m * VEC + j];
@@ -2450,11 +2514,68 @@ __global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : 2) k_sca
                 }
             } else {
 #pragma unroll
-                for (int i = 0; i < XTG_SCAN_IPT; ++i)
+                for (int i = 0; i < IPT; ++i)
                     if (kt + i < ke) o[(kt + i) * p.osa] = v[i];
             }
             carry.merge(tile_tot);
-        });
+        };
+        if constexpr (NS > 0) {
+            constexpr int EPC = 16 / (int)sizeof(RT);        // elements per 16-byte chunk
+            constexpr int CPL = IPT / EPC;                   // chunks per lane
+            constexpr int SB = 32 * IPT * (int)sizeof(RT);   // bytes of a warp tile
+            // a stage: the warp tile, then (CS) the 32 lanes' totals from pass A
+            constexpr int SBX = SB + (CS ? 32 * (int)sizeof(RT) : 0);
+            unsigned char* wbase = ring + (size_t)warp * NS * SBX;
+            unsigned char* wr = wbase + (size_t)lane * CPL * 16;
+            const int rot = (lane / (CPL >= 8 ? 1 : 8 / CPL)) % CPL;
+            const RT* src = reinterpret_cast<const RT*>(p.leaf[0]) + row * p.lso[0];
+            const i64 T = (ke - kb + WT - 1) / WT;
+            auto issue = [&](i64 t) {
+                const i64 kt = kb + t * WT + lofs;
+                if (t < T && kt + IPT <= ke) {
+                    unsigned char* d = wr + (int)(t % NS) * SBX;
+#pragma unroll
+                    for (int m = 0; m < CPL; ++m) cp_async<16>(d + ((m + rot) % CPL) * 16, src + kt + m * EPC);
+                }
+                if (CS && t < T)
+                    cp_async<(int)sizeof(RT)>(wbase + (int)(t % NS) * SBX + SB + lane * (int)sizeof(RT),
+                                              scan_csum<RT>(p) + (row * tiles_per_row + (kb + t * WT) / WT) * 32 + lane);
+                cp_async_commit();
+            };
+#pragma unroll 1
+            for (int j = 0; j < NS - 1; ++j) issue(j);
+            for (i64 t = 0; t < T; ++t) {
+                // the slot of tile t + NS - 1 was read back (into registers
+                // already used) while tile t - 1 was scanned
+                issue(t + NS - 1);
+                cp_async_wait<NS - 1>();
+                const i64 k0 = kb + t * WT, kt = k0 + lofs;
+                const RT csv =
+                    CS ? *reinterpret_cast<const RT*>(wbase + (int)(t % NS) * SBX + SB + lane * (int)sizeof(RT)) : RT(0);
+                RT v[IPT];
+                if (kt + IPT <= ke) {
+                    const unsigned char* d = wr + (int)(t % NS) * SBX;
+#pragma unroll
+                    for (int m = 0; m < CPL; ++m) {
+                        union {
+                            uint4 q;
+                            RT e[EPC];
+                        } u;
+                        u.q = *reinterpret_cast<const uint4*>(d + ((m + rot) % CPL) * 16);
+#pragma unroll
+                        for (int j = 0; j < EPC; ++j) v[m * EPC + j] = u.e[j];
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < IPT; ++i) v[i] = kt + i < ke ? src[kt + i] : RT(0);
+                }
+                tile(v, k0, csv);
+            }
+        } else {
+            static_assert(!CS, "lane totals from pass A come with the streamed form");
+            scan_walk<Tree, LS, RT, VEC, IPT>(p, c, row, kb, ke, wb,
+                                              [&](RT(&v)[IPT], i64 k0) { tile(v, k0, RT(0)); });
+        }
     }
 }
 

@@ -158,6 +158,7 @@ struct ScanParams {
     Scalars scal;
     i64 ntiles;         // segmented scan: tiles per row
     void* agg;          // segmented scan: one partial state (16 B) per segment
+    i64 csum_off;       // segmented scan: byte offset from agg of the lanes' tile sums (0: none)
 };
 
 // Indexed evaluation through index_view / filter (gathers and scatters).
