@@ -263,8 +263,8 @@ def scan_opts():
 @pytest.mark.parametrize("op", ["cumsum", "cumprod", "nancumsum"])
 def test_float64_streamed_scan_lane_totals(op, scan_opts, strategy):
     """float64 operands of the segmented scan stream through the apply pass's
-    cp.async ring, and pass A keeps the lanes' tile totals for it: the lane
-    totals are the same values pass C would fold, so results are identical
+    cp.async ring, and pass A keeps the lanes' tile folds for it (two chains
+    of 8 per lane): they are the same values pass C would fold, so results are identical
     bit for bit with and without them; and close to the reference's
     sequential fold (1e-12 of the prefix magnitude for sums, 1e-9 relative
     for products of 3M factors: both folds carry rounding errors growing with
@@ -284,10 +284,10 @@ def test_float64_streamed_scan_lane_totals(op, scan_opts, strategy):
         d = dev(x)
         on = ops.accumulate(op, d, axis).to_numpy()
         apply = last_kernels()[-1]
-        assert apply.startswith("k_scan_seg_apply") and apply.endswith(", 16, true>"), apply
+        assert apply.startswith("k_scan_seg_apply") and apply.endswith(", 16, true, 2>"), apply
         scan_opts("scan.lane_totals", 0)
         off = ops.accumulate(op, d, axis).to_numpy()
-        assert last_kernels()[-1].endswith(", 16, false>")
+        assert last_kernels()[-1].endswith(", 16, false, 2>")
         xg.set_option("scan.lane_totals", -1)
         np.testing.assert_array_equal(on.view(np.uint64), off.view(np.uint64))
         ref = O.accumulate(op, H(x), axis)
@@ -313,7 +313,7 @@ def test_streamed_and_register_forms_agree(scan_opts):
         scan_opts("scan.async", mode)
         outs[mode] = (ops.accumulate("cumsum", dev(xi), None).to_numpy(),
                       ops.accumulate("cumsum", dev(x), None).to_numpy())
-        assert last_kernels()[-1].endswith(", 3, 16, false>" if mode else ", 0, 8, false>"), last_kernels()[-1]
+        assert last_kernels()[-1].endswith(", 3, 16, false, 1>" if mode else ", 0, 8, false, 1>"), last_kernels()[-1]
     np.testing.assert_array_equal(outs[1][0], outs[0][0])
     np.testing.assert_array_equal(outs[1][0], np.cumsum(xi.astype(np.int64)).astype(np.int32))
     exact = np.cumsum(x.astype(np.float64))

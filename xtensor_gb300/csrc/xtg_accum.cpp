@@ -317,11 +317,16 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
     const int ipt_c = raw ? 16 : 8;
     const bool cs = raw && rt == XTG_FLOAT64 && opt("scan.lane_totals", 1);
     const int ipt_a = raw || rsz <= 4 ? 16 : 8;  // streamed operands: pass A's tiles are pass C's
-    // stages x warps x (warp tile + the lanes' totals)
-    const size_t ring = (size_t)ns * 8 * ((size_t)32 * ipt_c * rsz + (cs ? 32 * rsz : 0));
-    const std::string tail_a = ", " + svs + ", " + std::to_string(ipt_a) + ", " + (cs ? "true" : "false") + ">";
+    // lane chains: two for streamed float64, with or without CS, so that
+    // both give the same bits (four cost more FP64 adds than they hide:
+    // 1.11 against 0.90 ms on 2^27 elements)
+    const int nch = raw && rt == XTG_FLOAT64 ? 2 : 1;
+    // stages x warps x (warp tile + the lanes' folds)
+    const size_t ring = (size_t)ns * 8 * ((size_t)32 * ipt_c * rsz + (cs ? (size_t)32 * nch * rsz : 0));
+    const std::string tail_a = ", " + svs + ", " + std::to_string(ipt_a) + ", " + (cs ? "true" : "false") + ", " +
+                               std::to_string(nch) + ">";
     const std::string tail_c = ", " + svs + ", " + std::to_string(ns) + ", " + std::to_string(ipt_c) + ", " +
-                               (cs ? "true" : "false") + ">";
+                               (cs ? "true" : "false") + ", " + std::to_string(nch) + ">";
     Kernel *ka, *kb, *kc;
     XTG_TRY(get_kernel("xtg::k_scan_seg_reduce<" + tree + ", " + sls + ", " + rts + ", " + ops + tail_a, 256, &ka));
     XTG_TRY(get_kernel("xtg::k_scan_seg_apply<" + tree + ", " + sls + ", " + rts + ", " + ops + tail_c, 256, &kc, ring));
@@ -341,7 +346,7 @@ xtg_status scan_launch(const Tree& t, int rt, int op, const AccPlan& P, const xt
     // one scratch block: the segment states, then (CS) one value per lane
     // of every warp tile of every row
     const size_t agg_bytes = ((size_t)n_outer * (size_t)nseg * 16 + 255) & ~(size_t)255;
-    const size_t cs_bytes = cs ? (size_t)n_outer * (size_t)nunits * 32 * rsz : 0;
+    const size_t cs_bytes = cs ? (size_t)n_outer * (size_t)nunits * 32 * nch * rsz : 0;
     p.csum_off = cs ? (int64_t)agg_bytes : 0;
     void* agg = nullptr;
     XTG_TRY(scratch_alloc(&agg, agg_bytes + cs_bytes, stream));

@@ -2345,7 +2345,30 @@ template <class RT> XTG_DI RT* scan_csum(const ScanParams& p) {
     return reinterpret_cast<RT*>(reinterpret_cast<char*>(p.agg) + p.csum_off);
 }
 
-template <class Tree, class LS, class RT, int OP, int VEC, int IPT, bool CS>
+// A lane's fold of its IPT elements in H independent chains of IPT / H
+// consecutive elements (H = 2 for float64: the FP64 results come back
+// through a long-latency path, so two chains in flight halve the wait),
+// range-checked when the tile ends inside the lane.
+template <int H, class ST, class RT, int IPT>
+XTG_DI void lane_fold(ST (&h)[H], const RT (&v)[IPT], i64 kt, i64 ke) {
+    constexpr int L = IPT / H;
+#pragma unroll
+    for (int j = 0; j < H; ++j) h[j] = ST::ident();
+    if (kt + IPT <= ke) {
+#pragma unroll
+        for (int i = 0; i < L; ++i)
+#pragma unroll
+            for (int j = 0; j < H; ++j) h[j].add(v[j * L + i]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < L; ++i)
+#pragma unroll
+            for (int j = 0; j < H; ++j)
+                if (kt + j * L + i < ke) h[j].add(v[j * L + i]);
+    }
+}
+
+template <class Tree, class LS, class RT, int OP, int VEC, int IPT, bool CS, int H>
 __global__ void __launch_bounds__(256) k_scan_seg_reduce(const ScanParams p) {
     pdl_wait();
     typedef ScanState<RT, OP> ST;
@@ -2366,18 +2389,15 @@ __global__ void __launch_bounds__(256) k_scan_seg_reduce(const ScanParams p) {
         ST s = ST::ident();
         scan_walk<Tree, LS, RT, VEC, IPT>(p, c, row, kb, ke, wb, [&](RT(&v)[IPT], i64 k0) {
             // the lane's fold of each tile (what pass C folds), then merged
-            const i64 kt = k0 + lofs;
-            ST t = ST::ident();
-            if (kt + IPT <= ke) {
+            ST hs[H];
+            lane_fold<H>(hs, v, k0 + lofs, ke);
+            if constexpr (CS) {
+                RT* cs = scan_csum<RT>(p) + ((row * tiles_per_row + k0 / WT) * 32 + lane) * H;
 #pragma unroll
-                for (int i = 0; i < IPT; ++i) t.add(v[i]);
-            } else {
-#pragma unroll
-                for (int i = 0; i < IPT; ++i)
-                    if (kt + i < ke) t.add(v[i]);
+                for (int j = 0; j < H; ++j) cs[j] = hs[j].hi;
             }
-            if constexpr (CS) scan_csum<RT>(p)[(row * tiles_per_row + k0 / WT) * 32 + lane] = t.hi;
-            s.merge(t);
+#pragma unroll
+            for (int j = 0; j < H; ++j) s.merge(hs[j]);
         });
         const ST tot = warp_inorder_scan(s);
         if (lane == 31) reinterpret_cast<ST*>(p.agg)[it] = tot;
@@ -2441,7 +2461,7 @@ __global__ void __launch_bounds__(256) k_scan_seg_offsets(const ScanParams p) {
 // of the stage: the lanes of one 8-lane phase of a 16-byte read hit
 // distinct banks.  Four blocks per SM for 4-byte types with vector access
 // (a register bound of 64, no spill), fewer otherwise.
-template <class Tree, class LS, class RT, int OP, int VEC, int NS, int IPT, bool CS>
+template <class Tree, class LS, class RT, int OP, int VEC, int NS, int IPT, bool CS, int H>
 __global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : NS > 0 && IPT <= 8 ? 3 : 2)
     k_scan_seg_apply(const ScanParams p) {
     pdl_wait();
@@ -2463,32 +2483,45 @@ __global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : NS > 0 &
         const i64 ke = kb + su * XTG_SCAN_UNIT < p.len ? kb + su * XTG_SCAN_UNIT : p.len;
         ST carry = reinterpret_cast<const ST*>(p.agg)[it];
         RT* o = reinterpret_cast<RT*>(p.out) + row * p.oso;
-        auto tile = [&](RT(&v)[IPT], i64 k0, RT csv) {
+        auto tile = [&](RT(&v)[IPT], i64 k0, const RT* csv) {
             const i64 kt = k0 + lofs;
             // every tile but a row's last is whole: no per-element checks
             const bool full = kt + IPT <= ke;
-            ST s = ST::ident();
+            ST hs[H];
             if constexpr (CS) {
-                s.hi = csv;
-            } else if (full) {
 #pragma unroll
-                for (int i = 0; i < IPT; ++i) s.add(v[i]);
+                for (int j = 0; j < H; ++j) {
+                    hs[j] = ST::ident();
+                    hs[j].hi = csv[j];
+                }
             } else {
-#pragma unroll
-                for (int i = 0; i < IPT; ++i)
-                    if (kt + i < ke) s.add(v[i]);
+                lane_fold<H>(hs, v, kt, ke);
             }
+            ST s = ST::ident();
+#pragma unroll
+            for (int j = 0; j < H; ++j) s.merge(hs[j]);
             const ST inc = warp_inorder_scan(s);
             const ST lex = shfl_up_pod(inc, 1);
             const ST tile_tot = shfl_idx_pod(inc, 31);
             ST pre = carry;
             if (lane > 0) pre.merge(lex);
             if (full && kt != 0) {
+                // chain j starts from the prefix plus the folds before it
+                constexpr int L = IPT / H;
+                ST pr[H];
+                pr[0] = pre;
 #pragma unroll
-                for (int i = 0; i < IPT; ++i) {
-                    pre.add(v[i]);
-                    v[i] = pre.value();
+                for (int j = 1; j < H; ++j) {
+                    pr[j] = pr[j - 1];
+                    pr[j].merge(hs[j - 1]);
                 }
+#pragma unroll
+                for (int i = 0; i < L; ++i)
+#pragma unroll
+                    for (int j = 0; j < H; ++j) {
+                        pr[j].add(v[j * L + i]);
+                        v[j * L + i] = pr[j].value();
+                    }
             } else {
 #pragma unroll
                 for (int i = 0; i < IPT; ++i) {
@@ -2523,8 +2556,9 @@ __global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : NS > 0 &
             constexpr int EPC = 16 / (int)sizeof(RT);        // elements per 16-byte chunk
             constexpr int CPL = IPT / EPC;                   // chunks per lane
             constexpr int SB = 32 * IPT * (int)sizeof(RT);   // bytes of a warp tile
-            // a stage: the warp tile, then (CS) the 32 lanes' totals from pass A
-            constexpr int SBX = SB + (CS ? 32 * (int)sizeof(RT) : 0);
+            // a stage: the warp tile, then (CS) the 32 lanes' H folds from pass A
+            constexpr int CSB = H * (int)sizeof(RT);
+            constexpr int SBX = SB + (CS ? 32 * CSB : 0);
             unsigned char* wbase = ring + (size_t)warp * NS * SBX;
             unsigned char* wr = wbase + (size_t)lane * CPL * 16;
             const int rot = (lane / (CPL >= 8 ? 1 : 8 / CPL)) % CPL;
@@ -2538,8 +2572,8 @@ __global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : NS > 0 &
                     for (int m = 0; m < CPL; ++m) cp_async<16>(d + ((m + rot) % CPL) * 16, src + kt + m * EPC);
                 }
                 if (CS && t < T)
-                    cp_async<(int)sizeof(RT)>(wbase + (int)(t % NS) * SBX + SB + lane * (int)sizeof(RT),
-                                              scan_csum<RT>(p) + (row * tiles_per_row + (kb + t * WT) / WT) * 32 + lane);
+                    cp_async<CSB>(wbase + (int)(t % NS) * SBX + SB + lane * CSB,
+                                  scan_csum<RT>(p) + ((row * tiles_per_row + (kb + t * WT) / WT) * 32 + lane) * H);
                 cp_async_commit();
             };
 #pragma unroll 1
@@ -2550,8 +2584,10 @@ __global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : NS > 0 &
                 issue(t + NS - 1);
                 cp_async_wait<NS - 1>();
                 const i64 k0 = kb + t * WT, kt = k0 + lofs;
-                const RT csv =
-                    CS ? *reinterpret_cast<const RT*>(wbase + (int)(t % NS) * SBX + SB + lane * (int)sizeof(RT)) : RT(0);
+                RT csv[H];
+#pragma unroll
+                for (int j = 0; j < H; ++j)
+                    csv[j] = CS ? reinterpret_cast<const RT*>(wbase + (int)(t % NS) * SBX + SB + lane * CSB)[j] : RT(0);
                 RT v[IPT];
                 if (kt + IPT <= ke) {
                     const unsigned char* d = wr + (int)(t % NS) * SBX;
@@ -2574,7 +2610,7 @@ __global__ void __launch_bounds__(256, VEC > 1 && sizeof(RT) <= 4 ? 4 : NS > 0 &
         } else {
             static_assert(!CS, "lane totals from pass A come with the streamed form");
             scan_walk<Tree, LS, RT, VEC, IPT>(p, c, row, kb, ke, wb,
-                                              [&](RT(&v)[IPT], i64 k0) { tile(v, k0, RT(0)); });
+                                              [&](RT(&v)[IPT], i64 k0) { tile(v, k0, nullptr); });
         }
     }
 }
