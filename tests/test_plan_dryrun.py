@@ -168,6 +168,49 @@ def test_accumulator_plans(dt):
     assert fam(last_kernels())[0] == "k_transpose"
 
 
+def test_segmented_scan_variants():
+    """The segmented scan's apply pass streams a plain contiguous operand of
+    the accumulation type (4 or 8 bytes) through its cp.async ring in tiles
+    of 32 x 16 (template tail: stages, elements per lane, lane folds kept by
+    pass A, chains per lane); float64 keeps the lanes' folds from pass A and
+    folds in two chains, with or without them; expressions and unaligned or
+    strided operands take the register form (32 x 8).  Pass A's tiles match
+    pass C's for streamed operands; every variant compiles."""
+    from xtensor_gb300 import ops
+    n = 3_000_001
+
+    def plan(x, **opts):
+        for k, v in opts.items():
+            xg.set_option(k, v)
+        try:
+            ops.accumulate("cumsum", x, None, out=fake((x.size,), x.dtype))
+            return last_kernels()
+        finally:
+            for k in opts:
+                xg.set_option(k, -1)
+
+    ks = plan(fake((n,), "float64"))
+    assert fam(ks) == ["k_scan_seg_reduce", "k_scan_seg_offsets", "k_scan_seg_apply"]
+    assert ks[0].endswith(", 2, 16, true, 2>") and ks[2].endswith(", 2, 3, 16, true, 2>"), ks
+    ks = plan(fake((n,), "float64"), **{"scan.lane_totals": 0})
+    assert ks[0].endswith(", 2, 16, false, 2>") and ks[2].endswith(", 2, 3, 16, false, 2>"), ks
+    ks = plan(fake((n,), "float32"))
+    assert ks[0].endswith(", 4, 16, false, 1>") and ks[2].endswith(", 4, 3, 16, false, 1>"), ks
+    ks = plan(fake((n,), "int32"), **{"scan.seg_stages": 5})
+    assert ks[2].endswith(", 4, 5, 16, false, 1>"), ks
+    # the register form: no ring, 8 elements per lane in pass C (pass A
+    # keeps 16 for 4-byte types: its tiles only have to cover the segments)
+    ks = plan(fake((n,), "float32"), **{"scan.async": 0})
+    assert ks[0].endswith(", 4, 16, false, 1>") and ks[2].endswith(", 4, 0, 8, false, 1>"), ks
+    x = fake((n,), "float32")
+    ops.accumulate("cumsum", x + x, None, out=fake((n,), "float32"))
+    assert last_kernels()[2].endswith(", 0, 8, false, 1>"), last_kernels()
+    # a strided operand: scalar loads through the warp's buffer
+    y = fake((2, n), "float64")
+    ops.accumulate("cumsum", y[:, ::2], 1, out=fake((2, (n + 1) // 2), "float64"))
+    assert last_kernels()[-1].endswith(", 1, 0, 8, false, 1>"), last_kernels()
+
+
 def test_view_plans():
     """Masked writes lower to the elementwise kernel, index views to the
     indexed kernel, filters to the accumulator (positions) + indexed kernel;
