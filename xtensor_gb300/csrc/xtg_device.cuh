@@ -2089,7 +2089,8 @@ __global__ void __launch_bounds__(64) k_scan_rows(const ScanParams p) {
 }
 
 // K9c: a few long rows (and the flattened form) — segmented
-// reduce-then-scan (k_scan_seg_* below), no CTA waiting on another.
+// reduce-then-scan (k_scan_seg_* below), one warp per segment, no warp
+// waiting on another.
 // ScanState carries float32
 // values in double-float (TwoSum for sums, fma-exact TwoProd for products) so
 // the tile results are within a few ulp of the exact prefix; other types fold
