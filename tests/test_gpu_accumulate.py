@@ -320,3 +320,23 @@ def test_streamed_and_register_forms_agree(scan_opts):
     tol = 2.0**-23 * np.abs(exact) + 2.0**-36 * np.cumsum(np.abs(x.astype(np.float64)))
     for mode in (1, 0):
         assert (np.abs(outs[mode][1] - exact) <= tol).all(), mode
+
+
+def test_cached_plan_replay_after_smaller_call():
+    """Pass B stages a row's segment totals in dynamic shared memory sized by
+    the call (2^24 elements: ~4.7K segments, above 48 KiB; 10^5 elements: a
+    few KiB).  A kernel's dynamic limit is only ever raised, so the large
+    call's cached plan still launches after the small call configured the
+    same kernel for less, and gives the same bits."""
+    g = rng(63)
+    big = g.standard_normal(1 << 24).astype(np.float32)
+    small = g.standard_normal(100_000).astype(np.float32)
+    db, ds = dev(big), dev(small)
+    ob, os_ = DeviceArray.empty((big.size,), "float32"), DeviceArray.empty((small.size,), "float32")
+    first = ops.accumulate("cumsum", db, None, out=ob).to_numpy()
+    ops.accumulate("cumsum", ds, None, out=os_)
+    again = ops.accumulate("cumsum", db, None, out=ob).to_numpy()  # replayed from the plan cache
+    np.testing.assert_array_equal(first.view(np.uint32), again.view(np.uint32))
+    exact = np.cumsum(small.astype(np.float64))
+    tol = 2.0**-23 * np.abs(exact) + 2.0**-36 * np.cumsum(np.abs(small.astype(np.float64)))
+    assert (np.abs(os_.to_numpy() - exact) <= tol).all()

@@ -89,6 +89,8 @@ struct Kernel {
     int max_blocks_per_sm = 0;  // occupancy at the block size it was queried for
     int block = 0;
     size_t dyn_smem = 0;        // dynamic shared memory the occupancy was queried with
+    size_t smem_limit = 0;      // the kernel's dynamic shared-memory limit: only ever raised, so
+                                // the launches of a cached plan stay within it when replayed
 };
 // Compiles (or fetches) the kernel whose name expression is `expr`
 // (e.g. "xtg::k_assign<...>").  `block` / `dyn_smem` are used for the

@@ -145,9 +145,14 @@ static xtg_status configure(Kernel* k, int block, size_t dyn_smem) {
     }
     if (k->block == block && k->dyn_smem == dyn_smem && k->max_blocks_per_sm > 0) return XTG_OK;
     // the dynamic limit covers the request whatever the kernel's static
-    // shared memory (static + dynamic above 48 KiB needs the opt-in)
-    if (dyn_smem > 0)
+    // shared memory (static + dynamic above 48 KiB needs the opt-in); it is
+    // raised, never lowered: a kernel whose dynamic size depends on the call
+    // (a row length, a segment count) keeps the launches recorded in cached
+    // plans for larger calls valid
+    if (dyn_smem > k->smem_limit) {
         XTG_CU(drv().FuncSetAttribute(k->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)dyn_smem));
+        k->smem_limit = dyn_smem;
+    }
     int nb = 0;
     if (drv().OccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, block, dyn_smem) != CUDA_SUCCESS) nb = 1;
     k->max_blocks_per_sm = nb > 0 ? nb : 1;
