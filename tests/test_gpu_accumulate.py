@@ -8,8 +8,11 @@ Tolerances (stated here, checked below):
   * float results of the tile scan (a few long rows, the flattened form):
     float32 |gpu - exact| <= 2^-23 |exact| + 2^-36 * prefix sum|x| (sums;
     products 4 ulp of the exact product), float64 within the reference's own
-    sequential error envelope plus 1e-15 of the prefix magnitude;
-  * reproducible: the same call twice gives identical bits.
+    sequential error envelope plus 1e-15 of the prefix magnitude (rows of
+    3M elements: 1e-12 of the prefix magnitude for sums, 1e-9 relative for
+    products, where both folds' rounding grows with the length);
+  * reproducible: the same call twice gives identical bits; the streamed
+    float64 scan gives the same bits with and without pass A's lane folds.
 """
 from __future__ import annotations
 
